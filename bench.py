@@ -1,0 +1,326 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 bundle adjuster.
+
+Metric (one JSON line on rank 0):
+  "BA time-to-converge (rel cost 1e-6) mixed vs FP64 GPU; Mobs/s residual+Jacobian"
+
+* value -- residual + Jacobian evaluation throughput in Mobs/s (mixed
+  precision: FP64 camera centring, FP32 residual/Jacobian records) over the
+  whole workload with every input resident in HBM.  One step = one pass over
+  all observations (per-shot pose precompute + per-observation record
+  kernel).  Inputs (300+ MB) and records (1.5+ GB) exceed the 129 MB L2.
+* e2e -- the same metric through the reference-facing C-ABI call
+  gbba_evaluate_projections with host buffers: host->device copy of the
+  scene, evaluation, device->host copy of the FP64 residual/Jacobian blocks.
+* converge -- the other half of the metric: a full Levenberg-Marquardt solve
+  in mixed precision and in plain FP64 on the same workload (added when the
+  solver runs on the device).
+* roofline -- of the record kernel: algorithmic bytes (observation inputs,
+  points, records written) per launch / CUDA-event time of that launch.
+* cpu_baseline -- the FP64 CPU oracle (a restatement of the reference's
+  ReprojectionError2DAnalytic evaluation; Ceres/OpenSfM cannot be built on
+  these machines) on a bounded sample, all host threads.
+
+Usage:
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--workload aerial|street|ring]
+  python bench.py --impl reference ...   (CPU reference arm)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "BA time-to-converge (rel cost 1e-6) mixed vs FP64 GPU; Mobs/s residual+Jacobian"
+UNIT = "Mobs/s"
+
+
+def make_workload(name: str, seed_offset: int = 0):
+    from opensfm_gb300 import synthetic as syn
+    if name == "aerial":
+        scene = syn.aerial_scene(seed=3 + seed_offset)
+        cfg = {"workload": "aerial nadir BA: 70x72=5040 perspective cameras, 2M terrain points, "
+                           "~15M observations, GPS priors, UTM-scale coordinates",
+               "n_shots": 5040}
+    elif name == "street":
+        scene = syn.street_scene(seed=7 + seed_offset)
+        cfg = {"workload": "street BA: 500 Brown cameras (4 models), 200k points, ~1.4M observations, "
+                           "2% outliers", "n_shots": 500}
+    elif name == "ring":
+        scene = syn.ring_scene(seed=42 + seed_offset)
+        cfg = {"workload": "ring BA: 20 perspective cameras, 2k points, 12k observations", "n_shots": 20}
+    else:
+        raise SystemExit(f"unknown workload {name}")
+    cfg.update(n_points=int(len(scene.points)), n_observations=int(scene.n_observations))
+    return scene, cfg
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def traffic_per_obs(kernel: str, precision: str):
+    """DRAM bytes per observation of a kernel from a committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    return d.get(f"{kernel}:{precision}")
+
+
+def cpu_baseline(scene, target_s: float = 10.0) -> dict:
+    """FP64 CPU oracle evaluation on a bounded sample, all host threads."""
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    n = scene.n_observations
+    probe = min(n, 200_000)
+    sub = scene.subset_observations(np.arange(probe))
+    oracle.evaluate_scene(sub, threads)  # warm
+    t0 = time.perf_counter()
+    oracle.evaluate_scene(sub, threads)
+    rate = probe / max(time.perf_counter() - t0, 1e-9)
+    m = int(min(n, max(probe, rate * target_s)))
+    sub = scene.subset_observations(np.arange(m))
+    t0 = time.perf_counter()
+    oracle.evaluate_scene(sub, threads)
+    dt = time.perf_counter() - t0
+    return {"value": m / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {m} of {n} observations, FP64 residual+Jacobian blocks, {threads} threads, "
+                      f"{dt:.1f} s"}
+
+
+def run_reference(args) -> None:
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    scene, cfg = make_workload(args.workload)
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    n = scene.n_observations
+    # bounded sample: about 2 s of CPU work per step
+    probe = min(n, 200_000)
+    sub = scene.subset_observations(np.arange(probe))
+    t0 = time.perf_counter()
+    oracle.evaluate_scene(sub, threads)
+    rate = probe / max(time.perf_counter() - t0, 1e-9)
+    m = int(min(n, max(probe, rate * 2.0)))
+    sub = scene.subset_observations(np.arange(m))
+    for _ in range(args.warmup):
+        oracle.evaluate_scene(sub, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.evaluate_scene(sub, threads)
+    dt = time.perf_counter() - t0
+    value = m * args.steps / dt / 1e6
+    sample = f"first {m} of {n} observations per step, FP64 residual+Jacobian blocks, {threads} threads"
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic", "config": cfg,
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "CPU restatement of the reference's analytic residual/Jacobian evaluation "
+                   "(Ceres 2.2 / Eigen are not installable here, so the reference itself cannot be built)"}
+    print(json.dumps(out), flush=True)
+
+
+def run_ours(args) -> None:
+    import torch
+    from opensfm_gb300 import _lib
+    from opensfm_gb300.scene import Evaluator, alloc_outputs, output_struct
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    scene, cfg = make_workload(args.workload, seed_offset=rank)
+    n_obs = scene.n_observations
+    L = _lib.lib()
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+
+    ev = Evaluator(scene, _lib.PRECISION_MIXED)
+    for _ in range(args.warmup):
+        ev.run(sh)
+    torch.cuda.synchronize()
+
+    rec_bytes = ev.record_bytes
+    in_bytes = n_obs * (8 + 4 + 4 + 4) + len(scene.points) * 32
+    ev_start = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_mid = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ev_end = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_all0 = torch.cuda.Event(enable_timing=True)
+        t_all1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            t_all0.record(stream)
+            for k in range(args.steps):
+                ev_start[k].record(stream)
+                ev.prepare(sh)
+                ev_mid[k].record(stream)
+                ev.records(sh)
+                ev_end[k].record(stream)
+            t_all1.record(stream)
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    elapsed = t_all0.elapsed_time(t_all1) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    rec_ms = float(np.mean([ev_mid[k].elapsed_time(ev_end[k]) for k in range(args.steps)]))
+    value = n_obs * args.steps * world / elapsed / 1e6
+
+    # e2e: the one-shot host-buffer call
+    nr, cmax = scene.layout()
+    out = alloc_outputs(n_obs, nr, cmax)
+    o = output_struct(out)
+    s = scene.ctypes()
+    import ctypes as C
+    _lib.check(L.gbba_evaluate_projections(C.byref(s), _lib.PRECISION_MIXED, C.byref(o)))  # warm
+    e2e_steps = max(1, min(3, args.steps))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        _lib.check(L.gbba_evaluate_projections(C.byref(s), _lib.PRECISION_MIXED, C.byref(o)))
+    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    h2d = sum(a.nbytes for a in (scene.camera_projection, scene.camera_values, scene.rig_instance_poses,
+                                 scene.shot_rig_instance, scene.shot_camera, scene.shot_rig_camera,
+                                 scene.points, scene.obs_shot, scene.obs_point, scene.obs_xy, scene.obs_std))
+    d2h = sum(a.nbytes for a in (out.residuals, out.jac_camera, out.jac_instance, out.jac_rig_camera,
+                                 out.jac_point))
+
+    peaks = measured_peaks()
+    achieved = (in_bytes + rec_bytes) / (rec_ms / 1e3) / 1e9
+    tpo = traffic_per_obs("eval_records_kernel", "mixed")
+    result = None
+    if rank == 0:
+        result = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+            "data": "synthetic (seeded generator, opensfm_gb300.synthetic)",
+            "config": dict(cfg, precision="mixed: FP64 centring, FP32 records",
+                           l2="inputs and records larger than L2 (no flush needed)",
+                           parallelism=f"replicas x{world}"),
+            "e2e": {"value": n_obs / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h),
+                    "path": "gbba_evaluate_projections (host buffers, FP64 blocks out)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": (tpo * n_obs if tpo else None),
+                         "kernel": "eval_records_kernel", "algorithmic_bytes": int(in_bytes + rec_bytes),
+                         "kernel_ms": rec_ms, "peak_source": peaks["source"]},
+            "clocks": clocks.summary(),
+            "gpu_launches": args.steps * ev.launches_per_run,
+        }
+        if not args.no_cpu_baseline:
+            result["cpu_baseline"] = cpu_baseline(scene)
+        print(json.dumps(result), flush=True)
+    ev.close()
+    if dist:
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="aerial", choices=["aerial", "street", "ring"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,446 @@
+// Standalone batched residual + Jacobian evaluation behind the C ABI
+// (gbba_evaluate_projections / gbba_evaluator_*).  This is the GPU
+// counterpart of calling ReprojectionError2DAnalytic<C>::Evaluate
+// (opensfm/src/lib/bundle/error/projection_errors.h:67-207) for every
+// observation of a problem.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gbba.h"
+#include "capi_util.h"
+#include "device_buffer.h"
+#include "eval_kernels.cuh"
+
+namespace gbba {
+
+namespace {
+
+constexpr int kDynamicModel = -1;
+
+// Conversion of device records to the reference's per-block FP64 layout.
+template <typename R, int NR, int CMAX, bool RIG>
+__global__ void records_to_blocks_kernel(int64_t n, const typename Vec16<R>::type* __restrict__ rec_planes,
+                                         int64_t plane_stride, int nr_out, int cmax_out,
+                                         double* __restrict__ res, double* __restrict__ jc,
+                                         double* __restrict__ ji, double* __restrict__ jr,
+                                         double* __restrict__ jp) {
+  using L = RecordLayout<NR, CMAX, RIG>;
+  constexpr int NP = planes_of<R>(L::kWidth);
+  constexpr int VN = Vec16<R>::kN;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    R rec[NP * VN];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) load_plane<R>(rec_planes + p * plane_stride + i, rec + p * VN);
+    for (int r = 0; r < nr_out; ++r) {
+      const bool row = r < NR;
+      res[i * nr_out + r] = row ? double(rec[L::kR + r]) : 0.0;
+      if (jp)
+        for (int j = 0; j < 3; ++j) jp[(i * nr_out + r) * 3 + j] = row ? double(rec[L::kPt + r * 3 + j]) : 0.0;
+      if (ji)
+        for (int j = 0; j < 6; ++j) ji[(i * nr_out + r) * 6 + j] = row ? double(rec[L::kInst + r * 6 + j]) : 0.0;
+      if (jr)
+        for (int j = 0; j < 6; ++j)
+          jr[(i * nr_out + r) * 6 + j] = (row && RIG) ? double(rec[(RIG ? L::kRig : 0) + r * 6 + j]) : 0.0;
+      if (jc)
+        for (int j = 0; j < cmax_out; ++j)
+          jc[(i * nr_out + r) * cmax_out + j] = (row && j < CMAX) ? double(rec[L::kCam + r * CMAX + j]) : 0.0;
+    }
+  }
+}
+
+int grid_for(int64_t n, int block) {
+  const int64_t want = (n + block - 1) / block;
+  const int64_t cap = 152 * 16;
+  return int(std::max<int64_t>(1, std::min(want, cap)));
+}
+
+struct Layout {
+  int model;  // single model id, or kDynamicModel
+  int nr;
+  int cmax;   // record columns of the camera block
+  bool rig;
+  int cmax_out;
+};
+
+template <typename R>
+struct EvalState {
+  DeviceArray<ShotGeom<R>> geom;
+  DeviceArray<RigGeom<R>> rig;
+  DeviceArray<Point4> center;
+  DeviceArray<int> shot_cam, cam_model, shot_inst, shot_rig;
+  DeviceArray<R> cam_params;
+  DeviceArray<double> inst_pose, rig_pose;
+  DeviceArray<uint8_t> rig_used;
+  DeviceArray<Point4> points;
+  DeviceArray<int> obs_shot, obs_point;
+  DeviceArray<R> obs_xy, obs_w;
+  DeviceArray<typename Vec16<R>::type> records;
+  int64_t n_obs = 0;
+  int n_shots = 0;
+  int n_planes = 0;
+
+  SceneView<R> view() const {
+    SceneView<R> v;
+    v.n_slots = n_obs;
+    v.geom = geom.get();
+    v.rig = rig.size() ? rig.get() : nullptr;
+    v.center = center.get();
+    v.shot_cam = shot_cam.get();
+    v.cam_model = cam_model.get();
+    v.cam_params = cam_params.get();
+    v.points = points.get();
+    v.obs_shot = obs_shot.get();
+    v.obs_point = obs_point.get();
+    v.obs_xy = obs_xy.get();
+    v.obs_w = obs_w.get();
+    return v;
+  }
+};
+
+// Instantiation table of the record kernel.
+template <typename R, int M, int NR, int CMAX, bool RIG>
+void launch_eval(const SceneView<R>& v, typename Vec16<R>::type* out, int64_t stride, cudaStream_t st) {
+  eval_records_kernel<R, M, NR, CMAX, RIG><<<grid_for(v.n_slots, 256), 256, 0, st>>>(v, out, stride, ~uint64_t(0));
+}
+template <typename R, int NR, int CMAX, bool RIG>
+void launch_blocks(int64_t n, const typename Vec16<R>::type* rec, int64_t stride, int nr_out, int cmax_out,
+                   double* res, double* jc, double* ji, double* jr, double* jp, cudaStream_t st) {
+  records_to_blocks_kernel<R, NR, CMAX, RIG>
+      <<<grid_for(n, 256), 256, 0, st>>>(n, rec, stride, nr_out, cmax_out, res, jc, ji, jr, jp);
+}
+
+template <typename R>
+void dispatch_eval(const Layout& L, const SceneView<R>& v, typename Vec16<R>::type* out, int64_t stride,
+                   cudaStream_t st) {
+  if (L.model != kDynamicModel) {
+    switch (L.model) {
+      case kPerspective: launch_eval<R, kPerspective, 2, 3, false>(v, out, stride, st); return;
+      case kBrown: launch_eval<R, kBrown, 2, 9, false>(v, out, stride, st); return;
+      case kFisheye: launch_eval<R, kFisheye, 2, 3, false>(v, out, stride, st); return;
+      case kFisheyeOpencv: launch_eval<R, kFisheyeOpencv, 2, 8, false>(v, out, stride, st); return;
+      case kFisheye62: launch_eval<R, kFisheye62, 2, 12, false>(v, out, stride, st); return;
+      case kFisheye624: launch_eval<R, kFisheye624, 2, 16, false>(v, out, stride, st); return;
+      case kDual: launch_eval<R, kDual, 2, 4, false>(v, out, stride, st); return;
+      case kRadial: launch_eval<R, kRadial, 2, 6, false>(v, out, stride, st); return;
+      case kSimpleRadial: launch_eval<R, kSimpleRadial, 2, 5, false>(v, out, stride, st); return;
+    }
+  }
+  if (L.nr == 2) {
+    if (L.rig) launch_eval<R, kDynamicModel, 2, 16, true>(v, out, stride, st);
+    else launch_eval<R, kDynamicModel, 2, 16, false>(v, out, stride, st);
+  } else {
+    if (L.rig) launch_eval<R, kDynamicModel, 3, 16, true>(v, out, stride, st);
+    else launch_eval<R, kDynamicModel, 3, 16, false>(v, out, stride, st);
+  }
+}
+
+template <typename R>
+void dispatch_blocks(const Layout& L, int64_t n, const typename Vec16<R>::type* rec, int64_t stride,
+                     const gbba_eval_output_t& o, cudaStream_t st) {
+  double *res = o.residuals, *jc = o.jac_camera, *ji = o.jac_instance, *jr = o.jac_rig_camera,
+         *jp = o.jac_point;
+  const int nr = L.nr, co = L.cmax_out;
+  if (L.model != kDynamicModel) {
+    switch (L.cmax) {
+      case 3: launch_blocks<R, 2, 3, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 4: launch_blocks<R, 2, 4, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 5: launch_blocks<R, 2, 5, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 6: launch_blocks<R, 2, 6, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 8: launch_blocks<R, 2, 8, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 9: launch_blocks<R, 2, 9, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 12: launch_blocks<R, 2, 12, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+      case 16: launch_blocks<R, 2, 16, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st); return;
+    }
+  }
+  if (L.nr == 2) {
+    if (L.rig) launch_blocks<R, 2, 16, true>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st);
+    else launch_blocks<R, 2, 16, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st);
+  } else {
+    if (L.rig) launch_blocks<R, 3, 16, true>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st);
+    else launch_blocks<R, 3, 16, false>(n, rec, stride, nr, co, res, jc, ji, jr, jp, st);
+  }
+}
+
+template <int NR, int CMAX, bool RIG>
+int record_width() {
+  return RecordLayout<NR, CMAX, RIG>::kWidth;
+}
+
+int layout_width(const Layout& L) {
+  if (L.model != kDynamicModel) return RecordLayout<2, 1, false>::kCam + 2 * L.cmax;
+  const int base = L.nr + 3 * L.nr + 6 * L.nr + 16 * L.nr;
+  return base + (L.rig ? 6 * L.nr : 0);
+}
+
+void validate_scene(const gbba_scene_t* s) {
+  if (!s) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (s->n_cameras < 0 || s->n_rig_instances < 0 || s->n_rig_cameras < 0 || s->n_shots < 0 ||
+      s->n_points < 0 || s->n_observations < 0)
+    throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative count in scene");
+  for (int c = 0; c < s->n_cameras; ++c) {
+    const int m = s->camera_projection[c];
+    if (m < 0 || m >= kNumProjections)
+      throw ApiError(GBBA_ERR_RUNTIME, "Invalid ProjectionType for camera " + std::to_string(c));
+  }
+  for (int i = 0; i < s->n_shots; ++i) {
+    if (s->shot_rig_instance[i] < 0 || s->shot_rig_instance[i] >= s->n_rig_instances ||
+        s->shot_camera[i] < 0 || s->shot_camera[i] >= s->n_cameras ||
+        s->shot_rig_camera[i] < -1 || s->shot_rig_camera[i] >= s->n_rig_cameras)
+      throw ApiError(GBBA_ERR_OUT_OF_RANGE, "shot " + std::to_string(i) + " references a missing block");
+  }
+  for (int64_t i = 0; i < s->n_observations; ++i) {
+    if (s->obs_shot[i] < 0 || s->obs_shot[i] >= s->n_shots || s->obs_point[i] < 0 ||
+        s->obs_point[i] >= s->n_points)
+      throw ApiError(GBBA_ERR_OUT_OF_RANGE, "observation " + std::to_string(i) + " references a missing shot or point");
+    if (!(s->obs_std[i] > 0.0))
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "observation " + std::to_string(i) + " has non-positive std");
+  }
+}
+
+Layout scene_layout(const gbba_scene_t* s) {
+  Layout L;
+  bool any_sph = false, any_rig = false;
+  int cmax = 1, first = -1;
+  bool single = true;
+  std::vector<uint8_t> cam_used(s->n_cameras, 0);
+  for (int i = 0; i < s->n_shots; ++i) {
+    cam_used[s->shot_camera[i]] = 1;
+    const int rc = s->shot_rig_camera[i];
+    if (rc >= 0 && s->rig_camera_used && s->rig_camera_used[rc]) any_rig = true;
+  }
+  for (int c = 0; c < s->n_cameras; ++c) {
+    if (!cam_used[c]) continue;
+    const int m = s->camera_projection[c];
+    if (m == kSpherical) any_sph = true;
+    cmax = std::max(cmax, model_num_params(m));
+    if (first < 0) first = m;
+    else if (first != m) single = false;
+  }
+  L.nr = any_sph ? 3 : 2;
+  L.rig = any_rig;
+  L.cmax_out = cmax;
+  if (single && !any_sph && !any_rig && first >= 0) {
+    L.model = first;
+    L.cmax = model_num_params(first);
+  } else {
+    L.model = kDynamicModel;
+    L.cmax = 16;
+  }
+  return L;
+}
+
+}  // namespace
+
+// Holds a device-resident scene in one precision.
+struct EvaluatorImpl {
+  int precision = GBBA_PRECISION_MIXED;
+  Layout L{};
+  EvalState<float> f;
+  EvalState<double> d;
+
+  template <typename R>
+  EvalState<R>& st();
+
+  template <typename R>
+  void upload(const gbba_scene_t* s) {
+    EvalState<R>& e = st<R>();
+    e.n_obs = s->n_observations;
+    e.n_shots = s->n_shots;
+    std::vector<R> cam(size_t(s->n_cameras) * kMaxCameraParams);
+    for (size_t i = 0; i < cam.size(); ++i) cam[i] = R(s->camera_values[i]);
+    e.cam_params.upload(cam);
+    e.cam_model.upload(s->camera_projection, s->n_cameras);
+    e.shot_cam.upload(s->shot_camera, s->n_shots);
+    e.shot_inst.upload(s->shot_rig_instance, s->n_shots);
+    e.shot_rig.upload(s->shot_rig_camera, s->n_shots);
+    e.inst_pose.upload(s->rig_instance_poses, size_t(s->n_rig_instances) * 6);
+    std::vector<double> rp(size_t(std::max(1, s->n_rig_cameras)) * 6, 0.0);
+    std::vector<uint8_t> ru(size_t(std::max(1, s->n_rig_cameras)), 0);
+    for (int i = 0; i < s->n_rig_cameras; ++i) {
+      for (int k = 0; k < 6; ++k) rp[i * 6 + k] = s->rig_camera_poses[i * 6 + k];
+      ru[i] = s->rig_camera_used ? s->rig_camera_used[i] : 0;
+    }
+    e.rig_pose.upload(rp);
+    e.rig_used.upload(ru);
+    std::vector<Point4> pts(size_t(s->n_points));
+    for (int64_t i = 0; i < s->n_points; ++i)
+      pts[i] = Point4{s->points[3 * i], s->points[3 * i + 1], s->points[3 * i + 2], 0.0};
+    e.points.upload(pts);
+    e.obs_shot.upload(s->obs_shot, size_t(s->n_observations));
+    e.obs_point.upload(s->obs_point, size_t(s->n_observations));
+    std::vector<R> xy(size_t(s->n_observations) * 2), w(size_t(s->n_observations));
+    for (int64_t i = 0; i < s->n_observations; ++i) {
+      xy[2 * i] = R(s->obs_xy[2 * i]);
+      xy[2 * i + 1] = R(s->obs_xy[2 * i + 1]);
+      w[i] = R(1.0 / s->obs_std[i]);
+    }
+    e.obs_xy.upload(xy);
+    e.obs_w.upload(w);
+    e.geom.resize(std::max(1, s->n_shots));
+    e.center.resize(std::max(1, s->n_shots));
+    if (L.rig) e.rig.resize(std::max(1, s->n_shots));
+    e.n_planes = planes_of<R>(layout_width(L));
+    e.records.resize(size_t(e.n_planes) * std::max<int64_t>(1, e.n_obs));
+    GB_CUDA(cudaStreamSynchronize(0));
+  }
+
+  template <typename R>
+  void run(cudaStream_t stream) {
+    prepare<R>(stream);
+    records<R>(stream);
+  }
+
+  template <typename R>
+  void prepare(cudaStream_t stream) {
+    EvalState<R>& e = st<R>();
+    if (e.n_shots > 0) {
+      shot_prep_kernel<R><<<(e.n_shots + 127) / 128, 128, 0, stream>>>(
+          e.n_shots, e.shot_inst.get(), e.shot_rig.get(), e.inst_pose.get(), e.rig_pose.get(),
+          e.rig_used.get(), e.geom.get(), e.center.get(), L.rig ? e.rig.get() : nullptr);
+      GB_CUDA(cudaGetLastError());
+    }
+  }
+
+  template <typename R>
+  void records(cudaStream_t stream) {
+    EvalState<R>& e = st<R>();
+    if (e.n_obs > 0) {
+      dispatch_eval<R>(L, e.view(), e.records.get(), e.n_obs, stream);
+      GB_CUDA(cudaGetLastError());
+    }
+  }
+
+  template <typename R>
+  void download(gbba_eval_output_t* out) {
+    EvalState<R>& e = st<R>();
+    const int64_t n = e.n_obs;
+    if (n == 0) return;
+    const int nr = L.nr, co = L.cmax_out;
+    DeviceArray<double> res(size_t(n) * nr), jc, ji, jr, jp;
+    if (out->jac_camera) jc.resize(size_t(n) * nr * co);
+    if (out->jac_instance) ji.resize(size_t(n) * nr * 6);
+    if (out->jac_rig_camera) jr.resize(size_t(n) * nr * 6);
+    if (out->jac_point) jp.resize(size_t(n) * nr * 3);
+    gbba_eval_output_t dev{res.get(), jc.size() ? jc.get() : nullptr, ji.size() ? ji.get() : nullptr,
+                           jr.size() ? jr.get() : nullptr, jp.size() ? jp.get() : nullptr};
+    dispatch_blocks<R>(L, n, e.records.get(), n, dev, 0);
+    GB_CUDA(cudaGetLastError());
+    if (out->residuals) res.download(out->residuals, res.size());
+    if (out->jac_camera) jc.download(out->jac_camera, jc.size());
+    if (out->jac_instance) ji.download(out->jac_instance, ji.size());
+    if (out->jac_rig_camera) jr.download(out->jac_rig_camera, jr.size());
+    if (out->jac_point) jp.download(out->jac_point, jp.size());
+    GB_CUDA(cudaStreamSynchronize(0));
+  }
+
+  int64_t record_bytes() const {
+    return precision == GBBA_PRECISION_FP64 ? int64_t(d.n_planes) * 16 * d.n_obs
+                                            : int64_t(f.n_planes) * 16 * f.n_obs;
+  }
+};
+template <> EvalState<float>& EvaluatorImpl::st<float>() { return f; }
+template <> EvalState<double>& EvaluatorImpl::st<double>() { return d; }
+
+}  // namespace gbba
+
+struct gbba_evaluator {
+  gbba::EvaluatorImpl impl;
+};
+
+using gbba::ApiError;
+
+extern "C" {
+
+int gbba_camera_num_params(int projection) {
+  if (projection < 0 || projection >= gbba::kNumProjections) return -1;
+  return gbba::model_num_params(projection);
+}
+
+int gbba_scene_layout(const gbba_scene_t* scene, int* nr, int* cmax) {
+  return gbba::guarded([&] {
+    gbba::validate_scene(scene);
+    const gbba::Layout L = gbba::scene_layout(scene);
+    if (nr) *nr = L.nr;
+    if (cmax) *cmax = L.cmax_out;
+  });
+}
+
+gbba_evaluator_t* gbba_evaluator_create(const gbba_scene_t* scene, int precision) {
+  gbba_evaluator_t* ev = nullptr;
+  const int st = gbba::guarded([&] {
+    if (precision != GBBA_PRECISION_FP64 && precision != GBBA_PRECISION_MIXED)
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "unknown precision");
+    gbba::validate_scene(scene);
+    std::unique_ptr<gbba_evaluator_t> e(new gbba_evaluator_t);
+    e->impl.precision = precision;
+    e->impl.L = gbba::scene_layout(scene);
+    if (precision == GBBA_PRECISION_FP64) e->impl.upload<double>(scene);
+    else e->impl.upload<float>(scene);
+    ev = e.release();
+  });
+  return st == GBBA_OK ? ev : nullptr;
+}
+
+void gbba_evaluator_destroy(gbba_evaluator_t* ev) { delete ev; }
+
+int gbba_evaluator_run(gbba_evaluator_t* ev, void* stream) {
+  return gbba::guarded([&] {
+    if (!ev) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "evaluator is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (ev->impl.precision == GBBA_PRECISION_FP64) ev->impl.run<double>(s);
+    else ev->impl.run<float>(s);
+  });
+}
+
+int gbba_evaluator_prepare(gbba_evaluator_t* ev, void* stream) {
+  return gbba::guarded([&] {
+    if (!ev) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "evaluator is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (ev->impl.precision == GBBA_PRECISION_FP64) ev->impl.prepare<double>(s);
+    else ev->impl.prepare<float>(s);
+  });
+}
+
+int gbba_evaluator_records(gbba_evaluator_t* ev, void* stream) {
+  return gbba::guarded([&] {
+    if (!ev) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "evaluator is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (ev->impl.precision == GBBA_PRECISION_FP64) ev->impl.records<double>(s);
+    else ev->impl.records<float>(s);
+  });
+}
+
+int gbba_evaluator_download(gbba_evaluator_t* ev, gbba_eval_output_t* out) {
+  return gbba::guarded([&] {
+    if (!ev || !out) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "NULL argument");
+    GB_CUDA(cudaDeviceSynchronize());
+    if (ev->impl.precision == GBBA_PRECISION_FP64) ev->impl.download<double>(out);
+    else ev->impl.download<float>(out);
+  });
+}
+
+int gbba_evaluator_launches_per_run(const gbba_evaluator_t* ev) {
+  if (!ev) return 0;
+  const int64_t n = ev->impl.precision == GBBA_PRECISION_FP64 ? ev->impl.d.n_obs : ev->impl.f.n_obs;
+  const int shots = ev->impl.precision == GBBA_PRECISION_FP64 ? ev->impl.d.n_shots : ev->impl.f.n_shots;
+  return (shots > 0 ? 1 : 0) + (n > 0 ? 1 : 0);
+}
+
+int64_t gbba_evaluator_record_bytes(const gbba_evaluator_t* ev) { return ev ? ev->impl.record_bytes() : 0; }
+
+int gbba_evaluate_projections(const gbba_scene_t* scene, int precision, gbba_eval_output_t* out) {
+  return gbba::guarded([&] {
+    if (!out) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "output is NULL");
+    gbba_evaluator_t* ev = gbba_evaluator_create(scene, precision);
+    if (!ev) throw ApiError(gbba::last_status(), gbba_last_error());
+    std::unique_ptr<gbba_evaluator_t, void (*)(gbba_evaluator_t*)> hold(ev, gbba_evaluator_destroy);
+    if (gbba_evaluator_run(ev, nullptr) != GBBA_OK) throw ApiError(gbba::last_status(), gbba_last_error());
+    if (gbba_evaluator_download(ev, out) != GBBA_OK) throw ApiError(gbba::last_status(), gbba_last_error());
+  });
+}
+
+}  // extern "C"
