@@ -52,6 +52,10 @@ def make_workload(name: str, seed_offset: int = 0):
         cfg = {"workload": "aerial nadir BA: 70x72=5040 perspective cameras, 2M terrain points, "
                            "~15M observations, GPS priors, UTM-scale coordinates",
                "n_shots": 5040}
+    elif name == "aerial_small":
+        scene = syn.aerial_scene(seed=3 + seed_offset, n_points=300_000)
+        cfg = {"workload": "aerial nadir BA, profiling size: 5040 cameras, 300k points, ~2.2M observations",
+               "n_shots": 5040}
     elif name == "street":
         scene = syn.street_scene(seed=7 + seed_offset)
         cfg = {"workload": "street BA: 500 Brown cameras (4 models), 200k points, ~1.4M observations, "
@@ -260,13 +264,14 @@ def run_ours(args) -> None:
     o = output_struct(out)
     s = scene.ctypes()
     import ctypes as C
-    _lib.check(L.gbba_evaluate_projections(C.byref(s), _lib.PRECISION_MIXED, C.byref(o)))  # warm
-    e2e_steps = max(1, min(3, args.steps))
+    e2e_steps = 0 if args.no_e2e else max(1, min(3, args.steps))
+    if e2e_steps:
+        _lib.check(L.gbba_evaluate_projections(C.byref(s), _lib.PRECISION_MIXED, C.byref(o)))  # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         _lib.check(L.gbba_evaluate_projections(C.byref(s), _lib.PRECISION_MIXED, C.byref(o)))
-    e2e_dt = (time.perf_counter() - t0) / e2e_steps
+    e2e_dt = (time.perf_counter() - t0) / max(e2e_steps, 1)
     h2d = sum(a.nbytes for a in (scene.camera_projection, scene.camera_values, scene.rig_instance_poses,
                                  scene.shot_rig_instance, scene.shot_camera, scene.shot_rig_camera,
                                  scene.points, scene.obs_shot, scene.obs_point, scene.obs_xy, scene.obs_std))
@@ -286,7 +291,7 @@ def run_ours(args) -> None:
             "config": dict(cfg, precision="mixed: FP64 centring, FP32 records",
                            l2="inputs and records larger than L2 (no flush needed)",
                            parallelism=f"replicas x{world}"),
-            "e2e": {"value": n_obs / e2e_dt / 1e6, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "e2e": {"value": (n_obs / e2e_dt / 1e6) if e2e_steps else None, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h),
                     "path": "gbba_evaluate_projections (host buffers, FP64 blocks out)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
@@ -311,7 +316,8 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="aerial", choices=["aerial", "street", "ring"])
+    ap.add_argument("--workload", default="aerial", choices=["aerial", "aerial_small", "street", "ring"])
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

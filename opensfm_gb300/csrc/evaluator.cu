@@ -68,35 +68,34 @@ struct Layout {
 
 template <typename R>
 struct EvalState {
+  using PS = typename PointStore<R>::type;
   DeviceArray<ShotGeom<R>> geom;
   DeviceArray<RigGeom<R>> rig;
-  DeviceArray<Point4> center;
   DeviceArray<int> shot_cam, cam_model, shot_inst, shot_rig;
   DeviceArray<R> cam_params;
   DeviceArray<double> inst_pose, rig_pose;
   DeviceArray<uint8_t> rig_used;
-  DeviceArray<Point4> points;
-  DeviceArray<int> obs_shot, obs_point;
-  DeviceArray<R> obs_xy, obs_w;
+  DeviceArray<PS> points;
+  DeviceArray<ObsPack<R>> obs;
+  DeviceArray<int> obs_point;
   DeviceArray<typename Vec16<R>::type> records;
   int64_t n_obs = 0;
   int n_shots = 0;
+  int n_cameras = 0;
   int n_planes = 0;
 
   SceneView<R> view() const {
     SceneView<R> v;
     v.n_slots = n_obs;
+    v.n_cameras = n_cameras;
     v.geom = geom.get();
     v.rig = rig.size() ? rig.get() : nullptr;
-    v.center = center.get();
-    v.shot_cam = shot_cam.get();
+
     v.cam_model = cam_model.get();
     v.cam_params = cam_params.get();
     v.points = points.get();
-    v.obs_shot = obs_shot.get();
+    v.obs = obs.get();
     v.obs_point = obs_point.get();
-    v.obs_xy = obs_xy.get();
-    v.obs_w = obs_w.get();
     return v;
   }
 };
@@ -266,22 +265,24 @@ struct EvaluatorImpl {
     }
     e.rig_pose.upload(rp);
     e.rig_used.upload(ru);
-    std::vector<Point4> pts(size_t(s->n_points));
+    using PS = typename PointStore<R>::type;
+    std::vector<PS> pts(size_t(s->n_points));
     for (int64_t i = 0; i < s->n_points; ++i)
-      pts[i] = Point4{s->points[3 * i], s->points[3 * i + 1], s->points[3 * i + 2], 0.0};
+      pts[i] = make_point_store(s->points[3 * i], s->points[3 * i + 1], s->points[3 * i + 2],
+                                static_cast<R*>(nullptr));
     e.points.upload(pts);
-    e.obs_shot.upload(s->obs_shot, size_t(s->n_observations));
     e.obs_point.upload(s->obs_point, size_t(s->n_observations));
-    std::vector<R> xy(size_t(s->n_observations) * 2), w(size_t(s->n_observations));
+    std::vector<ObsPack<R>> ob(size_t(s->n_observations));
     for (int64_t i = 0; i < s->n_observations; ++i) {
-      xy[2 * i] = R(s->obs_xy[2 * i]);
-      xy[2 * i + 1] = R(s->obs_xy[2 * i + 1]);
-      w[i] = R(1.0 / s->obs_std[i]);
+      ob[i].x = R(s->obs_xy[2 * i]);
+      ob[i].y = R(s->obs_xy[2 * i + 1]);
+      ob[i].w = R(1.0 / s->obs_std[i]);
+      ob[i].shot = s->obs_shot[i];
     }
-    e.obs_xy.upload(xy);
-    e.obs_w.upload(w);
+    e.obs.upload(ob);
+    e.n_cameras = s->n_cameras;
     e.geom.resize(std::max(1, s->n_shots));
-    e.center.resize(std::max(1, s->n_shots));
+
     if (L.rig) e.rig.resize(std::max(1, s->n_shots));
     e.n_planes = planes_of<R>(layout_width(L));
     e.records.resize(size_t(e.n_planes) * std::max<int64_t>(1, e.n_obs));
@@ -299,8 +300,8 @@ struct EvaluatorImpl {
     EvalState<R>& e = st<R>();
     if (e.n_shots > 0) {
       shot_prep_kernel<R><<<(e.n_shots + 127) / 128, 128, 0, stream>>>(
-          e.n_shots, e.shot_inst.get(), e.shot_rig.get(), e.inst_pose.get(), e.rig_pose.get(),
-          e.rig_used.get(), e.geom.get(), e.center.get(), L.rig ? e.rig.get() : nullptr);
+          e.n_shots, e.shot_inst.get(), e.shot_rig.get(), e.shot_cam.get(), e.inst_pose.get(), e.rig_pose.get(),
+          e.rig_used.get(), e.geom.get(), L.rig ? e.rig.get() : nullptr);
       GB_CUDA(cudaGetLastError());
     }
   }

@@ -5,14 +5,24 @@
 // (opensfm/src/lib/bundle/data/pose.h:17,34-43).  A world point X is mapped
 // to the camera frame as R(-r_rc) (R(-r_inst) (X - c_inst) - c_rc)
 // (bundle/error/error_utils.h:449-461, geometry/transformations_functions.h:
-// 221-258).  The rotation and its derivative with respect to the angle-axis
-// parameters are computed once per shot in FP64 (the reference recomputes
-// them for every observation, transformations_functions.h:260-327); the
-// observation kernels only contract them with X - c_inst.
+// 221-258).
 //
-// Mixed precision: X - c_inst is formed in FP64 (georeferenced coordinates,
-// e.g. UTM with x ~ 5e5 m) and only the camera-centred difference is cast to
-// the working type R, so FP32 never sees the large offsets.
+// Rotation derivative.  The reference differentiates R(-r) with dual
+// numbers for every observation (transformations_functions.h:260-327).
+// Here each shot stores R and the SO(3) right Jacobian J_r of phi = -r, and
+// an observation uses
+//     d(R v)/d r = R [v]x J_r(phi),
+// so a residual row with point-Jacobian row j = a R becomes (j x v)^T J_r:
+// 18 values per shot instead of a 27-entry derivative tensor, and 15 FMAs per
+// row.  (J_r(phi) = I - (1 - cos t)/t^2 [phi]x + (t - sin t)/t^3 [phi]x^2,
+// t = |phi|.)
+//
+// Camera-centred coordinates.  In FP64 mode points and centres are FP64.
+// In mixed mode they are stored as double-float pairs (hi = float(x),
+// lo = float(x - hi)); v = (X_hi - c_hi) + (X_lo - c_lo) is then accurate
+// to FP32 relative precision of v itself even at UTM offsets (x ~ 5e5,
+// y ~ 4e6 m), with no FP64 instruction per observation (FP64 runs at a small
+// fraction of the FP32 rate on this GPU).
 #pragma once
 
 #include <cstdint>
@@ -21,112 +31,134 @@
 
 namespace gbba {
 
-// FP64 3-vector padded to 32 bytes (world points, shot centres).
+// FP64 3-vector padded to 32 bytes.
 struct alignas(32) Point4 {
   double x, y, z, w;
 };
-#ifdef __CUDACC__
-__device__ __forceinline__ Point4 ldg_point4(const Point4* p) {
-  const double2* q = reinterpret_cast<const double2*>(p);
-  const double2 a = __ldg(q), b = __ldg(q + 1);
-  return {a.x, a.y, b.x, b.y};
+// Double-float 3-vector: hi = float(x), lo = float(x - hi).
+struct alignas(32) PointF2 {
+  float hx, hy, hz, pad0, lx, ly, lz, pad1;
+};
+
+template <typename R> struct PointStore;
+template <> struct PointStore<double> { using type = Point4; };
+template <> struct PointStore<float> { using type = PointF2; };
+
+GB_HD Point4 make_point_store(double x, double y, double z, double*) { return {x, y, z, 0.0}; }
+GB_HD PointF2 make_point_store(double x, double y, double z, float*) {
+  const float hx = float(x), hy = float(y), hz = float(z);
+  return {hx, hy, hz, 0.0f, float(x - double(hx)), float(y - double(hy)), float(z - double(hz)), 0.0f};
 }
-#endif
 
 // ---------------------------------------------------------------------------
-// Per-shot geometry in the working precision R.
-//   rot[9]    world -> camera rotation R_rc * R_inst (row-major)
-//   drot[27]  d(rot)/d(r_inst) as drot[(m*3 + j)*3 + k] = d rot[m][j] / d r_inst[k]
-//   tc[3]     camera-frame offset -R_rc * c_rc (zero without rig camera)
+// Per-shot geometry in the working precision R (128 B in FP32):
+//   rot[9]  world -> camera rotation R_rc * R_inst (row-major)
+//   jr[9]   right Jacobian J_r(-r_inst) (row-major)
+//   tc[3]   camera-frame offset -R_rc * c_rc (zero without rig camera)
+//   cam     camera index of the shot (exact small integer)
+//   chi[3], clo[3]  rig instance centre (double-float in FP32; lo = 0 in FP64)
 template <typename R>
 struct alignas(16) ShotGeom {
   R rot[9];
-  R drot[27];
+  R jr[9];
   R tc[3];
-  R pad;
+  R cam;
+  R chi[3];
+  R clo[3];
+  R pad[sizeof(R) == 4 ? 4 : 2];
 };
 
-// Extra per-shot data used only when rig cameras are optimised.
-//   rinst[9]  R_inst;  rrc[9] R_rc;  drrc[27] d(R_rc)/d(r_rc);  crc[3]
+#ifdef __CUDACC__
+// v = X - c_inst in the working precision.
+__device__ __forceinline__ void centred(const Point4* X, const ShotGeom<double>& g, double* v) {
+  const double2* a = reinterpret_cast<const double2*>(X);
+  const double2 a0 = __ldg(a), a1 = __ldg(a + 1);
+  v[0] = a0.x - g.chi[0];
+  v[1] = a0.y - g.chi[1];
+  v[2] = a1.x - g.chi[2];
+}
+__device__ __forceinline__ void centred(const PointF2* X, const ShotGeom<float>& g, float* v) {
+  const float4* a = reinterpret_cast<const float4*>(X);
+  const float4 ah = __ldg(a), al = __ldg(a + 1);
+  v[0] = (ah.x - g.chi[0]) + (al.x - g.clo[0]);
+  v[1] = (ah.y - g.chi[1]) + (al.y - g.clo[1]);
+  v[2] = (ah.z - g.chi[2]) + (al.z - g.clo[2]);
+}
+#endif
+
+// Extra per-shot data used only when rig cameras are optimised:
+//   rinst[9] R_inst; rrc[9] R_rc; jrc[9] J_r(-r_rc); crc[3] rig camera centre.
 template <typename R>
 struct alignas(16) RigGeom {
   R rinst[9];
   R rrc[9];
-  R drrc[27];
+  R jrc[9];
   R crc[3];
+  R pad[2];
 };
 
-// Forward-mode dual number with three derivative slots (FP64), used for the
-// derivative of the Rodrigues rotation with respect to its angle-axis.
-struct D3 {
-  double v, d0, d1, d2;
-};
-GB_HD D3 d3(double v) { return {v, 0.0, 0.0, 0.0}; }
-GB_HD D3 operator+(D3 a, D3 b) { return {a.v + b.v, a.d0 + b.d0, a.d1 + b.d1, a.d2 + b.d2}; }
-GB_HD D3 operator-(D3 a, D3 b) { return {a.v - b.v, a.d0 - b.d0, a.d1 - b.d1, a.d2 - b.d2}; }
-GB_HD D3 operator*(D3 a, D3 b) {
-  return {a.v * b.v, a.d0 * b.v + a.v * b.d0, a.d1 * b.v + a.v * b.d1, a.d2 * b.v + a.v * b.d2};
+#ifdef __CUDACC__
+template <typename T>
+__device__ __forceinline__ void ldg_copy(const T* src, T& dst) {
+  static_assert(sizeof(T) % 16 == 0, "vector copy needs 16-byte multiples");
+  const float4* s = reinterpret_cast<const float4*>(src);
+  float4* d = reinterpret_cast<float4*>(&dst);
+#pragma unroll
+  for (int i = 0; i < int(sizeof(T) / 16); ++i) d[i] = __ldg(s + i);
 }
-GB_HD D3 operator*(double s, D3 a) { return {s * a.v, s * a.d0, s * a.d1, s * a.d2}; }
-GB_HD D3 d3_inv(D3 a) {
-  const double iv = 1.0 / a.v, k = -iv * iv;
-  return {iv, k * a.d0, k * a.d1, k * a.d2};
-}
-GB_HD D3 d3_sqrt(D3 a) {
-  const double s = sqrt(a.v), k = 0.5 / s;
-  return {s, k * a.d0, k * a.d1, k * a.d2};
-}
-GB_HD D3 d3_sin(D3 a) {
-  const double c = cos(a.v);
-  return {sin(a.v), c * a.d0, c * a.d1, c * a.d2};
-}
-GB_HD D3 d3_cos(D3 a) {
-  const double s = -sin(a.v);
-  return {cos(a.v), s * a.d0, s * a.d1, s * a.d2};
-}
+#endif
 
 // Rodrigues rotation of angle-axis w (row-major) with the first-order branch
 // I + [w]x below machine epsilon (transformations_functions.h:330-376).
-GB_HD void rodrigues_d3(const D3* w, D3* Rm) {
-  const D3 th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
-  if (th2.v < 2.220446049250313e-16) {
-    const D3 one = d3(1.0), mz = d3(0.0) - w[2], my = d3(0.0) - w[1], mx = d3(0.0) - w[0];
-    Rm[0] = one; Rm[1] = mz; Rm[2] = w[1];
-    Rm[3] = w[2]; Rm[4] = one; Rm[5] = mx;
-    Rm[6] = my; Rm[7] = w[0]; Rm[8] = one;
+GB_HD void rodrigues(const double* w, double* Rm) {
+  const double th2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2];
+  if (th2 < 2.220446049250313e-16) {
+    Rm[0] = 1.0; Rm[1] = -w[2]; Rm[2] = w[1];
+    Rm[3] = w[2]; Rm[4] = 1.0; Rm[5] = -w[0];
+    Rm[6] = -w[1]; Rm[7] = w[0]; Rm[8] = 1.0;
     return;
   }
-  const D3 th = d3_sqrt(th2);
-  const D3 c = d3_cos(th), s = d3_sin(th), t = d3(1.0) - c;
-  const D3 it2 = d3_inv(th2), it = d3_inv(th);
-  const D3 xx = w[0] * w[0] * it2, xy = w[0] * w[1] * it2, xz = w[0] * w[2] * it2;
-  const D3 yy = w[1] * w[1] * it2, yz = w[1] * w[2] * it2, zz = w[2] * w[2] * it2;
-  const D3 xs = w[0] * it * s, ys = w[1] * it * s, zs = w[2] * it * s;
+  const double th = sqrt(th2);
+  const double c = cos(th), s = sin(th), t = 1.0 - c;
+  const double it2 = 1.0 / th2, it = 1.0 / th;
+  const double xx = w[0] * w[0] * it2, xy = w[0] * w[1] * it2, xz = w[0] * w[2] * it2;
+  const double yy = w[1] * w[1] * it2, yz = w[1] * w[2] * it2, zz = w[2] * w[2] * it2;
+  const double xs = w[0] * it * s, ys = w[1] * it * s, zs = w[2] * it * s;
   Rm[0] = t * xx + c; Rm[1] = t * xy - zs; Rm[2] = t * xz + ys;
   Rm[3] = t * xy + zs; Rm[4] = t * yy + c; Rm[5] = t * yz - xs;
   Rm[6] = t * xz - ys; Rm[7] = t * yz + xs; Rm[8] = t * zz + c;
 }
 
-// R(-r) and d R(-r) / d r for a camera-to-world angle-axis r: the dual
-// seeds are -e_k, as PoseFunctor::ForwardDerivatives seeds them.
-GB_HD void pose_rotation(const double* r, double* Rm, double* dR /*27*/) {
-  D3 w[3];
-  w[0] = {-r[0], -1.0, 0.0, 0.0};
-  w[1] = {-r[1], 0.0, -1.0, 0.0};
-  w[2] = {-r[2], 0.0, 0.0, -1.0};
-  D3 M[9];
-  rodrigues_d3(w, M);
-  for (int i = 0; i < 9; ++i) {
-    Rm[i] = M[i].v;
-    dR[i * 3 + 0] = M[i].d0;
-    dR[i * 3 + 1] = M[i].d1;
-    dR[i * 3 + 2] = M[i].d2;
+// Right Jacobian of SO(3) at phi (row-major), with its Taylor expansion
+// near zero.
+GB_HD void right_jacobian(const double* phi, double* J) {
+  const double th2 = phi[0] * phi[0] + phi[1] * phi[1] + phi[2] * phi[2];
+  double a, b;
+  if (th2 < 1e-8) {
+    a = 0.5 - th2 / 24.0;
+    b = 1.0 / 6.0 - th2 / 120.0;
+  } else {
+    const double th = sqrt(th2);
+    a = (1.0 - cos(th)) / th2;
+    b = (th - sin(th)) / (th2 * th);
   }
+  const double K[9] = {0.0, -phi[2], phi[1], phi[2], 0.0, -phi[0], -phi[1], phi[0], 0.0};
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double k2 = 0.0;
+      for (int m = 0; m < 3; ++m) k2 += K[i * 3 + m] * K[m * 3 + j];
+      J[i * 3 + j] = (i == j ? 1.0 : 0.0) - a * K[i * 3 + j] + b * k2;
+    }
+}
+
+// R(-r) and J_r(-r) for a camera-to-world angle-axis r.
+GB_HD void pose_rotation(const double* r, double* Rm, double* Jr) {
+  const double phi[3] = {-r[0], -r[1], -r[2]};
+  rodrigues(phi, Rm);
+  right_jacobian(phi, Jr);
 }
 
 // ---------------------------------------------------------------------------
-// Per-observation residual and Jacobian in registers.
-//
 // Record layout (row-major blocks, NR residual rows):
 //   [ r (NR) | J_point (NR x 3) | J_instance (NR x 6: rx ry rz tx ty tz)
 //     | J_camera (NR x CMAX) | J_rig (NR x 6, only when RIG) ]
@@ -140,12 +172,10 @@ struct RecordLayout {
   static constexpr int kCam = kInst + 6 * NR;
   static constexpr int kRig = kCam + CMAX * NR;
   static constexpr int kWidth = kRig + (RIG ? 6 * NR : 0);
-  static constexpr int kPlanes4 = (kWidth + 3) / 4;  // float4 planes
-  static constexpr int kPlanes2 = (kWidth + 1) / 2;  // double2 planes
 };
 
-// Projection of a camera-frame point for a runtime model id (used by the
-// mixed-model kernels) or a compile-time model M >= 0.
+// Projection of a camera-frame point for a runtime model id (mixed-model
+// kernels) or a compile-time model M >= 0.
 template <int M, int CMAX, typename R>
 __device__ __forceinline__ void project_dispatch(int model, const R* p, const R* prm, R* uv,
                                                  R* Jp, R* Jc) {
@@ -188,14 +218,13 @@ __device__ __forceinline__ void project_dispatch(int model, const R* p, const R*
   }
 }
 
-// Inputs of one observation evaluation.
+// Inputs of one observation evaluation (all in registers).
 template <typename R>
 struct ObsInputs {
-  R ox, oy;      // observed normalized coordinates (or bearing angles)
-  R w;           // 1 / std_deviation
-  double X[3];   // world point (FP64)
-  double c[3];   // rig instance centre (FP64)
-  const ShotGeom<R>* g;
+  R ox, oy;     // observed normalized coordinates (or bearing angles / 2pi)
+  R w;          // 1 / std_deviation
+  R v[3];       // camera-centred world point X - c_inst
+  ShotGeom<R> g;
   const RigGeom<R>* rg;  // only read when RIG
   const R* cam;          // camera parameters
   int model;
@@ -208,11 +237,8 @@ struct ObsInputs {
 template <typename R, int M, int NR, int CMAX, bool RIG, bool JAC>
 __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec) {
   using L = RecordLayout<NR, CMAX, RIG>;
-  // camera-centred point: FP64 subtraction, then cast
-  const R v0 = R(in.X[0] - in.c[0]);
-  const R v1 = R(in.X[1] - in.c[1]);
-  const R v2 = R(in.X[2] - in.c[2]);
-  const ShotGeom<R>& g = *in.g;
+  const R v0 = in.v[0], v1 = in.v[1], v2 = in.v[2];
+  const ShotGeom<R>& g = in.g;
   R p[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) p[i] = g.rot[i * 3 + 0] * v0 + g.rot[i * 3 + 1] * v1 + g.rot[i * 3 + 2] * v2 + g.tc[i];
@@ -255,42 +281,39 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
   }
   if (!JAC) return;
 
-  // E[m][k] = sum_j drot[m][j][k] v_j  (3x3): derivative of p wrt r_inst
-  R E[9];
-#pragma unroll
-  for (int m = 0; m < 3; ++m)
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-      E[m * 3 + k] = g.drot[(m * 3 + 0) * 3 + k] * v0 + g.drot[(m * 3 + 1) * 3 + k] * v1 +
-                     g.drot[(m * 3 + 2) * 3 + k] * v2;
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     const R a0 = in.w * Jq[i * 3 + 0], a1 = in.w * Jq[i * 3 + 1], a2 = in.w * Jq[i * 3 + 2];
+    R jp[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-      const R jp = a0 * g.rot[0 * 3 + j] + a1 * g.rot[1 * 3 + j] + a2 * g.rot[2 * 3 + j];
-      rec[L::kPt + i * 3 + j] = jp;
-      rec[L::kInst + i * 6 + 3 + j] = -jp;  // d/d(centre) = -d/dX
-      rec[L::kInst + i * 6 + j] = a0 * E[0 * 3 + j] + a1 * E[1 * 3 + j] + a2 * E[2 * 3 + j];
+      jp[j] = a0 * g.rot[0 * 3 + j] + a1 * g.rot[1 * 3 + j] + a2 * g.rot[2 * 3 + j];
+      rec[L::kPt + i * 3 + j] = jp[j];
+      rec[L::kInst + i * 6 + 3 + j] = -jp[j];  // d/d(centre) = -d/dX
     }
+    // rotation: (jp x v)^T J_r
+    const R c0 = jp[1] * v2 - jp[2] * v1;
+    const R c1 = jp[2] * v0 - jp[0] * v2;
+    const R c2 = jp[0] * v1 - jp[1] * v0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) rec[L::kInst + i * 6 + k] = c0 * g.jr[0 * 3 + k] + c1 * g.jr[1 * 3 + k] + c2 * g.jr[2 * 3 + k];
     if constexpr (RIG) {
-      // d p / d r_rc = dR_rc (R_inst v - c_rc); d p / d c_rc = -R_rc
+      // p = R_rc (y - c_rc), y = R_inst v:  d p / d r_rc = R_rc [y - c_rc]x J_rc,
+      // d p / d c_rc = -R_rc
       const RigGeom<R>& rg = *in.rg;
-      R y[3];
+      R e[3], q[3];
 #pragma unroll
       for (int k = 0; k < 3; ++k)
-        y[k] = rg.rinst[k * 3 + 0] * v0 + rg.rinst[k * 3 + 1] * v1 + rg.rinst[k * 3 + 2] * v2 - rg.crc[k];
+        e[k] = rg.rinst[k * 3 + 0] * v0 + rg.rinst[k * 3 + 1] * v1 + rg.rinst[k * 3 + 2] * v2 - rg.crc[k];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) q[k] = a0 * rg.rrc[0 * 3 + k] + a1 * rg.rrc[1 * 3 + k] + a2 * rg.rrc[2 * 3 + k];
+      const R d0 = q[1] * e[2] - q[2] * e[1];
+      const R d1 = q[2] * e[0] - q[0] * e[2];
+      const R d2 = q[0] * e[1] - q[1] * e[0];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        R s = R(0);
-#pragma unroll
-        for (int m = 0; m < 3; ++m) {
-          const R e = rg.drrc[(m * 3 + 0) * 3 + k] * y[0] + rg.drrc[(m * 3 + 1) * 3 + k] * y[1] +
-                      rg.drrc[(m * 3 + 2) * 3 + k] * y[2];
-          s += (m == 0 ? a0 : (m == 1 ? a1 : a2)) * e;
-        }
-        rec[L::kRig + i * 6 + k] = s;
-        rec[L::kRig + i * 6 + 3 + k] = -(a0 * rg.rrc[0 * 3 + k] + a1 * rg.rrc[1 * 3 + k] + a2 * rg.rrc[2 * 3 + k]);
+        rec[L::kRig + i * 6 + k] = d0 * rg.jrc[0 * 3 + k] + d1 * rg.jrc[1 * 3 + k] + d2 * rg.jrc[2 * 3 + k];
+        rec[L::kRig + i * 6 + 3 + k] = -q[k];
       }
     }
   }
