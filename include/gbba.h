@@ -132,6 +132,132 @@ int gbba_evaluator_launches_per_run(const gbba_evaluator_t* ev);
 /* Bytes of the device-side residual+Jacobian records of one run. */
 int64_t gbba_evaluator_record_bytes(const gbba_evaluator_t* ev);
 
+/* ------------------------------------------------------------------------
+ * Bundle adjuster: bundle::BundleAdjuster (bundle_adjuster.h:173-386) and
+ * the methods its pybind module binds (python/pybind.cc:60-147).  Ids are
+ * NUL-terminated strings.  Unknown ids raise GBBA_ERR_RUNTIME (the
+ * reference's std::runtime_error) except in
+ * gbba_add_point_projection_observation, where an unknown shot or point is
+ * GBBA_ERR_OUT_OF_RANGE (std::map::at, bundle_adjuster.cc:279-281).
+ */
+typedef struct gbba_adjuster gbba_adjuster_t;
+
+/* BundleAdjuster::BundleAdjuster (bundle_adjuster.cc:56-75). */
+gbba_adjuster_t* gbba_create(void);
+void gbba_destroy(gbba_adjuster_t* h);
+
+/* AddCamera (bundle_adjuster.cc:107-129): values and prior_values hold the
+ * geometry::Camera parameter vectors; constant fixes every parameter. */
+int gbba_add_camera(gbba_adjuster_t* h, const char* id, int projection, const double* values,
+                    const double* prior_values, int n_values, int constant);
+/* SetCameraBias (bundle_adjuster.cc:131-140): similarity applied to the GPS
+ * priors of instances whose reference camera is camera_id (held fixed). */
+int gbba_set_camera_bias(gbba_adjuster_t* h, const char* camera_id, const double* rotation,
+                         const double* translation, double scale);
+/* AddRigCamera (bundle_adjuster.cc:179-198). */
+int gbba_add_rig_camera(gbba_adjuster_t* h, const char* id, const double* pose, const double* pose_prior,
+                        int fixed);
+/* AddRigInstance (bundle_adjuster.cc:142-177): creates one shot per entry
+ * of (shot_ids, camera_ids, rig_camera_ids). */
+int gbba_add_rig_instance(gbba_adjuster_t* h, const char* id, const double* pose, int n_shots,
+                          const char* const* shot_ids, const char* const* camera_ids,
+                          const char* const* rig_camera_ids, int fixed);
+/* AddRigInstancePositionPrior (bundle_adjuster.cc:200-217). */
+int gbba_add_rig_instance_position_prior(gbba_adjuster_t* h, const char* id, const double* position,
+                                         const double* std_dev, const char* scale_group);
+/* AddPoint (bundle_adjuster.cc:246-258). */
+int gbba_add_point(gbba_adjuster_t* h, const char* id, const double* position, int constant);
+/* AddPointPrior (bundle_adjuster.cc:260-272). */
+int gbba_add_point_prior(gbba_adjuster_t* h, const char* id, const double* position, const double* std_dev,
+                         int has_altitude);
+/* AddPointProjectionObservation (bundle_adjuster.cc:274-287). */
+int gbba_add_point_projection_observation(gbba_adjuster_t* h, const char* shot, const char* point,
+                                          const double* observation, double std_dev, int is_gcp);
+
+/* Index-based bulk interface, the counterpart of GetShotRaw / GetPointRaw /
+ * AddPointProjectionObservationRaw (bundle_adjuster.cc:289-301, 1336-1338,
+ * 1377-1379) used by sfm::BAHelpers.  Indices are assigned in insertion
+ * order; -1 when the id is unknown. */
+int64_t gbba_shot_index(const gbba_adjuster_t* h, const char* shot);
+int64_t gbba_point_index(const gbba_adjuster_t* h, const char* point);
+/* Adds n points; ids may be NULL (ids are then the decimal point indices). */
+int gbba_add_points_bulk(gbba_adjuster_t* h, int64_t n, const double* xyz, const uint8_t* constant,
+                         const char* const* ids, int64_t* first_index);
+int gbba_add_point_projection_observations_bulk(gbba_adjuster_t* h, int64_t n, const int32_t* shot_index,
+                                                const int32_t* point_index, const double* xy,
+                                                const double* std_dev, const uint8_t* is_gcp);
+
+/* Settings (bundle_adjuster.cc:400-483).  The point-projection loss
+ * (pybundle.pyi:131) takes the names of CreateLossFunction
+ * (bundle_adjuster.cc:485-499). */
+int gbba_set_point_projection_loss_function(gbba_adjuster_t* h, const char* name, double threshold);
+/* IRLS reweighting of projection residuals: 1 mixture (the reference's
+ * behaviour, default), 0 none (fixed objective with the robust loss). */
+int gbba_set_irls_mode(gbba_adjuster_t* h, int mode);
+/* GBBA_PRECISION_MIXED (default) or GBBA_PRECISION_FP64. */
+int gbba_set_precision(gbba_adjuster_t* h, int precision);
+int gbba_set_max_num_iterations(gbba_adjuster_t* h, int n);
+int gbba_set_num_threads(gbba_adjuster_t* h, int n);
+int gbba_set_use_analytic_derivatives(gbba_adjuster_t* h, int use);
+int gbba_set_linear_solver_type(gbba_adjuster_t* h, const char* type);
+int gbba_set_internal_parameters_prior_sd(gbba_adjuster_t* h, double focal_sd, double aspect_ratio_sd, double c_sd,
+                                          double k1_sd, double k2_sd, double p1_sd, double p2_sd, double k3_sd,
+                                          double k4_sd);
+int gbba_set_rig_parameters_prior_sd(gbba_adjuster_t* h, double translation_sd, double rotation_sd);
+int gbba_set_compute_reprojection_errors(gbba_adjuster_t* h, int v);
+int gbba_set_compute_covariances(gbba_adjuster_t* h, int v);
+int gbba_get_covariance_estimation_valid(const gbba_adjuster_t* h);
+int gbba_set_skip_initial_reweighting(gbba_adjuster_t* h, int v);
+int gbba_set_default_density_ratio(gbba_adjuster_t* h, double ratio);
+double gbba_get_default_density_ratio(const gbba_adjuster_t* h);
+int gbba_set_group_density_ratio(gbba_adjuster_t* h, const char* group, double ratio);
+double gbba_get_group_density_ratio(const gbba_adjuster_t* h, const char* group);
+/* Relative residual at which the reduced-camera-system PCG stops. */
+int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance);
+
+/* BundleAdjuster::Run (bundle_adjuster.cc:670-1203). */
+int gbba_run(gbba_adjuster_t* h);
+
+/* Getters (bundle_adjuster.cc:1303-1399). */
+int gbba_get_camera(const gbba_adjuster_t* h, const char* id, int* projection, double* values, int capacity,
+                    int* n_values);
+int gbba_get_rig_instance_pose(const gbba_adjuster_t* h, const char* id, double* pose);
+int gbba_get_rig_camera_pose(const gbba_adjuster_t* h, const char* id, double* pose);
+int gbba_get_point(const gbba_adjuster_t* h, const char* id, double* position);
+int gbba_has_point(const gbba_adjuster_t* h, const char* id);
+int64_t gbba_num_projections(const gbba_adjuster_t* h);
+int64_t gbba_num_points(const gbba_adjuster_t* h);
+int gbba_get_points_bulk(const gbba_adjuster_t* h, int64_t first, int64_t n, double* xyz);
+/* Per observation (insertion order): unscaled residual (std = 1) padded to
+ * 3 values, IRLS weight, residual dimension (ComputeReprojectionErrors and
+ * RetrieveProjectionWeights, bundle_adjuster.cc:1205-1216, 1289-1301). */
+int gbba_get_projection_results(const gbba_adjuster_t* h, int64_t n, double* errors, double* weights,
+                                int32_t* dims);
+/* Reports; return the full length of the text (written up to len - 1
+ * bytes, NUL-terminated), -1 on error. */
+int gbba_brief_report(const gbba_adjuster_t* h, char* buf, size_t len);
+int gbba_full_report(const gbba_adjuster_t* h, char* buf, size_t len);
+int gbba_irls_report(const gbba_adjuster_t* h, char* buf, size_t len);
+
+typedef struct gbba_summary {
+  double initial_cost;
+  double final_cost;
+  double seconds;
+  double linear_solver_seconds;
+  double jacobian_seconds;
+  double residual_seconds;
+  int iterations;
+  int successful_steps;
+  int unsuccessful_steps;
+  int usable;
+  int64_t kernel_launches;
+} gbba_summary_t;
+int gbba_get_summary(const gbba_adjuster_t* h, gbba_summary_t* out);
+/* Iteration trace of the last run: records of 8 doubles
+ * [iteration, cost, seconds since start, success, linear iterations,
+ *  trust-region radius, relative decrease, step norm]. */
+int gbba_get_trace(const gbba_adjuster_t* h, int capacity, double* records, int* n);
+
 #ifdef __cplusplus
 }
 #endif

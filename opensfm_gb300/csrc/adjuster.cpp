@@ -1,0 +1,413 @@
+#include "adjuster.h"
+
+#include <cmath>
+#include <cstdio>
+#include <sstream>
+#include <stdexcept>
+
+#include "camera_models.cuh"
+#include "solver.h"
+
+namespace gbba {
+
+std::vector<int> camera_parameter_types(int model) {
+  switch (model) {
+    case kPerspective: return {kParamK1, kParamK2, kParamFocal};
+    case kBrown:
+      return {kParamK1, kParamK2, kParamK3, kParamP1, kParamP2, kParamFocal, kParamAspectRatio, kParamCx, kParamCy};
+    case kFisheye: return {kParamK1, kParamK2, kParamFocal};
+    case kFisheyeOpencv:
+      return {kParamK1, kParamK2, kParamK3, kParamK4, kParamFocal, kParamAspectRatio, kParamCx, kParamCy};
+    case kFisheye62:
+      return {kParamK1, kParamK2, kParamK3, kParamK4, kParamK5, kParamK6, kParamP1, kParamP2,
+              kParamFocal, kParamAspectRatio, kParamCx, kParamCy};
+    case kFisheye624:
+      return {kParamK1, kParamK2, kParamK3, kParamK4, kParamK5, kParamK6, kParamP1, kParamP2,
+              kParamS0, kParamS1, kParamS2, kParamS3, kParamFocal, kParamAspectRatio, kParamCx, kParamCy};
+    case kSpherical: return {kParamNone};
+    case kDual: return {kParamTransition, kParamK1, kParamK2, kParamFocal};
+    case kRadial: return {kParamK1, kParamK2, kParamFocal, kParamAspectRatio, kParamCx, kParamCy};
+    case kSimpleRadial: return {kParamK1, kParamFocal, kParamAspectRatio, kParamCx, kParamCy};
+  }
+  throw std::runtime_error("Invalid ProjectionType");
+}
+
+BundleAdjuster::BundleAdjuster() {
+  // bundle_adjuster.cc:56-75
+  opts_.max_iterations = 500;
+  opts_.linear_solver = "SPARSE_SCHUR";
+  opts_.loss = kLossTrivial;
+  opts_.irls = kIrlsMixture;
+  opts_.default_density_ratio = 0.001;
+}
+
+// Prior standard deviations of a camera (GetDefaultCameraSigma,
+// bundle_adjuster.cc:77-98): parameters without a configured deviation get 0,
+// which the prior turns into a weight of 1/epsilon.
+void BundleAdjuster::camera_sigma(CameraBlock& c) const {
+  const std::vector<int> types = camera_parameter_types(c.model);
+  for (int k = 0; k < c.n; ++k) {
+    double sd = 0.0;
+    switch (types[k]) {
+      case kParamFocal: sd = focal_sd_; break;
+      case kParamAspectRatio: sd = aspect_sd_; break;
+      case kParamCx:
+      case kParamCy: sd = c_sd_; break;
+      case kParamK1: sd = k1_sd_; break;
+      case kParamK2: sd = k2_sd_; break;
+      case kParamK3: sd = k3_sd_; break;
+      case kParamP1: sd = p1_sd_; break;
+      case kParamP2: sd = p2_sd_; break;
+      case kParamTransition: sd = 1.0; break;
+      default: sd = 0.0;
+    }
+    c.sigma[k] = sd;
+    c.log_prior[k] = (types[k] == kParamFocal || types[k] == kParamAspectRatio) ? 1 : 0;
+  }
+}
+
+void BundleAdjuster::AddCamera(const std::string& id, int model, const double* values, const double* prior, int n,
+                               bool constant) {
+  if (model < 0 || model >= kNumProjections) throw std::runtime_error("Invalid ProjectionType");
+  if (n != model_num_params(model))
+    throw std::invalid_argument("camera " + id + ": expected " + std::to_string(model_num_params(model)) +
+                                " parameters, got " + std::to_string(n));
+  if (camera_index_.count(id)) return;  // std::map::emplace keeps the first
+  CameraBlock c;
+  c.model = model;
+  c.n = n;
+  for (int k = 0; k < n; ++k) {
+    c.value[k] = values[k];
+    c.prior[k] = prior[k];
+    c.free_mask[k] = constant ? 0 : 1;
+  }
+  camera_index_[id] = int(problem_.cameras.size());
+  problem_.cameras.push_back(c);
+  problem_.biases.push_back(Bias{});
+}
+
+void BundleAdjuster::SetCameraBias(const std::string& camera, const double* rotation, const double* translation,
+                                   double scale) {
+  auto it = camera_index_.find(camera);
+  if (it == camera_index_.end()) throw std::runtime_error("Camera " + camera + " doesn't exist.");
+  Bias& b = problem_.biases[it->second];
+  for (int k = 0; k < 3; ++k) {
+    b.r[k] = rotation[k];
+    b.t[k] = translation[k];
+  }
+  b.s = scale;
+}
+
+void BundleAdjuster::AddRigCamera(const std::string& id, const double* pose, const double* prior, bool fixed) {
+  if (rig_camera_index_.count(id)) throw std::runtime_error("Rig model " + id + " already exist.");
+  PoseBlock b;
+  for (int k = 0; k < 6; ++k) {
+    b.value[k] = pose[k];
+    b.prior[k] = prior[k];
+    b.free_mask[k] = fixed ? 0 : 1;
+  }
+  b.has_prior = true;
+  rig_camera_index_[id] = int(problem_.rig_cameras.size());
+  problem_.rig_cameras.push_back(b);
+}
+
+void BundleAdjuster::AddRigInstance(const std::string& id, const double* pose, const std::vector<std::string>& shots,
+                                    const std::vector<std::string>& cameras,
+                                    const std::vector<std::string>& rig_cameras, bool fixed) {
+  int inst;
+  auto it = instance_index_.find(id);
+  if (it == instance_index_.end()) {
+    PoseBlock b;
+    for (int k = 0; k < 6; ++k) {
+      b.value[k] = pose[k];
+      b.free_mask[k] = fixed ? 0 : 1;
+    }
+    inst = int(problem_.instances.size());
+    instance_index_[id] = inst;
+    problem_.instances.push_back(b);
+  } else {
+    inst = it->second;
+  }
+  for (size_t i = 0; i < shots.size(); ++i) {
+    auto c = camera_index_.find(cameras[i]);
+    if (c == camera_index_.end()) throw std::runtime_error("Camera " + cameras[i] + " doesn't exist.");
+    auto r = rig_camera_index_.find(rig_cameras[i]);
+    if (r == rig_camera_index_.end()) throw std::runtime_error("Rig camera " + rig_cameras[i] + " doesn't exist.");
+    if (shot_index_.count(shots[i])) continue;
+    Shot s;
+    s.instance = inst;
+    s.camera = c->second;
+    s.rig_camera = r->second;
+    shot_index_[shots[i]] = int(problem_.shots.size());
+    shot_ids_.push_back(shots[i]);
+    problem_.shots.push_back(s);
+    if (problem_.instances[inst].bias_camera < 0) problem_.instances[inst].bias_camera = c->second;
+  }
+}
+
+void BundleAdjuster::AddRigInstancePositionPrior(const std::string& id, const double* position,
+                                                 const double* std_dev, const std::string& scale_group) {
+  auto it = instance_index_.find(id);
+  if (it == instance_index_.end()) throw std::runtime_error("Rig instance " + id + " doesn't exist.");
+  PoseBlock& b = problem_.instances[it->second];
+  b.has_position_prior = true;
+  for (int k = 0; k < 3; ++k) {
+    b.position_prior[k] = position[k];
+    b.position_sigma[k] = std_dev[k];
+  }
+  int g = -1;
+  for (size_t i = 0; i < scale_groups_.size(); ++i)
+    if (scale_groups_[i] == scale_group) g = int(i);
+  if (g < 0) {
+    g = int(scale_groups_.size());
+    scale_groups_.push_back(scale_group);
+  }
+  b.scale_group = g;
+}
+
+int64_t BundleAdjuster::AddPoint(const std::string& id, const double* p, bool constant) {
+  auto it = point_index_.find(id);
+  if (it != point_index_.end()) return it->second;
+  PointBlock b;
+  for (int k = 0; k < 3; ++k) b.value[k] = p[k];
+  b.free = !constant;
+  const int64_t idx = int64_t(problem_.points.size());
+  point_index_[id] = idx;
+  problem_.points.push_back(b);
+  return idx;
+}
+
+void BundleAdjuster::AddPointPrior(const std::string& id, const double* p, const double* std_dev, bool has_altitude) {
+  auto it = point_index_.find(id);
+  if (it == point_index_.end()) throw std::runtime_error("Point " + id + " doesn't exist.");
+  PointBlock& b = problem_.points[it->second];
+  b.has_prior = true;
+  for (int k = 0; k < 3; ++k) {
+    b.prior[k] = p[k];
+    b.sigma[k] = std_dev[k];
+  }
+  b.has_altitude = has_altitude;
+}
+
+void BundleAdjuster::AddPointProjectionObservation(const std::string& shot, const std::string& point,
+                                                   const double* obs, double std_dev, bool is_gcp) {
+  auto s = shot_index_.find(shot);
+  if (s == shot_index_.end()) throw std::out_of_range("map::at: unknown shot " + shot);
+  auto p = point_index_.find(point);
+  if (p == point_index_.end()) throw std::out_of_range("map::at: unknown point " + point);
+  Observation o;
+  o.shot = s->second;
+  o.point = int(p->second);
+  o.x = obs[0];
+  o.y = obs[1];
+  o.std_dev = std_dev;
+  o.is_gcp = is_gcp;
+  problem_.observations.push_back(o);
+}
+
+int64_t BundleAdjuster::ShotIndex(const std::string& shot) const {
+  auto s = shot_index_.find(shot);
+  return s == shot_index_.end() ? -1 : s->second;
+}
+
+int64_t BundleAdjuster::PointIndex(const std::string& point) const {
+  auto p = point_index_.find(point);
+  return p == point_index_.end() ? -1 : p->second;
+}
+
+int64_t BundleAdjuster::AddPointsBulk(int64_t n, const double* xyz, const uint8_t* constant, const char* const* ids) {
+  const int64_t first = int64_t(problem_.points.size());
+  problem_.points.reserve(problem_.points.size() + n);
+  for (int64_t i = 0; i < n; ++i) {
+    const std::string id = ids ? std::string(ids[i]) : std::to_string(first + i);
+    if (point_index_.count(id)) throw std::runtime_error("Point " + id + " already exists.");
+    PointBlock b;
+    for (int k = 0; k < 3; ++k) b.value[k] = xyz[3 * i + k];
+    b.free = constant ? constant[i] == 0 : true;
+    point_index_[id] = int64_t(problem_.points.size());
+    problem_.points.push_back(b);
+  }
+  return first;
+}
+
+void BundleAdjuster::AddObservationsBulk(int64_t n, const int32_t* shot, const int32_t* point, const double* xy,
+                                         const double* std_dev, const uint8_t* is_gcp) {
+  const int64_t ns = int64_t(problem_.shots.size()), np = int64_t(problem_.points.size());
+  for (int64_t i = 0; i < n; ++i) {
+    if (shot[i] < 0 || shot[i] >= ns) throw std::out_of_range("observation references an unknown shot");
+    if (point[i] < 0 || point[i] >= np) throw std::out_of_range("observation references an unknown point");
+    if (!(std_dev[i] > 0.0)) throw std::invalid_argument("observation std deviation must be positive");
+  }
+  problem_.observations.reserve(problem_.observations.size() + n);
+  for (int64_t i = 0; i < n; ++i) {
+    Observation o;
+    o.shot = shot[i];
+    o.point = point[i];
+    o.x = xy[2 * i];
+    o.y = xy[2 * i + 1];
+    o.std_dev = std_dev[i];
+    o.is_gcp = is_gcp ? is_gcp[i] != 0 : false;
+    problem_.observations.push_back(o);
+  }
+}
+
+void BundleAdjuster::SetPointProjectionLossFunction(const std::string& name, double threshold) {
+  // CreateLossFunction, bundle_adjuster.cc:485-499
+  int loss;
+  if (name == "TrivialLoss") loss = kLossTrivial;
+  else if (name == "HuberLoss") loss = kLossHuber;
+  else if (name == "SoftLOneLoss") loss = kLossSoftLOne;
+  else if (name == "CauchyLoss") loss = kLossCauchy;
+  else if (name == "ArctanLoss") loss = kLossArctan;
+  else throw std::runtime_error("ceres::LossFunction with name " + name + " not found.");
+  opts_.loss = loss;
+  opts_.loss_threshold = threshold;
+  loss_name_ = name;
+}
+
+void BundleAdjuster::SetInternalParametersPriorSD(double focal, double aspect, double c, double k1, double k2,
+                                                  double p1, double p2, double k3, double k4) {
+  focal_sd_ = focal;
+  aspect_sd_ = aspect;
+  c_sd_ = c;
+  k1_sd_ = k1;
+  k2_sd_ = k2;
+  p1_sd_ = p1;
+  p2_sd_ = p2;
+  k3_sd_ = k3;
+  k4_sd_ = k4;
+}
+
+void BundleAdjuster::SetRigParametersPriorSD(double translation, double rotation) {
+  rig_translation_sd_ = translation;
+  rig_rotation_sd_ = rotation;
+}
+
+double BundleAdjuster::GetGroupDensityRatio(const std::string& g) const {
+  auto it = group_ratio_.find(g);
+  return it == group_ratio_.end() ? opts_.default_density_ratio : it->second;
+}
+
+void BundleAdjuster::Run() {
+  static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
+                                   "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
+  bool known = false;
+  for (const char* s : kSolvers) known |= opts_.linear_solver == s;
+  if (!known) throw std::runtime_error("Linear solver type " + opts_.linear_solver + " doesn't exist.");
+  // sigmas and usage flags at run time
+  for (CameraBlock& c : problem_.cameras) camera_sigma(c);
+  for (PoseBlock& r : problem_.rig_cameras) {
+    for (int k = 0; k < 3; ++k) {
+      r.sigma[k] = rig_rotation_sd_;
+      r.sigma[3 + k] = rig_translation_sd_;
+    }
+    bool any_free = false, all_zero = true;
+    for (int k = 0; k < 6; ++k) {
+      any_free |= r.free_mask[k] != 0;
+      all_zero &= r.value[k] == 0.0;
+    }
+    r.used = !(!any_free && all_zero);  // IsRigCameraUseful, bundle_adjuster.cc:20-23
+  }
+  // IRLS density ratios: defaults, then per-group overrides
+  problem_.group_density_ratio.assign(problem_.shots.size() + 1, opts_.default_density_ratio);
+  for (size_t s = 0; s < shot_ids_.size(); ++s) problem_.group_density_ratio[s] = GetGroupDensityRatio("PROJ_" + shot_ids_[s]);
+  problem_.group_density_ratio[shot_ids_.size()] = GetGroupDensityRatio("GCP2D");
+  problem_.ratio_cam = GetGroupDensityRatio("CAM");
+  problem_.ratio_rig = GetGroupDensityRatio("RCAM");
+  problem_.ratio_gps = GetGroupDensityRatio("GPS");
+  problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
+
+  auto solver = make_solver(opts_.precision);
+  summary_ = solver->solve(problem_, opts_);
+  if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
+  else {
+    errors_.clear();
+    weights_.clear();
+  }
+  covariance_valid_ = false;  // covariance estimation is not implemented (the reference's failure fallback)
+  has_run_ = true;
+}
+
+int BundleAdjuster::GetCamera(const std::string& id, int* model, double* values, int cap) const {
+  auto it = camera_index_.find(id);
+  if (it == camera_index_.end()) throw std::runtime_error("Camera " + id + " doesn't exists");
+  const CameraBlock& c = problem_.cameras[it->second];
+  if (model) *model = c.model;
+  for (int k = 0; k < std::min(cap, c.n); ++k) values[k] = c.value[k];
+  return c.n;
+}
+
+void BundleAdjuster::GetRigInstancePose(const std::string& id, double* pose) const {
+  auto it = instance_index_.find(id);
+  if (it == instance_index_.end()) throw std::runtime_error("Rig instance " + id + " doesn't exists");
+  for (int k = 0; k < 6; ++k) pose[k] = problem_.instances[it->second].value[k];
+}
+
+void BundleAdjuster::GetRigCameraPose(const std::string& id, double* pose) const {
+  auto it = rig_camera_index_.find(id);
+  if (it == rig_camera_index_.end()) throw std::runtime_error("Rig camera " + id + " doesn't exists");
+  for (int k = 0; k < 6; ++k) pose[k] = problem_.rig_cameras[it->second].value[k];
+}
+
+void BundleAdjuster::GetPoint(const std::string& id, double* p) const {
+  auto it = point_index_.find(id);
+  if (it == point_index_.end()) throw std::runtime_error("Point " + id + " doesn't exists");
+  for (int k = 0; k < 3; ++k) p[k] = problem_.points[it->second].value[k];
+}
+
+void BundleAdjuster::GetPointsBulk(int64_t first, int64_t n, double* xyz) const {
+  if (first < 0 || first + n > int64_t(problem_.points.size())) throw std::out_of_range("point range");
+  for (int64_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) xyz[3 * i + k] = problem_.points[first + i].value[k];
+}
+
+void BundleAdjuster::GetProjectionResults(int64_t n, double* errors, double* weights, int32_t* dims) const {
+  if (n != int64_t(problem_.observations.size())) throw std::invalid_argument("wrong observation count");
+  const bool have = has_run_ && errors_.size() == size_t(3 * n);
+  for (int64_t i = 0; i < n; ++i) {
+    const Observation& o = problem_.observations[i];
+    const int dim = problem_.cameras[problem_.shots[o.shot].camera].model == kSpherical ? 3 : 2;
+    if (dims) dims[i] = dim;
+    for (int k = 0; k < 3; ++k) errors[3 * i + k] = have ? errors_[3 * i + k] : 0.0;
+    if (weights) weights[i] = have ? weights_[i] : 1.0;
+  }
+}
+
+std::string BundleAdjuster::BriefReport() const {
+  char buf[512];
+  std::snprintf(buf, sizeof(buf),
+                "GB300 Bundle Adjuster Report: Iterations: %d, Initial cost: %e, Final cost: %e, Termination: %s",
+                summary_.iterations, summary_.initial_cost, summary_.final_cost, summary_.termination.c_str());
+  return buf;
+}
+
+std::string BundleAdjuster::FullReport() const {
+  std::ostringstream ss;
+  ss << "GB300 Bundle Adjuster Report\n";
+  ss << "  Precision            " << (opts_.precision == 0 ? "FP64" : "mixed FP32/FP64") << "\n";
+  ss << "  Linear solver        " << summary_.linear_solver << "\n";
+  ss << "  Loss                 " << loss_name_ << " (threshold " << opts_.loss_threshold << ")\n";
+  ss << "  IRLS                 " << (opts_.irls == kIrlsMixture ? "mixture" : "none") << "\n";
+  ss << "  Cameras / shots      " << problem_.cameras.size() << " / " << problem_.shots.size() << "\n";
+  ss << "  Points / projections " << problem_.points.size() << " / " << problem_.observations.size() << "\n";
+  ss << "  Initial cost         " << summary_.initial_cost << "\n";
+  ss << "  Final cost           " << summary_.final_cost << "\n";
+  ss << "  Iterations           " << summary_.iterations << " (" << summary_.successful_steps << " successful, "
+     << summary_.unsuccessful_steps << " unsuccessful)\n";
+  ss << "  Time (s)             total " << summary_.seconds << ", linear solver " << summary_.linear_solver_seconds
+     << ", jacobian " << summary_.jacobian_seconds << ", residuals " << summary_.residual_seconds << "\n";
+  ss << "  Kernel launches      " << summary_.kernel_launches << "\n";
+  ss << "  Termination          " << summary_.termination << "\n";
+  return ss.str();
+}
+
+std::string BundleAdjuster::IrlsReport() const {
+  std::ostringstream ss;
+  for (size_t i = 0; i < summary_.irls_lines.size(); ++i) {
+    if (i) ss << "\n";
+    ss << summary_.irls_lines[i];
+  }
+  return ss.str();
+}
+
+}  // namespace gbba

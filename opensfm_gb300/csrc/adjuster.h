@@ -1,0 +1,111 @@
+// Host-side bundle adjuster with the reference's API semantics
+// (bundle::BundleAdjuster, opensfm/src/lib/bundle/bundle_adjuster.h:173-386,
+// src/bundle_adjuster.cc:56-1400): string-keyed cameras, rig cameras, rig
+// instances (which create the shots), points and observations; settings;
+// Run(); getters and reports.  The optimisation itself runs on the GPU
+// (solver.h).
+#pragma once
+
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "problem.h"
+
+namespace gbba {
+
+class BundleAdjuster {
+ public:
+  BundleAdjuster();
+
+  // adders (bundle_adjuster.cc:107-301)
+  void AddCamera(const std::string& id, int model, const double* values, const double* prior, int n, bool constant);
+  void AddRigCamera(const std::string& id, const double* pose, const double* prior, bool fixed);
+  void AddRigInstance(const std::string& id, const double* pose, const std::vector<std::string>& shots,
+                      const std::vector<std::string>& cameras, const std::vector<std::string>& rig_cameras,
+                      bool fixed);
+  void AddRigInstancePositionPrior(const std::string& id, const double* position, const double* std_dev,
+                                   const std::string& scale_group);
+  int64_t AddPoint(const std::string& id, const double* p, bool constant);
+  void AddPointPrior(const std::string& id, const double* p, const double* std_dev, bool has_altitude);
+  void AddPointProjectionObservation(const std::string& shot, const std::string& point, const double* obs,
+                                     double std_dev, bool is_gcp);
+  // index-based adders (the raw-pointer path of AddPointProjectionObservationRaw)
+  int64_t ShotIndex(const std::string& shot) const;
+  int64_t PointIndex(const std::string& point) const;
+  int64_t AddPointsBulk(int64_t n, const double* xyz, const uint8_t* constant, const char* const* ids);
+  void AddObservationsBulk(int64_t n, const int32_t* shot, const int32_t* point, const double* xy,
+                           const double* std_dev, const uint8_t* is_gcp);
+  void SetCameraBias(const std::string& camera, const double* rotation, const double* translation, double scale);
+
+  // settings (bundle_adjuster.cc:400-483, pybundle.pyi:131)
+  void SetPointProjectionLossFunction(const std::string& name, double threshold);
+  void SetIrlsMode(int mode) { opts_.irls = mode; }
+  void SetPrecision(int p) { opts_.precision = p; }
+  void SetMaxNumIterations(int n) { opts_.max_iterations = n; }
+  void SetNumThreads(int n) { num_threads_ = n; }
+  void SetUseAnalyticDerivatives(bool v) { use_analytic_ = v; }
+  void SetLinearSolverType(const std::string& t) { opts_.linear_solver = t; }
+  void SetInternalParametersPriorSD(double focal, double aspect, double c, double k1, double k2, double p1,
+                                    double p2, double k3, double k4);
+  void SetRigParametersPriorSD(double translation, double rotation);
+  void SetComputeReprojectionErrors(bool v) { opts_.compute_reprojection_errors = v; }
+  void SetComputeCovariances(bool v) { compute_covariances_ = v; }
+  void SetSkipInitialReweighting(bool v) { opts_.skip_initial_reweighting = v; }
+  void SetDefaultDensityRatio(double r) { opts_.default_density_ratio = r; }
+  double GetDefaultDensityRatio() const { return opts_.default_density_ratio; }
+  void SetGroupDensityRatio(const std::string& g, double r) { group_ratio_[g] = r; }
+  double GetGroupDensityRatio(const std::string& g) const;
+  void SetPcgTolerance(double t) { opts_.pcg_tolerance = t; }
+
+  void Run();
+
+  // getters (bundle_adjuster.cc:1303-1399)
+  int GetCamera(const std::string& id, int* model, double* values, int cap) const;
+  void GetRigInstancePose(const std::string& id, double* pose) const;
+  void GetRigCameraPose(const std::string& id, double* pose) const;
+  void GetPoint(const std::string& id, double* p) const;
+  bool HasPoint(const std::string& id) const { return point_index_.count(id) != 0; }
+  int64_t NumProjections() const { return int64_t(problem_.observations.size()); }
+  int64_t NumPoints() const { return int64_t(problem_.points.size()); }
+  void GetPointsBulk(int64_t first, int64_t n, double* xyz) const;
+  void GetProjectionResults(int64_t n, double* errors, double* weights, int32_t* dims) const;
+  bool CovarianceValid() const { return covariance_valid_; }
+  std::string BriefReport() const;
+  std::string FullReport() const;
+  std::string IrlsReport() const;
+  const SolveSummary& Summary() const { return summary_; }
+
+ private:
+  void camera_sigma(CameraBlock& c) const;
+
+  Problem problem_;
+  SolverOptions opts_;
+  std::unordered_map<std::string, int> camera_index_, rig_camera_index_, instance_index_, shot_index_;
+  std::unordered_map<std::string, int64_t> point_index_;
+  std::vector<std::string> shot_ids_;
+  std::map<std::string, double> group_ratio_;
+  std::vector<std::string> scale_groups_;
+  double focal_sd_ = 1, aspect_sd_ = 1, c_sd_ = 1, k1_sd_ = 1, k2_sd_ = 1, p1_sd_ = 1, p2_sd_ = 1, k3_sd_ = 1,
+         k4_sd_ = 1;
+  double rig_translation_sd_ = 1.0, rig_rotation_sd_ = 1.0;
+  int num_threads_ = 1;
+  bool use_analytic_ = false;
+  bool compute_covariances_ = false;
+  bool covariance_valid_ = false;
+  std::string loss_name_ = "TrivialLoss";
+  SolveSummary summary_;
+  std::vector<double> errors_, weights_;
+  bool has_run_ = false;
+};
+
+// Parameter types of a camera model in geometry::Camera order
+// (camera.cc:11-172), as geometry::Camera::Parameters values.
+enum CameraParam {
+  kParamTransition, kParamK1, kParamK2, kParamK3, kParamK4, kParamK5, kParamK6, kParamP1, kParamP2,
+  kParamFocal, kParamAspectRatio, kParamCx, kParamCy, kParamS0, kParamS1, kParamS2, kParamS3, kParamNone
+};
+std::vector<int> camera_parameter_types(int model);
+
+}  // namespace gbba

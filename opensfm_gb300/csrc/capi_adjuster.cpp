@@ -1,0 +1,396 @@
+// extern "C" entry points of the bundle adjuster (include/gbba.h).
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gbba.h"
+#include "adjuster.h"
+#include "capi_util.h"
+
+struct gbba_adjuster {
+  gbba::BundleAdjuster ba;
+};
+
+using gbba::ApiError;
+using gbba::guarded;
+
+namespace {
+
+gbba::BundleAdjuster& ba_of(gbba_adjuster_t* h) {
+  if (!h) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "adjuster handle is NULL");
+  return h->ba;
+}
+const gbba::BundleAdjuster& ba_of(const gbba_adjuster_t* h) {
+  if (!h) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "adjuster handle is NULL");
+  return h->ba;
+}
+std::string str(const char* s) {
+  if (!s) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "string argument is NULL");
+  return std::string(s);
+}
+template <typename T>
+void need(const T* p, const char* what) {
+  if (!p) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, std::string(what) + " is NULL");
+}
+int copy_string(const std::string& s, char* buf, size_t len) {
+  if (buf && len) {
+    const size_t n = std::min(len - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+  }
+  return int(s.size());
+}
+
+}  // namespace
+
+extern "C" {
+
+gbba_adjuster_t* gbba_create(void) {
+  gbba_adjuster_t* h = nullptr;
+  guarded([&] { h = new gbba_adjuster_t; });
+  return h;
+}
+
+void gbba_destroy(gbba_adjuster_t* h) { delete h; }
+
+int gbba_add_camera(gbba_adjuster_t* h, const char* id, int projection, const double* values,
+                    const double* prior_values, int n_values, int constant) {
+  return guarded([&] {
+    need(values, "values");
+    need(prior_values, "prior_values");
+    try {
+      ba_of(h).AddCamera(str(id), projection, values, prior_values, n_values, constant != 0);
+    } catch (const std::invalid_argument& e) {
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+    }
+  });
+}
+
+int gbba_set_camera_bias(gbba_adjuster_t* h, const char* camera_id, const double* rotation,
+                         const double* translation, double scale) {
+  return guarded([&] {
+    need(rotation, "rotation");
+    need(translation, "translation");
+    ba_of(h).SetCameraBias(str(camera_id), rotation, translation, scale);
+  });
+}
+
+int gbba_add_rig_camera(gbba_adjuster_t* h, const char* id, const double* pose, const double* pose_prior, int fixed) {
+  return guarded([&] {
+    need(pose, "pose");
+    need(pose_prior, "pose_prior");
+    ba_of(h).AddRigCamera(str(id), pose, pose_prior, fixed != 0);
+  });
+}
+
+int gbba_add_rig_instance(gbba_adjuster_t* h, const char* id, const double* pose, int n_shots,
+                          const char* const* shot_ids, const char* const* camera_ids,
+                          const char* const* rig_camera_ids, int fixed) {
+  return guarded([&] {
+    need(pose, "pose");
+    if (n_shots < 0) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative shot count");
+    std::vector<std::string> s, c, r;
+    for (int i = 0; i < n_shots; ++i) {
+      s.push_back(str(shot_ids[i]));
+      c.push_back(str(camera_ids[i]));
+      r.push_back(str(rig_camera_ids[i]));
+    }
+    ba_of(h).AddRigInstance(str(id), pose, s, c, r, fixed != 0);
+  });
+}
+
+int gbba_add_rig_instance_position_prior(gbba_adjuster_t* h, const char* id, const double* position,
+                                         const double* std_dev, const char* scale_group) {
+  return guarded([&] {
+    need(position, "position");
+    need(std_dev, "std_dev");
+    ba_of(h).AddRigInstancePositionPrior(str(id), position, std_dev, scale_group ? scale_group : "");
+  });
+}
+
+int gbba_add_point(gbba_adjuster_t* h, const char* id, const double* position, int constant) {
+  return guarded([&] {
+    need(position, "position");
+    ba_of(h).AddPoint(str(id), position, constant != 0);
+  });
+}
+
+int gbba_add_point_prior(gbba_adjuster_t* h, const char* id, const double* position, const double* std_dev,
+                         int has_altitude) {
+  return guarded([&] {
+    need(position, "position");
+    need(std_dev, "std_dev");
+    ba_of(h).AddPointPrior(str(id), position, std_dev, has_altitude != 0);
+  });
+}
+
+int gbba_add_point_projection_observation(gbba_adjuster_t* h, const char* shot, const char* point,
+                                          const double* observation, double std_dev, int is_gcp) {
+  return guarded([&] {
+    need(observation, "observation");
+    ba_of(h).AddPointProjectionObservation(str(shot), str(point), observation, std_dev, is_gcp != 0);
+  });
+}
+
+int64_t gbba_shot_index(const gbba_adjuster_t* h, const char* shot) {
+  int64_t r = -1;
+  guarded([&] { r = ba_of(h).ShotIndex(str(shot)); });
+  return r;
+}
+
+int64_t gbba_point_index(const gbba_adjuster_t* h, const char* point) {
+  int64_t r = -1;
+  guarded([&] { r = ba_of(h).PointIndex(str(point)); });
+  return r;
+}
+
+int gbba_add_points_bulk(gbba_adjuster_t* h, int64_t n, const double* xyz, const uint8_t* constant,
+                         const char* const* ids, int64_t* first_index) {
+  return guarded([&] {
+    if (n < 0) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative point count");
+    if (n) need(xyz, "xyz");
+    const int64_t f = ba_of(h).AddPointsBulk(n, xyz, constant, ids);
+    if (first_index) *first_index = f;
+  });
+}
+
+int gbba_add_point_projection_observations_bulk(gbba_adjuster_t* h, int64_t n, const int32_t* shot_index,
+                                                const int32_t* point_index, const double* xy,
+                                                const double* std_dev, const uint8_t* is_gcp) {
+  return guarded([&] {
+    if (n < 0) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative observation count");
+    if (n) {
+      need(shot_index, "shot_index");
+      need(point_index, "point_index");
+      need(xy, "xy");
+      need(std_dev, "std_dev");
+    }
+    try {
+      ba_of(h).AddObservationsBulk(n, shot_index, point_index, xy, std_dev, is_gcp);
+    } catch (const std::invalid_argument& e) {
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+    }
+  });
+}
+
+int gbba_set_point_projection_loss_function(gbba_adjuster_t* h, const char* name, double threshold) {
+  return guarded([&] { ba_of(h).SetPointProjectionLossFunction(str(name), threshold); });
+}
+
+int gbba_set_irls_mode(gbba_adjuster_t* h, int mode) {
+  return guarded([&] {
+    if (mode != 0 && mode != 1) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "IRLS mode must be 0 (none) or 1 (mixture)");
+    ba_of(h).SetIrlsMode(mode);
+  });
+}
+
+int gbba_set_precision(gbba_adjuster_t* h, int precision) {
+  return guarded([&] {
+    if (precision != GBBA_PRECISION_FP64 && precision != GBBA_PRECISION_MIXED)
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "unknown precision");
+    ba_of(h).SetPrecision(precision);
+  });
+}
+
+int gbba_set_max_num_iterations(gbba_adjuster_t* h, int n) {
+  return guarded([&] { ba_of(h).SetMaxNumIterations(n); });
+}
+
+int gbba_set_num_threads(gbba_adjuster_t* h, int n) {
+  return guarded([&] { ba_of(h).SetNumThreads(n); });
+}
+
+int gbba_set_use_analytic_derivatives(gbba_adjuster_t* h, int use) {
+  return guarded([&] { ba_of(h).SetUseAnalyticDerivatives(use != 0); });
+}
+
+int gbba_set_linear_solver_type(gbba_adjuster_t* h, const char* type) {
+  return guarded([&] { ba_of(h).SetLinearSolverType(str(type)); });
+}
+
+int gbba_set_internal_parameters_prior_sd(gbba_adjuster_t* h, double focal_sd, double aspect_ratio_sd, double c_sd,
+                                          double k1_sd, double k2_sd, double p1_sd, double p2_sd, double k3_sd,
+                                          double k4_sd) {
+  return guarded([&] {
+    ba_of(h).SetInternalParametersPriorSD(focal_sd, aspect_ratio_sd, c_sd, k1_sd, k2_sd, p1_sd, p2_sd, k3_sd, k4_sd);
+  });
+}
+
+int gbba_set_rig_parameters_prior_sd(gbba_adjuster_t* h, double translation_sd, double rotation_sd) {
+  return guarded([&] { ba_of(h).SetRigParametersPriorSD(translation_sd, rotation_sd); });
+}
+
+int gbba_set_compute_reprojection_errors(gbba_adjuster_t* h, int v) {
+  return guarded([&] { ba_of(h).SetComputeReprojectionErrors(v != 0); });
+}
+
+int gbba_set_compute_covariances(gbba_adjuster_t* h, int v) {
+  return guarded([&] { ba_of(h).SetComputeCovariances(v != 0); });
+}
+
+int gbba_get_covariance_estimation_valid(const gbba_adjuster_t* h) {
+  int v = 0;
+  guarded([&] { v = ba_of(h).CovarianceValid() ? 1 : 0; });
+  return v;
+}
+
+int gbba_set_skip_initial_reweighting(gbba_adjuster_t* h, int v) {
+  return guarded([&] { ba_of(h).SetSkipInitialReweighting(v != 0); });
+}
+
+int gbba_set_default_density_ratio(gbba_adjuster_t* h, double ratio) {
+  return guarded([&] { ba_of(h).SetDefaultDensityRatio(ratio); });
+}
+
+double gbba_get_default_density_ratio(const gbba_adjuster_t* h) {
+  double v = 0.0;
+  guarded([&] { v = ba_of(h).GetDefaultDensityRatio(); });
+  return v;
+}
+
+int gbba_set_group_density_ratio(gbba_adjuster_t* h, const char* group, double ratio) {
+  return guarded([&] { ba_of(h).SetGroupDensityRatio(str(group), ratio); });
+}
+
+double gbba_get_group_density_ratio(const gbba_adjuster_t* h, const char* group) {
+  double v = 0.0;
+  guarded([&] { v = ba_of(h).GetGroupDensityRatio(str(group)); });
+  return v;
+}
+
+int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance) {
+  return guarded([&] {
+    if (!(tolerance > 0.0)) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "tolerance must be positive");
+    ba_of(h).SetPcgTolerance(tolerance);
+  });
+}
+
+int gbba_run(gbba_adjuster_t* h) {
+  return guarded([&] { ba_of(h).Run(); });
+}
+
+int gbba_get_camera(const gbba_adjuster_t* h, const char* id, int* projection, double* values, int capacity,
+                    int* n_values) {
+  return guarded([&] {
+    need(values, "values");
+    const int n = ba_of(h).GetCamera(str(id), projection, values, capacity);
+    if (n_values) *n_values = n;
+  });
+}
+
+int gbba_get_rig_instance_pose(const gbba_adjuster_t* h, const char* id, double* pose) {
+  return guarded([&] {
+    need(pose, "pose");
+    ba_of(h).GetRigInstancePose(str(id), pose);
+  });
+}
+
+int gbba_get_rig_camera_pose(const gbba_adjuster_t* h, const char* id, double* pose) {
+  return guarded([&] {
+    need(pose, "pose");
+    ba_of(h).GetRigCameraPose(str(id), pose);
+  });
+}
+
+int gbba_get_point(const gbba_adjuster_t* h, const char* id, double* position) {
+  return guarded([&] {
+    need(position, "position");
+    ba_of(h).GetPoint(str(id), position);
+  });
+}
+
+int gbba_has_point(const gbba_adjuster_t* h, const char* id) {
+  int v = 0;
+  guarded([&] { v = ba_of(h).HasPoint(str(id)) ? 1 : 0; });
+  return v;
+}
+
+int64_t gbba_num_projections(const gbba_adjuster_t* h) {
+  int64_t v = 0;
+  guarded([&] { v = ba_of(h).NumProjections(); });
+  return v;
+}
+
+int64_t gbba_num_points(const gbba_adjuster_t* h) {
+  int64_t v = 0;
+  guarded([&] { v = ba_of(h).NumPoints(); });
+  return v;
+}
+
+int gbba_get_points_bulk(const gbba_adjuster_t* h, int64_t first, int64_t n, double* xyz) {
+  return guarded([&] {
+    if (n) need(xyz, "xyz");
+    ba_of(h).GetPointsBulk(first, n, xyz);
+  });
+}
+
+int gbba_get_projection_results(const gbba_adjuster_t* h, int64_t n, double* errors, double* weights, int32_t* dims) {
+  return guarded([&] {
+    if (n) need(errors, "errors");
+    try {
+      ba_of(h).GetProjectionResults(n, errors, weights, dims);
+    } catch (const std::invalid_argument& e) {
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+    }
+  });
+}
+
+int gbba_brief_report(const gbba_adjuster_t* h, char* buf, size_t len) {
+  int n = 0;
+  const int st = guarded([&] { n = copy_string(ba_of(h).BriefReport(), buf, len); });
+  return st == GBBA_OK ? n : -1;
+}
+
+int gbba_full_report(const gbba_adjuster_t* h, char* buf, size_t len) {
+  int n = 0;
+  const int st = guarded([&] { n = copy_string(ba_of(h).FullReport(), buf, len); });
+  return st == GBBA_OK ? n : -1;
+}
+
+int gbba_irls_report(const gbba_adjuster_t* h, char* buf, size_t len) {
+  int n = 0;
+  const int st = guarded([&] { n = copy_string(ba_of(h).IrlsReport(), buf, len); });
+  return st == GBBA_OK ? n : -1;
+}
+
+int gbba_get_summary(const gbba_adjuster_t* h, gbba_summary_t* out) {
+  return guarded([&] {
+    need(out, "out");
+    const gbba::SolveSummary& s = ba_of(h).Summary();
+    out->initial_cost = s.initial_cost;
+    out->final_cost = s.final_cost;
+    out->seconds = s.seconds;
+    out->linear_solver_seconds = s.linear_solver_seconds;
+    out->jacobian_seconds = s.jacobian_seconds;
+    out->residual_seconds = s.residual_seconds;
+    out->iterations = s.iterations;
+    out->successful_steps = s.successful_steps;
+    out->unsuccessful_steps = s.unsuccessful_steps;
+    out->kernel_launches = s.kernel_launches;
+    out->usable = s.usable ? 1 : 0;
+  });
+}
+
+int gbba_get_trace(const gbba_adjuster_t* h, int capacity, double* records, int* n) {
+  return guarded([&] {
+    const gbba::SolveSummary& s = ba_of(h).Summary();
+    const int m = int(s.trace.size());
+    if (n) *n = m;
+    if (!records) return;
+    for (int i = 0; i < std::min(capacity, m); ++i) {
+      const gbba::IterationRecord& r = s.trace[i];
+      double* o = records + 8 * int64_t(i);
+      o[0] = r.iteration;
+      o[1] = r.cost;
+      o[2] = r.seconds;
+      o[3] = r.success ? 1.0 : 0.0;
+      o[4] = r.linear_iterations;
+      o[5] = r.radius;
+      o[6] = r.relative_decrease;
+      o[7] = r.step_norm;
+    }
+  });
+}
+
+}  // extern "C"

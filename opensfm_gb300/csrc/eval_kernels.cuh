@@ -157,6 +157,8 @@ __global__ void shot_prep_kernel(int n_shots, const int* __restrict__ shot_inst,
   }
   for (int i = 0; i < 3; ++i) g.tc[i] = R(tc[i]);
   g.cam = R(shot_cam[s]);
+  g.inst = R(shot_inst[s]);
+  g.rig = R(use_rig ? rc : -1);
   for (int i = 0; i < 3; ++i) {
     g.chi[i] = R(pi[3 + i]);
     g.clo[i] = R(pi[3 + i] - double(g.chi[i]));

@@ -57,6 +57,7 @@ GB_HD PointF2 make_point_store(double x, double y, double z, float*) {
 //   tc[3]   camera-frame offset -R_rc * c_rc (zero without rig camera)
 //   cam     camera index of the shot (exact small integer)
 //   chi[3], clo[3]  rig instance centre (double-float in FP32; lo = 0 in FP64)
+//   inst, rig  rig instance and rig camera indices (rig = -1: none)
 template <typename R>
 struct alignas(16) ShotGeom {
   R rot[9];
@@ -65,7 +66,9 @@ struct alignas(16) ShotGeom {
   R cam;
   R chi[3];
   R clo[3];
-  R pad[sizeof(R) == 4 ? 4 : 2];
+  R inst;
+  R rig;
+  R pad[sizeof(R) == 4 ? 2 : 0 + 2];
 };
 
 #ifdef __CUDACC__
@@ -279,7 +282,7 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
       }
     }
   }
-  if (!JAC) return;
+  if constexpr (!JAC) return;
 
 #pragma unroll
   for (int i = 0; i < NR; ++i) {

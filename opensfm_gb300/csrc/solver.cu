@@ -1,0 +1,1147 @@
+// GPU Levenberg-Marquardt bundle-adjustment solver (see solver.h).
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <numeric>
+#include <sstream>
+#include <vector>
+
+#include "device_buffer.h"
+#include "solver.h"
+#include "solver_kernels.cuh"
+
+namespace gbba {
+
+namespace {
+
+constexpr int kDyn = -1;
+constexpr double kEps = 2.220446049250313e-16;
+
+struct KernelConfig {
+  int model;  // single model or kDyn
+  int nr;
+  int cmax;
+  bool rig;
+};
+
+template <int C>
+constexpr int tri_pad() {
+  return TriSize<C>::kPad;
+}
+
+// Calls f.template run<M, NR, CMAX, RIG>() for a kernel configuration.
+template <typename F>
+void dispatch_config(const KernelConfig& k, F& f) {
+  if (k.model != kDyn) {
+    switch (k.model) {
+      case kPerspective: f.template run<kPerspective, 2, 3, false>(); return;
+      case kBrown: f.template run<kBrown, 2, 9, false>(); return;
+      case kFisheye: f.template run<kFisheye, 2, 3, false>(); return;
+      case kFisheyeOpencv: f.template run<kFisheyeOpencv, 2, 8, false>(); return;
+      case kFisheye62: f.template run<kFisheye62, 2, 12, false>(); return;
+      case kFisheye624: f.template run<kFisheye624, 2, 16, false>(); return;
+      case kDual: f.template run<kDual, 2, 4, false>(); return;
+      case kRadial: f.template run<kRadial, 2, 6, false>(); return;
+      case kSimpleRadial: f.template run<kSimpleRadial, 2, 5, false>(); return;
+    }
+  }
+  if (k.nr == 2) {
+    if (k.rig) f.template run<kDyn, 2, 16, true>();
+    else f.template run<kDyn, 2, 16, false>();
+  } else {
+    if (k.rig) f.template run<kDyn, 3, 16, true>();
+    else f.template run<kDyn, 3, 16, false>();
+  }
+}
+
+int slot_grid(int64_t n) {
+  const int64_t want = (n + 255) / 256;
+  return int(std::max<int64_t>(1, std::min<int64_t>(want, 152 * 8)));
+}
+int elem_grid(int64_t n, int block = 256) { return int(std::max<int64_t>(1, (n + block - 1) / block)); }
+
+// ---------------------------------------------------------------------------
+// Small camera-side kernels.
+
+template <typename R>
+__global__ void cam_damp_kernel(int n, const R* __restrict__ dc, const double* __restrict__ pdiag,
+                                const uint8_t* __restrict__ mask, R* __restrict__ cscale, R* __restrict__ damp,
+                                double mu, int first) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  if (!mask[j]) {
+    damp[j] = R(0);
+    if (first) cscale[j] = R(1);
+    return;
+  }
+  const double d = double(dc[j]) + pdiag[j];
+  if (first) cscale[j] = R(1.0 / (1.0 + sqrt(d)));
+  const double s = double(cscale[j]);
+  double c = s * s * d;
+  c = c < 1e-6 ? 1e-6 : (c > 1e32 ? 1e32 : c);
+  damp[j] = R(c / (s * s) * mu);
+}
+
+template <typename R>
+__global__ void rhs_finish_kernel(int n, const R* __restrict__ gc, const double* __restrict__ pgrad,
+                                  const uint8_t* __restrict__ mask, R* __restrict__ rhs, double* __restrict__ bb) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (j < n) {
+    const double b = mask[j] ? double(rhs[j]) - double(gc[j]) - pgrad[j] : 0.0;
+    rhs[j] = R(b);
+    v = b * b;
+  }
+  block_sum_add<256>(v, bb);
+}
+
+// Inverts a symmetric positive definite n x n matrix (row-major, double) in
+// place by Cholesky; returns false if not positive definite.
+__device__ inline bool spd_inverse(double* A, int n, int ld) {
+  // Cholesky A = L L^T (lower stored in A)
+  for (int j = 0; j < n; ++j) {
+    double d = A[j * ld + j];
+    for (int k = 0; k < j; ++k) d -= A[j * ld + k] * A[j * ld + k];
+    if (!(d > 0.0)) return false;
+    d = sqrt(d);
+    A[j * ld + j] = d;
+    for (int i = j + 1; i < n; ++i) {
+      double s = A[i * ld + j];
+      for (int k = 0; k < j; ++k) s -= A[i * ld + k] * A[j * ld + k];
+      A[i * ld + j] = s / d;
+    }
+  }
+  // inverse of L in place (lower)
+  for (int j = 0; j < n; ++j) {
+    A[j * ld + j] = 1.0 / A[j * ld + j];
+    for (int i = j + 1; i < n; ++i) {
+      double s = 0.0;
+      for (int k = j; k < i; ++k) s -= A[i * ld + k] * A[k * ld + j];
+      A[i * ld + j] = s / A[i * ld + i];
+    }
+  }
+  // A^-1 = L^-T L^-1, write full symmetric
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j <= i; ++j) {
+      double s = 0.0;
+      for (int k = i; k < n; ++k) s += A[k * ld + i] * A[k * ld + j];
+      A[j * ld + i] = s;  // upper
+    }
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < i; ++j) A[i * ld + j] = A[j * ld + i];
+  return true;
+}
+
+// Assembles and inverts the block-Jacobi preconditioner blocks.
+//   block = schur_tri + diag(pdiag + damp) on optimised coordinates,
+//   identity-free rows/columns for fixed coordinates (their inverse rows are 0).
+template <typename R>
+__global__ void precond_invert_kernel(CamLayout cl, int cam_tri_stride, int cmax, const R* __restrict__ tri_inst,
+                                      const R* __restrict__ tri_rig, const R* __restrict__ tri_cam,
+                                      const double* __restrict__ pdiag, const R* __restrict__ damp,
+                                      const uint8_t* __restrict__ mask, R* __restrict__ minv_inst,
+                                      R* __restrict__ minv_rig, R* __restrict__ minv_cam, int* __restrict__ n_bad) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = cl.n_inst + cl.n_rig + cl.n_cam;
+  if (b >= nb) return;
+  int size, start;
+  const R* tri;
+  R* out;
+  int w;  // logical block width
+  if (b < cl.n_inst) {
+    size = 8; w = 6; start = 8 * b; tri = tri_inst + 24 * int64_t(b); out = minv_inst + 64 * int64_t(b);
+  } else if (b < cl.n_inst + cl.n_rig) {
+    const int r = b - cl.n_inst;
+    size = 8; w = 6; start = cl.rig_base + 8 * r; tri = tri_rig + 24 * int64_t(r); out = minv_rig + 64 * int64_t(r);
+  } else {
+    const int k = b - cl.n_inst - cl.n_rig;
+    size = 16; w = cmax; start = cl.cam_base + 16 * k; tri = tri_cam + int64_t(cam_tri_stride) * k;
+    out = minv_cam + 256 * int64_t(k);
+  }
+  double A[16 * 16];
+  int idx[16];
+  int m = 0;
+  for (int a = 0; a < w; ++a)
+    if (mask[start + a]) idx[m++] = a;
+  // unpack the upper triangle (row-major over a <= c)
+  auto tri_at = [&](int a, int c) {
+    if (a > c) { const int t = a; a = c; c = t; }
+    const int off = a * w - a * (a - 1) / 2 + (c - a);
+    return double(tri[off]);
+  };
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) {
+      double v = tri_at(idx[i], idx[j]);
+      if (i == j) v += pdiag[start + idx[i]] + double(damp[start + idx[i]]);
+      A[i * 16 + j] = v;
+    }
+  for (int i = 0; i < size * size; ++i) out[i] = R(0);
+  if (m == 0) return;
+  if (!spd_inverse(A, m, 16)) {
+    atomicAdd(n_bad, 1);
+    // fall back to the inverse diagonal
+    for (int i = 0; i < m; ++i) {
+      const double d = tri_at(idx[i], idx[i]) + pdiag[start + idx[i]] + double(damp[start + idx[i]]);
+      out[idx[i] * size + idx[i]] = R(d > 0.0 ? 1.0 / d : 0.0);
+    }
+    return;
+  }
+  for (int i = 0; i < m; ++i)
+    for (int j = 0; j < m; ++j) out[idx[i] * size + idx[j]] = R(A[i * 16 + j]);
+}
+
+// z = M^-1 r (block diagonal), rz += r . z
+template <typename R>
+__global__ void precond_apply_kernel(CamLayout cl, const R* __restrict__ minv_inst, const R* __restrict__ minv_rig,
+                                     const R* __restrict__ minv_cam, const R* __restrict__ r, R* __restrict__ z,
+                                     double* __restrict__ rz) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (j < cl.n) {
+    const R* M;
+    int start, size, row;
+    if (j < cl.rig_base) {
+      const int b = j >> 3;
+      start = 8 * b; size = 8; row = j & 7; M = minv_inst + 64 * int64_t(b);
+    } else if (j < cl.cam_base) {
+      const int b = (j - cl.rig_base) >> 3;
+      start = cl.rig_base + 8 * b; size = 8; row = (j - cl.rig_base) & 7; M = minv_rig + 64 * int64_t(b);
+    } else {
+      const int b = (j - cl.cam_base) >> 4;
+      start = cl.cam_base + 16 * b; size = 16; row = (j - cl.cam_base) & 15; M = minv_cam + 256 * int64_t(b);
+    }
+    R s = R(0);
+    for (int k = 0; k < size; ++k) s += M[row * size + k] * r[start + k];
+    z[j] = s;
+    acc = double(r[j]) * double(s);
+  }
+  block_sum_add<256>(acc, rz);
+}
+
+// y = mask (y + diag p), pq += p . y
+template <typename R>
+__global__ void spmv_finish_kernel(int n, const R* __restrict__ p, const double* __restrict__ pdiag,
+                                   const R* __restrict__ damp, const uint8_t* __restrict__ mask, R* __restrict__ y,
+                                   double* __restrict__ pq) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (j < n) {
+    R v = R(0);
+    if (mask[j]) v = y[j] + R(pdiag[j] + double(damp[j])) * p[j];
+    y[j] = v;
+    acc = double(p[j]) * double(v);
+  }
+  block_sum_add<256>(acc, pq);
+}
+
+// x += alpha p, r -= alpha y, rr += r . r with alpha = s[RZ] / s[PQ]
+enum { kRZ = 0, kPQ = 1, kRR = 2, kRZN = 3, kBB = 4 };
+template <typename R>
+__global__ void pcg_step_kernel(int n, const double* __restrict__ s, R* __restrict__ x, R* __restrict__ r,
+                                const R* __restrict__ p, const R* __restrict__ y, double* __restrict__ rr) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  const double pq = s[kPQ];
+  const double alpha = pq > 0.0 ? s[kRZ] / pq : 0.0;
+  if (j < n) {
+    x[j] += R(alpha) * p[j];
+    const R rv = r[j] - R(alpha) * y[j];
+    r[j] = rv;
+    acc = double(rv) * double(rv);
+  }
+  block_sum_add<256>(acc, rr);
+}
+
+// p = z + beta p, beta = s[RZN] / s[RZ]
+template <typename R>
+__global__ void pcg_dir_kernel(int n, const double* __restrict__ s, R* __restrict__ p, const R* __restrict__ z) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const double beta = s[kRZ] != 0.0 ? s[kRZN] / s[kRZ] : 0.0;
+  p[j] = z[j] + R(beta) * p[j];
+}
+
+static __global__ void pcg_rotate_kernel(double* s) {
+  s[kRZ] = s[kRZN];
+  s[kPQ] = 0.0;
+  s[kRR] = 0.0;
+  s[kRZN] = 0.0;
+}
+
+template <typename R>
+__global__ void copy_kernel(int n, const R* __restrict__ a, R* __restrict__ b) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) b[j] = a[j];
+}
+
+// Point priors (GCP3D, prior_error.h:19-114 with indexes PX, PY[, PZ]):
+// r_j = (X_j - prior_j) / sigma_j, weighted by the group's IRLS weight.
+struct PointPriorDev {
+  int point;
+  int n;  // 2 or 3 constrained coordinates
+  double prior[3];
+  double scale[3];
+};
+
+template <typename R>
+__global__ void point_prior_linearize_kernel(int n, const PointPriorDev* __restrict__ pp, const double* __restrict__ w,
+                                             const Point4* __restrict__ X, const uint8_t* __restrict__ point_free,
+                                             R* __restrict__ Vp, R* __restrict__ gp) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const PointPriorDev P = pp[k];
+  if (!point_free[P.point]) return;
+  const Point4 x = X[P.point];
+  const double v[3] = {x.x, x.y, x.z};
+  const int dg[3] = {0, 3, 5};
+  for (int j = 0; j < P.n; ++j) {
+    const double r = P.scale[j] * (v[j] - P.prior[j]);
+    atomicAdd(Vp + 8 * int64_t(P.point) + dg[j], R(w[k] * P.scale[j] * P.scale[j]));
+    atomicAdd(gp + 4 * int64_t(P.point) + j, R(w[k] * P.scale[j] * r));
+  }
+}
+
+static __global__ void point_prior_cost_kernel(int n, const PointPriorDev* __restrict__ pp, const double* __restrict__ w,
+                                               const Point4* __restrict__ X, double* __restrict__ resid,
+                                               double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (k < n) {
+    const PointPriorDev P = pp[k];
+    const Point4 x = X[P.point];
+    const double v[3] = {x.x, x.y, x.z};
+    for (int j = 0; j < 3; ++j) {
+      const double r = j < P.n ? P.scale[j] * (v[j] - P.prior[j]) : 0.0;
+      resid[3 * k + j] = r;
+      acc += 0.5 * w[k] * r * r;
+    }
+  }
+  block_sum_add<256>(acc, out);
+}
+
+template <typename R>
+__global__ void point_prior_model_kernel(int n, const PointPriorDev* __restrict__ pp, const double* __restrict__ w,
+                                         const Point4* __restrict__ X, const R* __restrict__ dp,
+                                         const uint8_t* __restrict__ point_free, double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (k < n) {
+    const PointPriorDev P = pp[k];
+    if (point_free[P.point]) {
+      const Point4 x = X[P.point];
+      const double v[3] = {x.x, x.y, x.z};
+      for (int j = 0; j < P.n; ++j) {
+        const double r = P.scale[j] * (v[j] - P.prior[j]);
+        const double jd = P.scale[j] * double(dp[4 * int64_t(P.point) + j]);
+        acc += -0.5 * w[k] * jd * (2.0 * r + jd);
+      }
+    }
+  }
+  block_sum_add<256>(acc, out);
+}
+
+// ---------------------------------------------------------------------------
+// Host helpers: mixture reweighting of one group of residual vectors
+// (mixture_reweighting.cc:10-109 with ComputeWhitening, irls_helpers.cc:
+// 220-277).  res holds `count` residual vectors of dimension k; blocks with
+// another dimension are skipped (dims[i] != k).
+struct MixtureResult {
+  double log_likelihood = 0.0;
+  int outliers = 0;
+  int total = 0;
+};
+
+bool small_cholesky(std::vector<double>& A, int k, double& det) {
+  det = 1.0;
+  for (int j = 0; j < k; ++j) {
+    double d = A[j * k + j];
+    for (int m = 0; m < j; ++m) d -= A[j * k + m] * A[j * k + m];
+    if (!(d > 0.0)) return false;
+    det *= d;
+    d = std::sqrt(d);
+    A[j * k + j] = d;
+    for (int i = j + 1; i < k; ++i) {
+      double s = A[i * k + j];
+      for (int m = 0; m < j; ++m) s -= A[i * k + m] * A[j * k + m];
+      A[i * k + j] = s / d;
+    }
+  }
+  return true;
+}
+
+// Determinant and inverse of a small symmetric matrix (LU with pivoting, so
+// that indefinite matrices behave like Eigen's determinant()/inverse()).
+bool small_det_inverse(const std::vector<double>& A, int k, double& det, std::vector<double>& inv) {
+  std::vector<double> M = A;
+  std::vector<int> perm(k);
+  std::iota(perm.begin(), perm.end(), 0);
+  det = 1.0;
+  for (int c = 0; c < k; ++c) {
+    int p = c;
+    for (int r = c + 1; r < k; ++r)
+      if (std::fabs(M[r * k + c]) > std::fabs(M[p * k + c])) p = r;
+    if (M[p * k + c] == 0.0) {
+      det = 0.0;
+      return false;
+    }
+    if (p != c) {
+      for (int j = 0; j < k; ++j) std::swap(M[p * k + j], M[c * k + j]);
+      std::swap(perm[p], perm[c]);
+      det = -det;
+    }
+    det *= M[c * k + c];
+    for (int r = c + 1; r < k; ++r) {
+      const double f = M[r * k + c] / M[c * k + c];
+      M[r * k + c] = f;
+      for (int j = c + 1; j < k; ++j) M[r * k + j] -= f * M[c * k + j];
+    }
+  }
+  inv.assign(k * k, 0.0);
+  for (int col = 0; col < k; ++col) {
+    std::vector<double> b(k, 0.0);
+    for (int i = 0; i < k; ++i) b[i] = perm[i] == col ? 1.0 : 0.0;
+    for (int i = 0; i < k; ++i)
+      for (int j = 0; j < i; ++j) b[i] -= M[i * k + j] * b[j];
+    for (int i = k - 1; i >= 0; --i) {
+      for (int j = i + 1; j < k; ++j) b[i] -= M[i * k + j] * b[j];
+      b[i] /= M[i * k + i];
+    }
+    for (int i = 0; i < k; ++i) inv[i * k + col] = b[i];
+  }
+  return true;
+}
+
+constexpr double kMinDeterminant = 1e-3;
+constexpr double kMinVariance = 0.025;
+constexpr double kMinWeight = 1e-10;
+constexpr int kMinSampleSize = 10;
+constexpr int kMaxInnerIterations = 5;
+constexpr double kConvergenceThreshold = 1e-3;
+
+// Group covariance -> (inverse, 1/sqrt((2pi)^k det), K), mixture_reweighting.cc:34-58.
+void mixture_params(const std::vector<double>& cov_in, int k, double density_ratio, std::vector<double>& inv,
+                    double& norm, double& K) {
+  std::vector<double> cov = cov_in;
+  for (int i = 0; i < k; ++i) cov[i * k + i] += kMinVariance;
+  double det;
+  small_det_inverse(cov, k, det, inv);
+  if (det < kMinDeterminant) {
+    det = kMinVariance * kMinVariance;
+    inv.assign(k * k, 0.0);
+    for (int i = 0; i < k; ++i) inv[i * k + i] = 1.0 / kMinVariance;
+  }
+  const double normalizer = std::pow(2 * M_PI, k) * det;
+  const double sq = std::sqrt(normalizer);
+  norm = 1.0 / sq;
+  K = density_ratio / sq;
+}
+
+MixtureResult mixture_group(const std::vector<std::vector<double>>& res, std::vector<double>& weights,
+                            double density_ratio) {
+  MixtureResult out;
+  out.total = int(res.size());
+  if (res.empty() || int(res.size()) < kMinSampleSize) return out;
+  const int k = int(res[0].size());
+  double prev = std::numeric_limits<double>::max();
+  double ll = 0.0;
+  int outl = 0;
+  for (int it = 0; it < kMaxInnerIterations; ++it) {
+    std::vector<double> S(k * k, 0.0);
+    double W = 0.0;
+    for (size_t i = 0; i < res.size(); ++i) {
+      if (int(res[i].size()) != k) continue;
+      for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b) S[a * k + b] += weights[i] * res[i][a] * res[i][b];
+      W += weights[i];
+    }
+    if (W < 1e-9) return out;
+    for (auto& s : S) s /= W;
+    std::vector<double> inv;
+    double norm, K;
+    mixture_params(S, k, density_ratio, inv, norm, K);
+    ll = 0.0;
+    outl = 0;
+    for (size_t i = 0; i < res.size(); ++i) {
+      if (int(res[i].size()) != k) continue;
+      double m = 0.0;
+      for (int a = 0; a < k; ++a)
+        for (int b = 0; b < k; ++b) m += res[i][a] * inv[a * k + b] * res[i][b];
+      const double p_in = std::exp(-0.5 * m) * norm;
+      ll += std::log(p_in + K);
+      double w = p_in / (p_in + K);
+      w = std::max(kMinWeight, std::min(w, 1.0));
+      weights[i] = w;
+      if (w < 0.5) ++outl;
+    }
+    const double change = std::fabs(ll - prev) / std::fabs(prev);
+    if (change < kConvergenceThreshold) break;
+    prev = ll;
+  }
+  out.log_likelihood = ll;
+  out.outliers = outl;
+  return out;
+}
+
+// Angle-axis rotation of a vector (for the GPS-prior bias transform).
+void rotate_aa(const double* r, const double* p, double* out) {
+  const double th2 = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+  if (th2 < kEps) {
+    out[0] = p[0] + r[1] * p[2] - r[2] * p[1];
+    out[1] = p[1] + r[2] * p[0] - r[0] * p[2];
+    out[2] = p[2] + r[0] * p[1] - r[1] * p[0];
+    return;
+  }
+  const double th = std::sqrt(th2), c = std::cos(th), s = std::sin(th);
+  const double k[3] = {r[0] / th, r[1] / th, r[2] / th};
+  const double kxp[3] = {k[1] * p[2] - k[2] * p[1], k[2] * p[0] - k[0] * p[2], k[0] * p[1] - k[1] * p[0]};
+  const double kp = k[0] * p[0] + k[1] * p[1] + k[2] * p[2];
+  for (int i = 0; i < 3; ++i) out[i] = p[i] * c + kxp[i] * s + k[i] * kp * (1 - c);
+}
+
+double now_seconds() {
+  using clk = std::chrono::steady_clock;
+  return std::chrono::duration<double>(clk::now().time_since_epoch()).count();
+}
+
+}  // namespace
+}  // namespace gbba
+
+namespace gbba {
+namespace {
+
+template <typename R>
+class DeviceSolver final : public SolverBase {
+  using V16 = typename Vec16<R>::type;
+  using PS = typename PointStore<R>::type;
+  static constexpr bool kMixed = sizeof(R) == 4;
+
+ public:
+  SolveSummary solve(Problem& P, const SolverOptions& opts) override;
+  void reprojection(std::vector<double>& errors, std::vector<double>& weights) override {
+    errors = last_errors_;
+    weights = last_weights_;
+  }
+
+ private:
+  // ---- setup
+  void setup(const Problem& P, const SolverOptions& opts);
+  void upload_camera_side(const std::vector<double>& x, bool working, bool fp64);
+  // ---- device passes
+  SolveView<R> view();
+  SceneView<double> view64(bool candidate);
+  double cost_pass(bool candidate, bool store_residuals);
+  void linearize();
+  void point_priors_linearize(bool candidate);
+  // ---- host priors
+  double prior_terms(const std::vector<double>& x, bool want_derivs);
+  double prior_model_change(const std::vector<double>& x, const std::vector<double>& dx);
+  // ---- linear solve
+  int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
+  // ---- IRLS
+  double compute_weights(std::vector<std::string>& groups_report, int& proj_out, int& proj_total,
+                         std::vector<std::pair<std::string, std::pair<int, int>>>& other);
+  // ---- results
+  void finish(Problem& P);
+
+  Problem* prob_ = nullptr;
+  SolverOptions opts_;
+  KernelConfig kc_{};
+  CamLayout cl_{};
+  int n_inst_ = 0, n_rig_ = 0, n_cam_ = 0, n_shots_ = 0;
+  int64_t n_pt_ = 0, n_obs_ = 0, n_slots_ = 0;
+  int n_planes_ = 0;
+  uint64_t plane_mask_ = 0;
+  int cam_tri_stride_ = 0;
+  std::vector<int64_t> slot_obs_;
+  std::vector<double> xc_, xc_cand_;
+  std::vector<uint8_t> cmask_;
+  std::vector<double> pgrad_, pdiag_;
+  std::vector<int> group_count_, group_dim_;
+  std::vector<double> group_ratio_;
+  std::vector<double> prior_weight_cam_, prior_weight_rig_, prior_weight_gps_;
+  std::vector<int> gps_inst_;
+  std::vector<PointPriorDev> point_priors_;
+  std::vector<double> point_prior_w_;
+  double ratio_cam_ = 1e-3, ratio_rig_ = 1e-3, ratio_gps_ = 1e-3, ratio_gcp3d_ = 1e-3;
+  int64_t launches_ = 0;
+  std::vector<double> last_errors_, last_weights_;
+
+  // device state
+  DeviceArray<ObsPack<R>> d_obs_;
+  DeviceArray<ObsPack<double>> d_obs64_;
+  DeviceArray<int> d_obs_point_;
+  DeviceArray<uint8_t> d_gcp_;
+  DeviceArray<R> d_weight_;
+  DeviceArray<double> d_resid_;
+  DeviceArray<V16> d_rec_;
+  // geometry: working precision of the current state (d_geom_, d_cam_), FP64
+  // of the current state (mixed mode only; in FP64 mode d_geom_ is it), FP64
+  // of the candidate state (d_geomc_, d_camc_)
+  DeviceArray<ShotGeom<R>> d_geom_;
+  DeviceArray<ShotGeom<double>> d_geom64_, d_geomc_;
+  DeviceArray<RigGeom<R>> d_rig_;
+  DeviceArray<R> d_cam_;
+  DeviceArray<double> d_cam64_, d_camc_;
+  DeviceArray<int> d_cam_model_, d_shot_inst_, d_shot_rig_, d_shot_cam_;
+  DeviceArray<double> d_inst_pose_, d_rig_pose_;
+  DeviceArray<uint8_t> d_rig_used_;
+  DeviceArray<Point4> d_X_, d_Xc_;
+  DeviceArray<PS> d_Xw_;
+  DeviceArray<uint8_t> d_inst_free_, d_cam_free_, d_rig_free_, d_point_free_, d_cmask_;
+  DeviceArray<R> d_Vp_, d_gp_, d_Vinv_, d_pscale_, d_zbuf_, d_dp_;
+  DeviceArray<R> d_gc_, d_dc_, d_rhs_, d_cscale_, d_damp_;
+  DeviceArray<double> d_pdiag_, d_pgrad_;
+  DeviceArray<R> d_x_, d_r_, d_z_, d_p_, d_y_;
+  DeviceArray<R> d_tri_inst_, d_tri_rig_, d_tri_cam_, d_minv_inst_, d_minv_rig_, d_minv_cam_;
+  DeviceArray<double> d_scal_;
+  DeviceArray<int> d_bad_;
+  DeviceArray<double> d_irls_stats_, d_irls_ll_;
+  DeviceArray<IrlsGroupParams> d_irls_params_;
+  DeviceArray<int> d_group_dim_;
+  DeviceArray<PointPriorDev> d_pp_;
+  DeviceArray<double> d_pp_w_, d_pp_res_;
+};
+
+// ---------------------------------------------------------------------------
+template <typename R>
+void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
+  opts_ = opts;
+  n_inst_ = int(P.instances.size());
+  n_rig_ = int(P.rig_cameras.size());
+  n_cam_ = int(P.cameras.size());
+  n_shots_ = int(P.shots.size());
+  n_pt_ = int64_t(P.points.size());
+  n_obs_ = int64_t(P.observations.size());
+
+  // kernel configuration
+  bool any_sph = false, single = true, any_rig_free = false, any_rig_used = false;
+  int first = -1;
+  for (const Shot& s : P.shots) {
+    const int m = P.cameras[s.camera].model;
+    if (m == kSpherical) any_sph = true;
+    if (first < 0) first = m;
+    else if (m != first) single = false;
+    if (s.rig_camera >= 0 && P.rig_cameras[s.rig_camera].used) {
+      any_rig_used = true;
+      const PoseBlock& rc = P.rig_cameras[s.rig_camera];
+      for (int k = 0; k < 6; ++k) any_rig_free |= rc.free_mask[k] != 0;
+    }
+  }
+  kc_.nr = any_sph ? 3 : 2;
+  kc_.rig = any_rig_free;
+  if (single && !any_sph && !any_rig_used && first >= 0) {
+    kc_.model = first;
+    kc_.cmax = model_num_params(first);
+  } else {
+    kc_.model = kDyn;
+    kc_.cmax = 16;
+  }
+  const int width = kc_.nr + 3 * kc_.nr + 6 * kc_.nr + kc_.cmax * kc_.nr + (kc_.rig ? 6 * kc_.nr : 0);
+  n_planes_ = planes_of<R>(width);
+  bool any_cam_free = false;
+  for (const CameraBlock& c : P.cameras)
+    for (int k = 0; k < c.n; ++k) any_cam_free |= c.free_mask[k] != 0;
+  // planes holding only intrinsics columns are not written when every
+  // camera is fixed
+  plane_mask_ = 0;
+  {
+    const int cam_begin = 10 * kc_.nr;                      // RecordLayout::kCam
+    const int cam_end = cam_begin + kc_.cmax * kc_.nr;      // RecordLayout::kRig
+    const int VN = Vec16<R>::kN;
+    for (int p = 0; p < n_planes_; ++p) {
+      const bool cam_only = p * VN >= cam_begin && (p + 1) * VN <= cam_end;
+      if (!any_cam_free && cam_only) continue;
+      plane_mask_ |= uint64_t(1) << p;
+    }
+  }
+
+  // camera-side layout
+  cl_.n_inst = n_inst_;
+  cl_.n_rig = n_rig_;
+  cl_.n_cam = n_cam_;
+  cl_.rig_base = 8 * n_inst_;
+  cl_.cam_base = cl_.rig_base + 8 * n_rig_;
+  cl_.n = cl_.cam_base + 16 * n_cam_;
+  xc_.assign(cl_.n, 0.0);
+  cmask_.assign(cl_.n, 0);
+  for (int i = 0; i < n_inst_; ++i)
+    for (int k = 0; k < 6; ++k) {
+      xc_[8 * i + k] = P.instances[i].value[k];
+      cmask_[8 * i + k] = P.instances[i].free_mask[k];
+    }
+  for (int r = 0; r < n_rig_; ++r)
+    for (int k = 0; k < 6; ++k) {
+      xc_[cl_.rig_base + 8 * r + k] = P.rig_cameras[r].value[k];
+      cmask_[cl_.rig_base + 8 * r + k] = (P.rig_cameras[r].used && kc_.rig) ? P.rig_cameras[r].free_mask[k] : 0;
+    }
+  for (int c = 0; c < n_cam_; ++c)
+    for (int k = 0; k < P.cameras[c].n; ++k) {
+      xc_[cl_.cam_base + 16 * c + k] = P.cameras[c].value[k];
+      cmask_[cl_.cam_base + 16 * c + k] = P.cameras[c].free_mask[k];
+    }
+
+  // slots: observations sorted by point (stable), padded to a warp multiple
+  std::vector<int64_t> order(n_obs_);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
+    return P.observations[a].point < P.observations[b].point;
+  });
+  n_slots_ = std::max<int64_t>(32, (n_obs_ + 31) / 32 * 32);
+  slot_obs_.assign(n_slots_, -1);
+  std::vector<ObsPack<R>> ob(n_slots_);
+  std::vector<ObsPack<double>> ob64(kMixed ? n_slots_ : 0);
+  std::vector<int> opt(n_slots_, -1);
+  std::vector<uint8_t> gcp(n_slots_, 0);
+  for (int64_t s = 0; s < n_slots_; ++s) {
+    ObsPack<R> o{};
+    ObsPack<double> o64{};
+    if (s < n_obs_) {
+      const Observation& q = P.observations[order[s]];
+      slot_obs_[s] = order[s];
+      o.x = R(q.x); o.y = R(q.y); o.w = R(1.0 / q.std_dev); o.shot = q.shot;
+      o64.x = q.x; o64.y = q.y; o64.w = 1.0 / q.std_dev; o64.shot = q.shot;
+      opt[s] = q.point;
+      gcp[s] = q.is_gcp ? 1 : 0;
+    }
+    ob[s] = o;
+    if (kMixed) ob64[s] = o64;
+  }
+  d_obs_.upload(ob);
+  if (kMixed) d_obs64_.upload(ob64);
+  d_obs_point_.upload(opt);
+  d_gcp_.upload(gcp);
+  d_weight_.resize(n_slots_);
+  {
+    std::vector<R> w(n_slots_, R(1));
+    d_weight_.upload(w);
+  }
+  d_resid_.resize(4 * n_slots_);
+  d_resid_.zero();
+  d_rec_.resize(size_t(n_planes_) * n_slots_);
+  d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
+
+  // shots / cameras / rigs
+  std::vector<int> si(n_shots_), sr(n_shots_), sc(n_shots_);
+  for (int s = 0; s < n_shots_; ++s) {
+    si[s] = P.shots[s].instance;
+    sr[s] = P.shots[s].rig_camera;
+    sc[s] = P.shots[s].camera;
+  }
+  d_shot_inst_.upload(si);
+  d_shot_rig_.upload(sr);
+  d_shot_cam_.upload(sc);
+  std::vector<int> cm(n_cam_);
+  for (int c = 0; c < n_cam_; ++c) cm[c] = P.cameras[c].model;
+  d_cam_model_.upload(cm);
+  std::vector<uint8_t> ru(std::max(1, n_rig_), 0);
+  for (int r = 0; r < n_rig_; ++r) ru[r] = P.rig_cameras[r].used ? 1 : 0;
+  d_rig_used_.upload(ru);
+  d_geom_.resize(std::max(1, n_shots_));
+  if (kMixed) d_geom64_.resize(std::max(1, n_shots_));
+  d_geomc_.resize(std::max(1, n_shots_));
+  if (kc_.rig) d_rig_.resize(std::max(1, n_shots_));
+  d_inst_pose_.resize(std::max(1, n_inst_) * 6);
+  d_rig_pose_.resize(std::max(1, n_rig_) * 6);
+  d_cam_.resize(std::max(1, n_cam_) * 16);
+  if (kMixed) d_cam64_.resize(std::max(1, n_cam_) * 16);
+  d_camc_.resize(std::max(1, n_cam_) * 16);
+
+  // free flags
+  std::vector<uint8_t> fi(std::max(1, n_inst_), 0), fc(std::max(1, n_cam_), 0), fr(std::max(1, n_rig_), 0);
+  for (int i = 0; i < n_inst_; ++i)
+    for (int k = 0; k < 6; ++k) fi[i] |= cmask_[8 * i + k];
+  for (int r = 0; r < n_rig_; ++r)
+    for (int k = 0; k < 6; ++k) fr[r] |= cmask_[cl_.rig_base + 8 * r + k];
+  for (int c = 0; c < n_cam_; ++c)
+    for (int k = 0; k < 16; ++k) fc[c] |= cmask_[cl_.cam_base + 16 * c + k];
+  d_inst_free_.upload(fi);
+  d_cam_free_.upload(fc);
+  d_rig_free_.upload(fr);
+  d_cmask_.upload(cmask_);
+
+  // points
+  std::vector<Point4> X(std::max<int64_t>(1, n_pt_));
+  std::vector<uint8_t> pf(std::max<int64_t>(1, n_pt_), 0);
+  for (int64_t p = 0; p < n_pt_; ++p) {
+    X[p] = Point4{P.points[p].value[0], P.points[p].value[1], P.points[p].value[2], 0.0};
+    pf[p] = P.points[p].free ? 1 : 0;
+  }
+  d_X_.upload(X);
+  d_Xc_.resize(X.size());
+  if (kMixed) d_Xw_.resize(X.size());
+  d_point_free_.upload(pf);
+  const size_t np = X.size();
+  d_Vp_.resize(8 * np);
+  d_gp_.resize(4 * np);
+  d_Vinv_.resize(8 * np);
+  d_pscale_.resize(3 * np);
+  d_zbuf_.resize(4 * np);
+  d_dp_.resize(4 * np);
+  d_dp_.zero();
+
+  // camera-side vectors
+  for (auto* a : {&d_gc_, &d_dc_, &d_rhs_, &d_cscale_, &d_damp_, &d_x_, &d_r_, &d_z_, &d_p_, &d_y_}) a->resize(cl_.n);
+  d_pdiag_.resize(cl_.n);
+  d_pgrad_.resize(cl_.n);
+  d_tri_inst_.resize(24 * std::max(1, n_inst_));
+  d_tri_rig_.resize(24 * std::max(1, n_rig_));
+  cam_tri_stride_ = (kc_.cmax * (kc_.cmax + 1) / 2 + 3) / 4 * 4;
+  d_tri_cam_.resize(size_t(cam_tri_stride_) * std::max(1, n_cam_));
+  d_minv_inst_.resize(64 * std::max(1, n_inst_));
+  d_minv_rig_.resize(64 * std::max(1, n_rig_));
+  d_minv_cam_.resize(256 * std::max(1, n_cam_));
+  d_scal_.resize(8);
+  d_bad_.resize(2);
+
+  // IRLS projection groups: one per shot, plus GCP2D
+  group_count_.assign(n_shots_ + 1, 0);
+  group_dim_.assign(n_shots_ + 1, 2);
+  for (int s = 0; s < n_shots_; ++s) group_dim_[s] = P.cameras[P.shots[s].camera].model == kSpherical ? 3 : 2;
+  int gcp_dim = -1;
+  for (const Observation& q : P.observations) {
+    const int g = q.is_gcp ? n_shots_ : q.shot;
+    group_count_[g]++;
+    if (q.is_gcp && gcp_dim < 0) gcp_dim = group_dim_[q.shot];
+  }
+  if (gcp_dim > 0) group_dim_[n_shots_] = gcp_dim;
+  group_ratio_ = P.group_density_ratio;
+  if (group_ratio_.size() != size_t(n_shots_ + 1)) group_ratio_.assign(n_shots_ + 1, opts.default_density_ratio);
+  d_group_dim_.upload(group_dim_);
+  d_irls_stats_.resize(8 * (n_shots_ + 1));
+  d_irls_ll_.resize(2 * (n_shots_ + 1));
+  d_irls_params_.resize(n_shots_ + 1);
+
+  // priors
+  prior_weight_cam_.assign(n_cam_, 1.0);
+  prior_weight_rig_.assign(n_rig_, 1.0);
+  gps_inst_.clear();
+  for (int i = 0; i < n_inst_; ++i)
+    if (P.instances[i].has_position_prior) gps_inst_.push_back(i);
+  prior_weight_gps_.assign(gps_inst_.size(), 1.0);
+  point_priors_.clear();
+  for (int64_t p = 0; p < n_pt_; ++p) {
+    const PointBlock& b = P.points[p];
+    if (!b.has_prior) continue;
+    PointPriorDev d{};
+    d.point = int(p);
+    d.n = b.has_altitude ? 3 : 2;
+    for (int j = 0; j < 3; ++j) {
+      d.prior[j] = b.prior[j];
+      d.scale[j] = 1.0 / std::max(b.sigma[j], kEps);
+    }
+    point_priors_.push_back(d);
+  }
+  point_prior_w_.assign(point_priors_.size(), 1.0);
+  if (!point_priors_.empty()) {
+    d_pp_.upload(point_priors_);
+    d_pp_w_.upload(point_prior_w_);
+    d_pp_res_.resize(3 * point_priors_.size());
+  }
+  pgrad_.assign(cl_.n, 0.0);
+  pdiag_.assign(cl_.n, 0.0);
+  GB_CUDA(cudaDeviceSynchronize());
+}
+
+// Uploads camera-side FP64 parameters and rebuilds per-shot geometry.
+//   working = true:  geometry of the current state in the working precision
+//                    (linearization) and, with fp64 in mixed mode, its FP64
+//                    copy (cost passes of the current state);
+//   working = false: FP64 geometry of a candidate state (d_geomc_, d_camc_).
+template <typename R>
+void DeviceSolver<R>::upload_camera_side(const std::vector<double>& x, bool working, bool fp64) {
+  std::vector<double> ip(std::max(1, n_inst_) * 6, 0.0), rp(std::max(1, n_rig_) * 6, 0.0);
+  for (int i = 0; i < n_inst_; ++i)
+    for (int k = 0; k < 6; ++k) ip[6 * i + k] = x[8 * i + k];
+  for (int r = 0; r < n_rig_; ++r)
+    for (int k = 0; k < 6; ++k) rp[6 * r + k] = x[cl_.rig_base + 8 * r + k];
+  d_inst_pose_.upload(ip);
+  d_rig_pose_.upload(rp);
+  std::vector<double> cam(std::max(1, n_cam_) * 16, 0.0);
+  for (int c = 0; c < n_cam_; ++c)
+    for (int k = 0; k < 16; ++k) cam[16 * c + k] = x[cl_.cam_base + 16 * c + k];
+  const int blocks = (n_shots_ + 127) / 128;
+  if (working) {
+    std::vector<R> cw(cam.size());
+    for (size_t i = 0; i < cam.size(); ++i) cw[i] = R(cam[i]);
+    d_cam_.upload(cw);
+    if (n_shots_ > 0) {
+      shot_prep_kernel<R><<<blocks, 128>>>(n_shots_, d_shot_inst_.get(), d_shot_rig_.get(), d_shot_cam_.get(),
+                                           d_inst_pose_.get(), d_rig_pose_.get(), d_rig_used_.get(), d_geom_.get(),
+                                           kc_.rig ? d_rig_.get() : nullptr);
+      ++launches_;
+    }
+  }
+  if (fp64 && (kMixed || !working)) {
+    DeviceArray<ShotGeom<double>>& geom = working ? d_geom64_ : d_geomc_;
+    DeviceArray<double>& cams = working ? d_cam64_ : d_camc_;
+    cams.upload(cam);
+    if (n_shots_ > 0) {
+      shot_prep_kernel<double><<<blocks, 128>>>(n_shots_, d_shot_inst_.get(), d_shot_rig_.get(),
+                                                d_shot_cam_.get(), d_inst_pose_.get(), d_rig_pose_.get(),
+                                                d_rig_used_.get(), geom.get(), nullptr);
+      ++launches_;
+    }
+  }
+  GB_CUDA(cudaGetLastError());
+}
+
+template <typename R>
+SolveView<R> DeviceSolver<R>::view() {
+  SolveView<R> v{};
+  SceneView<R>& s = v.scene;
+  s.n_slots = n_slots_;
+  s.n_cameras = n_cam_;
+  s.geom = d_geom_.get();
+  s.rig = kc_.rig ? d_rig_.get() : nullptr;
+  s.cam_model = d_cam_model_.get();
+  s.cam_params = d_cam_.get();
+  if constexpr (kMixed) s.points = d_Xw_.get();
+  else s.points = reinterpret_cast<const PS*>(d_X_.get());
+  s.obs = d_obs_.get();
+  s.obs_point = d_obs_point_.get();
+  v.rec = d_rec_.get();
+  v.stride = n_slots_;
+  v.weight = d_weight_.get();
+  v.loss = opts_.loss;
+  v.loss_a = R(opts_.loss_threshold);
+  v.cl = cl_;
+  v.inst_free = d_inst_free_.get();
+  v.cam_free = d_cam_free_.get();
+  v.rig_free = d_rig_free_.get();
+  v.point_free = d_point_free_.get();
+  v.Vp = d_Vp_.get();
+  v.gp = d_gp_.get();
+  v.Vinv = d_Vinv_.get();
+  v.gc = d_gc_.get();
+  v.dc = d_dc_.get();
+  return v;
+}
+
+template <typename R>
+SceneView<double> DeviceSolver<R>::view64(bool candidate) {
+  SceneView<double> s{};
+  s.n_slots = n_slots_;
+  s.n_cameras = n_cam_;
+  s.rig = nullptr;  // the cost kernels evaluate residuals only
+  if (candidate) {
+    s.geom = d_geomc_.get();
+    s.cam_params = d_camc_.get();
+  } else if constexpr (kMixed) {
+    s.geom = d_geom64_.get();
+    s.cam_params = d_cam64_.get();
+  } else {
+    s.geom = reinterpret_cast<const ShotGeom<double>*>(d_geom_.get());
+    s.cam_params = reinterpret_cast<const double*>(d_cam_.get());
+  }
+  if constexpr (kMixed) s.obs = d_obs64_.get();
+  else s.obs = reinterpret_cast<const ObsPack<double>*>(d_obs_.get());
+  s.cam_model = d_cam_model_.get();
+  s.points = candidate ? d_Xc_.get() : d_X_.get();
+  s.obs_point = d_obs_point_.get();
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+template <typename R>
+struct CostLaunch {
+  SceneView<double> s;
+  const R* w;
+  int loss;
+  double a;
+  double* resid;
+  double* out;
+  template <int M, int NR, int CMAX, bool RIG>
+  void run() {
+    const float* wf = nullptr;
+    const double* wd = nullptr;
+    if constexpr (sizeof(R) == 4) wf = reinterpret_cast<const float*>(w);
+    else wd = reinterpret_cast<const double*>(w);
+    cost_kernel<M, NR, CMAX, RIG><<<slot_grid(s.n_slots), 256>>>(s, wf, wd, loss, a, resid, out);
+  }
+};
+
+// FP64 cost of the current (or candidate) state; projection part on the
+// device, priors on the host.
+template <typename R>
+double DeviceSolver<R>::cost_pass(bool candidate, bool store_residuals) {
+  GB_CUDA(cudaMemset(d_scal_.get() + 6, 0, 2 * sizeof(double)));
+  CostLaunch<R> f{view64(candidate), d_weight_.get(), opts_.loss, opts_.loss_threshold,
+                  store_residuals ? d_resid_.get() : nullptr, d_scal_.get() + 6};
+  dispatch_config(kc_, f);
+  ++launches_;
+  if (!point_priors_.empty()) {
+    point_prior_cost_kernel<<<elem_grid(int64_t(point_priors_.size())), 256>>>(
+        int(point_priors_.size()), d_pp_.get(), d_pp_w_.get(), candidate ? d_Xc_.get() : d_X_.get(),
+        d_pp_res_.get(), d_scal_.get() + 7);
+    ++launches_;
+  }
+  GB_CUDA(cudaGetLastError());
+  double c[2];
+  GB_CUDA(cudaMemcpy(c, d_scal_.get() + 6, sizeof(c), cudaMemcpyDeviceToHost));
+  return c[0] + c[1] + prior_terms(candidate ? xc_cand_ : xc_, false);
+}
+
+template <typename R>
+struct LinearizeLaunch {
+  SolveView<R> v;
+  uint64_t mask;
+  template <int M, int NR, int CMAX, bool RIG>
+  void run() {
+    linearize_kernel<R, M, NR, CMAX, RIG><<<slot_grid(v.scene.n_slots), 256>>>(v, mask);
+  }
+};
+
+template <typename R>
+void DeviceSolver<R>::linearize() {
+  d_Vp_.zero();
+  d_gp_.zero();
+  d_gc_.zero();
+  d_dc_.zero();
+  LinearizeLaunch<R> f{view(), plane_mask_};
+  dispatch_config(kc_, f);
+  ++launches_;
+  if (!point_priors_.empty()) {
+    point_prior_linearize_kernel<R><<<elem_grid(int64_t(point_priors_.size())), 256>>>(
+        int(point_priors_.size()), d_pp_.get(), d_pp_w_.get(), d_X_.get(), d_point_free_.get(), d_Vp_.get(),
+        d_gp_.get());
+    ++launches_;
+  }
+  GB_CUDA(cudaGetLastError());
+  prior_terms(xc_, true);
+  d_pgrad_.upload(pgrad_);
+  d_pdiag_.upload(pdiag_);
+}
+
+// Camera, rig-camera and GPS priors at camera-side state x (FP64, host).
+// Returns their cost; with want_derivs also fills pgrad_ / pdiag_ (J^T r and
+// diag(J^T J); every prior Jacobian is diagonal).
+//   camera   DataPriorError<Camera>, LOG scale for focal and aspect ratio
+//            (bundle_adjuster.cc:643-668, prior_error.h:54-93)
+//   rig cam  DataPriorError<Pose> on all six parameters (:839-851)
+//   GPS      DataPriorError<Pose, SimilarityPriorTransform> on TX TY TZ with
+//            the camera bias applied to the prior (:806-838, bias.h:34-54)
+template <typename R>
+double DeviceSolver<R>::prior_terms(const std::vector<double>& x, bool want_derivs) {
+  const Problem& P = *prob_;
+  if (want_derivs) {
+    std::fill(pgrad_.begin(), pgrad_.end(), 0.0);
+    std::fill(pdiag_.begin(), pdiag_.end(), 0.0);
+  }
+  double cost = 0.0;
+  for (int c = 0; c < n_cam_; ++c) {
+    const CameraBlock& cb = P.cameras[c];
+    const double w = prior_weight_cam_[c];
+    for (int k = 0; k < cb.n; ++k) {
+      const int j = cl_.cam_base + 16 * c + k;
+      const double scale = 1.0 / std::max(cb.sigma[k], kEps);
+      const double v = x[j];
+      double r, J;
+      if (cb.log_prior[k]) {
+        r = scale * std::log(v / cb.prior[k]);
+        J = scale / v;
+      } else {
+        r = scale * (v - cb.prior[k]);
+        J = scale;
+      }
+      cost += 0.5 * w * r * r;
+      if (want_derivs && cmask_[j]) {
+        pgrad_[j] += w * J * r;
+        pdiag_[j] += w * J * J;
+      }
+    }
+  }
+  for (int rc = 0; rc < n_rig_; ++rc) {
+    const PoseBlock& b = P.rig_cameras[rc];
+    if (!b.has_prior) continue;
+    const double w = prior_weight_rig_[rc];
+    for (int k = 0; k < 6; ++k) {
+      const int j = cl_.rig_base + 8 * rc + k;
+      const double scale = 1.0 / std::max(b.sigma[k], kEps);
+      const double r = scale * (x[j] - b.prior[k]);
+      cost += 0.5 * w * r * r;
+      if (want_derivs && cmask_[j]) {
+        pgrad_[j] += w * scale * r;
+        pdiag_[j] += w * scale * scale;
+      }
+    }
+  }
+  for (size_t g = 0; g < gps_inst_.size(); ++g) {
+    const int i = gps_inst_[g];
+    const PoseBlock& b = P.instances[i];
+    double prior[3] = {b.position_prior[0], b.position_prior[1], b.position_prior[2]};
+    if (b.bias_camera >= 0) {
+      const Bias& bs = P.biases[b.bias_camera];
+      double rp[3];
+      rotate_aa(bs.r, prior, rp);
+      for (int k = 0; k < 3; ++k) prior[k] = bs.s * rp[k] + bs.t[k];
+    }
+    const double w = prior_weight_gps_[g];
+    for (int k = 0; k < 3; ++k) {
+      const int j = 8 * i + 3 + k;
+      const double scale = 1.0 / std::max(b.position_sigma[k], kEps);
+      const double r = scale * (x[j] - prior[k]);
+      cost += 0.5 * w * r * r;
+      if (want_derivs && cmask_[j]) {
+        pgrad_[j] += w * scale * r;
+        pdiag_[j] += w * scale * scale;
+      }
+    }
+  }
+  return cost;
+}
+
+// Linear-model decrease of the priors for a camera-side step dx.
+template <typename R>
+double DeviceSolver<R>::prior_model_change(const std::vector<double>& x, const std::vector<double>& dx) {
+  // every prior residual depends on one coordinate: r(x + d) ~ r + J d
+  double total = 0.0;
+  const Problem& P = *prob_;
+  auto term = [&](double w, double r, double J, double d) { return -0.5 * w * (J * d) * (2.0 * r + J * d); };
+  for (int c = 0; c < n_cam_; ++c) {
+    const CameraBlock& cb = P.cameras[c];
+    for (int k = 0; k < cb.n; ++k) {
+      const int j = cl_.cam_base + 16 * c + k;
+      if (!cmask_[j]) continue;
+      const double scale = 1.0 / std::max(cb.sigma[k], kEps);
+      const double v = x[j];
+      const double r = cb.log_prior[k] ? scale * std::log(v / cb.prior[k]) : scale * (v - cb.prior[k]);
+      const double J = cb.log_prior[k] ? scale / v : scale;
+      total += term(prior_weight_cam_[c], r, J, dx[j]);
+    }
+  }
+  for (int rc = 0; rc < n_rig_; ++rc) {
+    const PoseBlock& b = P.rig_cameras[rc];
+    if (!b.has_prior) continue;
+    for (int k = 0; k < 6; ++k) {
+      const int j = cl_.rig_base + 8 * rc + k;
+      if (!cmask_[j]) continue;
+      const double scale = 1.0 / std::max(b.sigma[k], kEps);
+      total += term(prior_weight_rig_[rc], scale * (x[j] - b.prior[k]), scale, dx[j]);
+    }
+  }
+  for (size_t g = 0; g < gps_inst_.size(); ++g) {
+    const int i = gps_inst_[g];
+    const PoseBlock& b = P.instances[i];
+    double prior[3] = {b.position_prior[0], b.position_prior[1], b.position_prior[2]};
+    if (b.bias_camera >= 0) {
+      const Bias& bs = P.biases[b.bias_camera];
+      double rp[3];
+      rotate_aa(bs.r, prior, rp);
+      for (int k = 0; k < 3; ++k) prior[k] = bs.s * rp[k] + bs.t[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+      const int j = 8 * i + 3 + k;
+      if (!cmask_[j]) continue;
+      const double scale = 1.0 / std::max(b.position_sigma[k], kEps);
+      total += term(prior_weight_gps_[g], scale * (x[j] - prior[k]), scale, dx[j]);
+    }
+  }
+  return total;
+}
+
+}  // namespace
+}  // namespace gbba
+
+#include "solver_loop.inc"

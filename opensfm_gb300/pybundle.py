@@ -1,0 +1,438 @@
+"""Drop-in for ``opensfm.pybundle`` (bundle adjustment on the GPU).
+
+``BundleAdjuster`` has the method names, argument order and error behaviour
+of the reference's pybind module (opensfm/src/lib/bundle/python/pybind.cc:
+60-147, pybundle.pyi:31-134) and forwards every call to the C ABI of
+libgbba.so (include/gbba.h).  Unknown ids raise ``RuntimeError``, an unknown
+shot or point in ``add_point_projection_observation`` raises ``IndexError``
+(std::out_of_range in the reference).
+
+Beyond the reference's methods it exposes bulk (numpy) adders for large
+problems, the precision / IRLS switches of the GPU solver and the iteration
+trace.  Constraint types that the GPU solver does not implement (relative
+motions, absolute up-vector / pan / tilt / roll, linear motion, heatmaps,
+common positions, reconstruction scales, gauge fixing) raise
+``NotImplementedError`` instead of being silently ignored.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import _lib
+from .pygeometry import Camera, Pose
+
+_D = C.POINTER(C.c_double)
+_I32 = C.POINTER(C.c_int32)
+_U8 = C.POINTER(C.c_uint8)
+_H = C.c_void_p
+
+
+class Summary(C.Structure):
+    _fields_ = [("initial_cost", C.c_double), ("final_cost", C.c_double), ("seconds", C.c_double),
+                ("linear_solver_seconds", C.c_double), ("jacobian_seconds", C.c_double),
+                ("residual_seconds", C.c_double), ("iterations", C.c_int), ("successful_steps", C.c_int),
+                ("unsuccessful_steps", C.c_int), ("usable", C.c_int), ("kernel_launches", C.c_int64)]
+
+
+def _declare(L) -> None:
+    if getattr(L, "_gbba_adjuster_declared", False):
+        return
+    S = C.c_char_p
+    sig = {
+        "gbba_create": ([], _H),
+        "gbba_destroy": ([_H], None),
+        "gbba_add_camera": ([_H, S, C.c_int, _D, _D, C.c_int, C.c_int], C.c_int),
+        "gbba_set_camera_bias": ([_H, S, _D, _D, C.c_double], C.c_int),
+        "gbba_add_rig_camera": ([_H, S, _D, _D, C.c_int], C.c_int),
+        "gbba_add_rig_instance": ([_H, S, _D, C.c_int, C.POINTER(S), C.POINTER(S), C.POINTER(S), C.c_int], C.c_int),
+        "gbba_add_rig_instance_position_prior": ([_H, S, _D, _D, S], C.c_int),
+        "gbba_add_point": ([_H, S, _D, C.c_int], C.c_int),
+        "gbba_add_point_prior": ([_H, S, _D, _D, C.c_int], C.c_int),
+        "gbba_add_point_projection_observation": ([_H, S, S, _D, C.c_double, C.c_int], C.c_int),
+        "gbba_shot_index": ([_H, S], C.c_int64),
+        "gbba_point_index": ([_H, S], C.c_int64),
+        "gbba_add_points_bulk": ([_H, C.c_int64, _D, _U8, C.POINTER(S), C.POINTER(C.c_int64)], C.c_int),
+        "gbba_add_point_projection_observations_bulk": ([_H, C.c_int64, _I32, _I32, _D, _D, _U8], C.c_int),
+        "gbba_set_point_projection_loss_function": ([_H, S, C.c_double], C.c_int),
+        "gbba_set_irls_mode": ([_H, C.c_int], C.c_int),
+        "gbba_set_precision": ([_H, C.c_int], C.c_int),
+        "gbba_set_max_num_iterations": ([_H, C.c_int], C.c_int),
+        "gbba_set_num_threads": ([_H, C.c_int], C.c_int),
+        "gbba_set_use_analytic_derivatives": ([_H, C.c_int], C.c_int),
+        "gbba_set_linear_solver_type": ([_H, S], C.c_int),
+        "gbba_set_internal_parameters_prior_sd": ([_H] + [C.c_double] * 9, C.c_int),
+        "gbba_set_rig_parameters_prior_sd": ([_H, C.c_double, C.c_double], C.c_int),
+        "gbba_set_compute_reprojection_errors": ([_H, C.c_int], C.c_int),
+        "gbba_set_compute_covariances": ([_H, C.c_int], C.c_int),
+        "gbba_get_covariance_estimation_valid": ([_H], C.c_int),
+        "gbba_set_skip_initial_reweighting": ([_H, C.c_int], C.c_int),
+        "gbba_set_default_density_ratio": ([_H, C.c_double], C.c_int),
+        "gbba_get_default_density_ratio": ([_H], C.c_double),
+        "gbba_set_group_density_ratio": ([_H, S, C.c_double], C.c_int),
+        "gbba_get_group_density_ratio": ([_H, S], C.c_double),
+        "gbba_set_pcg_tolerance": ([_H, C.c_double], C.c_int),
+        "gbba_run": ([_H], C.c_int),
+        "gbba_get_camera": ([_H, S, C.POINTER(C.c_int), _D, C.c_int, C.POINTER(C.c_int)], C.c_int),
+        "gbba_get_rig_instance_pose": ([_H, S, _D], C.c_int),
+        "gbba_get_rig_camera_pose": ([_H, S, _D], C.c_int),
+        "gbba_get_point": ([_H, S, _D], C.c_int),
+        "gbba_has_point": ([_H, S], C.c_int),
+        "gbba_num_projections": ([_H], C.c_int64),
+        "gbba_num_points": ([_H], C.c_int64),
+        "gbba_get_points_bulk": ([_H, C.c_int64, C.c_int64, _D], C.c_int),
+        "gbba_get_projection_results": ([_H, C.c_int64, _D, _D, _I32], C.c_int),
+        "gbba_brief_report": ([_H, C.c_char_p, C.c_size_t], C.c_int),
+        "gbba_full_report": ([_H, C.c_char_p, C.c_size_t], C.c_int),
+        "gbba_irls_report": ([_H, C.c_char_p, C.c_size_t], C.c_int),
+        "gbba_get_summary": ([_H, C.POINTER(Summary)], C.c_int),
+        "gbba_get_trace": ([_H, C.c_int, _D, C.POINTER(C.c_int)], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    L._gbba_adjuster_declared = True
+
+
+def _b(s) -> bytes:
+    if isinstance(s, bytes):
+        return s
+    return str(s).encode("utf-8")
+
+
+def _vec(x, n: int) -> np.ndarray:
+    a = np.ascontiguousarray(np.asarray(x, dtype=np.float64).reshape(-1))
+    if a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+class Point:
+    """Result view of a point (bundle::Point, python/pybind.cc:51-58)."""
+
+    def __init__(self, id: str, p: np.ndarray):
+        self.id = id
+        self.p = p
+        self.reprojection_errors: Dict[str, np.ndarray] = {}
+        self.reprojection_weights: Dict[str, float] = {}
+
+
+class BundleAdjuster:
+    """GPU bundle adjuster with the reference's pybind surface."""
+
+    def __init__(self) -> None:
+        self._L = _lib.lib()
+        _declare(self._L)
+        self._h = self._L.gbba_create()
+        if not self._h:
+            raise RuntimeError(self._L.gbba_last_error().decode())
+        self._obs_keys: list = []      # (shot id, point id) per observation, when known
+        self._shot_ids: list = []      # index -> id
+        self._point_ids: Optional[list] = []
+
+    def __del__(self) -> None:
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.gbba_destroy(h)
+            self._h = None
+
+    def _check(self, status: int) -> None:
+        _lib.check(status)
+
+    # -- cameras / rigs / points ------------------------------------------
+    def add_camera(self, id: str, camera: Camera, prior: Camera, constant: bool) -> None:
+        v = np.ascontiguousarray(camera.get_parameters_values(), np.float64)
+        p = np.ascontiguousarray(prior.get_parameters_values(), np.float64)
+        self._check(self._L.gbba_add_camera(self._h, _b(id), camera.model, _dp(v), _dp(p), v.size, int(constant)))
+
+    def get_camera(self, id: str) -> Camera:
+        vals = np.zeros(16)
+        model = C.c_int(0)
+        n = C.c_int(0)
+        self._check(self._L.gbba_get_camera(self._h, _b(id), C.byref(model), _dp(vals), 16, C.byref(n)))
+        cam = Camera(model.value, vals[: n.value])
+        cam.id = id if isinstance(id, str) else id.decode()
+        return cam
+
+    def set_camera_bias(self, id: str, bias, parameters_to_optimize=()) -> None:
+        if parameters_to_optimize:
+            raise NotImplementedError("optimising camera biases is not implemented by the GPU bundle adjuster")
+        r = _vec(bias.rotation, 3)
+        t = _vec(bias.translation, 3)
+        self._check(self._L.gbba_set_camera_bias(self._h, _b(id), _dp(r), _dp(t), float(bias.scale)))
+
+    def get_bias(self, id: str):
+        raise NotImplementedError("get_bias: camera biases are held fixed by the GPU bundle adjuster")
+
+    def add_rig_camera(self, id: str, pose: Pose, pose_prior: Pose, fixed: bool) -> None:
+        a = np.ascontiguousarray(pose.ba_data())
+        b = np.ascontiguousarray(pose_prior.ba_data())
+        self._check(self._L.gbba_add_rig_camera(self._h, _b(id), _dp(a), _dp(b), int(fixed)))
+
+    def get_rig_camera_pose(self, id: str) -> Pose:
+        d = np.zeros(6)
+        self._check(self._L.gbba_get_rig_camera_pose(self._h, _b(id), _dp(d)))
+        return Pose.from_ba_data(d)
+
+    def add_rig_instance(self, id: str, pose: Pose, shot_cameras: Dict[str, str],
+                         shot_rig_cameras: Dict[str, str], fixed: bool) -> None:
+        shots = list(shot_cameras.keys())
+        missing = [s for s in shots if s not in shot_rig_cameras]
+        if missing:
+            raise IndexError(f"unordered_map::at: shot {missing[0]} has no rig camera")
+        n = len(shots)
+        arr = C.c_char_p * max(n, 1)
+        s_arr = arr(*[_b(s) for s in shots])
+        c_arr = arr(*[_b(shot_cameras[s]) for s in shots])
+        r_arr = arr(*[_b(shot_rig_cameras[s]) for s in shots])
+        d = np.ascontiguousarray(pose.ba_data())
+        self._check(self._L.gbba_add_rig_instance(self._h, _b(id), _dp(d), n, s_arr, c_arr, r_arr, int(fixed)))
+        for s in shots:
+            if s not in self._shot_ids:
+                self._shot_ids.append(s)
+
+    def get_rig_instance_pose(self, id: str) -> Pose:
+        d = np.zeros(6)
+        self._check(self._L.gbba_get_rig_instance_pose(self._h, _b(id), _dp(d)))
+        return Pose.from_ba_data(d)
+
+    def add_rig_instance_position_prior(self, id: str, position, std_deviation, scale_group: str) -> None:
+        p = _vec(position, 3)
+        s = _vec(std_deviation, 3)
+        self._check(self._L.gbba_add_rig_instance_position_prior(self._h, _b(id), _dp(p), _dp(s), _b(scale_group)))
+
+    def add_point(self, id: str, position, constant: bool) -> None:
+        p = _vec(position, 3)
+        self._check(self._L.gbba_add_point(self._h, _b(id), _dp(p), int(constant)))
+        if self._point_ids is not None:
+            self._point_ids.append(id)
+
+    def add_point_prior(self, id: str, position, std_deviation, has_altitude: bool) -> None:
+        p = _vec(position, 3)
+        s = _vec(std_deviation, 3)
+        self._check(self._L.gbba_add_point_prior(self._h, _b(id), _dp(p), _dp(s), int(has_altitude)))
+
+    def has_point(self, id: str) -> bool:
+        return bool(self._L.gbba_has_point(self._h, _b(id)))
+
+    def get_point(self, id: str) -> Point:
+        d = np.zeros(3)
+        self._check(self._L.gbba_get_point(self._h, _b(id), _dp(d)))
+        pt = Point(id, d)
+        if self._obs_keys:
+            errs, w, dims = self._projection_results()
+            for k, (s, p) in enumerate(self._obs_keys):
+                if p == id:
+                    pt.reprojection_errors[s] = errs[k, : dims[k]].copy()
+                    pt.reprojection_weights[s] = float(w[k])
+        return pt
+
+    def add_point_projection_observation(self, shot: str, point: str, observation, std_deviation: float,
+                                         is_gcp: bool = False, depth_prior=None) -> None:
+        if depth_prior is not None:
+            raise NotImplementedError("depth priors are not implemented by the GPU bundle adjuster")
+        o = _vec(observation, 2)
+        self._check(self._L.gbba_add_point_projection_observation(self._h, _b(shot), _b(point), _dp(o),
+                                                                  float(std_deviation), int(is_gcp)))
+        self._obs_keys.append((shot, point))
+
+    # -- bulk interface (raw-index path of BAHelpers) ----------------------
+    def shot_index(self, shot: str) -> int:
+        return int(self._L.gbba_shot_index(self._h, _b(shot)))
+
+    def point_index(self, point: str) -> int:
+        return int(self._L.gbba_point_index(self._h, _b(point)))
+
+    def add_points(self, positions: np.ndarray, constant: Optional[np.ndarray] = None) -> int:
+        """Adds points with ids "<index>"; returns the first index."""
+        xyz = np.ascontiguousarray(positions, np.float64).reshape(-1, 3)
+        c = None if constant is None else np.ascontiguousarray(constant, np.uint8)
+        first = C.c_int64(0)
+        self._check(self._L.gbba_add_points_bulk(self._h, len(xyz), _dp(xyz),
+                                                  None if c is None else c.ctypes.data_as(_U8), None,
+                                                  C.byref(first)))
+        self._point_ids = None
+        return int(first.value)
+
+    def add_point_projection_observations(self, shot_index, point_index, observations, std_deviation,
+                                          is_gcp=None) -> None:
+        s = np.ascontiguousarray(shot_index, np.int32)
+        p = np.ascontiguousarray(point_index, np.int32)
+        xy = np.ascontiguousarray(observations, np.float64).reshape(-1, 2)
+        sd = np.ascontiguousarray(np.broadcast_to(np.asarray(std_deviation, np.float64), (len(s),)))
+        g = None if is_gcp is None else np.ascontiguousarray(is_gcp, np.uint8)
+        self._check(self._L.gbba_add_point_projection_observations_bulk(
+            self._h, len(s), s.ctypes.data_as(_I32), p.ctypes.data_as(_I32), _dp(xy), _dp(sd),
+            None if g is None else g.ctypes.data_as(_U8)))
+        self._obs_keys = []
+
+    def get_points(self) -> np.ndarray:
+        n = int(self._L.gbba_num_points(self._h))
+        out = np.zeros((n, 3))
+        self._check(self._L.gbba_get_points_bulk(self._h, 0, n, _dp(out)))
+        return out
+
+    def _projection_results(self):
+        n = int(self._L.gbba_num_projections(self._h))
+        errs = np.zeros((n, 3))
+        w = np.zeros(n)
+        dims = np.zeros(n, np.int32)
+        self._check(self._L.gbba_get_projection_results(self._h, n, _dp(errs), _dp(w), dims.ctypes.data_as(_I32)))
+        return errs, w, dims
+
+    def projection_results(self):
+        """(errors [n, 3], weights [n], dims [n]) per observation in insertion order."""
+        return self._projection_results()
+
+    # -- settings -----------------------------------------------------------
+    def set_point_projection_loss_function(self, name: str, threshold: float) -> None:
+        self._check(self._L.gbba_set_point_projection_loss_function(self._h, _b(name), float(threshold)))
+
+    def set_irls_mode(self, mode: str) -> None:
+        self._check(self._L.gbba_set_irls_mode(self._h, {"none": 0, "mixture": 1}[mode]))
+
+    def set_precision(self, precision: str) -> None:
+        self._check(self._L.gbba_set_precision(self._h, {"fp64": 0, "mixed": 1}[precision]))
+
+    def set_pcg_tolerance(self, tolerance: float) -> None:
+        self._check(self._L.gbba_set_pcg_tolerance(self._h, float(tolerance)))
+
+    def set_max_num_iterations(self, n: int) -> None:
+        self._check(self._L.gbba_set_max_num_iterations(self._h, int(n)))
+
+    def set_num_threads(self, n: int) -> None:
+        self._check(self._L.gbba_set_num_threads(self._h, int(n)))
+
+    def set_use_analytic_derivatives(self, use: bool) -> None:
+        self._check(self._L.gbba_set_use_analytic_derivatives(self._h, int(use)))
+
+    def set_linear_solver_type(self, t: str) -> None:
+        self._check(self._L.gbba_set_linear_solver_type(self._h, _b(t)))
+
+    def set_internal_parameters_prior_sd(self, focal_sd, aspect_ratio_sd, c_sd, k1_sd, k2_sd, p1_sd, p2_sd, k3_sd,
+                                         k4_sd) -> None:
+        self._check(self._L.gbba_set_internal_parameters_prior_sd(
+            self._h, focal_sd, aspect_ratio_sd, c_sd, k1_sd, k2_sd, p1_sd, p2_sd, k3_sd, k4_sd))
+
+    def set_compute_reprojection_errors(self, v: bool) -> None:
+        self._check(self._L.gbba_set_compute_reprojection_errors(self._h, int(v)))
+
+    def set_compute_covariances(self, v: bool) -> None:
+        self._check(self._L.gbba_set_compute_covariances(self._h, int(v)))
+
+    def get_covariance_estimation_valid(self) -> bool:
+        return bool(self._L.gbba_get_covariance_estimation_valid(self._h))
+
+    def set_skip_initial_reweighting(self, v: bool) -> None:
+        self._check(self._L.gbba_set_skip_initial_reweighting(self._h, int(v)))
+
+    def set_default_density_ratio(self, r: float) -> None:
+        self._check(self._L.gbba_set_default_density_ratio(self._h, float(r)))
+
+    def get_default_density_ratio(self) -> float:
+        return float(self._L.gbba_get_default_density_ratio(self._h))
+
+    def set_group_density_ratio(self, group: str, r: float) -> None:
+        self._check(self._L.gbba_set_group_density_ratio(self._h, _b(group), float(r)))
+
+    def get_group_density_ratio(self, group: str) -> float:
+        return float(self._L.gbba_get_group_density_ratio(self._h, _b(group)))
+
+    # -- run and reports ----------------------------------------------------
+    def run(self) -> None:
+        self._check(self._L.gbba_run(self._h))
+
+    def _report(self, fn) -> str:
+        n = fn(self._h, None, 0)
+        if n < 0:
+            raise RuntimeError(self._L.gbba_last_error().decode())
+        buf = C.create_string_buffer(n + 1)
+        fn(self._h, buf, n + 1)
+        return buf.value.decode("utf-8", "replace")
+
+    def brief_report(self) -> str:
+        return self._report(self._L.gbba_brief_report)
+
+    def full_report(self) -> str:
+        return self._report(self._L.gbba_full_report)
+
+    def irls_report(self) -> list:
+        text = self._report(self._L.gbba_irls_report)
+        return text.split("\n") if text else []
+
+    def summary(self) -> dict:
+        s = Summary()
+        self._check(self._L.gbba_get_summary(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in Summary._fields_}
+
+    def trace(self) -> np.ndarray:
+        """Iteration records [iteration, cost, seconds, success, linear iterations,
+        radius, relative decrease, step norm]."""
+        n = C.c_int(0)
+        self._check(self._L.gbba_get_trace(self._h, 0, None, C.byref(n)))
+        out = np.zeros((n.value, 8))
+        self._check(self._L.gbba_get_trace(self._h, n.value, _dp(out), C.byref(n)))
+        return out
+
+    # -- constraint types outside the GPU solver ---------------------------
+    def _unsupported(self, *args, **kwargs):
+        raise NotImplementedError("this constraint type is not implemented by the GPU bundle adjuster")
+
+    add_relative_motion = _unsupported
+    add_relative_rotation = _unsupported
+    add_common_position = _unsupported
+    add_heatmap = _unsupported
+    add_absolute_position_heatmap = _unsupported
+    add_absolute_up_vector = _unsupported
+    add_absolute_pan = _unsupported
+    add_absolute_tilt = _unsupported
+    add_absolute_roll = _unsupported
+    add_linear_motion = _unsupported
+    set_gauge_fix_shots = _unsupported
+    add_reconstruction = _unsupported
+    add_reconstruction_instance = _unsupported
+    set_scale_sharing = _unsupported
+    get_reconstruction = _unsupported
+    set_relative_motion_loss_function = _unsupported
+    set_adjust_absolute_position_std = _unsupported
+
+
+def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
+                        gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
+                        pcg_tolerance: Optional[float] = None) -> BundleAdjuster:
+    """Builds a BundleAdjuster from a SceneArrays (bulk path)."""
+    ba = BundleAdjuster()
+    ba.set_precision(precision)
+    ba.set_irls_mode(irls)
+    ba.set_max_num_iterations(max_iterations)
+    if pcg_tolerance is not None:
+        ba.set_pcg_tolerance(pcg_tolerance)
+    if loss is not None:
+        ba.set_point_projection_loss_function(*loss)
+    for c in range(len(scene.camera_projection)):
+        m = int(scene.camera_projection[c])
+        from .scene import NUM_PARAMS
+        cam = Camera(m, scene.camera_values[c, : NUM_PARAMS[m]])
+        ba.add_camera(str(c), cam, cam, constant_cameras)
+    ba.add_rig_camera("rig", Pose(), Pose(), True)
+    for s in range(len(scene.shot_camera)):
+        inst = int(scene.shot_rig_instance[s])
+        pose = Pose.from_ba_data(scene.rig_instance_poses[inst])
+        ba.add_rig_instance(str(inst), pose, {str(s): str(int(scene.shot_camera[s]))}, {str(s): "rig"}, False)
+    if gps and "gps" in scene.extras:
+        for s in range(len(scene.shot_camera)):
+            ba.add_rig_instance_position_prior(str(int(scene.shot_rig_instance[s])), scene.extras["gps"][s],
+                                               scene.extras["gps_std"][s], "")
+    ba.add_points(scene.points)
+    ba.add_point_projection_observations(scene.obs_shot, scene.obs_point, scene.obs_xy, scene.obs_std)
+    return ba
+
+
+__all__ = ["BundleAdjuster", "Point", "adjuster_from_scene"]

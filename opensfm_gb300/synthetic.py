@@ -37,15 +37,45 @@ def rotation_matrix(aa: np.ndarray) -> np.ndarray:
 
 
 def rotation_vector(Rm: np.ndarray) -> np.ndarray:
-    """Angle-axis vectors of rotation matrices [..., 3, 3] (angles < pi)."""
+    """Angle-axis vectors of rotation matrices [..., 3, 3].
+
+    Goes through a unit quaternion built with Shepperd's method (the largest
+    of w, x, y, z is computed from the diagonal), which stays accurate for
+    angles near pi."""
     Rm = np.asarray(Rm, np.float64)
-    tr = np.clip((np.trace(Rm, axis1=-2, axis2=-1) - 1) / 2, -1.0, 1.0)
-    th = np.arccos(tr)
-    v = np.stack([Rm[..., 2, 1] - Rm[..., 1, 2], Rm[..., 0, 2] - Rm[..., 2, 0],
-                  Rm[..., 1, 0] - Rm[..., 0, 1]], axis=-1)
-    s = np.sin(th)
-    f = np.where(s > 1e-12, th / (2 * np.where(s > 1e-12, s, 1.0)), 0.5)
-    return v * f[..., None]
+    shape = Rm.shape[:-2]
+    M = Rm.reshape(-1, 3, 3)
+    tr = M[:, 0, 0] + M[:, 1, 1] + M[:, 2, 2]
+    cand = np.stack([tr, M[:, 0, 0], M[:, 1, 1], M[:, 2, 2]], axis=-1)
+    k = np.argmax(cand, axis=-1)
+    q = np.zeros((len(M), 4))
+    for case in range(4):
+        m = k == case
+        if not np.any(m):
+            continue
+        A = M[m]
+        if case == 0:
+            s = np.sqrt(1.0 + tr[m]) * 2
+            q[m] = np.stack([0.25 * s, (A[:, 2, 1] - A[:, 1, 2]) / s, (A[:, 0, 2] - A[:, 2, 0]) / s,
+                             (A[:, 1, 0] - A[:, 0, 1]) / s], -1)
+        elif case == 1:
+            s = np.sqrt(1.0 + A[:, 0, 0] - A[:, 1, 1] - A[:, 2, 2]) * 2
+            q[m] = np.stack([(A[:, 2, 1] - A[:, 1, 2]) / s, 0.25 * s, (A[:, 0, 1] + A[:, 1, 0]) / s,
+                             (A[:, 0, 2] + A[:, 2, 0]) / s], -1)
+        elif case == 2:
+            s = np.sqrt(1.0 + A[:, 1, 1] - A[:, 0, 0] - A[:, 2, 2]) * 2
+            q[m] = np.stack([(A[:, 0, 2] - A[:, 2, 0]) / s, (A[:, 0, 1] + A[:, 1, 0]) / s, 0.25 * s,
+                             (A[:, 1, 2] + A[:, 2, 1]) / s], -1)
+        else:
+            s = np.sqrt(1.0 + A[:, 2, 2] - A[:, 0, 0] - A[:, 1, 1]) * 2
+            q[m] = np.stack([(A[:, 1, 0] - A[:, 0, 1]) / s, (A[:, 0, 2] + A[:, 2, 0]) / s,
+                             (A[:, 1, 2] + A[:, 2, 1]) / s, 0.25 * s], -1)
+    q *= np.where(q[:, :1] < 0, -1.0, 1.0)
+    v = q[:, 1:]
+    n = np.linalg.norm(v, axis=-1)
+    ang = 2 * np.arctan2(n, q[:, 0])
+    f = np.where(n > 1e-15, ang / np.where(n > 1e-15, n, 1.0), 2.0)
+    return (v * f[:, None]).reshape(shape + (3,))
 
 
 def look_at(centres: np.ndarray, targets: np.ndarray, up=(0.0, 0.0, 1.0)) -> np.ndarray:

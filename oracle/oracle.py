@@ -115,3 +115,129 @@ def loss(kind: int, threshold: float, s: float):
     rho = np.zeros(3)
     lib().oracle_loss(kind, threshold, s, _p(rho))
     return rho
+
+
+# ---------------------------------------------------------------------------
+# FP64 CPU bundle-adjustment solve (oracle/solver.cpp)
+
+U8 = C.POINTER(C.c_uint8)
+I32 = C.POINTER(C.c_int32)
+
+
+class _Problem(C.Structure):
+    _fields_ = [
+        ("n_cameras", C.c_int32), ("camera_model", I32), ("camera_values", D), ("camera_prior", D),
+        ("camera_sigma", D), ("camera_free", U8), ("camera_log", U8),
+        ("n_instances", C.c_int32), ("instance_poses", D), ("instance_free", U8), ("instance_has_gps", U8),
+        ("gps_position", D), ("gps_std", D),
+        ("n_rig_cameras", C.c_int32), ("rig_poses", D), ("rig_free", U8), ("rig_used", U8), ("rig_has_prior", U8),
+        ("rig_prior", D), ("rig_sigma", D),
+        ("n_shots", C.c_int32), ("shot_instance", I32), ("shot_rig", I32), ("shot_camera", I32),
+        ("n_points", C.c_int64), ("points", D), ("point_free", U8), ("point_has_prior", U8), ("point_prior", D),
+        ("point_sigma", D), ("point_has_altitude", U8),
+        ("n_obs", C.c_int64), ("obs_shot", I32), ("obs_point", I32), ("obs_xy", D), ("obs_std", D), ("obs_gcp", U8),
+    ]
+
+
+class _Options(C.Structure):
+    _fields_ = [("max_iterations", C.c_int32), ("loss", C.c_int32), ("loss_threshold", C.c_double),
+                ("irls", C.c_int32), ("density_ratio", C.c_double), ("skip_initial_reweighting", C.c_int32),
+                ("threads", C.c_int32)]
+
+
+class _Result(C.Structure):
+    _fields_ = [("camera_values", D), ("instance_poses", D), ("rig_poses", D), ("points", D),
+                ("obs_weights", D), ("obs_errors", D), ("trace_cost", D), ("trace_capacity", C.c_int32),
+                ("trace_n", C.c_int32), ("initial_cost", C.c_double), ("final_cost", C.c_double),
+                ("iterations", C.c_int32), ("successful", C.c_int32), ("termination", C.c_int32)]
+
+
+LOSSES = {"TrivialLoss": 0, "HuberLoss": 1, "SoftLOneLoss": 2, "CauchyLoss": 3, "ArctanLoss": 4}
+
+# default prior standard deviation per parameter of each model (1 for the
+# parameters BundleAdjuster::GetDefaultCameraSigma configures, 0 otherwise)
+_SIGMA_ONE = {0: [1, 1, 1], 1: [1] * 9, 2: [1, 1, 1], 3: [1, 1, 1, 0, 1, 1, 1, 1],
+              4: [1, 1, 1, 0, 0, 0, 1, 1, 1, 1, 1, 1], 5: [1, 1, 1, 0, 0, 0, 1, 1, 0, 0, 0, 0, 1, 1, 1, 1],
+              6: [0], 7: [1, 1, 1, 1], 8: [1] * 6, 9: [1] * 5}
+_LOG = {0: [0, 0, 1], 1: [0, 0, 0, 0, 0, 1, 1, 0, 0], 2: [0, 0, 1], 3: [0, 0, 0, 0, 1, 1, 0, 0],
+        4: [0] * 8 + [1, 1, 0, 0], 5: [0] * 12 + [1, 1, 0, 0], 6: [0], 7: [0, 0, 0, 1], 8: [0, 0, 1, 1, 0, 0],
+        9: [0, 1, 1, 0, 0]}
+
+
+def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
+          density_ratio=1e-3, skip_initial_reweighting=False, threads=None):
+    """Solves the bundle adjustment of a SceneArrays the way
+    opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
+    Returns a dict with the final parameters, costs and the cost trace."""
+    L = lib()
+    L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
+    L.oracle_solve.restype = C.c_int
+    nc = len(scene.camera_projection)
+    cam_sigma = np.zeros((nc, 16))
+    cam_log = np.zeros((nc, 16), np.uint8)
+    for c in range(nc):
+        m = int(scene.camera_projection[c])
+        s = _SIGMA_ONE[m]
+        cam_sigma[c, : len(s)] = s
+        cam_log[c, : len(s)] = _LOG[m]
+    cam_free = np.zeros((nc, 16), np.uint8)
+    for c in range(nc):
+        cam_free[c, : num_params(int(scene.camera_projection[c]))] = 0 if constant_cameras else 1
+    cam_values = np.ascontiguousarray(scene.camera_values)
+    ni = len(scene.rig_instance_poses)
+    inst = np.ascontiguousarray(scene.rig_instance_poses)
+    inst_free = np.ones((ni, 6), np.uint8)
+    has_gps = np.zeros(ni, np.uint8)
+    gps_pos = np.zeros((ni, 3))
+    gps_std = np.ones((ni, 3))
+    if gps and "gps" in scene.extras:
+        for s in range(len(scene.shot_camera)):
+            i = int(scene.shot_rig_instance[s])
+            has_gps[i] = 1
+            gps_pos[i] = scene.extras["gps"][s]
+            gps_std[i] = scene.extras["gps_std"][s]
+    rig = np.zeros((1, 6))
+    rig_free = np.zeros((1, 6), np.uint8)
+    rig_used = np.zeros(1, np.uint8)
+    rig_has_prior = np.ones(1, np.uint8)
+    rig_prior = np.zeros((1, 6))
+    rig_sigma = np.ones((1, 6))
+    ns = len(scene.shot_camera)
+    shot_rig = np.zeros(ns, np.int32)
+    npt = len(scene.points)
+    pts = np.ascontiguousarray(scene.points)
+    pfree = np.ones(npt, np.uint8)
+    phas = np.zeros(npt, np.uint8)
+    pprior = np.zeros((npt, 3))
+    psig = np.ones((npt, 3))
+    palt = np.ones(npt, np.uint8)
+    gcp = np.zeros(scene.n_observations, np.uint8)
+    keep = [cam_values, cam_sigma, cam_log, cam_free, inst, inst_free, has_gps, gps_pos, gps_std, rig, rig_free,
+            rig_used, rig_has_prior, rig_prior, rig_sigma, shot_rig, pts, pfree, phas, pprior, psig, palt, gcp]
+    u8 = lambda a: a.ctypes.data_as(U8)  # noqa: E731
+    i32 = lambda a: a.ctypes.data_as(I32)  # noqa: E731
+    P = _Problem(nc, i32(scene.camera_projection), _p(cam_values), _p(cam_values.copy() if False else cam_values),
+                 _p(cam_sigma), u8(cam_free), u8(cam_log),
+                 ni, _p(inst), u8(inst_free), u8(has_gps), _p(gps_pos), _p(gps_std),
+                 1, _p(rig), u8(rig_free), u8(rig_used), u8(rig_has_prior), _p(rig_prior), _p(rig_sigma),
+                 ns, i32(scene.shot_rig_instance), i32(shot_rig), i32(scene.shot_camera),
+                 npt, _p(pts), u8(pfree), u8(phas), _p(pprior), _p(psig), u8(palt),
+                 scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
+                 _p(scene.obs_std), u8(gcp))
+    loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
+    O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
+                 int(skip_initial_reweighting), threads or os.cpu_count() or 1)
+    out_cam = np.zeros((nc, 16))
+    out_inst = np.zeros((ni, 6))
+    out_rig = np.zeros((1, 6))
+    out_pts = np.zeros((npt, 3))
+    out_w = np.zeros(scene.n_observations)
+    out_err = np.zeros((scene.n_observations, 3))
+    trace = np.zeros(max_iterations + 2)
+    R = _Result(_p(out_cam), _p(out_inst), _p(out_rig), _p(out_pts), _p(out_w), _p(out_err), _p(trace),
+                len(trace), 0, 0.0, 0.0, 0, 0, 0)
+    L.oracle_solve(C.byref(P), C.byref(O), C.byref(R))
+    del keep
+    return dict(cameras=out_cam, instances=out_inst, points=out_pts, weights=out_w, errors=out_err,
+                trace=trace[: R.trace_n].copy(), initial_cost=R.initial_cost, final_cost=R.final_cost,
+                iterations=R.iterations, successful=R.successful, termination=R.termination)

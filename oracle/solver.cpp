@@ -1,0 +1,902 @@
+// Oracle (test infrastructure only) -- FP64 CPU bundle-adjustment solver.
+//
+// Restates the optimisation the reference runs through Ceres
+// (bundle_adjuster.cc:670-1203, irls_solver.cc:93-474, mixture_reweighting.cc)
+// with an exact linear solve: points are eliminated by the Schur complement
+// and the dense reduced camera system is factorised by Cholesky (the
+// reference's DENSE_SCHUR).  The trust-region and robust-loss rules follow
+// Ceres' public documentation:
+//   * Levenberg-Marquardt, initial radius 1e4, max radius 1e8, min relative
+//     decrease 1e-3, radius /= max(1/3, 1 - (2 rho - 1)^3) on success,
+//     radius /= factor and factor *= 2 on failure; non-monotonic steps;
+//   * Jacobi scaling 1/(1 + |J_j|) from the first iteration, LM diagonal
+//     clamped to [1e-6, 1e32];
+//   * robust loss through the residual/Jacobian correction of Triggs et al.;
+//   * IRLS mixture reweighting every max_iterations/10 successful iterations
+//     or on inner convergence, terminating on a relative log-likelihood
+//     change below 1e-3.
+// Cost, gradient and every linear-algebra step are FP64.  Only the tests and
+// the bench's CPU-baseline leg call it.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <thread>
+#include <vector>
+
+#include "residuals.h"
+
+using namespace oracle;
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;
+
+}  // namespace
+
+extern "C" {
+
+struct OracleProblem {
+  int32_t n_cameras;
+  const int32_t* camera_model;
+  const double* camera_values;  // [n][16]
+  const double* camera_prior;   // [n][16]
+  const double* camera_sigma;   // [n][16]
+  const uint8_t* camera_free;   // [n][16]
+  const uint8_t* camera_log;    // [n][16]
+  int32_t n_instances;
+  const double* instance_poses;  // [n][6]
+  const uint8_t* instance_free;  // [n][6]
+  const uint8_t* instance_has_gps;
+  const double* gps_position;  // [n][3]
+  const double* gps_std;       // [n][3]
+  int32_t n_rig_cameras;
+  const double* rig_poses;  // [n][6]
+  const uint8_t* rig_free;  // [n][6]
+  const uint8_t* rig_used;
+  const uint8_t* rig_has_prior;
+  const double* rig_prior;  // [n][6]
+  const double* rig_sigma;  // [n][6]
+  int32_t n_shots;
+  const int32_t* shot_instance;
+  const int32_t* shot_rig;
+  const int32_t* shot_camera;
+  int64_t n_points;
+  const double* points;  // [n][3]
+  const uint8_t* point_free;
+  const uint8_t* point_has_prior;
+  const double* point_prior;  // [n][3]
+  const double* point_sigma;  // [n][3]
+  const uint8_t* point_has_altitude;
+  int64_t n_obs;
+  const int32_t* obs_shot;
+  const int32_t* obs_point;
+  const double* obs_xy;
+  const double* obs_std;
+  const uint8_t* obs_gcp;
+};
+
+struct OracleOptions {
+  int32_t max_iterations;
+  int32_t loss;
+  double loss_threshold;
+  int32_t irls;  // 0 none, 1 mixture
+  double density_ratio;
+  int32_t skip_initial_reweighting;
+  int32_t threads;
+};
+
+struct OracleResult {
+  double* camera_values;   // [n][16]
+  double* instance_poses;  // [n][6]
+  double* rig_poses;       // [n][6]
+  double* points;          // [n][3]
+  double* obs_weights;     // [n_obs]
+  double* obs_errors;      // [n_obs][3] unscaled residuals
+  double* trace_cost;      // [capacity]
+  int32_t trace_capacity;
+  int32_t trace_n;
+  double initial_cost;
+  double final_cost;
+  int32_t iterations;
+  int32_t successful;
+  int32_t termination;  // 0 no convergence, 1 convergence, 2 IRLS success, 3 failure
+};
+
+}  // extern "C"
+
+namespace {
+
+struct State {
+  std::vector<double> cam, inst, rig, pts;  // cam [n][16], inst/rig [n][6], pts [n][3]
+};
+
+// Compact indices of the optimised camera-side coordinates.
+struct Index {
+  std::vector<int> inst, rig, cam;  // -1 for fixed coordinates
+  int n = 0;
+};
+
+struct Mixture {
+  double ll = 0.0;
+};
+
+struct Solver {
+  const OracleProblem& P;
+  const OracleOptions& O;
+  Index idx;
+  std::vector<double> w_obs, w_cam, w_rig, w_gps, w_pp;
+  std::vector<int> gps_list, pp_list;
+  int threads;
+
+  Solver(const OracleProblem& p, const OracleOptions& o) : P(p), O(o) {
+    threads = std::max(1, o.threads);
+    idx.inst.assign(6 * P.n_instances, -1);
+    idx.rig.assign(6 * std::max(0, P.n_rig_cameras), -1);
+    idx.cam.assign(16 * P.n_cameras, -1);
+    for (int i = 0; i < P.n_instances; ++i)
+      for (int k = 0; k < 6; ++k)
+        if (P.instance_free[6 * i + k]) idx.inst[6 * i + k] = idx.n++;
+    for (int r = 0; r < P.n_rig_cameras; ++r)
+      for (int k = 0; k < 6; ++k)
+        if (P.rig_used[r] && P.rig_free[6 * r + k]) idx.rig[6 * r + k] = idx.n++;
+    for (int c = 0; c < P.n_cameras; ++c) {
+      const int C = model_desc(P.camera_model[c]).n_params;
+      for (int k = 0; k < C; ++k)
+        if (P.camera_free[16 * c + k]) idx.cam[16 * c + k] = idx.n++;
+    }
+    w_obs.assign(P.n_obs, 1.0);
+    w_cam.assign(P.n_cameras, 1.0);
+    w_rig.assign(P.n_rig_cameras, 1.0);
+    for (int i = 0; i < P.n_instances; ++i)
+      if (P.instance_has_gps[i]) gps_list.push_back(i);
+    w_gps.assign(gps_list.size(), 1.0);
+    for (int64_t p = 0; p < P.n_points; ++p)
+      if (P.point_has_prior[p]) pp_list.push_back(int(p));
+    w_pp.assign(pp_list.size(), 1.0);
+  }
+
+  template <typename F>
+  void par(int64_t n, F&& f) const {
+    if (threads <= 1 || n < 2048) {
+      for (int64_t i = 0; i < n; ++i) f(i, 0);
+      return;
+    }
+    std::vector<std::thread> pool;
+    const int64_t chunk = (n + threads - 1) / threads;
+    for (int t = 0; t < threads; ++t) {
+      const int64_t b = t * chunk, e = std::min(n, b + chunk);
+      if (b >= e) break;
+      pool.emplace_back([b, e, t, &f] {
+        for (int64_t i = b; i < e; ++i) f(i, t);
+      });
+    }
+    for (auto& th : pool) th.join();
+  }
+
+  // scaled residual of observation i at state s
+  int obs_residual(const State& s, int64_t i, double* r) const {
+    const int sh = P.obs_shot[i];
+    const int cam = P.shot_camera[sh];
+    const int model = P.camera_model[cam];
+    const int rc = P.shot_rig[sh];
+    const double* rig = (rc >= 0 && P.rig_used[rc]) ? &s.rig[6 * rc] : nullptr;
+    residual_generic<double>(model, &s.cam[16 * cam], &s.inst[6 * P.shot_instance[sh]], rig,
+                             &s.pts[3 * P.obs_point[i]], P.obs_xy + 2 * i, P.obs_std[i], r);
+    return residual_size(model);
+  }
+
+  // prior residuals
+  int cam_prior(const State& s, int c, double* r, double* J) const {
+    const int C = model_desc(P.camera_model[c]).n_params;
+    for (int k = 0; k < C; ++k) {
+      const double scale = 1.0 / std::max(P.camera_sigma[16 * c + k], kEps);
+      const double v = s.cam[16 * c + k], pr = P.camera_prior[16 * c + k];
+      if (P.camera_log[16 * c + k]) {
+        r[k] = scale * std::log(v / pr);
+        J[k] = scale / v;
+      } else {
+        r[k] = scale * (v - pr);
+        J[k] = scale;
+      }
+    }
+    return C;
+  }
+
+  double cost(const State& s, std::vector<double>* resid) const {
+    std::vector<double> part(threads, 0.0);
+    par(P.n_obs, [&](int64_t i, int t) {
+      double r[3] = {0, 0, 0};
+      const int nr = obs_residual(s, i, r);
+      double sq = 0.0;
+      for (int k = 0; k < nr; ++k) sq += r[k] * r[k];
+      double rho[3];
+      loss_eval(O.loss, O.loss_threshold, sq, rho);
+      part[t] += 0.5 * w_obs[i] * rho[0];
+      if (resid)
+        for (int k = 0; k < 3; ++k) (*resid)[3 * i + k] = r[k];
+    });
+    double c = 0.0;
+    for (double v : part) c += v;
+    c += prior_cost(s);
+    return c;
+  }
+
+  double prior_cost(const State& s) const {
+    double c = 0.0;
+    double r[16], J[16];
+    for (int k = 0; k < P.n_cameras; ++k) {
+      const int n = cam_prior(s, k, r, J);
+      for (int j = 0; j < n; ++j) c += 0.5 * w_cam[k] * r[j] * r[j];
+    }
+    for (int rc = 0; rc < P.n_rig_cameras; ++rc) {
+      if (!P.rig_has_prior[rc]) continue;
+      for (int j = 0; j < 6; ++j) {
+        const double v = (s.rig[6 * rc + j] - P.rig_prior[6 * rc + j]) / std::max(P.rig_sigma[6 * rc + j], kEps);
+        c += 0.5 * w_rig[rc] * v * v;
+      }
+    }
+    for (size_t g = 0; g < gps_list.size(); ++g) {
+      const int i = gps_list[g];
+      for (int j = 0; j < 3; ++j) {
+        const double v = (s.inst[6 * i + 3 + j] - P.gps_position[3 * i + j]) / std::max(P.gps_std[3 * i + j], kEps);
+        c += 0.5 * w_gps[g] * v * v;
+      }
+    }
+    for (size_t g = 0; g < pp_list.size(); ++g) {
+      const int p = pp_list[g];
+      const int n = P.point_has_altitude[p] ? 3 : 2;
+      for (int j = 0; j < n; ++j) {
+        const double v = (s.pts[3 * p + j] - P.point_prior[3 * p + j]) / std::max(P.point_sigma[3 * p + j], kEps);
+        c += 0.5 * w_pp[g] * v * v;
+      }
+    }
+    return c;
+  }
+
+  // ---- linearization storage
+  struct ObsLin {
+    int nr = 0;
+    double r[3];
+    double Jp[9];
+    int m = 0;        // camera-side columns
+    int col[28];      // compact indices
+    double Jc[3 * 28];
+  };
+  std::vector<ObsLin> lin;
+  std::vector<double> U, g;            // camera side (dense)
+  std::vector<double> V, gp;           // points [n][9], [n][3]
+  std::vector<double> colnorm_c, colnorm_p;
+
+  void linearize(const State& s) {
+    const int n = idx.n;
+    lin.assign(P.n_obs, ObsLin());
+    par(P.n_obs, [&](int64_t i, int) {
+      ObsLin& L = lin[i];
+      const int sh = P.obs_shot[i];
+      const int cam = P.shot_camera[sh];
+      const int model = P.camera_model[cam];
+      const int C = model_desc(model).n_params;
+      const int inst = P.shot_instance[sh];
+      const int rc = P.shot_rig[sh];
+      const bool use_rig = rc >= 0 && P.rig_used[rc];
+      double r[3] = {0, 0, 0}, Jc[48] = {0}, Ji[18] = {0}, Jr[18] = {0}, Jp[9] = {0};
+      residual_jac(model, &s.cam[16 * cam], &s.inst[6 * inst], use_rig ? &s.rig[6 * rc] : nullptr,
+                   &s.pts[3 * P.obs_point[i]], P.obs_xy + 2 * i, P.obs_std[i], r, Jc, Ji, Jr, Jp);
+      const int nr = residual_size(model);
+      L.nr = nr;
+      // gather camera-side columns
+      int m = 0;
+      double cols[3][28];
+      auto add_col = [&](int ci, const double* J, int stride, int k) {
+        if (ci < 0) return;
+        L.col[m] = ci;
+        for (int a = 0; a < nr; ++a) cols[a][m] = J[a * stride + k];
+        ++m;
+      };
+      for (int k = 0; k < 6; ++k) add_col(idx.inst[6 * inst + k], Ji, 6, k);
+      if (use_rig)
+        for (int k = 0; k < 6; ++k) add_col(idx.rig[6 * rc + k], Jr, 6, k);
+      if (model != SPHERICAL)
+        for (int k = 0; k < C; ++k) add_col(idx.cam[16 * cam + k], Jc, C, k);
+      L.m = m;
+      // robust correction
+      double sq = 0.0;
+      for (int a = 0; a < nr; ++a) sq += r[a] * r[a];
+      double rho[3];
+      loss_eval(O.loss, O.loss_threshold, sq, rho);
+      for (double& v : rho) v *= w_obs[i];
+      const double sq1 = std::sqrt(rho[1]);
+      double rs = sq1, as = 0.0;
+      if (sq > 0.0 && rho[2] > 0.0) {
+        const double D = 1.0 + 2.0 * sq * rho[2] / rho[1];
+        const double alpha = 1.0 - std::sqrt(D);
+        rs = sq1 / (1.0 - alpha);
+        as = alpha / sq;
+      }
+      auto corr = [&](double* colv /*nr values with stride*/, int stride) {
+        double rj = 0.0;
+        for (int a = 0; a < nr; ++a) rj += r[a] * colv[a * stride];
+        for (int a = 0; a < nr; ++a) colv[a * stride] = sq1 * (colv[a * stride] - as * r[a] * rj);
+      };
+      for (int k = 0; k < 3; ++k) corr(Jp + k, 3);
+      for (int k = 0; k < m; ++k) corr(&cols[0][k], 28);
+      for (int a = 0; a < nr; ++a) {
+        L.r[a] = rs * r[a];
+        for (int k = 0; k < 3; ++k) L.Jp[a * 3 + k] = P.point_free[P.obs_point[i]] ? Jp[a * 3 + k] : 0.0;
+        for (int k = 0; k < m; ++k) L.Jc[a * 28 + k] = cols[a][k];
+      }
+    });
+    U.assign(size_t(n) * n, 0.0);
+    g.assign(n, 0.0);
+    V.assign(9 * P.n_points, 0.0);
+    gp.assign(3 * P.n_points, 0.0);
+    for (int64_t i = 0; i < P.n_obs; ++i) {
+      const ObsLin& L = lin[i];
+      const int p = P.obs_point[i];
+      for (int a = 0; a < L.nr; ++a) {
+        for (int k = 0; k < L.m; ++k) {
+          g[L.col[k]] += L.Jc[a * 28 + k] * L.r[a];
+          for (int l = 0; l < L.m; ++l) U[size_t(L.col[k]) * n + L.col[l]] += L.Jc[a * 28 + k] * L.Jc[a * 28 + l];
+        }
+        for (int k = 0; k < 3; ++k) {
+          gp[3 * p + k] += L.Jp[a * 3 + k] * L.r[a];
+          for (int l = 0; l < 3; ++l) V[9 * p + 3 * k + l] += L.Jp[a * 3 + k] * L.Jp[a * 3 + l];
+        }
+      }
+    }
+    // priors (diagonal Jacobians)
+    double r[16], J[16];
+    for (int c = 0; c < P.n_cameras; ++c) {
+      const int C = cam_prior(s, c, r, J);
+      for (int k = 0; k < C; ++k) {
+        const int ci = idx.cam[16 * c + k];
+        if (ci < 0) continue;
+        g[ci] += w_cam[c] * J[k] * r[k];
+        U[size_t(ci) * n + ci] += w_cam[c] * J[k] * J[k];
+      }
+    }
+    for (int rc = 0; rc < P.n_rig_cameras; ++rc) {
+      if (!P.rig_has_prior[rc]) continue;
+      for (int k = 0; k < 6; ++k) {
+        const int ci = idx.rig[6 * rc + k];
+        if (ci < 0) continue;
+        const double sc = 1.0 / std::max(P.rig_sigma[6 * rc + k], kEps);
+        g[ci] += w_rig[rc] * sc * sc * (s.rig[6 * rc + k] - P.rig_prior[6 * rc + k]);
+        U[size_t(ci) * n + ci] += w_rig[rc] * sc * sc;
+      }
+    }
+    for (size_t q = 0; q < gps_list.size(); ++q) {
+      const int i = gps_list[q];
+      for (int k = 0; k < 3; ++k) {
+        const int ci = idx.inst[6 * i + 3 + k];
+        if (ci < 0) continue;
+        const double sc = 1.0 / std::max(P.gps_std[3 * i + k], kEps);
+        g[ci] += w_gps[q] * sc * sc * (s.inst[6 * i + 3 + k] - P.gps_position[3 * i + k]);
+        U[size_t(ci) * n + ci] += w_gps[q] * sc * sc;
+      }
+    }
+    for (size_t q = 0; q < pp_list.size(); ++q) {
+      const int p = pp_list[q];
+      if (!P.point_free[p]) continue;
+      const int nn = P.point_has_altitude[p] ? 3 : 2;
+      for (int k = 0; k < nn; ++k) {
+        const double sc = 1.0 / std::max(P.point_sigma[3 * p + k], kEps);
+        gp[3 * p + k] += w_pp[q] * sc * sc * (s.pts[3 * p + k] - P.point_prior[3 * p + k]);
+        V[9 * p + 4 * k] += w_pp[q] * sc * sc;
+      }
+    }
+  }
+
+  // ---- linear step
+  std::vector<double> scale_c, scale_p;
+  bool solve(double mu, bool first, std::vector<double>& dc, std::vector<double>& dp, double& model_change) {
+    const int n = idx.n;
+    if (first) {
+      scale_c.assign(n, 1.0);
+      for (int j = 0; j < n; ++j) scale_c[j] = 1.0 / (1.0 + std::sqrt(U[size_t(j) * n + j]));
+      scale_p.assign(3 * P.n_points, 1.0);
+      for (int64_t p = 0; p < P.n_points; ++p)
+        for (int k = 0; k < 3; ++k) scale_p[3 * p + k] = 1.0 / (1.0 + std::sqrt(V[9 * p + 4 * k]));
+    }
+    auto damp = [&](double d, double s) {
+      double c = s * s * d;
+      c = std::min(std::max(c, 1e-6), 1e32);
+      return c / (s * s) * mu;
+    };
+    std::vector<double> S(U), b(n);
+    for (int j = 0; j < n; ++j) {
+      S[size_t(j) * n + j] += damp(U[size_t(j) * n + j], scale_c[j]);
+      b[j] = -g[j];
+    }
+    // point inverses
+    std::vector<double> Vi(9 * P.n_points, 0.0);
+    for (int64_t p = 0; p < P.n_points; ++p) {
+      if (!P.point_free[p]) continue;
+      double A[9];
+      for (int k = 0; k < 9; ++k) A[k] = V[9 * p + k];
+      for (int k = 0; k < 3; ++k) A[4 * k] += damp(V[9 * p + 4 * k], scale_p[3 * p + k]);
+      const double det = A[0] * (A[4] * A[8] - A[5] * A[7]) - A[1] * (A[3] * A[8] - A[5] * A[6]) +
+                         A[2] * (A[3] * A[7] - A[4] * A[6]);
+      if (!(std::fabs(det) > 0.0)) continue;
+      double* I = &Vi[9 * p];
+      I[0] = (A[4] * A[8] - A[5] * A[7]) / det;
+      I[1] = (A[2] * A[7] - A[1] * A[8]) / det;
+      I[2] = (A[1] * A[5] - A[2] * A[4]) / det;
+      I[3] = (A[5] * A[6] - A[3] * A[8]) / det;
+      I[4] = (A[0] * A[8] - A[2] * A[6]) / det;
+      I[5] = (A[2] * A[3] - A[0] * A[5]) / det;
+      I[6] = (A[3] * A[7] - A[4] * A[6]) / det;
+      I[7] = (A[1] * A[6] - A[0] * A[7]) / det;
+      I[8] = (A[0] * A[4] - A[1] * A[3]) / det;
+    }
+    // Schur complement, grouped by point
+    std::vector<int64_t> order(P.n_obs);
+    for (int64_t i = 0; i < P.n_obs; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t c) { return P.obs_point[a] < P.obs_point[c]; });
+    std::vector<int> wcol;
+    std::vector<double> wval;  // [3] per entry: W = J_c^T J_p (entry per column)
+    for (int64_t a = 0; a < P.n_obs;) {
+      const int p = P.obs_point[order[a]];
+      int64_t e = a;
+      while (e < P.n_obs && P.obs_point[order[e]] == p) ++e;
+      if (P.point_free[p]) {
+        wcol.clear();
+        wval.clear();
+        for (int64_t q = a; q < e; ++q) {
+          const ObsLin& L = lin[order[q]];
+          for (int k = 0; k < L.m; ++k) {
+            double w3[3] = {0, 0, 0};
+            for (int r = 0; r < L.nr; ++r)
+              for (int l = 0; l < 3; ++l) w3[l] += L.Jc[r * 28 + k] * L.Jp[r * 3 + l];
+            // merge equal columns
+            int pos = -1;
+            for (size_t t = 0; t < wcol.size(); ++t)
+              if (wcol[t] == L.col[k]) pos = int(t);
+            if (pos < 0) {
+              wcol.push_back(L.col[k]);
+              wval.insert(wval.end(), w3, w3 + 3);
+            } else {
+              for (int l = 0; l < 3; ++l) wval[3 * pos + l] += w3[l];
+            }
+          }
+        }
+        const double* I = &Vi[9 * p];
+        const size_t m = wcol.size();
+        std::vector<double> T(3 * m);  // W V^-1
+        for (size_t t = 0; t < m; ++t)
+          for (int l = 0; l < 3; ++l)
+            T[3 * t + l] = wval[3 * t] * I[l] + wval[3 * t + 1] * I[3 + l] + wval[3 * t + 2] * I[6 + l];
+        for (size_t t = 0; t < m; ++t) {
+          for (size_t u = 0; u < m; ++u) {
+            const double v = T[3 * t] * wval[3 * u] + T[3 * t + 1] * wval[3 * u + 1] + T[3 * t + 2] * wval[3 * u + 2];
+            S[size_t(wcol[t]) * n + wcol[u]] -= v;
+          }
+          b[wcol[t]] += T[3 * t] * gp[3 * p] + T[3 * t + 1] * gp[3 * p + 1] + T[3 * t + 2] * gp[3 * p + 2];
+        }
+      }
+      a = e;
+    }
+    // Cholesky solve
+    std::vector<double> Lm(S);
+    for (int j = 0; j < n; ++j) {
+      double d = Lm[size_t(j) * n + j];
+      for (int k = 0; k < j; ++k) d -= Lm[size_t(j) * n + k] * Lm[size_t(j) * n + k];
+      if (!(d > 0.0)) return false;
+      d = std::sqrt(d);
+      Lm[size_t(j) * n + j] = d;
+      for (int i = j + 1; i < n; ++i) {
+        double s = Lm[size_t(i) * n + j];
+        for (int k = 0; k < j; ++k) s -= Lm[size_t(i) * n + k] * Lm[size_t(j) * n + k];
+        Lm[size_t(i) * n + j] = s / d;
+      }
+    }
+    dc.assign(n, 0.0);
+    std::vector<double> y(n);
+    for (int i = 0; i < n; ++i) {
+      double s = b[i];
+      for (int k = 0; k < i; ++k) s -= Lm[size_t(i) * n + k] * y[k];
+      y[i] = s / Lm[size_t(i) * n + i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double s = y[i];
+      for (int k = i + 1; k < n; ++k) s -= Lm[size_t(k) * n + i] * dc[k];
+      dc[i] = s / Lm[size_t(i) * n + i];
+    }
+    // back-substitution
+    std::vector<double> wd(3 * P.n_points, 0.0);
+    for (int64_t i = 0; i < P.n_obs; ++i) {
+      const ObsLin& L = lin[i];
+      const int p = P.obs_point[i];
+      for (int r = 0; r < L.nr; ++r) {
+        double t = 0.0;
+        for (int k = 0; k < L.m; ++k) t += L.Jc[r * 28 + k] * dc[L.col[k]];
+        for (int l = 0; l < 3; ++l) wd[3 * p + l] += L.Jp[r * 3 + l] * t;
+      }
+    }
+    dp.assign(3 * P.n_points, 0.0);
+    for (int64_t p = 0; p < P.n_points; ++p) {
+      if (!P.point_free[p]) continue;
+      const double* I = &Vi[9 * p];
+      double q[3];
+      for (int l = 0; l < 3; ++l) q[l] = -gp[3 * p + l] - wd[3 * p + l];
+      for (int l = 0; l < 3; ++l) dp[3 * p + l] = I[3 * l] * q[0] + I[3 * l + 1] * q[1] + I[3 * l + 2] * q[2];
+    }
+    // linear model decrease
+    double mc = 0.0;
+    for (int64_t i = 0; i < P.n_obs; ++i) {
+      const ObsLin& L = lin[i];
+      const int p = P.obs_point[i];
+      for (int r = 0; r < L.nr; ++r) {
+        double t = 0.0;
+        for (int k = 0; k < L.m; ++k) t += L.Jc[r * 28 + k] * dc[L.col[k]];
+        for (int l = 0; l < 3; ++l) t += L.Jp[r * 3 + l] * dp[3 * p + l];
+        mc += -0.5 * t * (2.0 * L.r[r] + t);
+      }
+    }
+    // priors: J diagonal -> model change from g restricted to priors is
+    // already inside U, g; compute it directly
+    mc += prior_model_change(dc, dp);
+    model_change = mc;
+    return true;
+  }
+
+  const State* cur = nullptr;
+  double prior_model_change(const std::vector<double>& dc, const std::vector<double>& dp) const {
+    const State& s = *cur;
+    double mc = 0.0;
+    auto term = [](double w, double r, double J, double d) { return -0.5 * w * (J * d) * (2.0 * r + J * d); };
+    double r[16], J[16];
+    for (int c = 0; c < P.n_cameras; ++c) {
+      const int C = cam_prior(s, c, r, J);
+      for (int k = 0; k < C; ++k) {
+        const int ci = idx.cam[16 * c + k];
+        if (ci >= 0) mc += term(w_cam[c], r[k], J[k], dc[ci]);
+      }
+    }
+    for (int rc = 0; rc < P.n_rig_cameras; ++rc) {
+      if (!P.rig_has_prior[rc]) continue;
+      for (int k = 0; k < 6; ++k) {
+        const int ci = idx.rig[6 * rc + k];
+        if (ci < 0) continue;
+        const double sc = 1.0 / std::max(P.rig_sigma[6 * rc + k], kEps);
+        mc += term(w_rig[rc], sc * (s.rig[6 * rc + k] - P.rig_prior[6 * rc + k]), sc, dc[ci]);
+      }
+    }
+    for (size_t q = 0; q < gps_list.size(); ++q) {
+      const int i = gps_list[q];
+      for (int k = 0; k < 3; ++k) {
+        const int ci = idx.inst[6 * i + 3 + k];
+        if (ci < 0) continue;
+        const double sc = 1.0 / std::max(P.gps_std[3 * i + k], kEps);
+        mc += term(w_gps[q], sc * (s.inst[6 * i + 3 + k] - P.gps_position[3 * i + k]), sc, dc[ci]);
+      }
+    }
+    for (size_t q = 0; q < pp_list.size(); ++q) {
+      const int p = pp_list[q];
+      if (!P.point_free[p]) continue;
+      const int nn = P.point_has_altitude[p] ? 3 : 2;
+      for (int k = 0; k < nn; ++k) {
+        const double sc = 1.0 / std::max(P.point_sigma[3 * p + k], kEps);
+        mc += term(w_pp[q], sc * (s.pts[3 * p + k] - P.point_prior[3 * p + k]), sc, dp[3 * p + k]);
+      }
+    }
+    return mc;
+  }
+
+  State apply(const State& s, const std::vector<double>& dc, const std::vector<double>& dp) const {
+    State t = s;
+    for (int i = 0; i < P.n_instances; ++i)
+      for (int k = 0; k < 6; ++k)
+        if (idx.inst[6 * i + k] >= 0) t.inst[6 * i + k] += dc[idx.inst[6 * i + k]];
+    for (int r = 0; r < P.n_rig_cameras; ++r)
+      for (int k = 0; k < 6; ++k)
+        if (idx.rig[6 * r + k] >= 0) t.rig[6 * r + k] += dc[idx.rig[6 * r + k]];
+    for (int c = 0; c < P.n_cameras; ++c)
+      for (int k = 0; k < 16; ++k)
+        if (idx.cam[16 * c + k] >= 0) t.cam[16 * c + k] += dc[idx.cam[16 * c + k]];
+    for (int64_t p = 0; p < P.n_points; ++p)
+      if (P.point_free[p])
+        for (int k = 0; k < 3; ++k) t.pts[3 * p + k] += dp[3 * p + k];
+    return t;
+  }
+
+  // ---- IRLS mixture (mixture_reweighting.cc:10-109)
+  static double mixture(const std::vector<std::vector<double>>& res, std::vector<double*>& w, double ratio) {
+    if (res.size() < 10) return 0.0;
+    const int k = int(res[0].size());
+    double prev = std::numeric_limits<double>::max(), ll = 0.0;
+    for (int it = 0; it < 5; ++it) {
+      std::vector<double> S(k * k, 0.0);
+      double W = 0.0;
+      for (size_t i = 0; i < res.size(); ++i) {
+        if (int(res[i].size()) != k) continue;
+        for (int a = 0; a < k; ++a)
+          for (int b = 0; b < k; ++b) S[a * k + b] += *w[i] * res[i][a] * res[i][b];
+        W += *w[i];
+      }
+      if (W < 1e-9) return 0.0;
+      for (auto& v : S) v /= W;
+      for (int a = 0; a < k; ++a) S[a * k + a] += 0.025;
+      // determinant and inverse by Gauss-Jordan with partial pivoting
+      std::vector<double> M(S), I(k * k, 0.0);
+      for (int a = 0; a < k; ++a) I[a * k + a] = 1.0;
+      double det = 1.0;
+      for (int c = 0; c < k; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < k; ++r)
+          if (std::fabs(M[r * k + c]) > std::fabs(M[piv * k + c])) piv = r;
+        if (M[piv * k + c] == 0.0) {
+          det = 0.0;
+          break;
+        }
+        if (piv != c) {
+          for (int j = 0; j < k; ++j) {
+            std::swap(M[piv * k + j], M[c * k + j]);
+            std::swap(I[piv * k + j], I[c * k + j]);
+          }
+          det = -det;
+        }
+        const double d = M[c * k + c];
+        det *= d;
+        for (int j = 0; j < k; ++j) {
+          M[c * k + j] /= d;
+          I[c * k + j] /= d;
+        }
+        for (int r = 0; r < k; ++r) {
+          if (r == c) continue;
+          const double f = M[r * k + c];
+          for (int j = 0; j < k; ++j) {
+            M[r * k + j] -= f * M[c * k + j];
+            I[r * k + j] -= f * I[c * k + j];
+          }
+        }
+      }
+      if (det < 1e-3) {
+        det = 0.025 * 0.025;
+        std::fill(I.begin(), I.end(), 0.0);
+        for (int a = 0; a < k; ++a) I[a * k + a] = 1.0 / 0.025;
+      }
+      const double sqn = std::sqrt(std::pow(2 * M_PI, k) * det);
+      const double K = ratio / sqn;
+      ll = 0.0;
+      for (size_t i = 0; i < res.size(); ++i) {
+        if (int(res[i].size()) != k) continue;
+        double m = 0.0;
+        for (int a = 0; a < k; ++a)
+          for (int b = 0; b < k; ++b) m += res[i][a] * I[a * k + b] * res[i][b];
+        const double pin = std::exp(-0.5 * m) / sqn;
+        ll += std::log(pin + K);
+        *w[i] = std::max(1e-10, std::min(pin / (pin + K), 1.0));
+      }
+      const double change = std::fabs(ll - prev) / std::fabs(prev);
+      if (change < 1e-3) break;
+      prev = ll;
+    }
+    return ll;
+  }
+
+  double reweight(const State& s) {
+    std::vector<double> resid(3 * P.n_obs);
+    cost(s, &resid);
+    double total = 0.0;
+    // projection groups: one per shot, plus GCP2D
+    std::vector<std::vector<int64_t>> groups(P.n_shots + 1);
+    for (int64_t i = 0; i < P.n_obs; ++i) groups[P.obs_gcp[i] ? P.n_shots : P.obs_shot[i]].push_back(i);
+    for (auto& grp : groups) {
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      for (int64_t i : grp) {
+        const int model = P.camera_model[P.shot_camera[P.obs_shot[i]]];
+        const int nr = residual_size(model);
+        res.emplace_back(&resid[3 * i], &resid[3 * i] + nr);
+        w.push_back(&w_obs[i]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
+    {
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      double r[16], J[16];
+      for (int c = 0; c < P.n_cameras; ++c) {
+        const int C = cam_prior(s, c, r, J);
+        res.emplace_back(r, r + C);
+        w.push_back(&w_cam[c]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
+    {
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      for (int rc = 0; rc < P.n_rig_cameras; ++rc) {
+        if (!P.rig_has_prior[rc]) continue;
+        std::vector<double> r(6);
+        for (int k = 0; k < 6; ++k)
+          r[k] = (s.rig[6 * rc + k] - P.rig_prior[6 * rc + k]) / std::max(P.rig_sigma[6 * rc + k], kEps);
+        res.push_back(r);
+        w.push_back(&w_rig[rc]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
+    {
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      for (size_t q = 0; q < gps_list.size(); ++q) {
+        const int i = gps_list[q];
+        std::vector<double> r(3);
+        for (int k = 0; k < 3; ++k)
+          r[k] = (s.inst[6 * i + 3 + k] - P.gps_position[3 * i + k]) / std::max(P.gps_std[3 * i + k], kEps);
+        res.push_back(r);
+        w.push_back(&w_gps[q]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
+    {
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      for (size_t q = 0; q < pp_list.size(); ++q) {
+        const int p = pp_list[q];
+        const int nn = P.point_has_altitude[p] ? 3 : 2;
+        std::vector<double> r(nn);
+        for (int k = 0; k < nn; ++k)
+          r[k] = (s.pts[3 * p + k] - P.point_prior[3 * p + k]) / std::max(P.point_sigma[3 * p + k], kEps);
+        res.push_back(r);
+        w.push_back(&w_pp[q]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
+    return total;
+  }
+};
+
+}  // namespace
+
+extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, OracleResult* out) {
+  const OracleProblem& P = *Pp;
+  const OracleOptions& O = *Op;
+  Solver S(P, O);
+  State x;
+  x.cam.assign(P.camera_values, P.camera_values + 16 * P.n_cameras);
+  x.inst.assign(P.instance_poses, P.instance_poses + 6 * P.n_instances);
+  x.rig.assign(P.rig_poses, P.rig_poses + 6 * std::max(0, P.n_rig_cameras));
+  x.pts.assign(P.points, P.points + 3 * P.n_points);
+  S.cur = &x;
+  double ll = -std::numeric_limits<double>::infinity();
+  const bool irls = O.irls == 1;
+  if (irls && !O.skip_initial_reweighting) ll = S.reweight(x);
+  double cost = S.cost(x, nullptr);
+  out->initial_cost = cost;
+  out->trace_n = 0;
+  auto trace = [&](double c) {
+    if (out->trace_cost && out->trace_n < out->trace_capacity) out->trace_cost[out->trace_n++] = c;
+  };
+  trace(cost);
+  double radius = 1e4, decrease = 2.0;
+  double reference_cost = cost, candidate_cost = cost, minimum_cost = cost, acc_ref = 0.0, acc_cand = 0.0;
+  int n_nonmono = 0, invalid = 0;
+  const int interval = std::max(1, O.max_iterations / 10);
+  bool first = true;
+  S.linearize(x);
+  out->termination = 0;
+  out->successful = 0;
+  int iter;
+  for (iter = 1; iter <= O.max_iterations; ++iter) {
+    std::vector<double> dc, dp;
+    double mc = 0.0;
+    S.cur = &x;
+    const bool ok = S.solve(1.0 / radius, first, dc, dp, mc);
+    first = false;
+    bool success = false;
+    double new_cost = cost;
+    State cand;
+    double step2 = 0.0;
+    if (ok && mc > 0.0 && std::isfinite(mc)) {
+      for (double v : dc) step2 += v * v;
+      for (double v : dp) step2 += v * v;
+      cand = S.apply(x, dc, dp);
+      new_cost = S.cost(cand, nullptr);
+      if (std::isfinite(new_cost)) {
+        invalid = 0;
+        double rho = (cost - new_cost) / mc;
+        rho = std::max(rho, (reference_cost - new_cost) / (acc_ref + mc));
+        success = rho > 1e-3;
+        if (success) {
+          acc_cand += mc;
+          acc_ref += mc;
+          if (new_cost < minimum_cost) {
+            minimum_cost = new_cost;
+            candidate_cost = new_cost;
+            acc_cand = 0.0;
+            n_nonmono = 0;
+          } else {
+            ++n_nonmono;
+            if (new_cost > candidate_cost) {
+              candidate_cost = new_cost;
+              acc_cand = 0.0;
+            }
+          }
+          if (n_nonmono == 5) {
+            reference_cost = candidate_cost;
+            acc_ref = acc_cand;
+          }
+          radius = std::min(1e8, radius / std::max(1.0 / 3.0, 1.0 - std::pow(2.0 * rho - 1.0, 3)));
+          decrease = 2.0;
+        }
+      } else {
+        ++invalid;
+      }
+    } else {
+      ++invalid;
+    }
+    double cost_change = 0.0, grad_max = 0.0;
+    if (success) {
+      cost_change = cost - new_cost;
+      x = cand;
+      cost = new_cost;
+      S.cur = &x;
+      S.linearize(x);
+      for (double v : S.g) grad_max = std::max(grad_max, std::fabs(v));
+      for (double v : S.gp) grad_max = std::max(grad_max, std::fabs(v));
+      out->successful++;
+    } else {
+      radius /= decrease;
+      decrease *= 2.0;
+    }
+    trace(cost);
+    bool inner = false;
+    if (success) {
+      if (std::fabs(cost_change) <= 1e-7 * cost) inner = true;
+      else if (grad_max <= 1e-10) inner = true;
+      else {
+        double xn = 0.0;
+        for (double v : x.cam) xn += v * v;
+        for (double v : x.inst) xn += v * v;
+        for (double v : x.rig) xn += v * v;
+        for (double v : x.pts) xn += v * v;
+        if (std::sqrt(step2) <= 1e-8 * (std::sqrt(xn) + 1e-8)) inner = true;
+      }
+    }
+    if (irls) {
+      if ((success && iter % interval == 0) || inner) {
+        const double prev = ll;
+        ll = S.reweight(x);
+        cost = S.cost(x, nullptr);
+        reference_cost = candidate_cost = minimum_cost = cost;
+        acc_ref = acc_cand = 0.0;
+        n_nonmono = 0;
+        S.linearize(x);
+        if (prev > -std::numeric_limits<double>::infinity() &&
+            std::fabs(ll - prev) / (std::fabs(prev) + 1e-20) < 1e-3) {
+          out->termination = 2;
+          break;
+        }
+      }
+    } else if (inner) {
+      out->termination = 1;
+      break;
+    }
+    if (radius < 1e-32) {
+      out->termination = 1;
+      break;
+    }
+    if (invalid >= 5) {
+      out->termination = 3;
+      break;
+    }
+  }
+  out->iterations = std::min(iter, O.max_iterations);
+  out->final_cost = cost;
+  std::memcpy(out->camera_values, x.cam.data(), sizeof(double) * x.cam.size());
+  std::memcpy(out->instance_poses, x.inst.data(), sizeof(double) * x.inst.size());
+  if (P.n_rig_cameras) std::memcpy(out->rig_poses, x.rig.data(), sizeof(double) * x.rig.size());
+  std::memcpy(out->points, x.pts.data(), sizeof(double) * x.pts.size());
+  std::vector<double> resid(3 * P.n_obs);
+  S.cost(x, &resid);
+  for (int64_t i = 0; i < P.n_obs; ++i) {
+    if (out->obs_weights) out->obs_weights[i] = S.w_obs[i];
+    if (out->obs_errors)
+      for (int k = 0; k < 3; ++k) out->obs_errors[3 * i + k] = resid[3 * i + k] * P.obs_std[i];
+  }
+  return 0;
+}

