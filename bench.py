@@ -166,6 +166,46 @@ def cpu_baseline(scene, target_s: float = 10.0) -> dict:
                       f"{dt:.1f} s"}
 
 
+def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_tolerance: float = 1e-3) -> dict:
+    """Time to converge: FP64 and mixed-precision GPU solves of the same
+    scene with a fixed objective (robust loss, IRLS off).  The FP64 solve's
+    final cost C64 defines the target C64 * (1 + 1e-6); each solve reports
+    the wall time (from the start of the solve, setup included) at which its
+    cost first reaches the target."""
+    from opensfm_gb300.pybundle import adjuster_from_scene
+    out = {"loss": list(loss), "irls": "none", "max_iterations": max_iterations, "pcg_tolerance": pcg_tolerance}
+    runs = {}
+    for precision in ("fp64", "mixed"):
+        ba = adjuster_from_scene(scene, precision=precision, loss=loss, irls="none",
+                                 max_iterations=max_iterations, pcg_tolerance=pcg_tolerance, gps=True)
+        t0 = time.perf_counter()
+        ba.run()
+        wall = time.perf_counter() - t0
+        s = ba.summary()
+        runs[precision] = {"trace": ba.trace(), "summary": s, "wall_s": wall}
+        del ba
+    c64 = runs["fp64"]["summary"]["final_cost"]
+    target = c64 * (1.0 + 1e-6)
+    for precision, r in runs.items():
+        tr = r["trace"]
+        hit = np.nonzero(tr[:, 1] <= target)[0]
+        s = r["summary"]
+        out[precision] = {
+            "time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None,
+            "iterations_to_target": int(tr[hit[0], 0]) if len(hit) else None,
+            "final_cost": s["final_cost"], "initial_cost": s["initial_cost"], "iterations": s["iterations"],
+            "solve_s": s["seconds"], "linear_solver_s": s["linear_solver_seconds"],
+            "jacobian_s": s["jacobian_seconds"], "residual_s": s["residual_seconds"],
+            "kernel_launches": s["kernel_launches"],
+            "pcg_iterations": int(tr[:, 4].sum()),
+        }
+    out["target_cost"] = target
+    out["mixed_final_rel_to_fp64"] = abs(runs["mixed"]["summary"]["final_cost"] - c64) / c64
+    tm, tf = out["mixed"]["time_to_target_s"], out["fp64"]["time_to_target_s"]
+    out["speedup_mixed_vs_fp64"] = (tf / tm) if (tm and tf) else None
+    return out
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -304,6 +344,9 @@ def run_ours(args) -> None:
         }
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene)
+        if not args.no_converge:
+            ev.close()
+            result["converge"] = converge_benchmark(scene, args.converge_iterations)
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -318,6 +361,8 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="aerial", choices=["aerial", "aerial_small", "street", "ring"])
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-converge", action="store_true")
+    ap.add_argument("--converge-iterations", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
