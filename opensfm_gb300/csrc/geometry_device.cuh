@@ -301,6 +301,13 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
 #pragma unroll
     for (int k = 0; k < 3; ++k) rec[L::kInst + i * 6 + k] = c0 * g.jr[0 * 3 + k] + c1 * g.jr[1 * 3 + k] + c2 * g.jr[2 * 3 + k];
     if constexpr (RIG) {
+      // shots without an applied rig camera have a zero rig-camera block
+      // (projection_errors.h:184-188)
+      if (g.rig < R(0)) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) rec[L::kRig + i * 6 + k] = R(0);
+        continue;
+      }
       // p = R_rc (y - c_rc), y = R_inst v:  d p / d r_rc = R_rc [y - c_rc]x J_rc,
       // d p / d c_rc = -R_rc
       const RigGeom<R>& rg = *in.rg;

@@ -11,6 +11,7 @@
 #include "device_buffer.h"
 #include "solver.h"
 #include "solver_kernels.cuh"
+#include "solver_shot_major.cuh"
 
 namespace gbba {
 
@@ -530,6 +531,7 @@ class DeviceSolver final : public SolverBase {
   void upload_camera_side(const std::vector<double>& x, bool working, bool fp64);
   // ---- device passes
   SolveView<R> view();
+  ShotMajorView<R> sm_view();
   SceneView<double> view64(bool candidate);
   double cost_pass(bool candidate, bool store_residuals);
   void linearize();
@@ -576,6 +578,10 @@ class DeviceSolver final : public SolverBase {
   DeviceArray<R> d_weight_;
   DeviceArray<double> d_resid_;
   DeviceArray<V16> d_rec_;
+  // shot-major order: point-major slot, point and shot of every shot-major
+  // slot, and the shot-major copy of the records
+  DeviceArray<int> d_sm_src_, d_sm_point_, d_sm_shot_;
+  DeviceArray<V16> d_rec_sm_;
   // geometry: working precision of the current state (d_geom_, d_cam_), FP64
   // of the current state (mixed mode only; in FP64 mode d_geom_ is it), FP64
   // of the candidate state (d_geomc_, d_camc_)
@@ -682,12 +688,15 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
       cmask_[cl_.cam_base + 16 * c + k] = P.cameras[c].free_mask[k];
     }
 
-  // slots: observations sorted by point (stable), padded to a warp multiple
+  // slots: observations sorted by point (stable counting sort), padded to a
+  // warp multiple
   std::vector<int64_t> order(n_obs_);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) {
-    return P.observations[a].point < P.observations[b].point;
-  });
+  {
+    std::vector<int64_t> start(n_pt_ + 1, 0);
+    for (const Observation& q : P.observations) ++start[q.point + 1];
+    for (int64_t p = 0; p < n_pt_; ++p) start[p + 1] += start[p];
+    for (int64_t o = 0; o < n_obs_; ++o) order[start[P.observations[o].point]++] = o;
+  }
   n_slots_ = std::max<int64_t>(32, (n_obs_ + 31) / 32 * 32);
   slot_obs_.assign(n_slots_, -1);
   std::vector<ObsPack<R>> ob(n_slots_);
@@ -721,6 +730,33 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   d_resid_.zero();
   d_rec_.resize(size_t(n_planes_) * n_slots_);
   d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
+
+  // shot-major order of the same slots: by rig instance, then shot, then
+  // point (a stable counting sort of the point-major slots by shot rank);
+  // padding slots go last
+  {
+    std::vector<int> shots(n_shots_), rank(n_shots_);
+    std::iota(shots.begin(), shots.end(), 0);
+    std::stable_sort(shots.begin(), shots.end(),
+                     [&](int a, int b) { return P.shots[a].instance < P.shots[b].instance; });
+    for (int r = 0; r < n_shots_; ++r) rank[shots[r]] = r;
+    std::vector<int64_t> start(n_shots_ + 1, 0);
+    for (int64_t s = 0; s < n_obs_; ++s) ++start[rank[P.observations[order[s]].shot] + 1];
+    for (int r = 0; r < n_shots_; ++r) start[r + 1] += start[r];
+    std::vector<int> src(n_slots_, -1), pt(n_slots_, -1), sh(n_slots_, 0);
+    for (int64_t s = 0; s < n_obs_; ++s) {
+      const Observation& q = P.observations[order[s]];
+      const int64_t j = start[rank[q.shot]]++;
+      src[j] = int(s);
+      pt[j] = q.point;
+      sh[j] = q.shot;
+    }
+    d_sm_src_.upload(src);
+    d_sm_point_.upload(pt);
+    d_sm_shot_.upload(sh);
+  }
+  d_rec_sm_.resize(size_t(n_planes_) * n_slots_);
+  d_rec_sm_.zero();
 
   // shots / cameras / rigs
   std::vector<int> si(n_shots_), sr(n_shots_), sc(n_shots_);
@@ -920,6 +956,11 @@ SolveView<R> DeviceSolver<R>::view() {
 }
 
 template <typename R>
+ShotMajorView<R> DeviceSolver<R>::sm_view() {
+  return ShotMajorView<R>{d_sm_src_.get(), d_sm_point_.get(), d_sm_shot_.get(), d_rec_sm_.get()};
+}
+
+template <typename R>
 SceneView<double> DeviceSolver<R>::view64(bool candidate) {
   SceneView<double> s{};
   s.n_slots = n_slots_;
@@ -986,10 +1027,13 @@ double DeviceSolver<R>::cost_pass(bool candidate, bool store_residuals) {
 template <typename R>
 struct LinearizeLaunch {
   SolveView<R> v;
+  ShotMajorView<R> sm;
   uint64_t mask;
   template <int M, int NR, int CMAX, bool RIG>
   void run() {
-    linearize_kernel<R, M, NR, CMAX, RIG><<<slot_grid(v.scene.n_slots), 256>>>(v, mask);
+    const int g = slot_grid(v.scene.n_slots);
+    linearize_kernel<R, M, NR, CMAX, RIG><<<g, 256>>>(v, mask);
+    permute_records_kernel<R, NR, CMAX, RIG><<<g, 256>>>(v, sm, mask);
   }
 };
 
@@ -999,9 +1043,9 @@ void DeviceSolver<R>::linearize() {
   d_gp_.zero();
   d_gc_.zero();
   d_dc_.zero();
-  LinearizeLaunch<R> f{view(), plane_mask_};
+  LinearizeLaunch<R> f{view(), sm_view(), plane_mask_};
   dispatch_config(kc_, f);
-  ++launches_;
+  launches_ += 2;
   if (!point_priors_.empty()) {
     point_prior_linearize_kernel<R><<<elem_grid(int64_t(point_priors_.size())), 256>>>(
         int(point_priors_.size()), d_pp_.get(), d_pp_w_.get(), d_X_.get(), d_point_free_.get(), d_Vp_.get(),

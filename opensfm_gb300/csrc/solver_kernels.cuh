@@ -14,8 +14,8 @@
 // Per-point sums (V_p = sum J_p^T J_p, g_p = sum J_p^T r, and the point
 // halves of the Schur products) are warp-level segmented reductions over the
 // point-major slots; each segment tail adds its sum to global memory.
-// Camera-side sums are scattered with vector reductions (instances) or
-// warp-aggregated when all lanes of a warp hit the same intrinsics block.
+// Camera-side sums run over a shot-major copy of the records
+// (solver_shot_major.cuh).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -91,30 +91,6 @@ template <typename R>
 __device__ __forceinline__ void red_block6(R* dst, const R* v) {
   red_add4(dst, v[0], v[1], v[2], v[3]);
   red_add4(dst + 4, v[4], v[5], R(0), R(0));
-}
-
-// Adds a C-vector to an intrinsics block: warp-aggregated when every lane
-// targets the same block (and is valid), per lane otherwise.
-template <int C, typename R>
-__device__ __forceinline__ void red_camera_block(R* base, int cam, bool valid, const R* v) {
-  const int lead = __shfl_sync(kFullMask, cam, 0);
-  const bool uniform = __all_sync(kFullMask, valid && cam == lead);
-  if (uniform) {
-    R s[C];
-#pragma unroll
-    for (int k = 0; k < C; ++k) {
-      s[k] = v[k];
-#pragma unroll
-      for (int d = 16; d > 0; d >>= 1) s[k] += __shfl_xor_sync(kFullMask, s[k], d);
-    }
-    if ((threadIdx.x & 31u) == 0) {
-#pragma unroll
-      for (int k = 0; k < C; ++k) red_add(base + cam * 16 + k, s[k]);
-    }
-  } else if (valid) {
-#pragma unroll
-    for (int k = 0; k < C; ++k) red_add(base + cam * 16 + k, v[k]);
-  }
 }
 
 // Record access helpers.
@@ -296,49 +272,6 @@ __device__ __forceinline__ void apply_cam(const R* rec, const CamGather<R, CMAX>
   }
 }
 
-// y_c += J_c^T e for one observation.
-template <typename R, int NR, int CMAX, bool RIG>
-__device__ __forceinline__ void scatter_cam(const SolveView<R>& v, R* y, const R* rec, const R* e, bool valid,
-                                            int inst, int cam, int rig) {
-  using L = RecordLayout<NR, CMAX, RIG>;
-  if (valid && v.inst_free[inst]) {
-    R a[6];
-#pragma unroll
-    for (int k = 0; k < 6; ++k) {
-      R s = R(0);
-#pragma unroll
-      for (int i = 0; i < NR; ++i) s += rec[L::kInst + i * 6 + k] * e[i];
-      a[k] = s;
-    }
-    red_block6(y + 8 * inst, a);
-  }
-  {
-    const bool cvalid = valid && v.cam_free[cam];
-    R c[CMAX];
-#pragma unroll
-    for (int k = 0; k < CMAX; ++k) {
-      R s = R(0);
-#pragma unroll
-      for (int i = 0; i < NR; ++i) s += rec[L::kCam + i * CMAX + k] * e[i];
-      c[k] = cvalid ? s : R(0);
-    }
-    if (__any_sync(kFullMask, cvalid)) red_camera_block<CMAX>(y + v.cl.cam_base, cam, cvalid, c);
-  }
-  if constexpr (RIG) {
-    if (valid && rig >= 0 && v.rig_free[rig]) {
-      R a[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        R s = R(0);
-#pragma unroll
-        for (int i = 0; i < NR; ++i) s += rec[L::kRig + i * 6 + k] * e[i];
-        a[k] = s;
-      }
-      red_block6(y + v.cl.rig_base + 8 * rig, a);
-    }
-  }
-}
-
 // Shot indices of a slot (valid slots only).
 template <typename R>
 __device__ __forceinline__ void shot_indices(const SceneView<R>& s, int sh, int& inst, int& cam, int& rig) {
@@ -357,8 +290,7 @@ __device__ __forceinline__ void shot_indices(const SceneView<R>& s, int sh, int&
   for (int64_t base = warp0 * 32; base < (n_slots); base += nwarps * 32)
 
 // ---------------------------------------------------------------------------
-// Linearization: records (with robust correction), point blocks, camera
-// gradient and column norms.
+// Linearization: records (with robust correction) and point blocks.
 template <typename R, int M, int NR, int CMAX, bool RIG>
 __global__ void __launch_bounds__(256) linearize_kernel(SolveView<R> v, uint64_t plane_mask) {
   using L = RecordLayout<NR, CMAX, RIG>;
@@ -376,7 +308,6 @@ __global__ void __launch_bounds__(256) linearize_kernel(SolveView<R> v, uint64_t
     R rec[NP * VN];
 #pragma unroll
     for (int k = 0; k < NP * VN; ++k) rec[k] = R(0);
-    int inst = 0, cam = 0, rig = -1;
     if (valid) {
       ObsPack<R> ob;
       ldg_copy(s.obs + i, ob);
@@ -384,9 +315,6 @@ __global__ void __launch_bounds__(256) linearize_kernel(SolveView<R> v, uint64_t
       load_inputs<R, M>(s, ob, pt, cams, models, in);
       eval_observation<R, M, NR, CMAX, RIG, true>(in, rec);
       robust_correct<R, NR, CMAX, RIG>(v.loss, v.loss_a, v.weight[i], rec);
-      inst = int(in.g.inst);
-      cam = int(in.g.cam);
-      rig = int(in.g.rig);
     }
 #pragma unroll
     for (int p = 0; p < NP; ++p)
@@ -414,64 +342,8 @@ __global__ void __launch_bounds__(256) linearize_kernel(SolveView<R> v, uint64_t
       red_add4(v.Vp + 8 * int64_t(pt) + 4, acc[4], acc[5], R(0), R(0));
       red_add4(v.gp + 4 * int64_t(pt), acc[6], acc[7], acc[8], R(0));
     }
-
-    // camera side: gradient and squared column norms
-    if (valid && v.inst_free[inst]) {
-      R g6[6], d6[6];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) {
-        R gs = R(0), ds = R(0);
-#pragma unroll
-        for (int q = 0; q < NR; ++q) {
-          const R j = rec[L::kInst + q * 6 + k];
-          gs += j * rec[L::kR + q];
-          ds += j * j;
-        }
-        g6[k] = gs;
-        d6[k] = ds;
-      }
-      red_block6(v.gc + 8 * inst, g6);
-      red_block6(v.dc + 8 * inst, d6);
-    }
-    {
-      const bool cvalid = valid && v.cam_free[cam];
-      if (__any_sync(kFullMask, cvalid)) {
-        R gcv[CMAX], dcv[CMAX];
-#pragma unroll
-        for (int k = 0; k < CMAX; ++k) {
-          R gs = R(0), ds = R(0);
-#pragma unroll
-          for (int q = 0; q < NR; ++q) {
-            const R j = rec[L::kCam + q * CMAX + k];
-            gs += j * rec[L::kR + q];
-            ds += j * j;
-          }
-          gcv[k] = cvalid ? gs : R(0);
-          dcv[k] = cvalid ? ds : R(0);
-        }
-        red_camera_block<CMAX>(v.gc + v.cl.cam_base, cam, cvalid, gcv);
-        red_camera_block<CMAX>(v.dc + v.cl.cam_base, cam, cvalid, dcv);
-      }
-    }
-    if constexpr (RIG) {
-      if (valid && rig >= 0 && v.rig_free[rig]) {
-        R g6[6], d6[6];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) {
-          R gs = R(0), ds = R(0);
-#pragma unroll
-          for (int q = 0; q < NR; ++q) {
-            const R j = rec[L::kRig + q * 6 + k];
-            gs += j * rec[L::kR + q];
-            ds += j * j;
-          }
-          g6[k] = gs;
-          d6[k] = ds;
-        }
-        red_block6(v.gc + v.cl.rig_base + 8 * rig, g6);
-        red_block6(v.dc + v.cl.rig_base + 8 * rig, d6);
-      }
-    }
+    // the camera-side gradient and column norms are summed in shot-major
+    // order by permute_records_kernel
   }
 }
 
@@ -595,90 +467,9 @@ struct PrecondView {
   int cam_stride;
 };
 
-template <typename R, int NR, int CMAX, bool RIG>
-__global__ void __launch_bounds__(256) schur_rhs_precond_kernel(SolveView<R> v, R* __restrict__ rhs, PrecondView<R> pc) {
-  using L = RecordLayout<NR, CMAX, RIG>;
-  constexpr int NP = planes_of<R>(L::kWidth);
-  constexpr int VN = Vec16<R>::kN;
-  const SceneView<R>& s = v.scene;
-  GB_WARP_SLOT_LOOP(s.n_slots) {
-    const int64_t i = base + lane;
-    const int pt = s.obs_point[i];
-    const bool valid = pt >= 0;
-    R rec[NP * VN];
-    int inst = 0, cam = 0, rig = -1;
-    R e[NR];
-    R Vi[6];
-#pragma unroll
-    for (int q = 0; q < NR; ++q) e[q] = R(0);
-    if (valid) {
-      load_record<R, NP>(v.rec, v.stride, i, rec);
-      shot_indices(s, shot_of(s, i), inst, cam, rig);
-#pragma unroll
-      for (int k = 0; k < 6; ++k) Vi[k] = v.Vinv[8 * int64_t(pt) + k];
-      R g[3] = {v.gp[4 * int64_t(pt)], v.gp[4 * int64_t(pt) + 1], v.gp[4 * int64_t(pt) + 2]};
-      R q3[3];
-      sym3_mul(Vi, g, q3);
-#pragma unroll
-      for (int q = 0; q < NR; ++q)
-        e[q] = rec[L::kPt + q * 3] * q3[0] + rec[L::kPt + q * 3 + 1] * q3[1] + rec[L::kPt + q * 3 + 2] * q3[2];
-    } else {
-#pragma unroll
-      for (int k = 0; k < NP * VN; ++k) rec[k] = R(0);
-#pragma unroll
-      for (int k = 0; k < 6; ++k) Vi[k] = R(0);
-    }
-    scatter_cam<R, NR, CMAX, RIG>(v, rhs, rec, e, valid, inst, cam, rig);
-    // preconditioner blocks
-    if (valid && v.inst_free[inst]) {
-      R tri[21];
-      schur_block<R, NR, 6>(rec + L::kInst, rec + L::kPt, Vi, tri);
-      R* dst = pc.inst + 24 * int64_t(inst);
-#pragma unroll
-      for (int k = 0; k < 20; k += 4) red_add4(dst + k, tri[k], tri[k + 1], tri[k + 2], tri[k + 3]);
-      red_add(dst + 20, tri[20]);
-    }
-    {
-      const bool cvalid = valid && v.cam_free[cam];
-      if (__any_sync(kFullMask, cvalid)) {
-        constexpr int T = TriSize<CMAX>::kN;
-        R tri[T];
-        if (cvalid) {
-          schur_block<R, NR, CMAX>(rec + L::kCam, rec + L::kPt, Vi, tri);
-        } else {
-#pragma unroll
-          for (int k = 0; k < T; ++k) tri[k] = R(0);
-        }
-        // aggregate over the warp when all lanes share the camera
-        const int lead = __shfl_sync(kFullMask, cam, 0);
-        const bool uniform = __all_sync(kFullMask, cvalid && cam == lead);
-        R* dst = pc.cam + int64_t(pc.cam_stride) * cam;
-        if (uniform) {
-#pragma unroll
-          for (int k = 0; k < T; ++k) {
-            R x = tri[k];
-#pragma unroll
-            for (int d = 16; d > 0; d >>= 1) x += __shfl_xor_sync(kFullMask, x, d);
-            if (lane == 0) red_add(dst + k, x);
-          }
-        } else if (cvalid) {
-#pragma unroll
-          for (int k = 0; k < T; ++k) red_add(dst + k, tri[k]);
-        }
-      }
-    }
-    if constexpr (RIG) {
-      if (valid && rig >= 0 && v.rig_free[rig]) {
-        R tri[21];
-        schur_block<R, NR, 6>(rec + L::kRig, rec + L::kPt, Vi, tri);
-        R* dst = pc.rig + 24 * int64_t(rig);
-#pragma unroll
-        for (int k = 0; k < 20; k += 4) red_add4(dst + k, tri[k], tri[k + 1], tri[k + 2], tri[k + 3]);
-        red_add(dst + 20, tri[20]);
-      }
-    }
-  }
-}
+// The right-hand side and preconditioner blocks, and the camera half of the
+// implicit Schur product, are summed in shot-major order
+// (solver_shot_major.cuh).
 
 // ---------------------------------------------------------------------------
 // Implicit Schur product, first half: zbuf_p += J_p^T (J_c x_c) per point.
@@ -712,47 +503,6 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, c
     }
     const bool tail = warp_segment_sum<3, R>(valid ? pt : -1, u);
     if (tail && valid && v.point_free[pt]) red_add4(zbuf + 4 * int64_t(pt), u[0], u[1], u[2], R(0));
-  }
-}
-
-// Implicit Schur product, second half:
-//   y_c += J_c^T (J_c x_c - J_p V^-1 zbuf_p).
-template <typename R, int NR, int CMAX, bool RIG>
-__global__ void __launch_bounds__(256) schur_camera_pass_kernel(SolveView<R> v, const R* __restrict__ x,
-                                                                const R* __restrict__ zbuf, R* __restrict__ y) {
-  using L = RecordLayout<NR, CMAX, RIG>;
-  constexpr int NP = planes_of<R>(L::kWidth);
-  constexpr int VN = Vec16<R>::kN;
-  const SceneView<R>& s = v.scene;
-  GB_WARP_SLOT_LOOP(s.n_slots) {
-    const int64_t i = base + lane;
-    const int pt = s.obs_point[i];
-    const bool valid = pt >= 0;
-    R rec[NP * VN];
-    R e[NR];
-    int inst = 0, cam = 0, rig = -1;
-    if (valid) {
-      load_record<R, NP>(v.rec, v.stride, i, rec);
-      shot_indices(s, shot_of(s, i), inst, cam, rig);
-      CamGather<R, CMAX> g;
-      gather_cam<R, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
-      apply_cam<R, NR, CMAX, RIG>(rec, g, e);
-      R Vi[6], zb[3], z[3];
-#pragma unroll
-      for (int k = 0; k < 6; ++k) Vi[k] = v.Vinv[8 * int64_t(pt) + k];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) zb[k] = zbuf[4 * int64_t(pt) + k];
-      sym3_mul(Vi, zb, z);
-#pragma unroll
-      for (int q = 0; q < NR; ++q)
-        e[q] -= rec[L::kPt + q * 3] * z[0] + rec[L::kPt + q * 3 + 1] * z[1] + rec[L::kPt + q * 3 + 2] * z[2];
-    } else {
-#pragma unroll
-      for (int k = 0; k < NP * VN; ++k) rec[k] = R(0);
-#pragma unroll
-      for (int q = 0; q < NR; ++q) e[q] = R(0);
-    }
-    scatter_cam<R, NR, CMAX, RIG>(v, y, rec, e, valid, inst, cam, rig);
   }
 }
 

@@ -321,6 +321,9 @@ class BundleAdjuster:
         self._check(self._L.gbba_set_internal_parameters_prior_sd(
             self._h, focal_sd, aspect_ratio_sd, c_sd, k1_sd, k2_sd, p1_sd, p2_sd, k3_sd, k4_sd))
 
+    def set_rig_parameters_prior_sd(self, rig_translation_sd, rig_rotation_sd) -> None:
+        self._check(self._L.gbba_set_rig_parameters_prior_sd(self._h, rig_translation_sd, rig_rotation_sd))
+
     def set_compute_reprojection_errors(self, v: bool) -> None:
         self._check(self._L.gbba_set_compute_reprojection_errors(self._h, int(v)))
 

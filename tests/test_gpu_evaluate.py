@@ -58,6 +58,21 @@ def test_rig_without_spherical_fp64():
     _compare(scene, evaluate_projections(scene, _lib.PRECISION_FP64), 1e-10)
 
 
+@pytest.mark.parametrize("precision,tol", [(_lib.PRECISION_FP64, 1e-10), (_lib.PRECISION_MIXED, 2e-4)])
+def test_rig_partly_applied(precision, tol):
+    # some shots have no rig camera, others an unused one: their rig-camera
+    # block is zero (projection_errors.h:184-188) while rig shots keep theirs
+    scene = syn.random_scene(13, [PERSPECTIVE, BROWN], n_shots=12, rig=True)
+    scene.shot_rig_camera[::3] = -1
+    scene.rig_camera_used[1] = 0
+    got = evaluate_projections(scene, precision)
+    _compare(scene, got, tol)
+    no_rig = (scene.shot_rig_camera[scene.obs_shot] < 0) | (scene.rig_camera_used[scene.shot_rig_camera[scene.obs_shot]] == 0)
+    assert no_rig.any() and (~no_rig).any()
+    assert np.all(got.jac_rig_camera[no_rig] == 0)
+    assert np.abs(got.jac_rig_camera[~no_rig]).max() > 0
+
+
 def test_utm_offsets_mixed_precision():
     """Georeferenced scene (x ~ 5e5, y ~ 4e6): the mixed path centres in FP64
     before the FP32 cast, so residuals stay within 1e-3 px."""
