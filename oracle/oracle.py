@@ -117,6 +117,17 @@ def loss(kind: int, threshold: float, s: float):
     return rho
 
 
+def mixture_group(residuals: np.ndarray, weights: np.ndarray, density_ratio: float):
+    """One mixture-reweighting group: returns (log-likelihood, new weights)."""
+    r = np.ascontiguousarray(residuals, np.float64)
+    w = np.array(weights, np.float64)
+    f = lib().oracle_mixture_group
+    f.argtypes = [C.c_int, C.c_int64, D, D, C.c_double]
+    f.restype = C.c_double
+    ll = f(r.shape[1], r.shape[0], _p(r), _p(w), density_ratio)
+    return ll, w
+
+
 # ---------------------------------------------------------------------------
 # FP64 CPU bundle-adjustment solve (oracle/solver.cpp)
 

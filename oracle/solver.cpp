@@ -752,6 +752,20 @@ struct Solver {
 
 }  // namespace
 
+// One group of MixtureReweighting::ComputeGroupWeights
+// (mixture_reweighting.cc:10-109): n residual vectors of dimension k
+// (row-major), weights updated in place; returns the log-likelihood.
+extern "C" double oracle_mixture_group(int k, int64_t n, const double* residuals, double* weights,
+                                       double density_ratio) {
+  std::vector<std::vector<double>> res(n, std::vector<double>(k));
+  std::vector<double*> w(n);
+  for (int64_t i = 0; i < n; ++i) {
+    for (int a = 0; a < k; ++a) res[i][a] = residuals[i * k + a];
+    w[i] = weights + i;
+  }
+  return Solver::mixture(res, w, density_ratio);
+}
+
 extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, OracleResult* out) {
   const OracleProblem& P = *Pp;
   const OracleOptions& O = *Op;

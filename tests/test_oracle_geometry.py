@@ -168,3 +168,23 @@ def test_loss_derivatives(kind, s):
 def test_trivial_and_small_huber_are_identity():
     assert np.allclose(oracle.loss(0, 1.0, 2.5), [2.5, 1.0, 0.0])
     assert np.allclose(oracle.loss(1, 2.0, 1.0), [1.0, 1.0, 0.0])
+
+
+def test_mixture_reweighting_separates_mixture():
+    # bundle/test/reweighting_test.cc:131-160 (MixtureReweighting_SeparatesMixture):
+    # 200 inliers at (0.1, 0.1), 20 outliers at (10, 10) starting at weight
+    # 0.01, outlier density 0.1 -> inliers above 0.8, outliers below 0.1.
+    res = np.array([[0.1, 0.1]] * 200 + [[10.0, 10.0]] * 20)
+    w0 = np.array([1.0] * 200 + [0.01] * 20)
+    ll, w = oracle.mixture_group(res, w0, 0.1)
+    assert ll != 0.0
+    assert w[0] > 0.8
+    assert w[200] < 0.1
+
+
+def test_mixture_reweighting_small_group_untouched():
+    # groups below the minimum sample size (10) keep their weights
+    # (mixture_reweighting.cc:22-24)
+    res = np.full((9, 2), 5.0)
+    ll, w = oracle.mixture_group(res, np.ones(9), 0.1)
+    assert ll == 0.0 and np.all(w == 1.0)
