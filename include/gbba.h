@@ -132,6 +132,28 @@ int gbba_evaluator_launches_per_run(const gbba_evaluator_t* ev);
 /* Bytes of the device-side residual+Jacobian records of one run. */
 int64_t gbba_evaluator_record_bytes(const gbba_evaluator_t* ev);
 
+/* Evaluation that allocates no memory.  No counterpart in the reference.
+ *
+ * For callers that cannot allocate device memory when they evaluate (a
+ * process whose device memory is all carved into its own pool, a real-time
+ * loop that must not stall on an allocation): every array of `scene` and of
+ * `out` is DEVICE memory of the current device, owned by the caller and
+ * sized as for gbba_evaluate_projections; the counts in `scene` are host
+ * values.  nr and cmax_out give the output layout (gbba_scene_layout on a
+ * host copy of the scene returns them).  FP64 arithmetic, the same as
+ * gbba_evaluate_projections with GBBA_PRECISION_FP64.  The per-shot geometry
+ * lives in a fixed device array of the library:
+ *   - at most 8192 shots (more: GBBA_ERR_INVALID_ARGUMENT);
+ *   - calls that overlap on one device race on that array: serialise them;
+ *   - the first call on a device looks the array up (this may load the
+ *     library's device code): make it before any stream capture there.
+ * stream is a cudaStream_t (NULL: default stream); the call returns after
+ * the stream has finished the evaluation.  Bad indices, unknown projection
+ * types and non-positive std deviations are found on the device and
+ * returned as the same status codes gbba_evaluate_projections uses. */
+int gbba_evaluate_projections_noalloc(const gbba_scene_t* scene, int nr, int cmax_out,
+                                      gbba_eval_output_t* out, void* stream);
+
 /* ------------------------------------------------------------------------
  * Bundle adjuster: bundle::BundleAdjuster (bundle_adjuster.h:173-386) and
  * the methods its pybind module binds (python/pybind.cc:60-147).  Ids are
