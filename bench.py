@@ -43,6 +43,7 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "BA time-to-converge (rel cost 1e-6) mixed vs FP64 GPU; Mobs/s residual+Jacobian"
 UNIT = "Mobs/s"
+CLOCK_WINDOW_S = 1.5
 
 
 def make_workload(name: str, seed_offset: int = 0):
@@ -158,12 +159,18 @@ def cpu_baseline(scene, target_s: float = 10.0) -> dict:
     rate = probe / max(time.perf_counter() - t0, 1e-9)
     m = int(min(n, max(probe, rate * target_s)))
     sub = scene.subset_observations(np.arange(m))
+    # one timed pass over the sample, then whole passes up to about target_s
     t0 = time.perf_counter()
     oracle.evaluate_scene(sub, threads)
+    one = time.perf_counter() - t0
+    reps = max(1, int(round(target_s / max(one, 1e-9))))
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        oracle.evaluate_scene(sub, threads)
     dt = time.perf_counter() - t0
-    return {"value": m / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {m} of {n} observations, FP64 residual+Jacobian blocks, {threads} threads, "
-                      f"{dt:.1f} s"}
+    return {"value": m * reps / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {m} of {n} observations x {reps} passes, FP64 residual+Jacobian blocks, "
+                      f"{threads} threads, {dt:.1f} s"}
 
 
 def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_tolerance: float = 1e-3) -> dict:
@@ -196,6 +203,7 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
             "final_cost": s["final_cost"], "initial_cost": s["initial_cost"], "iterations": s["iterations"],
             "solve_s": s["seconds"], "linear_solver_s": s["linear_solver_seconds"],
             "jacobian_s": s["jacobian_seconds"], "residual_s": s["residual_seconds"],
+            "setup_s": s["setup_seconds"], "first_iterate_s": float(tr[0, 2]), "run_wall_s": r["wall_s"],
             "kernel_launches": s["kernel_launches"],
             "pcg_iterations": int(tr[:, 4].sum()),
         }
@@ -276,6 +284,7 @@ def run_ours(args) -> None:
         dist.barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
+        w0 = time.perf_counter()
         t_all0 = torch.cuda.Event(enable_timing=True)
         t_all1 = torch.cuda.Event(enable_timing=True)
         with torch.cuda.stream(stream):
@@ -288,6 +297,15 @@ def run_ours(args) -> None:
                 ev_end[k].record(stream)
             t_all1.record(stream)
         torch.cuda.synchronize()
+        # The timed region is milliseconds long, shorter than the sampler's
+        # 200 ms period: keep the same kernel loop running (untimed) until
+        # the window holds several clock samples.
+        clock_window = CLOCK_WINDOW_S
+        with torch.cuda.stream(stream):
+            while time.perf_counter() - w0 < clock_window:
+                for _ in range(50):
+                    ev.run(sh)
+                torch.cuda.synchronize()
     if dist:
         dist.barrier()
     elapsed = t_all0.elapsed_time(t_all1) / 1e3
@@ -339,7 +357,8 @@ def run_ours(args) -> None:
                          "traffic": (tpo * n_obs if tpo else None),
                          "kernel": "eval_records_kernel", "algorithmic_bytes": int(in_bytes + rec_bytes),
                          "kernel_ms": rec_ms, "peak_source": peaks["source"]},
-            "clocks": clocks.summary(),
+            "clocks": dict(clocks.summary(), window=f"timed region plus an untimed continuation of the same "
+                                                    f"kernel loop, {CLOCK_WINDOW_S:.1f} s in all"),
             "gpu_launches": args.steps * ev.launches_per_run,
         }
         if not args.no_cpu_baseline:

@@ -395,8 +395,10 @@ std::string BundleAdjuster::FullReport() const {
   ss << "  Iterations           " << summary_.iterations << " (" << summary_.successful_steps << " successful, "
      << summary_.unsuccessful_steps << " unsuccessful)\n";
   ss << "  Time (s)             total " << summary_.seconds << ", linear solver " << summary_.linear_solver_seconds
-     << ", jacobian " << summary_.jacobian_seconds << ", residuals " << summary_.residual_seconds << "\n";
+     << ", jacobian " << summary_.jacobian_seconds << ", residuals " << summary_.residual_seconds << ", setup "
+     << summary_.setup_seconds << "\n";
   ss << "  Kernel launches      " << summary_.kernel_launches << "\n";
+  ss << "  PCG refinements      " << summary_.pcg_refinements << " (FP64 residuals of the mixed-precision solve)\n";
   ss << "  Termination          " << summary_.termination << "\n";
   return ss.str();
 }

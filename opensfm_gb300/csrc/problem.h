@@ -134,7 +134,9 @@ struct SolveSummary {
   double linear_solver_seconds = 0;
   double jacobian_seconds = 0;
   double residual_seconds = 0;
+  double setup_seconds = 0;  // slot sorts, uploads, device buffers
   int64_t kernel_launches = 0;
+  int64_t pcg_refinements = 0;  // FP64 residual evaluations (mixed-precision iterative refinement)
   std::string linear_solver;
   std::vector<IterationRecord> trace;
   std::vector<std::string> irls_lines;

@@ -19,6 +19,13 @@ namespace {
 
 constexpr int kDyn = -1;
 constexpr double kEps = 2.220446049250313e-16;
+// Iterative refinement of the mixed-precision linear solve: used when the
+// requested PCG tolerance is tighter than kRefineThreshold; every FP32 PCG
+// round reduces the residual by kRefineInnerTolerance; at most
+// kMaxRefinements FP64 residual evaluations per step.
+constexpr double kRefineThreshold = 1e-4;
+constexpr double kRefineInnerTolerance = 1e-3;
+constexpr int kMaxRefinements = 4;
 
 struct KernelConfig {
   int model;  // single model or kDyn
@@ -64,6 +71,56 @@ int slot_grid(int64_t n) {
 int elem_grid(int64_t n, int block = 256) { return int(std::max<int64_t>(1, (n + block - 1) / block)); }
 
 // ---------------------------------------------------------------------------
+// Slot construction from the uploaded observations (point-major order given
+// by `order`): observation packs, point index, GCP flag and unit IRLS
+// weights; padding slots get point -1.
+template <typename R>
+__global__ void build_slots_kernel(int64_t n_obs, int64_t n_slots, const Observation* __restrict__ raw,
+                                   const int32_t* __restrict__ order, ObsPack<R>* __restrict__ ob,
+                                   ObsPack<double>* __restrict__ ob64, int* __restrict__ opt,
+                                   uint8_t* __restrict__ gcp, R* __restrict__ weight) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < n_slots; s += stride) {
+    ObsPack<R> o{};
+    ObsPack<double> o64{};
+    int pt = -1;
+    uint8_t g = 0;
+    if (s < n_obs) {
+      const Observation q = raw[order[s]];
+      const double w = 1.0 / q.std_dev;
+      o.x = R(q.x);
+      o.y = R(q.y);
+      o.w = R(w);
+      o.shot = q.shot;
+      o64.x = q.x;
+      o64.y = q.y;
+      o64.w = w;
+      o64.shot = q.shot;
+      pt = q.point;
+      g = q.is_gcp ? 1 : 0;
+    }
+    ob[s] = o;
+    if (ob64) ob64[s] = o64;
+    opt[s] = pt;
+    gcp[s] = g;
+    weight[s] = R(1);
+  }
+}
+
+// Point and shot of every shot-major slot.
+template <typename R>
+__global__ void build_shot_major_kernel(int64_t n_slots, const int32_t* __restrict__ src, const int* __restrict__ opt,
+                                        const ObsPack<R>* __restrict__ ob, int* __restrict__ pt,
+                                        int* __restrict__ sh) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n_slots; j += stride) {
+    const int s = src[j];
+    pt[j] = s >= 0 ? opt[s] : -1;
+    sh[j] = s >= 0 ? ob[s].shot : 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Small camera-side kernels.
 
 template <typename R>
@@ -86,12 +143,14 @@ __global__ void cam_damp_kernel(int n, const R* __restrict__ dc, const double* _
 }
 
 template <typename R>
-__global__ void rhs_finish_kernel(int n, const R* __restrict__ gc, const double* __restrict__ pgrad,
-                                  const uint8_t* __restrict__ mask, R* __restrict__ rhs, double* __restrict__ bb) {
+__global__ void rhs_finish_kernel(int n, const double* __restrict__ gc, const double* __restrict__ pgrad,
+                                  const uint8_t* __restrict__ mask, double* __restrict__ rhs64, R* __restrict__ rhs,
+                                  double* __restrict__ bb) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   double v = 0.0;
   if (j < n) {
-    const double b = mask[j] ? double(rhs[j]) - double(gc[j]) - pgrad[j] : 0.0;
+    const double b = mask[j] ? rhs64[j] - gc[j] - pgrad[j] : 0.0;
+    rhs64[j] = b;
     rhs[j] = R(b);
     v = b * b;
   }
@@ -262,6 +321,38 @@ __global__ void pcg_dir_kernel(int n, const double* __restrict__ s, R* __restric
   if (j >= n) return;
   const double beta = s[kRZ] != 0.0 ? s[kRZN] / s[kRZ] : 0.0;
   p[j] = z[j] + R(beta) * p[j];
+}
+
+template <typename From, typename To>
+__global__ void convert_kernel(int n, const From* __restrict__ a, To* __restrict__ b) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) b[j] = To(a[j]);
+}
+
+// Residual of iterative refinement: r = b - (y + (pdiag + damp) x) on the
+// free coordinates, in FP64 (y = the FP64 implicit Schur product W/V part);
+// writes r in the working precision for the next PCG round and |r|^2.
+template <typename R>
+__global__ void refine_residual_kernel(int n, const double* __restrict__ x, const double* __restrict__ pdiag,
+                                       const R* __restrict__ damp, const uint8_t* __restrict__ mask,
+                                       const double* __restrict__ b, const double* __restrict__ y,
+                                       R* __restrict__ r, double* __restrict__ rr) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (j < n) {
+    double v = 0.0;
+    if (mask[j]) v = b[j] - (y[j] + (pdiag[j] + double(damp[j])) * x[j]);
+    r[j] = R(v);
+    acc = v * v;
+  }
+  block_sum_add<256>(acc, rr);
+}
+
+// x64 += e (the correction from a PCG round).
+template <typename R>
+__global__ void add_correction_kernel(int n, const R* __restrict__ e, double* __restrict__ x) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < n) x[j] += double(e[j]);
 }
 
 static __global__ void pcg_rotate_kernel(double* s) {
@@ -541,6 +632,7 @@ class DeviceSolver final : public SolverBase {
   double prior_model_change(const std::vector<double>& x, const std::vector<double>& dx);
   // ---- linear solve
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
+  int run_pcg(const R* rhs, double bb, double tol, int max_it);
   // ---- IRLS
   double compute_weights(std::vector<std::string>& groups_report, int& proj_out, int& proj_total,
                          std::vector<std::pair<std::string, std::pair<int, int>>>& other);
@@ -568,6 +660,7 @@ class DeviceSolver final : public SolverBase {
   std::vector<double> point_prior_w_;
   double ratio_cam_ = 1e-3, ratio_rig_ = 1e-3, ratio_gps_ = 1e-3, ratio_gcp3d_ = 1e-3;
   int64_t launches_ = 0;
+  int64_t refinements_ = 0;  // FP64 residual evaluations of iterative refinement
   std::vector<double> last_errors_, last_weights_;
 
   // device state
@@ -576,7 +669,9 @@ class DeviceSolver final : public SolverBase {
   DeviceArray<int> d_obs_point_;
   DeviceArray<uint8_t> d_gcp_;
   DeviceArray<R> d_weight_;
-  DeviceArray<double> d_resid_;
+  // FP64 residuals of the current state, and (mixed mode) of the last
+  // candidate: swapped in when the candidate is accepted
+  DeviceArray<double> d_resid_, d_resid_cand_;
   DeviceArray<V16> d_rec_;
   // shot-major order: point-major slot, point and shot of every shot-major
   // slot, and the shot-major copy of the records
@@ -597,7 +692,12 @@ class DeviceSolver final : public SolverBase {
   DeviceArray<PS> d_Xw_;
   DeviceArray<uint8_t> d_inst_free_, d_cam_free_, d_rig_free_, d_point_free_, d_cmask_;
   DeviceArray<R> d_Vp_, d_gp_, d_Vinv_, d_pscale_, d_zbuf_, d_dp_;
-  DeviceArray<R> d_gc_, d_dc_, d_rhs_, d_cscale_, d_damp_;
+  DeviceArray<double> d_gc_, d_rhs64_;  // FP64 sums: gradient, reduced right-hand side
+  // iterative refinement (mixed mode): FP64 step, FP64 Schur product, the
+  // FP32 residual handed to PCG and its squared norm
+  DeviceArray<double> d_x64_, d_zbuf64_, d_y64_, d_rr64_;
+  DeviceArray<R> d_rref_;
+  DeviceArray<R> d_dc_, d_rhs_, d_cscale_, d_damp_;
   DeviceArray<double> d_pdiag_, d_pgrad_;
   DeviceArray<R> d_x_, d_r_, d_z_, d_p_, d_y_;
   DeviceArray<R> d_tri_inst_, d_tri_rig_, d_tri_cam_, d_minv_inst_, d_minv_rig_, d_minv_cam_;
@@ -688,73 +788,71 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
       cmask_[cl_.cam_base + 16 * c + k] = P.cameras[c].free_mask[k];
     }
 
-  // slots: observations sorted by point (stable counting sort), padded to a
-  // warp multiple
-  std::vector<int64_t> order(n_obs_);
-  {
-    std::vector<int64_t> start(n_pt_ + 1, 0);
-    for (const Observation& q : P.observations) ++start[q.point + 1];
-    for (int64_t p = 0; p < n_pt_; ++p) start[p + 1] += start[p];
-    for (int64_t o = 0; o < n_obs_; ++o) order[start[P.observations[o].point]++] = o;
-  }
+  // Slots.  Point-major order: observations sorted by point (stable
+  // counting sort), padded to a warp multiple.  Shot-major order of the same
+  // slots: by rig instance, then shot, then point (a stable counting sort of
+  // the point-major slots by shot rank); padding slots go last.  The host
+  // makes three sequential passes over the observations (counts, point
+  // scatter, shot scatter); the per-slot arrays are built on the device from
+  // the uploaded observations.
+  if (n_obs_ > int64_t(std::numeric_limits<int32_t>::max()) - 32)
+    throw std::invalid_argument("more observations than a 32-bit slot index can address");
   n_slots_ = std::max<int64_t>(32, (n_obs_ + 31) / 32 * 32);
-  slot_obs_.assign(n_slots_, -1);
-  std::vector<ObsPack<R>> ob(n_slots_);
-  std::vector<ObsPack<double>> ob64(kMixed ? n_slots_ : 0);
-  std::vector<int> opt(n_slots_, -1);
-  std::vector<uint8_t> gcp(n_slots_, 0);
-  for (int64_t s = 0; s < n_slots_; ++s) {
-    ObsPack<R> o{};
-    ObsPack<double> o64{};
-    if (s < n_obs_) {
-      const Observation& q = P.observations[order[s]];
-      slot_obs_[s] = order[s];
-      o.x = R(q.x); o.y = R(q.y); o.w = R(1.0 / q.std_dev); o.shot = q.shot;
-      o64.x = q.x; o64.y = q.y; o64.w = 1.0 / q.std_dev; o64.shot = q.shot;
-      opt[s] = q.point;
-      gcp[s] = q.is_gcp ? 1 : 0;
-    }
-    ob[s] = o;
-    if (kMixed) ob64[s] = o64;
-  }
-  d_obs_.upload(ob);
-  if (kMixed) d_obs64_.upload(ob64);
-  d_obs_point_.upload(opt);
-  d_gcp_.upload(gcp);
-  d_weight_.resize(n_slots_);
+  std::vector<int> rank(n_shots_);
   {
-    std::vector<R> w(n_slots_, R(1));
-    d_weight_.upload(w);
-  }
-  d_resid_.resize(4 * n_slots_);
-  d_resid_.zero();
-  d_rec_.resize(size_t(n_planes_) * n_slots_);
-  d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
-
-  // shot-major order of the same slots: by rig instance, then shot, then
-  // point (a stable counting sort of the point-major slots by shot rank);
-  // padding slots go last
-  {
-    std::vector<int> shots(n_shots_), rank(n_shots_);
+    std::vector<int> shots(n_shots_);
     std::iota(shots.begin(), shots.end(), 0);
     std::stable_sort(shots.begin(), shots.end(),
                      [&](int a, int b) { return P.shots[a].instance < P.shots[b].instance; });
     for (int r = 0; r < n_shots_; ++r) rank[shots[r]] = r;
-    std::vector<int64_t> start(n_shots_ + 1, 0);
-    for (int64_t s = 0; s < n_obs_; ++s) ++start[rank[P.observations[order[s]].shot] + 1];
-    for (int r = 0; r < n_shots_; ++r) start[r + 1] += start[r];
-    std::vector<int> src(n_slots_, -1), pt(n_slots_, -1), sh(n_slots_, 0);
-    for (int64_t s = 0; s < n_obs_; ++s) {
-      const Observation& q = P.observations[order[s]];
-      const int64_t j = start[rank[q.shot]]++;
-      src[j] = int(s);
-      pt[j] = q.point;
-      sh[j] = q.shot;
-    }
-    d_sm_src_.upload(src);
-    d_sm_point_.upload(pt);
-    d_sm_shot_.upload(sh);
   }
+  std::vector<int64_t> pstart(n_pt_ + 1, 0), sstart(n_shots_ + 1, 0);
+  group_count_.assign(n_shots_ + 1, 0);
+  int gcp_shot = -1;
+  for (const Observation& q : P.observations) {
+    ++pstart[q.point + 1];
+    ++sstart[rank[q.shot] + 1];
+    ++group_count_[q.is_gcp ? n_shots_ : q.shot];
+    if (q.is_gcp && gcp_shot < 0) gcp_shot = q.shot;
+  }
+  for (int64_t p = 0; p < n_pt_; ++p) pstart[p + 1] += pstart[p];
+  for (int r = 0; r < n_shots_; ++r) sstart[r + 1] += sstart[r];
+  std::vector<int32_t> order(n_obs_);
+  for (int64_t o = 0; o < n_obs_; ++o) order[pstart[P.observations[o].point]++] = int32_t(o);
+  std::vector<int32_t> src(n_slots_, -1);
+  for (int64_t s = 0; s < n_obs_; ++s) src[sstart[rank[P.observations[order[s]].shot]]++] = int32_t(s);
+  slot_obs_.assign(n_slots_, -1);
+  for (int64_t s = 0; s < n_obs_; ++s) slot_obs_[s] = order[s];
+  {
+    DeviceArray<Observation> raw;
+    DeviceArray<int32_t> d_order;
+    raw.upload(P.observations);
+    d_order.upload(order);
+    d_sm_src_.upload(src);
+    d_obs_.resize(n_slots_);
+    if (kMixed) d_obs64_.resize(n_slots_);
+    d_obs_point_.resize(n_slots_);
+    d_gcp_.resize(n_slots_);
+    d_weight_.resize(n_slots_);
+    d_sm_point_.resize(n_slots_);
+    d_sm_shot_.resize(n_slots_);
+    build_slots_kernel<R><<<elem_grid(n_slots_), 256>>>(n_obs_, n_slots_, raw.get(), d_order.get(), d_obs_.get(),
+                                                         kMixed ? d_obs64_.get() : nullptr, d_obs_point_.get(),
+                                                         d_gcp_.get(), d_weight_.get());
+    build_shot_major_kernel<R><<<elem_grid(n_slots_), 256>>>(n_slots_, d_sm_src_.get(), d_obs_point_.get(),
+                                                              d_obs_.get(), d_sm_point_.get(), d_sm_shot_.get());
+    launches_ += 2;
+    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cudaDeviceSynchronize());  // raw and d_order are released here
+  }
+  d_resid_.resize(4 * n_slots_);
+  d_resid_.zero();
+  if (kMixed) {
+    d_resid_cand_.resize(4 * n_slots_);
+    d_resid_cand_.zero();
+  }
+  d_rec_.resize(size_t(n_planes_) * n_slots_);
+  d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
   d_rec_sm_.resize(size_t(n_planes_) * n_slots_);
   d_rec_sm_.zero();
 
@@ -816,9 +914,18 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   d_zbuf_.resize(4 * np);
   d_dp_.resize(4 * np);
   d_dp_.zero();
+  if (kMixed) {
+    d_zbuf64_.resize(4 * np);
+    d_x64_.resize(cl_.n);
+    d_y64_.resize(cl_.n);
+    d_rref_.resize(cl_.n);
+    d_rr64_.resize(1);
+  }
 
   // camera-side vectors
-  for (auto* a : {&d_gc_, &d_dc_, &d_rhs_, &d_cscale_, &d_damp_, &d_x_, &d_r_, &d_z_, &d_p_, &d_y_}) a->resize(cl_.n);
+  for (auto* a : {&d_dc_, &d_rhs_, &d_cscale_, &d_damp_, &d_x_, &d_r_, &d_z_, &d_p_, &d_y_}) a->resize(cl_.n);
+  d_gc_.resize(cl_.n);
+  d_rhs64_.resize(cl_.n);
   d_pdiag_.resize(cl_.n);
   d_pgrad_.resize(cl_.n);
   d_tri_inst_.resize(24 * std::max(1, n_inst_));
@@ -831,17 +938,10 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   d_scal_.resize(8);
   d_bad_.resize(2);
 
-  // IRLS projection groups: one per shot, plus GCP2D
-  group_count_.assign(n_shots_ + 1, 0);
+  // IRLS projection groups: one per shot, plus GCP2D (counted with the slots)
   group_dim_.assign(n_shots_ + 1, 2);
   for (int s = 0; s < n_shots_; ++s) group_dim_[s] = P.cameras[P.shots[s].camera].model == kSpherical ? 3 : 2;
-  int gcp_dim = -1;
-  for (const Observation& q : P.observations) {
-    const int g = q.is_gcp ? n_shots_ : q.shot;
-    group_count_[g]++;
-    if (q.is_gcp && gcp_dim < 0) gcp_dim = group_dim_[q.shot];
-  }
-  if (gcp_dim > 0) group_dim_[n_shots_] = gcp_dim;
+  if (gcp_shot >= 0) group_dim_[n_shots_] = group_dim_[gcp_shot];
   group_ratio_ = P.group_density_ratio;
   if (group_ratio_.size() != size_t(n_shots_ + 1)) group_ratio_.assign(n_shots_ + 1, opts.default_density_ratio);
   d_group_dim_.upload(group_dim_);
@@ -952,6 +1052,7 @@ SolveView<R> DeviceSolver<R>::view() {
   v.Vinv = d_Vinv_.get();
   v.gc = d_gc_.get();
   v.dc = d_dc_.get();
+  v.resid64 = kMixed ? d_resid_.get() : nullptr;
   return v;
 }
 
@@ -1004,12 +1105,17 @@ struct CostLaunch {
 };
 
 // FP64 cost of the current (or candidate) state; projection part on the
-// device, priors on the host.
+// device, priors on the host.  In mixed mode a candidate's residuals are
+// always kept (d_resid_cand_): the next linearization uses them if the
+// candidate is accepted.
 template <typename R>
 double DeviceSolver<R>::cost_pass(bool candidate, bool store_residuals) {
   GB_CUDA(cudaMemset(d_scal_.get() + 6, 0, 2 * sizeof(double)));
-  CostLaunch<R> f{view64(candidate), d_weight_.get(), opts_.loss, opts_.loss_threshold,
-                  store_residuals ? d_resid_.get() : nullptr, d_scal_.get() + 6};
+  double* resid = nullptr;
+  if (candidate && kMixed) resid = d_resid_cand_.get();
+  else if (store_residuals) resid = d_resid_.get();
+  CostLaunch<R> f{view64(candidate), d_weight_.get(), opts_.loss, opts_.loss_threshold, resid,
+                  d_scal_.get() + 6};
   dispatch_config(kc_, f);
   ++launches_;
   if (!point_priors_.empty()) {

@@ -217,8 +217,9 @@ struct SolveView {
   R* Vp;                         // [n_points][8] xx xy xz yy yz zz
   R* gp;                         // [n_points][4]
   R* Vinv;                       // [n_points][8]
-  R* gc;                         // [cl.n] camera-side gradient J^T r
+  double* gc;                    // [cl.n] camera-side gradient J^T r (FP64 sums)
   R* dc;                         // [cl.n] camera-side squared column norms
+  const double* resid64;         // [n_slots][4] FP64 residuals of the current state, or null
 };
 
 template <typename R>
@@ -314,6 +315,13 @@ __global__ void __launch_bounds__(256) linearize_kernel(SolveView<R> v, uint64_t
       ObsInputs<R> in;
       load_inputs<R, M>(s, ob, pt, cams, models, in);
       eval_observation<R, M, NR, CMAX, RIG, true>(in, rec);
+      if (v.resid64) {
+        // mixed precision: the residual itself comes from the FP64 cost pass
+        // of the same state (the FP32 one carries ~1e-4 sigma of rounding
+        // at normalized-coordinate magnitudes); the Jacobian stays FP32
+#pragma unroll
+        for (int q = 0; q < NR; ++q) rec[L::kR + q] = R(v.resid64[4 * i + q]);
+      }
       robust_correct<R, NR, CMAX, RIG>(v.loss, v.loss_a, v.weight[i], rec);
     }
 #pragma unroll
@@ -473,9 +481,12 @@ struct PrecondView {
 
 // ---------------------------------------------------------------------------
 // Implicit Schur product, first half: zbuf_p += J_p^T (J_c x_c) per point.
-template <typename R, int NR, int CMAX, bool RIG>
-__global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, const R* __restrict__ x,
-                                                               R* __restrict__ zbuf) {
+// A is the arithmetic of the product: the working precision R for the PCG
+// iterations, FP64 (on the same records) for the residual of iterative
+// refinement.
+template <typename R, typename A, int NR, int CMAX, bool RIG>
+__global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, const A* __restrict__ x,
+                                                               A* __restrict__ zbuf) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
   constexpr int VN = Vec16<R>::kN;
@@ -484,16 +495,19 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, c
     const int64_t i = base + lane;
     const int pt = s.obs_point[i];
     const bool valid = pt >= 0;
-    R u[3] = {R(0), R(0), R(0)};
+    A u[3] = {A(0), A(0), A(0)};
     if (valid) {
-      R rec[NP * VN];
-      load_record<R, NP>(v.rec, v.stride, i, rec);
+      R rec_r[NP * VN];
+      load_record<R, NP>(v.rec, v.stride, i, rec_r);
+      A rec[NP * VN];
+#pragma unroll
+      for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
       int inst, cam, rig;
       shot_indices(s, shot_of(s, i), inst, cam, rig);
-      CamGather<R, CMAX> g;
-      gather_cam<R, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
-      R t[NR];
-      apply_cam<R, NR, CMAX, RIG>(rec, g, t);
+      CamGather<A, CMAX> g;
+      gather_cam<A, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
+      A t[NR];
+      apply_cam<A, NR, CMAX, RIG>(rec, g, t);
 #pragma unroll
       for (int q = 0; q < NR; ++q) {
         u[0] += rec[L::kPt + q * 3] * t[q];
@@ -501,8 +515,8 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, c
         u[2] += rec[L::kPt + q * 3 + 2] * t[q];
       }
     }
-    const bool tail = warp_segment_sum<3, R>(valid ? pt : -1, u);
-    if (tail && valid && v.point_free[pt]) red_add4(zbuf + 4 * int64_t(pt), u[0], u[1], u[2], R(0));
+    const bool tail = warp_segment_sum<3, A>(valid ? pt : -1, u);
+    if (tail && valid && v.point_free[pt]) red_add4(zbuf + 4 * int64_t(pt), u[0], u[1], u[2], A(0));
   }
 }
 

@@ -161,21 +161,24 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
   constexpr int VN = Vec16<R>::kN;
-  constexpr bool kCarryCam = carry_fits<R, 2 * CMAX>();
+  // the gradient is summed in FP64 (near the optimum it is a small
+  // difference of large sums); the column norms in the working precision
   const SceneView<R>& s = v.scene;
-  R* gc = v.gc;
+  double* gc = v.gc;
   R* dc = v.dc;
   const CamLayout cl = v.cl;
-  auto d_inst = [gc, dc](int b, int k) { return k < 6 ? gc + 8 * b + k : dc + 8 * b + (k - 6); };
-  auto d_cam = [gc, dc, cl](int b, int k) {
-    return k < CMAX ? gc + cl.cam_base + 16 * b + k : dc + cl.cam_base + 16 * b + (k - CMAX);
-  };
-  auto d_rig = [gc, dc, cl](int b, int k) {
-    return k < 6 ? gc + cl.rig_base + 8 * b + k : dc + cl.rig_base + 8 * b + (k - 6);
-  };
-  KeyCarry<12, R, true> c_inst;
-  KeyCarry<2 * CMAX, R, kCarryCam> c_cam;
-  KeyCarry<12, R, true> c_rig;
+  auto g_inst = [gc](int b, int k) { return gc + 8 * b + k; };
+  auto d_inst = [dc](int b, int k) { return dc + 8 * b + k; };
+  auto g_cam = [gc, cl](int b, int k) { return gc + cl.cam_base + 16 * b + k; };
+  auto d_cam = [dc, cl](int b, int k) { return dc + cl.cam_base + 16 * b + k; };
+  auto g_rig = [gc, cl](int b, int k) { return gc + cl.rig_base + 8 * b + k; };
+  auto d_rig = [dc, cl](int b, int k) { return dc + cl.rig_base + 8 * b + k; };
+  KeyCarry<6, double, true> cg_inst;
+  KeyCarry<6, R, true> cd_inst;
+  KeyCarry<CMAX, double, carry_fits<double, CMAX>()> cg_cam;
+  KeyCarry<CMAX, R, carry_fits<R, CMAX>()> cd_cam;
+  KeyCarry<6, double, true> cg_rig;
+  KeyCarry<6, R, true> cd_rig;
   GB_WARP_CHUNK_LOOP(s.n_slots) {
     const int64_t j = base + lane;
     const int src = sm.src[j];
@@ -193,7 +196,8 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
     int inst = 0, cam = 0, rig = -1;
     if (valid) shot_indices(s, sm.shot[j], inst, cam, rig);
     {
-      R gd[12];
+      double g6[6];
+      R d6[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         R gs = R(0), ds = R(0);
@@ -203,15 +207,18 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
           gs += jv * rec[L::kR + q];
           ds += jv * jv;
         }
-        gd[k] = gs;
-        gd[6 + k] = ds;
+        g6[k] = double(gs);
+        d6[k] = ds;
       }
-      c_inst.add((valid && v.inst_free[inst]) ? inst : -1, gd, d_inst);
+      const int key = (valid && v.inst_free[inst]) ? inst : -1;
+      cg_inst.add(key, g6, g_inst);
+      cd_inst.add(key, d6, d_inst);
     }
     {
       const bool cvalid = valid && v.cam_free[cam];
       if (__any_sync(kFullMask, cvalid)) {
-        R gd[2 * CMAX];
+        double gcv[CMAX];
+        R dcv[CMAX];
 #pragma unroll
         for (int k = 0; k < CMAX; ++k) {
           R gs = R(0), ds = R(0);
@@ -221,16 +228,18 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
             gs += jv * rec[L::kR + q];
             ds += jv * jv;
           }
-          gd[k] = gs;
-          gd[CMAX + k] = ds;
+          gcv[k] = double(gs);
+          dcv[k] = ds;
         }
-        c_cam.add(cvalid ? cam : -1, gd, d_cam);
+        cg_cam.add(cvalid ? cam : -1, gcv, g_cam);
+        cd_cam.add(cvalid ? cam : -1, dcv, d_cam);
       }
     }
     if constexpr (RIG) {
       const bool rvalid = valid && rig >= 0 && v.rig_free[rig];
       if (__any_sync(kFullMask, rvalid)) {
-        R gd[12];
+        double g6[6];
+        R d6[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
           R gs = R(0), ds = R(0);
@@ -240,44 +249,53 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
             gs += jv * rec[L::kR + q];
             ds += jv * jv;
           }
-          gd[k] = gs;
-          gd[6 + k] = ds;
+          g6[k] = double(gs);
+          d6[k] = ds;
         }
-        c_rig.add(rvalid ? rig : -1, gd, d_rig);
+        cg_rig.add(rvalid ? rig : -1, g6, g_rig);
+        cd_rig.add(rvalid ? rig : -1, d6, d_rig);
       }
     }
   }
-  constexpr int KS = (2 * CMAX > 12) ? 2 * CMAX : 12;
-  __shared__ CarryStage<R, KS> st;
-  c_inst.finish(d_inst, st.key, st.val);
-  c_cam.finish(d_cam, st.key, st.val);
-  if constexpr (RIG) c_rig.finish(d_rig, st.key, st.val);
+  constexpr int KS = CMAX > 6 ? CMAX : 6;
+  __shared__ CarryStage<double, KS> sg;
+  __shared__ CarryStage<R, KS> sd;
+  cg_inst.finish(g_inst, sg.key, sg.val);
+  cd_inst.finish(d_inst, sd.key, sd.val);
+  cg_cam.finish(g_cam, sg.key, sg.val);
+  cd_cam.finish(d_cam, sd.key, sd.val);
+  if constexpr (RIG) {
+    cg_rig.finish(g_rig, sg.key, sg.val);
+    cd_rig.finish(d_rig, sd.key, sd.val);
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Right-hand side sum_o J_c^T J_p V^-1 g_p and Schur-Jacobi blocks, shot-major.
 template <typename R, int NR, int CMAX, bool RIG>
 __global__ void __launch_bounds__(kShotMajorBlock) schur_rhs_precond_sm_kernel(SolveView<R> v, ShotMajorView<R> sm,
-                                                                               R* __restrict__ rhs,
+                                                                               double* __restrict__ rhs,
                                                                                PrecondView<R> pc) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
   constexpr int VN = Vec16<R>::kN;
   constexpr int T = TriSize<CMAX>::kN;
-  constexpr bool kCarryCam = carry_fits<R, CMAX + T>();
-  constexpr bool kCarry6 = carry_fits<R, 27>();
+  // right-hand side summed in FP64 (it cancels against the gradient),
+  // preconditioner blocks in the working precision
   const SceneView<R>& s = v.scene;
   const CamLayout cl = v.cl;
-  auto d_inst = [rhs, pc](int b, int k) { return k < 6 ? rhs + 8 * b + k : pc.inst + 24 * int64_t(b) + (k - 6); };
-  auto d_cam = [rhs, pc, cl](int b, int k) {
-    return k < CMAX ? rhs + cl.cam_base + 16 * b + k : pc.cam + int64_t(pc.cam_stride) * b + (k - CMAX);
-  };
-  auto d_rig = [rhs, pc, cl](int b, int k) {
-    return k < 6 ? rhs + cl.rig_base + 8 * b + k : pc.rig + 24 * int64_t(b) + (k - 6);
-  };
-  KeyCarry<27, R, kCarry6> c_inst;
-  KeyCarry<CMAX + T, R, kCarryCam> c_cam;
-  KeyCarry<27, R, kCarry6> c_rig;
+  auto b_inst = [rhs](int b, int k) { return rhs + 8 * b + k; };
+  auto t_inst = [pc](int b, int k) { return pc.inst + 24 * int64_t(b) + k; };
+  auto b_cam = [rhs, cl](int b, int k) { return rhs + cl.cam_base + 16 * b + k; };
+  auto t_cam = [pc](int b, int k) { return pc.cam + int64_t(pc.cam_stride) * b + k; };
+  auto b_rig = [rhs, cl](int b, int k) { return rhs + cl.rig_base + 8 * b + k; };
+  auto t_rig = [pc](int b, int k) { return pc.rig + 24 * int64_t(b) + k; };
+  KeyCarry<6, double, true> cb_inst;
+  KeyCarry<21, R, carry_fits<R, 21>()> ct_inst;
+  KeyCarry<CMAX, double, carry_fits<double, CMAX>()> cb_cam;
+  KeyCarry<T, R, carry_fits<R, T>()> ct_cam;
+  KeyCarry<6, double, true> cb_rig;
+  KeyCarry<21, R, carry_fits<R, 21>()> ct_rig;
   GB_WARP_CHUNK_LOOP(s.n_slots) {
     const int64_t j = base + lane;
     const int pt = sm.point[j];
@@ -306,63 +324,78 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_rhs_precond_sm_kernel(S
     }
     {
       // instance: rhs (6) + Schur-Jacobi block (21)
-      R acc[27];
+      double b6[6];
+      R tri[21];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
         R t = R(0);
 #pragma unroll
         for (int q = 0; q < NR; ++q) t += rec[L::kInst + q * 6 + k] * e[q];
-        acc[k] = t;
+        b6[k] = double(t);
       }
-      schur_block<R, NR, 6>(rec + L::kInst, rec + L::kPt, Vi, acc + 6);
-      c_inst.add((valid && v.inst_free[inst]) ? inst : -1, acc, d_inst);
+      schur_block<R, NR, 6>(rec + L::kInst, rec + L::kPt, Vi, tri);
+      const int key = (valid && v.inst_free[inst]) ? inst : -1;
+      cb_inst.add(key, b6, b_inst);
+      ct_inst.add(key, tri, t_inst);
     }
     {
       const bool cvalid = valid && v.cam_free[cam];
       if (__any_sync(kFullMask, cvalid)) {
-        R acc[CMAX + T];
+        double bc[CMAX];
+        R tri[T];
 #pragma unroll
         for (int k = 0; k < CMAX; ++k) {
           R t = R(0);
 #pragma unroll
           for (int q = 0; q < NR; ++q) t += rec[L::kCam + q * CMAX + k] * e[q];
-          acc[k] = t;
+          bc[k] = double(t);
         }
-        schur_block<R, NR, CMAX>(rec + L::kCam, rec + L::kPt, Vi, acc + CMAX);
-        c_cam.add(cvalid ? cam : -1, acc, d_cam);
+        schur_block<R, NR, CMAX>(rec + L::kCam, rec + L::kPt, Vi, tri);
+        cb_cam.add(cvalid ? cam : -1, bc, b_cam);
+        ct_cam.add(cvalid ? cam : -1, tri, t_cam);
       }
     }
     if constexpr (RIG) {
       const bool rvalid = valid && rig >= 0 && v.rig_free[rig];
       if (__any_sync(kFullMask, rvalid)) {
-        R acc[27];
+        double b6[6];
+        R tri[21];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
           R t = R(0);
 #pragma unroll
           for (int q = 0; q < NR; ++q) t += rec[L::kRig + q * 6 + k] * e[q];
-          acc[k] = t;
+          b6[k] = double(t);
         }
-        schur_block<R, NR, 6>(rec + L::kRig, rec + L::kPt, Vi, acc + 6);
-        c_rig.add(rvalid ? rig : -1, acc, d_rig);
+        schur_block<R, NR, 6>(rec + L::kRig, rec + L::kPt, Vi, tri);
+        cb_rig.add(rvalid ? rig : -1, b6, b_rig);
+        ct_rig.add(rvalid ? rig : -1, tri, t_rig);
       }
     }
   }
-  constexpr int KS = (CMAX + T > 27) ? CMAX + T : 27;
-  __shared__ CarryStage<R, KS> st;
-  c_inst.finish(d_inst, st.key, st.val);
-  c_cam.finish(d_cam, st.key, st.val);
-  if constexpr (RIG) c_rig.finish(d_rig, st.key, st.val);
+  constexpr int KB = CMAX > 6 ? CMAX : 6;
+  constexpr int KT = T > 21 ? T : 21;
+  __shared__ CarryStage<double, KB> sb;
+  __shared__ CarryStage<R, KT> stt;
+  cb_inst.finish(b_inst, sb.key, sb.val);
+  ct_inst.finish(t_inst, stt.key, stt.val);
+  cb_cam.finish(b_cam, sb.key, sb.val);
+  ct_cam.finish(t_cam, stt.key, stt.val);
+  if constexpr (RIG) {
+    cb_rig.finish(b_rig, sb.key, sb.val);
+    ct_rig.finish(t_rig, stt.key, stt.val);
+  }
 }
 
 // ---------------------------------------------------------------------------
 // Implicit Schur product, camera half, shot-major:
 //   y_c += J_c^T (J_c x_c - J_p V^-1 zbuf_p).
-template <typename R, int NR, int CMAX, bool RIG>
+// A is the arithmetic of the product (see schur_point_pass_kernel).
+template <typename R, typename A, int NR, int CMAX, bool RIG>
 __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(SolveView<R> v, ShotMajorView<R> sm,
-                                                                               const R* __restrict__ x,
-                                                                               const R* __restrict__ zbuf,
-                                                                               R* __restrict__ y) {
+                                                                               const A* __restrict__ x,
+                                                                               const A* __restrict__ zbuf,
+                                                                               A* __restrict__ y) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
   constexpr int VN = Vec16<R>::kN;
@@ -371,25 +404,28 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
   auto d_inst = [y](int b, int k) { return y + 8 * b + k; };
   auto d_cam = [y, cl](int b, int k) { return y + cl.cam_base + 16 * b + k; };
   auto d_rig = [y, cl](int b, int k) { return y + cl.rig_base + 8 * b + k; };
-  KeyCarry<6, R, true> c_inst;
-  KeyCarry<CMAX, R, carry_fits<R, CMAX>()> c_cam;
-  KeyCarry<6, R, true> c_rig;
+  KeyCarry<6, A, true> c_inst;
+  KeyCarry<CMAX, A, carry_fits<A, CMAX>()> c_cam;
+  KeyCarry<6, A, true> c_rig;
   GB_WARP_CHUNK_LOOP(s.n_slots) {
     const int64_t j = base + lane;
     const int pt = sm.point[j];
     const bool valid = pt >= 0;
-    R rec[NP * VN];
-    R e[NR];
+    A rec[NP * VN];
+    A e[NR];
     int inst = 0, cam = 0, rig = -1;
     if (valid) {
-      load_record<R, NP>(sm.rec, v.stride, j, rec);
-      shot_indices(s, sm.shot[j], inst, cam, rig);
-      CamGather<R, CMAX> g;
-      gather_cam<R, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
-      apply_cam<R, NR, CMAX, RIG>(rec, g, e);
-      R Vi[6], zb[3], z[3];
+      R rec_r[NP * VN];
+      load_record<R, NP>(sm.rec, v.stride, j, rec_r);
 #pragma unroll
-      for (int k = 0; k < 6; ++k) Vi[k] = v.Vinv[8 * int64_t(pt) + k];
+      for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
+      shot_indices(s, sm.shot[j], inst, cam, rig);
+      CamGather<A, CMAX> g;
+      gather_cam<A, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
+      apply_cam<A, NR, CMAX, RIG>(rec, g, e);
+      A Vi[6], zb[3], z[3];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) Vi[k] = A(v.Vinv[8 * int64_t(pt) + k]);
 #pragma unroll
       for (int k = 0; k < 3; ++k) zb[k] = zbuf[4 * int64_t(pt) + k];
       sym3_mul(Vi, zb, z);
@@ -398,15 +434,15 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
         e[q] -= rec[L::kPt + q * 3] * z[0] + rec[L::kPt + q * 3 + 1] * z[1] + rec[L::kPt + q * 3 + 2] * z[2];
     } else {
 #pragma unroll
-      for (int k = 0; k < NP * VN; ++k) rec[k] = R(0);
+      for (int k = 0; k < NP * VN; ++k) rec[k] = A(0);
 #pragma unroll
-      for (int q = 0; q < NR; ++q) e[q] = R(0);
+      for (int q = 0; q < NR; ++q) e[q] = A(0);
     }
     {
-      R a[6];
+      A a[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) {
-        R t = R(0);
+        A t = A(0);
 #pragma unroll
         for (int q = 0; q < NR; ++q) t += rec[L::kInst + q * 6 + k] * e[q];
         a[k] = t;
@@ -416,10 +452,10 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
     {
       const bool cvalid = valid && v.cam_free[cam];
       if (__any_sync(kFullMask, cvalid)) {
-        R c[CMAX];
+        A c[CMAX];
 #pragma unroll
         for (int k = 0; k < CMAX; ++k) {
-          R t = R(0);
+          A t = A(0);
 #pragma unroll
           for (int q = 0; q < NR; ++q) t += rec[L::kCam + q * CMAX + k] * e[q];
           c[k] = t;
@@ -430,10 +466,10 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
     if constexpr (RIG) {
       const bool rvalid = valid && rig >= 0 && v.rig_free[rig];
       if (__any_sync(kFullMask, rvalid)) {
-        R a[6];
+        A a[6];
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-          R t = R(0);
+          A t = A(0);
 #pragma unroll
           for (int q = 0; q < NR; ++q) t += rec[L::kRig + q * 6 + k] * e[q];
           a[k] = t;
@@ -443,7 +479,7 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
     }
   }
   constexpr int KS = CMAX > 6 ? CMAX : 6;
-  __shared__ CarryStage<R, KS> st;
+  __shared__ CarryStage<A, KS> st;
   c_inst.finish(d_inst, st.key, st.val);
   c_cam.finish(d_cam, st.key, st.val);
   if constexpr (RIG) c_rig.finish(d_rig, st.key, st.val);

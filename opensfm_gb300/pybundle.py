@@ -34,7 +34,8 @@ class Summary(C.Structure):
     _fields_ = [("initial_cost", C.c_double), ("final_cost", C.c_double), ("seconds", C.c_double),
                 ("linear_solver_seconds", C.c_double), ("jacobian_seconds", C.c_double),
                 ("residual_seconds", C.c_double), ("iterations", C.c_int), ("successful_steps", C.c_int),
-                ("unsuccessful_steps", C.c_int), ("usable", C.c_int), ("kernel_launches", C.c_int64)]
+                ("unsuccessful_steps", C.c_int), ("usable", C.c_int), ("kernel_launches", C.c_int64),
+                ("setup_seconds", C.c_double)]
 
 
 def _declare(L) -> None:

@@ -3,7 +3,9 @@
 Bar: converged cost within 1e-6 relative of the oracle's, RMS reprojection
 within 1e-3 px.  FP64 runs use a tight PCG tolerance so their trajectory
 tracks the oracle's exact dense Schur solves; mixed-precision runs are held
-to the same converged-cost bar.
+to the same converged-cost bar at a PCG tolerance of 1e-4, about what FP32
+conjugate gradients attain on these systems (tighter tolerances switch on
+FP64 iterative refinement, exercised by its own test).
 """
 import numpy as np
 import pytest
@@ -21,7 +23,7 @@ def _rms_px(errors, width=1000):
 
 
 def _run(scene, precision, **kw):
-    pcg = kw.pop("pcg_tolerance", 1e-10 if precision == "fp64" else 1e-6)
+    pcg = kw.pop("pcg_tolerance", 1e-10 if precision == "fp64" else 1e-4)
     ba = adjuster_from_scene(scene, precision=precision, pcg_tolerance=pcg, **kw)
     ba.run()
     errs, w, _ = ba.projection_results()
@@ -96,6 +98,21 @@ def test_aerial_gps_utm_mixed_matches_oracle():
     rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
     assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
     assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < 1e-3
+
+
+def test_mixed_iterative_refinement_reaches_fp64_accuracy():
+    # a PCG tolerance below what FP32 conjugate gradients attain engages FP64
+    # iterative refinement of the linear solve (residuals recomputed in FP64
+    # on the same records)
+    scene = syn.ring_scene(n_points=2000)
+    kw = dict(loss=("HuberLoss", 1.0), irls="none", max_iterations=50, gps=False)
+    ref = oracle.solve(scene, **kw)
+    ba, errs, _ = _run(scene, "mixed", pcg_tolerance=1e-6, **kw)
+    assert "PCG refinements" in ba.full_report()
+    refinements = int([l for l in ba.full_report().split("\n") if "PCG refinements" in l][0].split()[2])
+    assert refinements > 0
+    rel = abs(ba.summary()["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel < 1e-8, (ba.summary()["final_cost"], ref["final_cost"])
 
 
 def test_solution_written_back_and_reports():
