@@ -111,8 +111,13 @@ typedef struct gbba_eval_output {
 /* Layout of the evaluation outputs for a scene (nr and cmax above). */
 int gbba_scene_layout(const gbba_scene_t* scene, int* nr, int* cmax);
 
-/* One-shot evaluation from host buffers: upload, evaluate on the GPU,
- * download.  precision is GBBA_PRECISION_FP64 or GBBA_PRECISION_MIXED. */
+/* One-shot evaluation from host buffers.  precision is GBBA_PRECISION_FP64
+ * or GBBA_PRECISION_MIXED.  Where the GPU reads and writes pageable host
+ * memory directly (a GB300 next to a Grace CPU), the kernels stream the
+ * observation arrays and write the output arrays in place; elsewhere the
+ * scene is uploaded and the blocks downloaded.  An observation with a bad
+ * index or a non-positive std returns an error status; the output arrays
+ * are then unspecified. */
 int gbba_evaluate_projections(const gbba_scene_t* scene, int precision,
                               gbba_eval_output_t* out);
 

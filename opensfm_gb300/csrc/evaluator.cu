@@ -52,6 +52,132 @@ __global__ void records_to_blocks_kernel(int64_t n, const typename Vec16<R>::typ
   }
 }
 
+// ---------------------------------------------------------------------------
+// Direct evaluation for devices that read and write pageable host memory
+// (GB300 next to a Grace CPU: address translation over NVLink-C2C).  The
+// one-shot entry point then streams the caller's observation arrays into
+// the kernel and writes the FP64 blocks straight into the caller's output
+// arrays: no staging copies, no device-side records.  Observation indices
+// and std deviations are checked in the kernel; a bad one is recorded in
+// `status` (flags, first bad observation) and its outputs are zeros.
+enum : unsigned long long { kDirectBadIndex = 1, kDirectBadStd = 2 };
+
+struct DirectObs {
+  int64_t n;
+  int32_t n_shots;
+  int64_t n_points;
+  const int32_t* shot;
+  const int32_t* point;
+  const double* xy;
+  const double* std_dev;
+};
+
+template <typename R>
+__global__ void convert_points_kernel(int64_t n, const double* __restrict__ xyz,
+                                      typename PointStore<R>::type* __restrict__ out) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < n; p += stride)
+    out[p] = make_point_store(xyz[3 * p], xyz[3 * p + 1], xyz[3 * p + 2], static_cast<R*>(nullptr));
+}
+
+// Per-warp staging of one output array: every lane puts its observation's
+// NR x width block into shared memory, then the warp writes the 32
+// observations' contiguous range with consecutive lanes on consecutive
+// doubles (whole-line writes over the CPU link instead of strided ones).
+__device__ __forceinline__ void flush_staged(double* __restrict__ dst, const double* __restrict__ buf, int64_t first,
+                                             int per_obs, int count) {
+  __syncwarp();
+  double* base = dst + first * per_obs;
+  const int total = count * per_obs;
+  for (int k = int(threadIdx.x & 31u); k < total; k += 32) base[k] = buf[k];
+  __syncwarp();
+}
+
+constexpr int kDirectBlock = 128;
+
+template <int NR, int CMAX>
+constexpr int direct_stage_doubles() {
+  return 32 * NR * (CMAX > 6 ? CMAX : 6);
+}
+
+template <typename R, int M, int NR, int CMAX, bool RIG>
+__global__ void __launch_bounds__(kDirectBlock) direct_eval_kernel(SceneView<R> s, DirectObs d, gbba_eval_output_t o,
+                                                                   int cmax_out,
+                                                                   unsigned long long* __restrict__ status) {
+  using L = RecordLayout<NR, CMAX, RIG>;
+  __shared__ R s_cam[kSharedCameras * kMaxCameraParams];
+  __shared__ int s_model[kSharedCameras];
+  extern __shared__ double s_stage[];
+  const int* models;
+  const R* cams = stage_cameras(s, s_cam, s_model, models);
+  const int lane = int(threadIdx.x & 31u);
+  double* buf = s_stage + (threadIdx.x >> 5) * direct_stage_doubles<NR, CMAX>();
+  const int64_t warp0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t first = warp0 * 32; first < d.n; first += nwarps * 32) {
+    const int64_t i = first + lane;
+    const int count = int(d.n - first < 32 ? d.n - first : 32);
+    R rec[L::kWidth];
+#pragma unroll
+    for (int k = 0; k < L::kWidth; ++k) rec[k] = R(0);
+    if (i < d.n) {
+      const int sh = d.shot[i], pt = d.point[i];
+      const double sd = d.std_dev[i];
+      if (sh < 0 || sh >= d.n_shots || pt < 0 || pt >= d.n_points) {
+        atomicOr(status, kDirectBadIndex);
+        atomicMin(status + 1, static_cast<unsigned long long>(i));
+      } else if (!(sd > 0.0)) {
+        atomicOr(status, kDirectBadStd);
+        atomicMin(status + 1, static_cast<unsigned long long>(i));
+      } else {
+        ObsPack<R> ob{};
+        ob.x = R(d.xy[2 * i]);
+        ob.y = R(d.xy[2 * i + 1]);
+        ob.w = R(1.0 / sd);
+        ob.shot = sh;
+        ObsInputs<R> in;
+        load_inputs<R, M>(s, ob, pt, cams, models, in);
+        eval_observation<R, M, NR, CMAX, RIG, true>(in, rec);
+      }
+    }
+    if (o.residuals) {
+#pragma unroll
+      for (int r = 0; r < NR; ++r) buf[lane * NR + r] = double(rec[L::kR + r]);
+      flush_staged(o.residuals, buf, first, NR, count);
+    }
+    if (o.jac_point) {
+#pragma unroll
+      for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) buf[(lane * NR + r) * 3 + j] = double(rec[L::kPt + r * 3 + j]);
+      flush_staged(o.jac_point, buf, first, NR * 3, count);
+    }
+    if (o.jac_instance) {
+#pragma unroll
+      for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) buf[(lane * NR + r) * 6 + j] = double(rec[L::kInst + r * 6 + j]);
+      flush_staged(o.jac_instance, buf, first, NR * 6, count);
+    }
+    if (o.jac_rig_camera) {
+#pragma unroll
+      for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int j = 0; j < 6; ++j)
+          buf[(lane * NR + r) * 6 + j] = RIG ? double(rec[(RIG ? L::kRig : 0) + r * 6 + j]) : 0.0;
+      flush_staged(o.jac_rig_camera, buf, first, NR * 6, count);
+    }
+    if (o.jac_camera) {
+#pragma unroll
+      for (int r = 0; r < NR; ++r)
+#pragma unroll
+        for (int j = 0; j < CMAX; ++j)
+          if (j < cmax_out) buf[(lane * NR + r) * cmax_out + j] = double(rec[L::kCam + r * CMAX + j]);
+      flush_staged(o.jac_camera, buf, first, NR * cmax_out, count);
+    }
+  }
+}
+
 int grid_for(int64_t n, int block) {
   const int64_t want = (n + block - 1) / block;
   const int64_t cap = 152 * 16;
@@ -175,6 +301,69 @@ int layout_width(const Layout& L) {
   return base + (L.rig ? 6 * L.nr : 0);
 }
 
+template <typename R, int M, int NR, int CMAX, bool RIG>
+void launch_direct(const SceneView<R>& v, const DirectObs& d, const gbba_eval_output_t& o, int nr_out,
+                   int cmax_out, unsigned long long* status) {
+  if (nr_out != NR || cmax_out > CMAX) throw std::logic_error("direct evaluation layout mismatch");
+  auto* k = direct_eval_kernel<R, M, NR, CMAX, RIG>;
+  const int smem = int(sizeof(double)) * direct_stage_doubles<NR, CMAX>() * (kDirectBlock / 32);
+  GB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  k<<<grid_for(d.n, kDirectBlock), kDirectBlock, smem>>>(v, d, o, cmax_out, status);
+}
+
+template <typename R>
+void dispatch_direct(const Layout& L, const SceneView<R>& v, const DirectObs& d, const gbba_eval_output_t& o,
+                     unsigned long long* status) {
+  const int nr = L.nr, co = L.cmax_out;
+  if (L.model != kDynamicModel) {
+    switch (L.model) {
+      case kPerspective: launch_direct<R, kPerspective, 2, 3, false>(v, d, o, nr, co, status); return;
+      case kBrown: launch_direct<R, kBrown, 2, 9, false>(v, d, o, nr, co, status); return;
+      case kFisheye: launch_direct<R, kFisheye, 2, 3, false>(v, d, o, nr, co, status); return;
+      case kFisheyeOpencv: launch_direct<R, kFisheyeOpencv, 2, 8, false>(v, d, o, nr, co, status); return;
+      case kFisheye62: launch_direct<R, kFisheye62, 2, 12, false>(v, d, o, nr, co, status); return;
+      case kFisheye624: launch_direct<R, kFisheye624, 2, 16, false>(v, d, o, nr, co, status); return;
+      case kDual: launch_direct<R, kDual, 2, 4, false>(v, d, o, nr, co, status); return;
+      case kRadial: launch_direct<R, kRadial, 2, 6, false>(v, d, o, nr, co, status); return;
+      case kSimpleRadial: launch_direct<R, kSimpleRadial, 2, 5, false>(v, d, o, nr, co, status); return;
+    }
+  }
+  if (L.nr == 2) {
+    if (L.rig) launch_direct<R, kDynamicModel, 2, 16, true>(v, d, o, nr, co, status);
+    else launch_direct<R, kDynamicModel, 2, 16, false>(v, d, o, nr, co, status);
+  } else {
+    if (L.rig) launch_direct<R, kDynamicModel, 3, 16, true>(v, d, o, nr, co, status);
+    else launch_direct<R, kDynamicModel, 3, 16, false>(v, d, o, nr, co, status);
+  }
+}
+
+bool device_reads_host_memory() {
+  int dev = 0, v = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) return false;
+  return v != 0;
+}
+
+// Counts, camera models and shot references (small arrays, checked on the
+// host before anything is launched).
+void validate_scene_blocks(const gbba_scene_t* s) {
+  if (!s) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "scene is NULL");
+  if (s->n_cameras < 0 || s->n_rig_instances < 0 || s->n_rig_cameras < 0 || s->n_shots < 0 ||
+      s->n_points < 0 || s->n_observations < 0)
+    throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative count in scene");
+  for (int c = 0; c < s->n_cameras; ++c) {
+    const int m = s->camera_projection[c];
+    if (m < 0 || m >= kNumProjections)
+      throw ApiError(GBBA_ERR_RUNTIME, "Invalid ProjectionType for camera " + std::to_string(c));
+  }
+  for (int i = 0; i < s->n_shots; ++i) {
+    if (s->shot_rig_instance[i] < 0 || s->shot_rig_instance[i] >= s->n_rig_instances ||
+        s->shot_camera[i] < 0 || s->shot_camera[i] >= s->n_cameras ||
+        s->shot_rig_camera[i] < -1 || s->shot_rig_camera[i] >= s->n_rig_cameras)
+      throw ApiError(GBBA_ERR_OUT_OF_RANGE, "shot " + std::to_string(i) + " references a missing block");
+  }
+}
+
 void validate_scene(const gbba_scene_t* s) {
   if (!s) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "scene is NULL");
   if (s->n_cameras < 0 || s->n_rig_instances < 0 || s->n_rig_cameras < 0 || s->n_shots < 0 ||
@@ -230,6 +419,74 @@ Layout scene_layout(const gbba_scene_t* s) {
     L.cmax = 16;
   }
   return L;
+}
+
+// One-shot evaluation reading the scene's arrays and writing the output
+// arrays in place (device_reads_host_memory() must hold).  Only the small
+// per-camera / per-shot tables and the points (converted to the working
+// precision) are staged in device memory.
+template <typename R>
+void evaluate_direct(const gbba_scene_t* s, const Layout& L, gbba_eval_output_t* out) {
+  using PS = typename PointStore<R>::type;
+  const int ns = s->n_shots;
+  DeviceArray<R> cam_params;
+  DeviceArray<int> cam_model, shot_inst, shot_rig, shot_cam;
+  DeviceArray<double> inst_pose, rig_pose;
+  DeviceArray<uint8_t> rig_used;
+  DeviceArray<ShotGeom<R>> geom(std::max(1, ns));
+  DeviceArray<RigGeom<R>> rig;
+  DeviceArray<PS> points(std::max<int64_t>(1, s->n_points));
+  DeviceArray<unsigned long long> status(2);
+  {
+    std::vector<R> cam(size_t(s->n_cameras) * kMaxCameraParams);
+    for (size_t i = 0; i < cam.size(); ++i) cam[i] = R(s->camera_values[i]);
+    cam_params.upload(cam);
+  }
+  cam_model.upload(s->camera_projection, s->n_cameras);
+  shot_cam.upload(s->shot_camera, ns);
+  shot_inst.upload(s->shot_rig_instance, ns);
+  shot_rig.upload(s->shot_rig_camera, ns);
+  inst_pose.upload(s->rig_instance_poses, size_t(s->n_rig_instances) * 6);
+  {
+    std::vector<double> rp(size_t(std::max(1, s->n_rig_cameras)) * 6, 0.0);
+    std::vector<uint8_t> ru(size_t(std::max(1, s->n_rig_cameras)), 0);
+    for (int i = 0; i < s->n_rig_cameras; ++i) {
+      for (int k = 0; k < 6; ++k) rp[i * 6 + k] = s->rig_camera_poses[i * 6 + k];
+      ru[i] = s->rig_camera_used ? s->rig_camera_used[i] : 0;
+    }
+    rig_pose.upload(rp);
+    rig_used.upload(ru);
+  }
+  if (L.rig) rig.resize(std::max(1, ns));
+  GB_CUDA(cudaMemset(status.get(), 0, sizeof(unsigned long long)));
+  GB_CUDA(cudaMemset(status.get() + 1, 0xff, sizeof(unsigned long long)));
+  if (s->n_points > 0) {
+    convert_points_kernel<R><<<grid_for(s->n_points, 256), 256>>>(s->n_points, s->points, points.get());
+    GB_CUDA(cudaGetLastError());
+  }
+  if (ns > 0) {
+    shot_prep_kernel<R><<<(ns + 127) / 128, 128>>>(ns, shot_inst.get(), shot_rig.get(), shot_cam.get(),
+                                                   inst_pose.get(), rig_pose.get(), rig_used.get(), geom.get(),
+                                                   L.rig ? rig.get() : nullptr);
+    GB_CUDA(cudaGetLastError());
+  }
+  SceneView<R> v{};
+  v.n_slots = s->n_observations;
+  v.n_cameras = s->n_cameras;
+  v.geom = geom.get();
+  v.rig = L.rig ? rig.get() : nullptr;
+  v.cam_model = cam_model.get();
+  v.cam_params = cam_params.get();
+  v.points = points.get();
+  DirectObs d{s->n_observations, s->n_shots, s->n_points, s->obs_shot, s->obs_point, s->obs_xy, s->obs_std};
+  dispatch_direct<R>(L, v, d, *out, status.get());
+  GB_CUDA(cudaGetLastError());
+  unsigned long long h[2] = {0, 0};
+  GB_CUDA(cudaMemcpy(h, status.get(), sizeof(h), cudaMemcpyDeviceToHost));
+  if (h[0] & kDirectBadIndex)
+    throw ApiError(GBBA_ERR_OUT_OF_RANGE, "observation " + std::to_string(h[1]) + " references a missing shot or point");
+  if (h[0] & kDirectBadStd)
+    throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "observation " + std::to_string(h[1]) + " has non-positive std");
 }
 
 }  // namespace
@@ -436,6 +693,17 @@ int64_t gbba_evaluator_record_bytes(const gbba_evaluator_t* ev) { return ev ? ev
 int gbba_evaluate_projections(const gbba_scene_t* scene, int precision, gbba_eval_output_t* out) {
   return gbba::guarded([&] {
     if (!out) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "output is NULL");
+    if (precision != GBBA_PRECISION_FP64 && precision != GBBA_PRECISION_MIXED)
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (gbba::device_reads_host_memory()) {
+      // the kernels read the caller's arrays and write its outputs in place
+      gbba::validate_scene_blocks(scene);
+      if (scene->n_observations == 0) return;
+      const gbba::Layout L = gbba::scene_layout(scene);
+      if (precision == GBBA_PRECISION_FP64) gbba::evaluate_direct<double>(scene, L, out);
+      else gbba::evaluate_direct<float>(scene, L, out);
+      return;
+    }
     gbba_evaluator_t* ev = gbba_evaluator_create(scene, precision);
     if (!ev) throw ApiError(gbba::last_status(), gbba_last_error());
     std::unique_ptr<gbba_evaluator_t, void (*)(gbba_evaluator_t*)> hold(ev, gbba_evaluator_destroy);
