@@ -214,6 +214,50 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
     return out
 
 
+def autograd_benchmark(n_obs: int = 4_000_000, steps: int = 5, seed: int = 17) -> dict:
+    """Differentiable projection operator over n_obs observations: forward +
+    backward (gradients for intrinsics, poses and points) for Brown and
+    FISHEYE62 cameras, FP32 and FP64, with the Jacobian saved by the forward
+    pass ("stored") or evaluated again in the backward pass ("recompute")."""
+    import torch
+    from opensfm_gb300 import autograd as ag
+    from opensfm_gb300 import synthetic as syn
+    from opensfm_gb300.scene import BROWN, FISHEYE62
+    out = {"n_observations": n_obs, "steps": steps, "runs": []}
+    for model, mname in ((BROWN, "brown"), (FISHEYE62, "fisheye62")):
+        scene = syn.projection_scene(n_obs, model, seed=seed)
+        for dtype, dname in ((torch.float32, "f32"), (torch.float64, "f64")):
+            cams, poses, pts, obs = ag.observations_from_scene(scene, dtype=dtype)
+            leaves = [t.requires_grad_(True) for t in (cams, poses, pts)]
+            for recompute in (False, True):
+                stream = torch.cuda.current_stream()
+                for _ in range(2):  # warm-up
+                    r = ag.project_residuals(*leaves, obs, recompute)
+                    r.backward(torch.ones_like(r))
+                torch.cuda.synchronize()
+                torch.cuda.reset_peak_memory_stats()
+                base = torch.cuda.memory_allocated()
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                fwd = bwd = 0.0
+                for _ in range(steps):
+                    e0.record(stream)
+                    r = ag.project_residuals(*leaves, obs, recompute)
+                    e1.record(stream)
+                    r.backward(torch.ones_like(r))
+                    e2.record(stream)
+                    torch.cuda.synchronize()
+                    fwd += e0.elapsed_time(e1)
+                    bwd += e1.elapsed_time(e2)
+                del r
+                out["runs"].append({"model": mname, "dtype": dname, "mode": "recompute" if recompute else "stored",
+                                    "forward_ms": fwd / steps, "backward_ms": bwd / steps,
+                                    "forward_backward_mobs_per_s": n_obs / ((fwd + bwd) / steps / 1e3) / 1e6,
+                                    "peak_extra_bytes": int(torch.cuda.max_memory_allocated() - base)})
+            for t in leaves:
+                t.grad = None
+    return out
+
+
 def run_reference(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -373,6 +417,9 @@ def run_ours(args) -> None:
         if not args.no_converge:
             ev.close()
             result["converge"] = converge_benchmark(scene, args.converge_iterations)
+        if not args.no_autograd:
+            ev.close()
+            result["autograd"] = autograd_benchmark()
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -390,6 +437,7 @@ def main() -> None:
     ap.add_argument("--no-converge", action="store_true")
     ap.add_argument("--converge-iterations", type=int, default=60)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autograd", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -160,6 +160,54 @@ int gbba_evaluate_projections_noalloc(const gbba_scene_t* scene, int nr, int cma
                                       gbba_eval_output_t* out, void* stream);
 
 /* ------------------------------------------------------------------------
+ * Differentiable projection + residual (an autograd operator).
+ *
+ * Forward: r_i = (pi(camera, pose, X) - obs_i) / std_i for every
+ * observation, as ReprojectionError2DAnalytic<C>::Evaluate
+ * (projection_errors.h:67-207) with the shot pose equal to its rig
+ * instance's (no rig camera).  Backward: J^T g for an incoming gradient g
+ * of the residuals, added into the gradients of the camera parameter
+ * vectors, the instance poses [rx ry rz tx ty tz] and the points.  All
+ * arrays are device memory of the caller; every floating array has the
+ * problem's dtype.  Spherical cameras are not supported (3-row residual).
+ */
+enum { GBBA_DTYPE_F64 = 0, GBBA_DTYPE_F32 = 1 };
+
+typedef struct gbba_device_problem {
+  int32_t dtype;                     /* GBBA_DTYPE_F64 or GBBA_DTYPE_F32 */
+  int32_t model_hint;                /* the single camera model of the problem, or -1 (mixed models) */
+  int32_t n_cameras;
+  const int32_t* camera_projection;  /* [n_cameras] */
+  const void* camera_values;         /* [n_cameras][GBBA_MAX_CAMERA_PARAMS] */
+  int32_t n_instances;
+  const void* instance_poses;        /* [n_instances][6] */
+  int64_t n_points;
+  const void* points;                /* [n_points][3] */
+  int32_t n_shots;
+  const int32_t* shot_instance;      /* [n_shots] */
+  const int32_t* shot_camera;        /* [n_shots] */
+  int64_t n_observations;
+  const int32_t* obs_shot;           /* [n_observations] */
+  const int32_t* obs_point;          /* [n_observations] */
+  const void* obs_xy;                /* [n_observations][2] */
+  const void* obs_std;               /* [n_observations] */
+} gbba_device_problem_t;
+
+/* Bytes of the scratch the forward pass fills (per-shot geometry) and the
+ * backward pass reads; of the Jacobian records saved by a storing forward. */
+int gbba_projection_scratch_bytes(const gbba_device_problem_t* p, int64_t* bytes);
+int gbba_projection_record_bytes(const gbba_device_problem_t* p, int64_t* bytes);
+/* residuals [n_observations][2]; records NULL to keep no Jacobian (the
+ * backward then recomputes it).  Validates every index on the device and
+ * waits for the stream; invalid observations get NaN residuals. */
+int gbba_projection_forward(const gbba_device_problem_t* p, void* residuals, void* records, void* scratch,
+                            void* stream);
+/* Any gradient pointer may be NULL; the others are accumulated into. */
+int gbba_projection_backward(const gbba_device_problem_t* p, const void* grad_residuals, const void* records,
+                             const void* scratch, void* grad_camera_values, void* grad_instance_poses,
+                             void* grad_points, void* stream);
+
+/* ------------------------------------------------------------------------
  * Bundle adjuster: bundle::BundleAdjuster (bundle_adjuster.h:173-386) and
  * the methods its pybind module binds (python/pybind.cc:60-147).  Ids are
  * NUL-terminated strings.  Unknown ids raise GBBA_ERR_RUNTIME (the

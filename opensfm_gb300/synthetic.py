@@ -469,3 +469,35 @@ def random_scene(seed: int, models, n_shots: int = 12, n_points: int = 300, obs_
                         obs_xy=rng.uniform(-0.3, 0.3, (len(obs_shot), 2)),
                         obs_std=rng.uniform(0.5e-3, 2e-3, len(obs_shot)), **kw)
     return scene
+
+
+def projection_scene(n_obs: int, model: int, seed: int = 17, n_shots: int = 64, obs_per_point: int = 4,
+                     n_cameras: int = 4) -> SceneArrays:
+    """Large scene for the differentiable projection operator: n_shots
+    cameras of one model (n_cameras intrinsics sets) on a ring looking at a
+    cube of points, each point seen by obs_per_point random shots;
+    observations are the exact projections plus 1 px noise."""
+    rng = np.random.default_rng(seed)
+    n_points = max(1, n_obs // obs_per_point)
+    cams = np.zeros((n_cameras, 16))
+    for i in range(n_cameras):
+        v = random_model_params(model, rng)
+        cams[i, : len(v)] = v
+    ang = np.linspace(0, 2 * np.pi, n_shots, endpoint=False) + rng.normal(0, 0.05, n_shots)
+    centres = np.stack([6 * np.cos(ang), 6 * np.sin(ang), rng.normal(0, 0.3, n_shots)], axis=-1)
+    poses = pose_from_rotation(look_at(centres, rng.normal(0, 0.3, (n_shots, 3))), centres)
+    pts = rng.uniform(-1.5, 1.5, (n_points, 3))
+    obs_point = np.repeat(np.arange(n_points), obs_per_point).astype(np.int32)[:n_obs]
+    obs_shot = rng.integers(0, n_shots, len(obs_point)).astype(np.int32)
+    shot_camera = (np.arange(n_shots) % n_cameras).astype(np.int32)
+    scene = SceneArrays(camera_projection=np.full(n_cameras, model), camera_values=cams, rig_instance_poses=poses,
+                        shot_rig_instance=np.arange(n_shots), shot_camera=shot_camera, points=pts,
+                        obs_shot=obs_shot, obs_point=obs_point, obs_xy=np.zeros((len(obs_shot), 2)),
+                        obs_std=np.full(len(obs_shot), 1e-3))
+    from .scene import evaluate_projections
+    from . import _lib as lib
+    # exact projections (residuals at zero observations, scaled by std),
+    # then noise
+    r = evaluate_projections(scene, lib.PRECISION_FP64).residuals
+    scene.obs_xy = np.ascontiguousarray(r[:, :2] * 1e-3 + rng.normal(0, 1e-3, (len(obs_shot), 2)))
+    return scene
