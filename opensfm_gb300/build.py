@@ -40,7 +40,8 @@ def _nvcc() -> str:
 
 
 def _headers(directory: Path) -> list[Path]:
-    return sorted(list(directory.glob("*.h")) + list(directory.glob("*.cuh")) + [ROOT / "include" / "gbba.h"])
+    return sorted(list(directory.glob("*.h")) + list(directory.glob("*.cuh")) + list(directory.glob("*.inc")) +
+                  [ROOT / "include" / "gbba.h"])
 
 
 def _stale(target: Path, deps: list[Path]) -> bool:

@@ -34,6 +34,9 @@ class SolverBase {
   virtual void reprojection(std::vector<double>& errors /* n x 3 */, std::vector<double>& weights) = 0;
 };
 
+// precision 0: FP64; otherwise mixed FP32/FP64.
 std::unique_ptr<SolverBase> make_solver(int precision);
+std::unique_ptr<SolverBase> make_solver_fp64();
+std::unique_ptr<SolverBase> make_solver_mixed();
 
 }  // namespace gbba

@@ -1,4 +1,7 @@
-// GPU Levenberg-Marquardt bundle-adjustment solver (see solver.h).
+// GPU Levenberg-Marquardt bundle-adjustment solver (see solver.h): the
+// implementation, compiled once per working precision by solver_fp64.cu and
+// solver_mixed.cu.
+#pragma once
 #include <algorithm>
 #include <chrono>
 #include <cmath>
