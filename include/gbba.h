@@ -334,6 +334,44 @@ int gbba_get_summary(const gbba_adjuster_t* h, gbba_summary_t* out);
  *  trust-region radius, relative decrease, step norm]. */
 int gbba_get_trace(const gbba_adjuster_t* h, int capacity, double* records, int* n);
 
+/* ------------------------------------------------------------------------
+ * Batched runs: many adjusters solved together on the GPU.  The reference
+ * runs one bundle::BundleAdjuster per local bundle adjustment
+ * (sfm::BAHelpers::BundleLocal, ba_helpers.cc:442-804); a batch solves many
+ * such problems in one device layout, with per-problem trust regions and
+ * PCG scalars on the device and one LM iteration recorded as a CUDA graph.
+ * Each adjuster is filled as usual; after gbba_batch_run its getters and
+ * reports hold its own result.  Batches take fixed intrinsics and rig
+ * cameras and no priors (as BundleLocal, ba_helpers.cc:478-486); IRLS is
+ * not applied; every adjuster needs the same loss function.  The adjusters
+ * are borrowed and must outlive the batch's use of them. */
+typedef struct gbba_batch gbba_batch_t;
+gbba_batch_t* gbba_batch_create(void);
+void gbba_batch_destroy(gbba_batch_t* b);
+int gbba_batch_add(gbba_batch_t* b, gbba_adjuster_t* h);
+int gbba_batch_size(const gbba_batch_t* b);
+/* precision GBBA_PRECISION_*; LM iterations; PCG iterations per LM step;
+ * PCG relative tolerance; record the iteration as a CUDA graph (1) or
+ * launch it kernel by kernel (0); pick the slot-kernel grid by timing (1). */
+int gbba_batch_set_options(gbba_batch_t* b, int precision, int max_iterations, int pcg_iterations,
+                           double pcg_tolerance, int use_graph, int autotune);
+/* A problem has converged when an accepted step changes its cost by at
+ * most tolerance * cost (default 1e-7, as gbba_run's convergence test). */
+int gbba_batch_set_function_tolerance(gbba_batch_t* b, double tolerance);
+int gbba_batch_run(gbba_batch_t* b);
+typedef struct gbba_batch_summary {
+  double seconds;        /* whole run, set-up included */
+  double setup_seconds;  /* layout, uploads, first linearization, autotuning */
+  double solve_seconds;  /* the LM iterations */
+  int lm_iterations;     /* iterations of the batch (its slowest problem) */
+  int grid;              /* slot-kernel grid the autotuner chose */
+  int n_problems;
+  int n_converged;
+  int64_t graph_nodes;   /* nodes of the recorded LM iteration */
+  int64_t kernel_launches;
+} gbba_batch_summary_t;
+int gbba_batch_get_summary(const gbba_batch_t* b, gbba_batch_summary_t* out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -289,6 +289,32 @@ double BundleAdjuster::GetGroupDensityRatio(const std::string& g) const {
 }
 
 void BundleAdjuster::Run() {
+  PrepareRun();
+  auto solver = make_solver(opts_.precision);
+  summary_ = solver->solve(problem_, opts_);
+  if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
+  else {
+    errors_.clear();
+    weights_.clear();
+  }
+  covariance_valid_ = false;  // covariance estimation is not implemented (the reference's failure fallback)
+  has_run_ = true;
+}
+
+void BundleAdjuster::SetBatchResult(const SolveSummary& s, std::vector<double> errors) {
+  summary_ = s;
+  if (opts_.compute_reprojection_errors) {
+    errors_ = std::move(errors);
+    weights_.assign(problem_.observations.size(), 1.0);
+  } else {
+    errors_.clear();
+    weights_.clear();
+  }
+  covariance_valid_ = false;
+  has_run_ = true;
+}
+
+void BundleAdjuster::PrepareRun() {
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
   bool known = false;
@@ -316,16 +342,6 @@ void BundleAdjuster::Run() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
-
-  auto solver = make_solver(opts_.precision);
-  summary_ = solver->solve(problem_, opts_);
-  if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
-  else {
-    errors_.clear();
-    weights_.clear();
-  }
-  covariance_valid_ = false;  // covariance estimation is not implemented (the reference's failure fallback)
-  has_run_ = true;
 }
 
 int BundleAdjuster::GetCamera(const std::string& id, int* model, double* values, int cap) const {

@@ -61,6 +61,14 @@ class BundleAdjuster {
 
   void Run();
 
+  // Batched runs (gbba_batch_*): the run-time set-up of Run() without the
+  // solve, the problem and options the batch solves, and the result of the
+  // batch for this problem.
+  void PrepareRun();
+  Problem& MutableProblem() { return problem_; }
+  const SolverOptions& Options() const { return opts_; }
+  void SetBatchResult(const SolveSummary& s, std::vector<double> errors);
+
   // getters (bundle_adjuster.cc:1303-1399)
   int GetCamera(const std::string& id, int* model, double* values, int cap) const;
   void GetRigInstancePose(const std::string& id, double* pose) const;

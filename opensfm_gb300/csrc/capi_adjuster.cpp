@@ -1,4 +1,5 @@
 // extern "C" entry points of the bundle adjuster (include/gbba.h).
+#include <cmath>
 #include <cstring>
 #include <memory>
 #include <string>
@@ -7,6 +8,7 @@
 #include "../../include/gbba.h"
 #include "adjuster.h"
 #include "capi_util.h"
+#include "solver.h"
 
 struct gbba_adjuster {
   gbba::BundleAdjuster ba;
@@ -391,6 +393,124 @@ int gbba_get_trace(const gbba_adjuster_t* h, int capacity, double* records, int*
       o[6] = r.relative_decrease;
       o[7] = r.step_norm;
     }
+  });
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Batched runs: many adjusters solved together on the device.
+
+struct gbba_batch {
+  std::vector<gbba_adjuster_t*> items;
+  gbba::BatchOptions opts;
+  int precision = 1;
+  gbba::BatchSummary summary;
+  bool has_run = false;
+};
+
+extern "C" {
+
+gbba_batch_t* gbba_batch_create(void) {
+  gbba_batch_t* b = nullptr;
+  guarded([&] { b = new gbba_batch_t(); });
+  return b;
+}
+
+void gbba_batch_destroy(gbba_batch_t* b) { delete b; }
+
+int gbba_batch_add(gbba_batch_t* b, gbba_adjuster_t* h) {
+  return guarded([&] {
+    if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
+    ba_of(h);
+    b->items.push_back(h);
+  });
+}
+
+int gbba_batch_size(const gbba_batch_t* b) { return b ? int(b->items.size()) : 0; }
+
+int gbba_batch_set_options(gbba_batch_t* b, int precision, int max_iterations, int pcg_iterations,
+                           double pcg_tolerance, int use_graph, int autotune) {
+  return guarded([&] {
+    if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
+    if (precision != GBBA_PRECISION_FP64 && precision != GBBA_PRECISION_MIXED)
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "unknown precision");
+    if (max_iterations < 1 || pcg_iterations < 1 || !(pcg_tolerance > 0.0))
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "iteration counts and tolerance must be positive");
+    b->precision = precision;
+    b->opts.max_iterations = max_iterations;
+    b->opts.pcg_iterations = pcg_iterations;
+    b->opts.pcg_tolerance = pcg_tolerance;
+    b->opts.use_graph = use_graph != 0;
+    b->opts.autotune = autotune != 0;
+  });
+}
+
+int gbba_batch_set_function_tolerance(gbba_batch_t* b, double tolerance) {
+  return guarded([&] {
+    if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
+    if (!(tolerance >= 0.0)) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "tolerance must be non-negative");
+    b->opts.function_tolerance = tolerance;
+  });
+}
+
+int gbba_batch_run(gbba_batch_t* b) {
+  return guarded([&] {
+    if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
+    if (b->items.empty()) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch is empty");
+    std::vector<gbba::Problem*> problems;
+    for (size_t i = 0; i < b->items.size(); ++i) {
+      gbba::BundleAdjuster& ba = ba_of(b->items[i]);
+      ba.PrepareRun();
+      const gbba::SolverOptions& o = ba.Options();
+      if (i == 0) {
+        b->opts.loss = o.loss;
+        b->opts.loss_threshold = o.loss_threshold;
+      } else if (o.loss != b->opts.loss || o.loss_threshold != b->opts.loss_threshold) {
+        throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "every adjuster of a batch needs the same loss function");
+      }
+      problems.push_back(&ba.MutableProblem());
+    }
+    auto solver = gbba::make_batch_solver(b->precision);
+    try {
+      b->summary = solver->solve_batch(problems, b->opts);
+    } catch (const std::invalid_argument& e) {
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+    }
+    for (size_t i = 0; i < b->items.size(); ++i) {
+      gbba::BatchProblemSummary& p = b->summary.problems[i];
+      gbba::SolveSummary s;
+      s.initial_cost = p.initial_cost;
+      s.final_cost = p.final_cost;
+      s.iterations = p.iterations;
+      s.successful_steps = p.successful_steps;
+      s.unsuccessful_steps = p.unsuccessful_steps;
+      s.termination = p.converged ? "CONVERGENCE" : "NO_CONVERGENCE";
+      s.usable = std::isfinite(p.final_cost);
+      s.seconds = b->summary.seconds;
+      s.linear_solver = "ITERATIVE_SCHUR (GPU batched implicit Schur, block-Jacobi PCG)";
+      ba_of(b->items[i]).SetBatchResult(s, std::move(p.errors));
+    }
+    b->has_run = true;
+  });
+}
+
+int gbba_batch_get_summary(const gbba_batch_t* b, gbba_batch_summary_t* out) {
+  return guarded([&] {
+    if (!b || !out) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "NULL argument");
+    if (!b->has_run) throw ApiError(GBBA_ERR_RUNTIME, "the batch has not run");
+    const gbba::BatchSummary& s = b->summary;
+    out->seconds = s.seconds;
+    out->setup_seconds = s.setup_seconds;
+    out->solve_seconds = s.solve_seconds;
+    out->lm_iterations = s.lm_iterations;
+    out->grid = s.grid;
+    out->n_problems = int(s.problems.size());
+    int conv = 0;
+    for (const auto& p : s.problems) conv += p.converged ? 1 : 0;
+    out->n_converged = conv;
+    out->graph_nodes = s.graph_nodes;
+    out->kernel_launches = s.kernel_launches;
   });
 }
 

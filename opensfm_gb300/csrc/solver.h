@@ -34,6 +34,45 @@ class SolverBase {
   virtual void reprojection(std::vector<double>& errors /* n x 3 */, std::vector<double>& weights) = 0;
 };
 
+// Many independent problems solved together (batched local bundle
+// adjustment): see batch_loop.inc.
+struct BatchOptions {
+  int max_iterations = 50;
+  int loss = kLossTrivial;
+  double loss_threshold = 1.0;
+  int pcg_iterations = 50;           // per LM iteration (each problem stops at its tolerance)
+  double pcg_tolerance = 1e-3;
+  double function_tolerance = 1e-7;  // as the single-problem solver's inner convergence test
+  bool use_graph = true;             // record one LM iteration as a CUDA graph
+  bool autotune = true;              // pick the slot-kernel grid by timing
+};
+
+struct BatchProblemSummary {
+  double initial_cost = 0, final_cost = 0;
+  int iterations = 0, successful_steps = 0, unsuccessful_steps = 0, pcg_iterations = 0;
+  bool converged = false;
+  std::vector<double> errors;  // n x 3 unscaled residuals of the final state
+};
+
+struct BatchSummary {
+  std::vector<BatchProblemSummary> problems;
+  double seconds = 0, setup_seconds = 0, solve_seconds = 0;
+  int lm_iterations = 0;  // iterations of the batch (the slowest problem)
+  int grid = 0;           // slot-kernel grid chosen by the autotuner
+  int64_t graph_nodes = 0, kernel_launches = 0;
+};
+
+class BatchSolverBase {
+ public:
+  virtual ~BatchSolverBase() = default;
+  // Optimises every problem; results are written back into the problems.
+  virtual BatchSummary solve_batch(const std::vector<Problem*>& problems, const BatchOptions& opts) = 0;
+};
+
+std::unique_ptr<BatchSolverBase> make_batch_solver(int precision);
+std::unique_ptr<BatchSolverBase> make_batch_solver_fp64();
+std::unique_ptr<BatchSolverBase> make_batch_solver_mixed();
+
 // precision 0: FP64; otherwise mixed FP32/FP64.
 std::unique_ptr<SolverBase> make_solver(int precision);
 std::unique_ptr<SolverBase> make_solver_fp64();

@@ -7,3 +7,11 @@ namespace gbba {
 std::unique_ptr<SolverBase> make_solver_fp64() { return std::unique_ptr<SolverBase>(new DeviceSolver<double>()); }
 
 }  // namespace gbba
+
+namespace gbba {
+
+std::unique_ptr<BatchSolverBase> make_batch_solver_fp64() {
+  return std::unique_ptr<BatchSolverBase>(new BatchSolver<double>());
+}
+
+}  // namespace gbba

@@ -607,7 +607,8 @@ namespace gbba {
 namespace {
 
 template <typename R>
-class DeviceSolver final : public SolverBase {
+class DeviceSolver : public SolverBase {
+ protected:
   using V16 = typename Vec16<R>::type;
   using PS = typename PointStore<R>::type;
   static constexpr bool kMixed = sizeof(R) == 4;
@@ -619,7 +620,7 @@ class DeviceSolver final : public SolverBase {
     weights = last_weights_;
   }
 
- private:
+ protected:
   // ---- setup
   void setup(const Problem& P, const SolverOptions& opts);
   void upload_camera_side(const std::vector<double>& x, bool working, bool fp64);
@@ -1298,3 +1299,4 @@ double DeviceSolver<R>::prior_model_change(const std::vector<double>& x, const s
 }  // namespace gbba
 
 #include "solver_loop.inc"
+#include "batch_loop.inc"

@@ -220,7 +220,17 @@ struct SolveView {
   double* gc;                    // [cl.n] camera-side gradient J^T r (FP64 sums)
   R* dc;                         // [cl.n] camera-side squared column norms
   const double* resid64;         // [n_slots][4] FP64 residuals of the current state, or null
+  // batched solves: the problem of every point and whether each problem's
+  // linear solve is still running (the Schur products skip the others); null
+  // for a single problem
+  const int* point_pid;
+  const int* active;
 };
+
+template <typename R>
+__device__ __forceinline__ bool slot_active(const SolveView<R>& v, int pt) {
+  return v.active == nullptr || v.active[v.point_pid[pt]] != 0;
+}
 
 template <typename R>
 __device__ __forceinline__ int shot_of(const SceneView<R>& s, int64_t i) {
@@ -494,7 +504,7 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, c
   GB_WARP_SLOT_LOOP(s.n_slots) {
     const int64_t i = base + lane;
     const int pt = s.obs_point[i];
-    const bool valid = pt >= 0;
+    const bool valid = pt >= 0 && slot_active(v, pt);
     A u[3] = {A(0), A(0), A(0)};
     if (valid) {
       R rec_r[NP * VN];

@@ -11,3 +11,15 @@ std::unique_ptr<SolverBase> make_solver(int precision) {
 }
 
 }  // namespace gbba
+
+namespace gbba {
+
+std::unique_ptr<BatchSolverBase> make_batch_solver_mixed() {
+  return std::unique_ptr<BatchSolverBase>(new BatchSolver<float>());
+}
+
+std::unique_ptr<BatchSolverBase> make_batch_solver(int precision) {
+  return precision == 0 ? make_batch_solver_fp64() : make_batch_solver_mixed();
+}
+
+}  // namespace gbba

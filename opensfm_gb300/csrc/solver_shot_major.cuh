@@ -410,7 +410,7 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
   GB_WARP_CHUNK_LOOP(s.n_slots) {
     const int64_t j = base + lane;
     const int pt = sm.point[j];
-    const bool valid = pt >= 0;
+    const bool valid = pt >= 0 && slot_active(v, pt);
     A rec[NP * VN];
     A e[NR];
     int inst = 0, cam = 0, rig = -1;

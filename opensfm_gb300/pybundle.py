@@ -408,6 +408,69 @@ class BundleAdjuster:
     set_adjust_absolute_position_std = _unsupported
 
 
+class BatchSummary(C.Structure):
+    _fields_ = [("seconds", C.c_double), ("setup_seconds", C.c_double), ("solve_seconds", C.c_double),
+                ("lm_iterations", C.c_int), ("grid", C.c_int), ("n_problems", C.c_int), ("n_converged", C.c_int),
+                ("graph_nodes", C.c_int64), ("kernel_launches", C.c_int64)]
+
+
+class BundleBatch:
+    """Many BundleAdjusters solved together on the GPU (gbba_batch_*).
+
+    The reference solves one local bundle adjustment per call
+    (sfm::BAHelpers::BundleLocal); a batch solves many of them in one device
+    layout with per-problem trust regions, replaying one recorded LM
+    iteration.  After run() every adjuster's getters and reports hold its
+    own result."""
+
+    def __init__(self) -> None:
+        self._L = _lib.lib()
+        _declare(self._L)
+        L = self._L
+        for name, args, res in (("gbba_batch_create", [], _H), ("gbba_batch_destroy", [_H], None),
+                                ("gbba_batch_add", [_H, _H], C.c_int), ("gbba_batch_size", [_H], C.c_int),
+                                ("gbba_batch_set_options", [_H, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int,
+                                                            C.c_int], C.c_int),
+                                ("gbba_batch_run", [_H], C.c_int),
+                                ("gbba_batch_set_function_tolerance", [_H, C.c_double], C.c_int),
+                                ("gbba_batch_get_summary", [_H, C.POINTER(BatchSummary)], C.c_int)):
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        self._h = L.gbba_batch_create()
+        self._members: list = []  # keeps the adjusters alive while the batch refers to them
+
+    def __del__(self) -> None:
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.gbba_batch_destroy(h)
+            self._h = None
+
+    def add(self, ba: BundleAdjuster) -> None:
+        _lib.check(self._L.gbba_batch_add(self._h, ba._h))
+        self._members.append(ba)
+
+    def __len__(self) -> int:
+        return int(self._L.gbba_batch_size(self._h))
+
+    def set_options(self, precision: str = "mixed", max_iterations: int = 50, pcg_iterations: int = 50,
+                    pcg_tolerance: float = 1e-3, use_graph: bool = True, autotune: bool = True) -> None:
+        p = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
+        _lib.check(self._L.gbba_batch_set_options(self._h, p, max_iterations, pcg_iterations, pcg_tolerance,
+                                                  int(use_graph), int(autotune)))
+
+    def set_function_tolerance(self, tolerance: float) -> None:
+        _lib.check(self._L.gbba_batch_set_function_tolerance(self._h, tolerance))
+
+    def run(self) -> None:
+        _lib.check(self._L.gbba_batch_run(self._h))
+
+    def summary(self) -> dict:
+        s = BatchSummary()
+        _lib.check(self._L.gbba_batch_get_summary(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in BatchSummary._fields_}
+
+
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None) -> BundleAdjuster:
@@ -439,4 +502,4 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
     return ba
 
 
-__all__ = ["BundleAdjuster", "Point", "adjuster_from_scene"]
+__all__ = ["BundleAdjuster", "BundleBatch", "Point", "adjuster_from_scene"]

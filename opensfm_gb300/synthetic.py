@@ -471,6 +471,30 @@ def random_scene(seed: int, models, n_shots: int = 12, n_points: int = 300, obs_
     return scene
 
 
+def local_ba_problems(n_problems: int = 256, seed: int = 23, shots=(5, 60), points=(500, 20_000),
+                      observations=(3_000, 150_000), models=(BROWN, FISHEYE, SPHERICAL)) -> list:
+    """Uneven local bundle adjustments: per problem, shots, points and
+    observations drawn log-uniformly from the given ranges and one camera
+    model from `models`; ring geometry (ring_scene) with 1 px noise and
+    perturbed initial poses and points."""
+    rng = np.random.default_rng(seed)
+
+    def lu(lo, hi):
+        return float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+
+    out = []
+    for q in range(n_problems):
+        n_shots = int(round(lu(*shots)))
+        n_points = int(round(lu(*points)))
+        n_obs = lu(*observations)
+        k = int(np.clip(round(n_obs / n_points), 2, n_shots))
+        model = int(models[rng.integers(len(models))])
+        params = tuple(random_model_params(model, rng))
+        out.append(ring_scene(seed=int(rng.integers(1 << 30)), n_shots=n_shots, n_points=n_points,
+                              obs_per_point=k, model=model, params=params))
+    return out
+
+
 def projection_scene(n_obs: int, model: int, seed: int = 17, n_shots: int = 64, obs_per_point: int = 4,
                      n_cameras: int = 4) -> SceneArrays:
     """Large scene for the differentiable projection operator: n_shots

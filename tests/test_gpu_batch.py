@@ -1,0 +1,76 @@
+"""Batched local bundle adjustment (gbba_batch_*) against the FP64 oracle and
+the single-problem GPU solver, on uneven problems mixing Brown, fisheye and
+spherical cameras with fixed intrinsics (as the reference's local bundle)."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from opensfm_gb300 import synthetic as syn
+from opensfm_gb300.pybundle import BundleBatch, adjuster_from_scene
+
+pytestmark = pytest.mark.gpu
+
+LOSS = ("HuberLoss", 2.0)
+
+
+def _problems(n=6, seed=3):
+    return syn.local_ba_problems(n, seed=seed, shots=(5, 16), points=(300, 1500), observations=(2_000, 8_000))
+
+
+def _adjusters(scenes, precision="mixed"):
+    return [adjuster_from_scene(s, precision=precision, loss=LOSS, irls="none", gps=False, constant_cameras=True,
+                                max_iterations=100) for s in scenes]
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_batch_matches_oracle(precision):
+    scenes = _problems()
+    bas = _adjusters(scenes, precision)
+    batch = BundleBatch()
+    for ba in bas:
+        batch.add(ba)
+    batch.set_options(precision=precision, max_iterations=100, pcg_iterations=100,
+                      pcg_tolerance=1e-4 if precision == "mixed" else 1e-10)
+    batch.run()
+    s = batch.summary()
+    assert s["n_problems"] == len(scenes)
+    assert s["n_converged"] == len(scenes)
+    assert s["graph_nodes"] > 0
+    for scene, ba in zip(scenes, bas):
+        ref = oracle.solve(scene, loss=LOSS, irls="none", max_iterations=100, gps=False, constant_cameras=True)
+        got = ba.summary()
+        assert got["final_cost"] < got["initial_cost"]
+        rel = abs(got["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+        # same trust-region rules as the oracle: FP64 follows its trajectory
+        assert rel < (1e-6 if precision == "mixed" else 1e-12), (got["final_cost"], ref["final_cost"])
+        assert got["iterations"] == ref["iterations"] or precision == "mixed"
+        # the solution was written back into the adjuster
+        assert np.abs(ba.get_points() - scene.points).max() > 0
+        errs, _, _ = ba.projection_results()
+        ref_rms = np.sqrt((ref["errors"][:, :2] ** 2).sum(1).mean())
+        got_rms = np.sqrt((errs[:, :2] ** 2).sum(1).mean())
+        assert abs(got_rms - ref_rms) < 1e-3 * max(ref_rms, 1e-12) + 1e-9
+
+
+def test_graph_and_plain_launches_agree():
+    scenes = _problems(4, seed=9)
+    costs = []
+    for use_graph in (True, False):
+        bas = _adjusters(scenes)
+        batch = BundleBatch()
+        for ba in bas:
+            batch.add(ba)
+        batch.set_options(max_iterations=60, use_graph=use_graph, autotune=False)
+        batch.run()
+        costs.append([ba.summary()["final_cost"] for ba in bas])
+        assert (batch.summary()["graph_nodes"] > 0) == use_graph
+    np.testing.assert_allclose(costs[0], costs[1], rtol=1e-6)
+
+
+def test_batch_rejects_free_intrinsics():
+    scene = _problems(1)[0]
+    ba = adjuster_from_scene(scene, loss=LOSS, irls="none", gps=False, constant_cameras=False)
+    batch = BundleBatch()
+    batch.add(ba)
+    with pytest.raises(Exception, match="fixed intrinsics"):
+        batch.run()
