@@ -215,7 +215,7 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
 
 
 def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int = 50,
-                    loss=("HuberLoss", 2.0)) -> dict:
+                    loss=("HuberLoss", 2.0), one_at_a_time: bool = True) -> dict:
     """Batched local bundle adjustment: n_problems uneven problems (5-60
     shots, 500-20k points, 3k-150k observations, log-uniform; Brown, fisheye
     and spherical cameras with fixed intrinsics) solved by one batch
@@ -252,6 +252,12 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
     batch_costs = np.array([ba.summary()["final_cost"] for ba in bas])
     init_costs = np.array([ba.summary()["initial_cost"] for ba in bas])
     batch_conv = np.array([ba.summary()["iterations"] < max_iterations for ba in bas])
+    out.update({"batch_s": batch_s, "batch_setup_s": s["setup_seconds"], "batch_solve_s": s["solve_seconds"],
+                "batch_lm_iterations": s["lm_iterations"], "graph_nodes": s["graph_nodes"],
+                "autotuned_grid": s["grid"], "converged_batch": int(batch_conv.sum()),
+                "batch_mobs_per_s": out["n_observations"] / batch_s / 1e6})
+    if not one_at_a_time:
+        return out
     # one at a time
     singles = adjusters()
     t0 = time.perf_counter()
@@ -480,10 +486,11 @@ def run_ours(args) -> None:
             result["converge"] = converge_benchmark(scene, args.converge_iterations)
         if not args.no_autograd:
             ev.close()
-            result["autograd"] = autograd_benchmark()
+            result["autograd"] = autograd_benchmark(n_obs=args.autograd_observations)
         if not args.no_batch:
             ev.close()
-            result["batched_local_ba"] = batch_benchmark()
+            result["batched_local_ba"] = batch_benchmark(n_problems=args.batch_problems,
+                                                         one_at_a_time=not args.batch_only)
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -503,6 +510,9 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autograd", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-problems", type=int, default=256)
+    ap.add_argument("--batch-only", action="store_true", help="skip the one-at-a-time comparison")
+    ap.add_argument("--autograd-observations", type=int, default=4_000_000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -282,8 +282,7 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
       }
     }
   }
-  if constexpr (!JAC) return;
-
+  if constexpr (JAC) {
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
     const R a0 = in.w * Jq[i * 3 + 0], a1 = in.w * Jq[i * 3 + 1], a2 = in.w * Jq[i * 3 + 2];
@@ -327,6 +326,7 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
       }
     }
   }
+  }  // JAC
 }
 
 }  // namespace gbba

@@ -29,6 +29,8 @@ constexpr double kEps = 2.220446049250313e-16;
 constexpr double kRefineThreshold = 1e-4;
 constexpr double kRefineInnerTolerance = 1e-3;
 constexpr int kMaxRefinements = 4;
+// Mixed precision: PCG tolerance of the step that confirms convergence.
+constexpr double kConfirmTolerance = 1e-6;
 
 struct KernelConfig {
   int model;  // single model or kDyn
@@ -665,6 +667,8 @@ class DeviceSolver : public SolverBase {
   double ratio_cam_ = 1e-3, ratio_rig_ = 1e-3, ratio_gps_ = 1e-3, ratio_gcp3d_ = 1e-3;
   int64_t launches_ = 0;
   int64_t refinements_ = 0;  // FP64 residual evaluations of iterative refinement
+  int64_t confirmations_ = 0;  // convergence confirmations with a refined step (mixed)
+  double pcg_tolerance_override_ = 0.0;  // > 0: PCG tolerance of the next steps
   std::vector<double> last_errors_, last_weights_;
 
   // device state

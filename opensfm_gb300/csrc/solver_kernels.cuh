@@ -225,6 +225,7 @@ struct SolveView {
   // for a single problem
   const int* point_pid;
   const int* active;
+  const int* any_active;  // number of problems still active (0: nothing to do)
 };
 
 template <typename R>
@@ -501,6 +502,7 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, c
   constexpr int NP = planes_of<R>(L::kWidth);
   constexpr int VN = Vec16<R>::kN;
   const SceneView<R>& s = v.scene;
+  if (v.any_active && *v.any_active == 0) return;
   GB_WARP_SLOT_LOOP(s.n_slots) {
     const int64_t i = base + lane;
     const int pt = s.obs_point[i];

@@ -404,6 +404,7 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
   auto d_inst = [y](int b, int k) { return y + 8 * b + k; };
   auto d_cam = [y, cl](int b, int k) { return y + cl.cam_base + 16 * b + k; };
   auto d_rig = [y, cl](int b, int k) { return y + cl.rig_base + 8 * b + k; };
+  if (v.any_active && *v.any_active == 0) return;  // uniform over the grid: no barrier is skipped by part of a block
   KeyCarry<6, A, true> c_inst;
   KeyCarry<CMAX, A, carry_fits<A, CMAX>()> c_cam;
   KeyCarry<6, A, true> c_rig;
