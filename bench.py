@@ -228,8 +228,10 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
     scenes = syn.local_ba_problems(n_problems, seed=seed)
 
     def adjusters():
+        # the same linear solver as the batch (PCG on the implicit Schur product)
         return [adjuster_from_scene(s, precision="mixed", loss=loss, irls="none", gps=False, constant_cameras=True,
-                                    max_iterations=max_iterations, pcg_tolerance=1e-3) for s in scenes]
+                                    max_iterations=max_iterations, pcg_tolerance=1e-3,
+                                    linear_solver="ITERATIVE_SCHUR") for s in scenes]
 
     out = {"n_problems": n_problems, "n_observations": int(sum(s.n_observations for s in scenes)),
            "n_points": int(sum(len(s.points) for s in scenes)), "max_iterations": max_iterations,

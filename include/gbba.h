@@ -372,6 +372,41 @@ typedef struct gbba_batch_summary {
 } gbba_batch_summary_t;
 int gbba_batch_get_summary(const gbba_batch_t* b, gbba_batch_summary_t* out);
 
+/* ---- Dense reduced-camera-system solver
+ *
+ * The linear solver behind gbba_run's dense mode (linear solver types
+ * DENSE_SCHUR, DENSE_QR and DENSE_NORMAL_CHOLESKY, and SPARSE_SCHUR /
+ * SPARSE_NORMAL_CHOLESKY up to a few thousand camera-side unknowns): the
+ * GPU counterpart of the Cholesky factorization Ceres' DENSE_SCHUR and
+ * SPARSE_SCHUR solvers apply to the reduced camera system
+ * (bundle_adjuster.cc:1159-1190; DENSE_SCHUR up to 200 shots in
+ * sfm::BAHelpers, ba_helpers.cc:42-49).  Exposed on its own for callers
+ * that form such systems themselves, and for tests.
+ *
+ * gbba_dense_spd_solve solves A x = b for a symmetric positive definite
+ * n x n row-major FP64 matrix (host buffers; the lower triangle is read).
+ * The factorization runs on the tensor cores (TF32 operands, three products
+ * per term for FP32 accuracy) after a symmetric Jacobi scaling; conjugate
+ * gradients in FP64 on the FP64 matrix, preconditioned by that factor, then
+ * drive the scaled residual |D (b - A x)| / |D b| below tol, D =
+ * diag(A)^-1/2, within max_refinements
+ * iterations (one FP64 matrix-vector product each).  status: 0 solved, 1
+ * not positive definite, 2 a device wait timed out, 3 not converged to tol
+ * within max_refinements iterations (x is the last iterate). */
+typedef struct gbba_dense_stats {
+  int status;
+  int refinements;
+  double rel_residual;
+  double factor_seconds;
+  double solve_seconds;
+} gbba_dense_stats_t;
+int gbba_dense_spd_solve(const double* a, int n, const double* b, double* x, double tol, int max_refinements,
+                         gbba_dense_stats_t* stats);
+/* C = A B^T on the tensor cores for row-major FP32 A (m x k), B (n x k),
+ * C (m x n), host buffers; m and n multiples of 128, k a multiple of 32.
+ * The product kernel of the factorization, exposed for tests. */
+int gbba_dense_gemm_nt(const float* a, const float* b, float* c, int m, int n, int k);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,747 @@
+// Dense SPD solver of the reduced camera system on GB300: a blocked
+// left-looking Cholesky factorization with tensor-core block products, and
+// FP64 conjugate gradients preconditioned by the factor.
+//
+// Factorization of the Jacobi-scaled FP32 matrix, tiles of 128 x 128, for
+// every block column k:
+//   update   A_ik -= sum_{j<k} L_ij L_kj^T   (i >= k; tensor cores, K = 128 k)
+//   potrf    L_kk = chol(A_kk), Dinv_k = L_kk^-1   (one CTA, shared memory)
+//   trsm     L_ik = A_ik Dinv_k^T               (i > k; tensor cores, K = 128)
+// The block products use tcgen05.mma kind::tf32 with operands in shared
+// memory (128-byte swizzled, K-major) and the FP32 accumulator in tensor
+// memory.  Each FP32 operand is split into a TF32 high part and a TF32
+// remainder; hi*hi + hi*lo + lo*hi restores FP32-level accuracy of every
+// product ("3xTF32").  The solve is conjugate gradients in FP64 on the FP64
+// matrix, preconditioned by the FP32 factor (flexible Polak-Ribiere form, as
+// the FP32 triangular solves are not an exactly linear operator): one or two
+// iterations when the scaled condition number times the FP32 unit roundoff
+// is small, and still convergent where plain iterative refinement would
+// stall (nearly singular gauge directions under small LM damping).  If the
+// FP32 factorization meets a non-positive pivot, it is repeated with a
+// growing diagonal shift; the shifted factor remains a valid preconditioner.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdint>
+#include <stdexcept>
+#include <vector>
+
+#include "capi_util.h"
+#include "dense_cholesky.h"
+
+namespace gbba {
+namespace {
+
+constexpr int kTile = 128;                      // output tile rows = columns
+constexpr int kKb = 32;                         // FP32 K values per stage: one 128-byte row
+constexpr int kOpBytes = kTile * kKb * 4;       // one operand part per stage (16 KB)
+constexpr int kStageBytes = 4 * kOpBytes;       // A hi, A lo, B hi, B lo
+constexpr int kStages = 2;
+constexpr int kGemmSmem = kStages * kStageBytes + 1024;  // + slack for 1024-byte alignment
+constexpr int kGemmThreads = 128;               // four warps: one per 32 accumulator lanes
+constexpr long long kSpinLimit = 1ll << 24;     // mbarrier polls before a wait gives up
+constexpr int kTmemCols = 128;                  // FP32 accumulator: 128 lanes x 128 columns
+
+// Instruction descriptor of tcgen05.mma kind::tf32: FP32 accumulator (bits
+// 4-5 = 1), TF32 A and B (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 =
+// 0), N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc =
+    (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(kTile >> 3) << 17) | (uint32_t(kTile >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: K-major operand with the 128-byte
+// swizzle, 8-row core groups 1024 bytes apart (stride byte offset), start
+// address in 16-byte units, descriptor version 1 (bits 46-47), swizzle mode
+// 2 = 128 bytes (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = uint64_t((saddr >> 4) & 0x3FFFu);
+  d |= uint64_t(1) << 16;
+  d |= uint64_t(1024 >> 4) << 32;
+  d |= uint64_t(1) << 46;
+  d |= uint64_t(2) << 61;
+  return d;
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long it = 0; it < kSpinLimit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 32 consecutive FP32 accumulator columns of this thread's lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Loads a 128 x 32 FP32 block (rows of `src`, columns k0..k0+31), splits it
+// into TF32 high and remainder parts and stores both in the 128-byte
+// swizzled K-major layout: row r at byte r * 128, its 16-byte chunk c at
+// position c ^ (r & 7).
+__device__ __forceinline__ void load_split(const float* src, int ld, int k0, uint8_t* hi, uint8_t* lo, int tid) {
+  float4 x[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int f = tid + q * kGemmThreads;
+    const int r = f >> 3, c = f & 7;
+    x[q] = *reinterpret_cast<const float4*>(src + int64_t(r) * ld + k0 + c * 4);
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int f = tid + q * kGemmThreads;
+    const int r = f >> 3, c = f & 7;
+    float4 h, l;
+    h.x = tf32_round(x[q].x);
+    h.y = tf32_round(x[q].y);
+    h.z = tf32_round(x[q].z);
+    h.w = tf32_round(x[q].w);
+    l.x = tf32_round(x[q].x - h.x);
+    l.y = tf32_round(x[q].y - h.y);
+    l.z = tf32_round(x[q].z - h.z);
+    l.w = tf32_round(x[q].w - h.w);
+    const int off = r * 128 + ((c ^ (r & 7)) << 4);
+    *reinterpret_cast<float4*>(hi + off) = h;
+    *reinterpret_cast<float4*>(lo + off) = l;
+  }
+}
+
+struct GemmArgs {
+  const float* a;    // A rows of tile row 0
+  int lda;
+  const float* b;    // B rows of tile column 0
+  int ldb;
+  float* c;          // C tile (0, 0)
+  int ldc;
+  const float* cin;  // mode 1: C = cin - A B^T (cin laid out as C), else null
+  int k;             // multiple of kKb, > 0
+  int* status;
+};
+
+// One 128 x 128 tile of C = A B^T (or cin - A B^T) per CTA: tile row
+// blockIdx.x, tile column blockIdx.y.  A and C may alias (the in-place
+// triangular solve): every A row of the tile is read before the epilogue
+// writes C.
+__global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g) {
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ __align__(8) uint64_t bars[kStages];
+  __shared__ uint32_t tmem_holder;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t raw = smem_u32(smem_raw);
+  uint8_t* smem = smem_raw + ((1024u - (raw & 1023u)) & 1023u);
+  const uint32_t sbase = smem_u32(smem);
+  if (tid == 0) {
+    for (int s = 0; s < kStages; ++s) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bars[s])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_holder)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_holder;
+
+  const float* A = g.a + int64_t(blockIdx.x) * kTile * g.lda;
+  const float* B = g.b + int64_t(blockIdx.y) * kTile * g.ldb;
+  const int nkb = g.k / kKb;
+  bool ok = true;
+  int committed = 0;  // stages whose products were issued
+  for (int kb = 0; kb < nkb; ++kb) {
+    const int s = kb & 1;
+    if (kb >= kStages) {
+      // the products of stage kb - 2 have finished reading buffer s
+      const bool w = mbar_wait(smem_u32(&bars[s]), uint32_t((kb >> 1) - 1) & 1u);
+      ok = __syncthreads_and(w ? 1 : 0) != 0;
+      if (!ok) break;
+    }
+    uint8_t* st = smem + s * kStageBytes;
+    load_split(A, g.lda, kb * kKb, st, st + kOpBytes, tid);
+    load_split(B, g.ldb, kb * kKb, st + 2 * kOpBytes, st + 3 * kOpBytes, tid);
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t a_hi = sbase + uint32_t(s * kStageBytes);
+      const uint32_t a_lo = a_hi + kOpBytes, b_hi = a_hi + 2 * kOpBytes, b_lo = a_hi + 3 * kOpBytes;
+#pragma unroll
+      for (int kk = 0; kk < kKb / 8; ++kk) {
+        const uint32_t off = uint32_t(kk * 32);  // 8 TF32 values = 32 bytes along K
+        mma_tf32(tmem, sw128_desc(a_lo + off), sw128_desc(b_hi + off), (kb | kk) != 0 ? 1u : 0u);
+        mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_lo + off), 1u);
+        mma_tf32(tmem, sw128_desc(a_hi + off), sw128_desc(b_hi + off), 1u);
+      }
+      mma_commit(smem_u32(&bars[s]));
+    }
+    committed = kb + 1;
+  }
+  if (committed > 0) {
+    // a commit tracks every earlier product of the issuing thread: waiting
+    // for the last one covers all (also after a timeout, so that tensor
+    // memory is not released under running products)
+    const int last = committed - 1;
+    const bool w = mbar_wait(smem_u32(&bars[last & 1]), uint32_t(last >> 1) & 1u);
+    ok = (__syncthreads_and(w ? 1 : 0) != 0) && ok;
+  }
+  tc_fence_after();
+  if (ok && committed == nkb) {
+    const int row = warp * 32 + lane;
+    float* C = g.c + int64_t(blockIdx.x) * kTile * g.ldc + int64_t(blockIdx.y) * kTile + int64_t(row) * g.ldc;
+    const float* Cin =
+        g.cin ? g.cin + int64_t(blockIdx.x) * kTile * g.ldc + int64_t(blockIdx.y) * kTile + int64_t(row) * g.ldc
+              : nullptr;
+#pragma unroll 1
+    for (int cc = 0; cc < kTile / 32; ++cc) {
+      float v[32];
+      tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(cc * 32), v);
+#pragma unroll
+      for (int q = 0; q < 32; q += 4) {
+        float4 o = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+        if (Cin) {
+          const float4 ci = *reinterpret_cast<const float4*>(Cin + cc * 32 + q);
+          o = make_float4(ci.x - o.x, ci.y - o.y, ci.z - o.z, ci.w - o.w);
+        }
+        *reinterpret_cast<float4*>(C + cc * 32 + q) = o;
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(g.status, 2);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagonal tile: L_kk = chol(A_kk) and Dinv_k = L_kk^-1, in shared memory.
+constexpr int kPotrfThreads = 512;
+constexpr int kLdS = kTile + 1;
+constexpr int kPotrfSmem = 2 * kTile * kLdS * 4 + kTile * 4;
+
+__global__ void __launch_bounds__(kPotrfThreads) potrf_tile_kernel(float* L, int ld, int k, float* dinv,
+                                                                   int* status) {
+  extern __shared__ float sm[];
+  float* a = sm;                  // the tile, then its factor (lower)
+  float* x = sm + kTile * kLdS;   // the inverse of the factor (lower)
+  float* rdiag = x + kTile * kLdS;
+  __shared__ int bad;
+  const int tid = threadIdx.x;
+  float* tile = L + int64_t(k) * kTile * ld + int64_t(k) * kTile;
+  for (int t = tid; t < kTile * kTile; t += kPotrfThreads) {
+    const int i = t >> 7, j = t & (kTile - 1);
+    a[i * kLdS + j] = tile[int64_t(i) * ld + j];
+    x[i * kLdS + j] = 0.f;
+  }
+  if (tid == 0) bad = 0;
+  __syncthreads();
+  // right-looking unblocked Cholesky of the lower triangle
+  for (int j = 0; j < kTile; ++j) {
+    if (tid == 0) {
+      float d = a[j * kLdS + j];
+      if (!(d > 0.f) || !isfinite(d)) {
+        bad = 1;
+        d = 1.f;
+      }
+      const float l = sqrtf(d);
+      a[j * kLdS + j] = l;
+      rdiag[j] = 1.f / l;
+    }
+    __syncthreads();
+    const float inv = rdiag[j];
+    for (int i = j + 1 + tid; i < kTile; i += kPotrfThreads) a[i * kLdS + j] *= inv;
+    __syncthreads();
+    for (int i = j + 1 + (tid >> 4); i < kTile; i += kPotrfThreads / 16) {
+      const float lij = a[i * kLdS + j];
+      for (int c = j + 1 + (tid & 15); c <= i; c += 16) a[i * kLdS + c] -= lij * a[c * kLdS + j];
+    }
+    __syncthreads();
+  }
+  // X = L^-1 by forward substitution, four threads per column
+  {
+    const int c = tid >> 2, s = tid & 3;
+    for (int i = 0; i < kTile; ++i) {
+      float part = 0.f;
+      if (i >= c)
+        for (int m = c + s; m < i; m += 4) part += a[i * kLdS + m] * x[m * kLdS + c];
+      part += __shfl_xor_sync(0xffffffffu, part, 1);
+      part += __shfl_xor_sync(0xffffffffu, part, 2);
+      if (s == 0 && i >= c) x[i * kLdS + c] = ((i == c ? 1.f : 0.f) - part) * rdiag[i];
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  float* dk = dinv + int64_t(k) * kTile * kTile;
+  for (int t = tid; t < kTile * kTile; t += kPotrfThreads) {
+    const int i = t >> 7, j = t & (kTile - 1);
+    tile[int64_t(i) * ld + j] = j <= i ? a[i * kLdS + j] : 0.f;
+    dk[t] = j <= i ? x[i * kLdS + j] : 0.f;
+  }
+  if (tid == 0 && bad) atomicExch(status + 1, 1);
+}
+
+// ---------------------------------------------------------------------------
+// Scaling and conversion.
+__global__ void jacobi_scale_kernel(int n, const double* __restrict__ A, int lda, double* __restrict__ d,
+                                    int* status) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double a = A[int64_t(i) * lda + i];
+  if (!(a > 0.0) || !isfinite(a)) {
+    atomicExch(status, 1);
+    d[i] = 1.0;
+  } else {
+    d[i] = 1.0 / sqrt(a);
+  }
+}
+
+// L = fp32(D A D) on the lower triangle (identity on the padding), zero
+// above; A's upper triangle becomes the mirror of its lower triangle.
+__global__ void load_scaled_kernel(int n, int n_pad, double* A, int lda, const double* __restrict__ d,
+                                   float* __restrict__ L, double shift) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n_pad) * n_pad) return;
+  const int i = int(t / n_pad), j = int(t % n_pad);
+  float v = 0.f;
+  if (i < n && j < n) {
+    if (j <= i) {
+      const double a = A[int64_t(i) * lda + j];
+      v = float(a * d[i] * d[j] + (i == j ? shift : 0.0));
+      if (j < i) A[int64_t(j) * lda + i] = a;
+    }
+  } else if (i == j) {
+    v = 1.f;
+  }
+  L[t] = v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Triangular solves with the tiled factor (one CTA): v = (L L^T)^-1 rhs, then
+// z = D v.  Forward: y_k = Dinv_k (rhs_k - sum_{j<k} L_kj y_j); backward:
+// x_k = Dinv_k^T (y_k - sum_{j>k} L_jk^T x_j).
+constexpr int kTrsvThreads = 1024;
+
+__global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(const float* __restrict__ L, int ld,
+                                                            const float* __restrict__ dinv, int nt, int n,
+                                                            const float* __restrict__ rhs,
+                                                            const double* __restrict__ d, double* __restrict__ z) {
+  extern __shared__ float v[];  // nt * 128
+  __shared__ float t[kTile];
+  __shared__ float part[kTrsvThreads / kTile][kTile];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int np = nt * kTile;
+  for (int i = tid; i < np; i += kTrsvThreads) v[i] = i < n ? rhs[i] : 0.f;
+  __syncthreads();
+  for (int k = 0; k < nt; ++k) {
+    for (int r = warp; r < kTile; r += kTrsvThreads / 32) {
+      const float* row = L + int64_t(k * kTile + r) * ld;
+      float s = 0.f;
+      for (int j = lane; j < k * kTile; j += 32) s += row[j] * v[j];
+      s = warp_sum_f(s);
+      if (lane == 0) t[r] = v[k * kTile + r] - s;
+    }
+    __syncthreads();
+    const float* dk = dinv + int64_t(k) * kTile * kTile;
+    for (int r = warp; r < kTile; r += kTrsvThreads / 32) {
+      float s = 0.f;
+      for (int j = lane; j <= r; j += 32) s += dk[r * kTile + j] * t[j];
+      s = warp_sum_f(s);
+      if (lane == 0) v[k * kTile + r] = s;
+    }
+    __syncthreads();
+  }
+  const int c = tid & (kTile - 1), g = tid >> 7;
+  constexpr int G = kTrsvThreads / kTile;
+  for (int k = nt - 1; k >= 0; --k) {
+    float s = 0.f;
+    for (int j = (k + 1) * kTile + g; j < np; j += G) s += L[int64_t(j) * ld + k * kTile + c] * v[j];
+    part[g][c] = s;
+    __syncthreads();
+    if (tid < kTile) {
+      float acc = 0.f;
+      for (int q = 0; q < G; ++q) acc += part[q][tid];
+      t[tid] = v[k * kTile + tid] - acc;
+    }
+    __syncthreads();
+    const float* dk = dinv + int64_t(k) * kTile * kTile;
+    float s2 = 0.f;
+    for (int r = g; r < kTile; r += G) s2 += dk[r * kTile + c] * t[r];  // zero above the diagonal
+    part[g][c] = s2;
+    __syncthreads();
+    if (tid < kTile) {
+      float acc = 0.f;
+      for (int q = 0; q < G; ++q) acc += part[q][tid];
+      v[k * kTile + tid] = acc;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += kTrsvThreads) z[i] = d[i] * double(v[i]);
+}
+
+// Flexible preconditioned conjugate gradients in FP64.  Scalars live on the
+// device: rz = r.z, pq = p.(A p), rr = |D r|^2, rz_new = r.z_new, rz_mix =
+// r.z_old (Polak-Ribiere beta = (rz_new - rz_mix) / rz), bb = |D b|^2.  The
+// residual is measured after the Jacobi scaling D, which makes the
+// tolerance independent of the units of the unknowns.
+enum { kRz = 0, kPq = 1, kRr = 2, kRzNew = 3, kRzMix = 4, kBb = 5, kNumScal = 6 };
+
+__device__ __forceinline__ void block_add(double v, double* out) {
+  __shared__ double wsum[32];
+  v = warp_sum_d(v);
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) wsum[w] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int k = 0; k < int(blockDim.x >> 5); ++k) s += wsum[k];
+    atomicAdd(out, s);
+  }
+  __syncthreads();
+}
+
+// x = 0, r = b, rs = fp32(D b), bb = |b|^2
+__global__ void cg_init_kernel(int n, const double* __restrict__ b, const double* __restrict__ d,
+                               double* __restrict__ x, double* __restrict__ r, float* __restrict__ rs,
+                               double* __restrict__ scal) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double e = 0.0;
+  if (i < n) {
+    const double v = b[i];
+    x[i] = 0.0;
+    r[i] = v;
+    const double sv = d[i] * v;
+    rs[i] = float(sv);
+    e = sv * sv;
+  }
+  block_add(e, scal + kBb);
+}
+
+// q = A p (full FP64 matrix, one warp per row), pq += p.q
+__global__ void symv_kernel(int n, const double* __restrict__ A, int lda, const double* __restrict__ p,
+                            double* __restrict__ q, double* __restrict__ scal) {
+  const int row = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  double e = 0.0;
+  if (row < n) {
+    const double* ar = A + int64_t(row) * lda;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s += ar[j] * p[j];
+    s = warp_sum_d(s);
+    if (lane == 0) {
+      q[row] = s;
+      e = s * p[row];
+    }
+  }
+  block_add(e, scal + kPq);
+}
+
+// alpha = rz / pq; x += alpha p; r -= alpha q; rs = fp32(D r); rr += |r|^2
+__global__ void cg_update_kernel(int n, const double* __restrict__ p, const double* __restrict__ q,
+                                 const double* __restrict__ d, double* __restrict__ x, double* __restrict__ r,
+                                 float* __restrict__ rs, double* __restrict__ scal) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double pq = scal[kPq];
+  const double alpha = pq > 0.0 ? scal[kRz] / pq : 0.0;
+  double e = 0.0;
+  if (i < n) {
+    x[i] += alpha * p[i];
+    const double v = r[i] - alpha * q[i];
+    r[i] = v;
+    const double sv = d[i] * v;
+    rs[i] = float(sv);
+    e = sv * sv;
+  }
+  block_add(e, scal + kRr);
+}
+
+// rz_new += r.z_new, rz_mix += r.z_old (z_old null: first direction)
+__global__ void cg_dots_kernel(int n, const double* __restrict__ r, const double* __restrict__ z,
+                               const double* __restrict__ z_old, double* __restrict__ scal) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double a = 0.0, b = 0.0;
+  if (i < n) {
+    a = r[i] * z[i];
+    if (z_old) b = r[i] * z_old[i];
+  }
+  block_add(a, scal + kRzNew);
+  if (z_old) block_add(b, scal + kRzMix);
+}
+
+// p = z + beta p (beta = 0 on the first direction)
+__global__ void cg_dir_kernel(int n, const double* __restrict__ z, double* __restrict__ p,
+                              const double* __restrict__ scal, int first) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double rz = scal[kRz];
+  const double beta = first || !(rz != 0.0) ? 0.0 : (scal[kRzNew] - scal[kRzMix]) / rz;
+  p[i] = z[i] + beta * p[i];
+}
+
+__global__ void cg_rotate_kernel(double* scal) {
+  scal[kRz] = scal[kRzNew];
+  scal[kPq] = 0.0;
+  scal[kRr] = 0.0;
+  scal[kRzNew] = 0.0;
+  scal[kRzMix] = 0.0;
+}
+
+void set_smem(const void* f, int bytes) {
+  GB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+}
+
+void launch_gemm(const GemmArgs& g, int tiles_m, int tiles_n) {
+  static bool configured = false;
+  if (!configured) {
+    set_smem(reinterpret_cast<const void*>(tc_gemm_nt_kernel), kGemmSmem);
+    configured = true;
+  }
+  tc_gemm_nt_kernel<<<dim3(tiles_m, tiles_n), kGemmThreads, kGemmSmem>>>(g);
+}
+
+double seconds_now() {
+  using clk = std::chrono::steady_clock;
+  return std::chrono::duration<double>(clk::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+void tc_gemm_nt(const float* A, int lda, const float* B, int ldb, float* C, int ldc, int m, int n, int k,
+                int* status) {
+  if (m % kTile || n % kTile || k % kKb || k <= 0 || lda % 4 || ldb % 4 || ldc % 4)
+    throw std::invalid_argument("tc_gemm_nt: m, n must be multiples of 128, k a positive multiple of 32");
+  GemmArgs g{A, lda, B, ldb, C, ldc, nullptr, k, status};
+  launch_gemm(g, m / kTile, n / kTile);
+  GB_CUDA(cudaGetLastError());
+}
+
+int DenseSpdSolver::factor(double* A, int n, int lda) {
+  n_ = n;
+  A_ = A;
+  lda_ = lda;
+  nt_ = (n + kTile - 1) / kTile;
+  n_pad_ = nt_ * kTile;
+  shift_ = 0.0;
+  if (n <= 0) return 0;
+  static bool configured = false;
+  if (!configured) {
+    set_smem(reinterpret_cast<const void*>(potrf_tile_kernel), kPotrfSmem);
+    set_smem(reinterpret_cast<const void*>(trsv_kernel), 64 * 1024);
+    configured = true;
+  }
+  if (n_pad_ > 64 * 1024 / 4) throw std::invalid_argument("dense solver: system larger than 16384 unknowns");
+  L_.resize(size_t(n_pad_) * n_pad_);
+  dinv_.resize(size_t(nt_) * kTile * kTile);
+  rs_.resize(n_pad_);
+  dscale_.resize(n_pad_);
+  r_.resize(4 * size_t(n_pad_));  // r, p, q and the second preconditioned residual
+  z_.resize(n_pad_);
+  scal_.resize(kNumScal);
+  // status: [0] non-positive diagonal, [1] non-positive pivot, [2] wait timed out
+  status_.resize(3);
+  status_.zero();
+  jacobi_scale_kernel<<<(n + 255) / 256, 256>>>(n, A, lda, dscale_.get(), status_.get());
+  int st[3] = {0, 0, 0};
+  GB_CUDA(cudaMemcpy(st, status_.get(), sizeof(st), cudaMemcpyDeviceToHost));
+  if (st[0]) return 1;
+  // the scaled matrix has a unit diagonal: the shifts are relative to it
+  static const double kShifts[] = {0.0, 1e-6, 1e-4, 1e-2, 1.0};
+  for (double shift : kShifts) {
+    const int64_t total = int64_t(n_pad_) * n_pad_;
+    load_scaled_kernel<<<int((total + 255) / 256), 256>>>(n, n_pad_, A, lda, dscale_.get(), L_.get(), shift);
+    float* L = L_.get();
+    const int ld = n_pad_;
+    for (int k = 0; k < nt_; ++k) {
+      float* rowk = L + int64_t(k) * kTile * ld;
+      if (k > 0) {
+        GemmArgs g{rowk, ld, rowk, ld, rowk + int64_t(k) * kTile, ld, rowk + int64_t(k) * kTile, k * kTile,
+                   status_.get() + 2};
+        launch_gemm(g, nt_ - k, 1);
+      }
+      potrf_tile_kernel<<<1, kPotrfThreads, kPotrfSmem>>>(L, ld, k, dinv_.get(), status_.get());
+      if (k + 1 < nt_) {
+        float* below = L + int64_t(k + 1) * kTile * ld + int64_t(k) * kTile;
+        GemmArgs g{below, ld, dinv_.get() + int64_t(k) * kTile * kTile, kTile, below, ld, nullptr, kTile,
+                   status_.get() + 2};
+        launch_gemm(g, nt_ - k - 1, 1);
+      }
+    }
+    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cudaMemcpy(st, status_.get(), sizeof(st), cudaMemcpyDeviceToHost));
+    if (st[2]) return 2;
+    shift_ = shift;
+    if (!st[1]) return 0;
+    GB_CUDA(cudaMemset(status_.get() + 1, 0, sizeof(int)));
+  }
+  return 1;
+}
+
+int DenseSpdSolver::solve(const double* b, double* x, double tol, int max_iterations, DenseSolveStats* stats) {
+  DenseSolveStats out;
+  if (n_ <= 0) {
+    if (stats) *stats = out;
+    return 0;
+  }
+  const int n = n_;
+  const int eg = (n + 255) / 256;
+  const int rows_per_block = 8;
+  const int mg = (n + rows_per_block - 1) / rows_per_block;
+  double* r = r_.get();
+  double* p = r + n_pad_;
+  double* q = p + n_pad_;
+  double* z_new = q + n_pad_;
+  double* z_old = z_.get();
+  double* scal = scal_.get();
+  const size_t trsv_smem = size_t(n_pad_) * sizeof(float);
+  scal_.zero();
+  cg_init_kernel<<<eg, 256>>>(n, b, dscale_.get(), x, r, rs_.get(), scal);
+  trsv_kernel<<<1, kTrsvThreads, trsv_smem>>>(L_.get(), n_pad_, dinv_.get(), nt_, n, rs_.get(), dscale_.get(),
+                                              z_old);
+  cg_dots_kernel<<<eg, 256>>>(n, r, z_old, nullptr, scal);
+  cg_dir_kernel<<<eg, 256>>>(n, z_old, p, scal, 1);
+  cg_rotate_kernel<<<1, 1>>>(scal);
+  GB_CUDA(cudaGetLastError());
+  double bb = 0.0;
+  GB_CUDA(cudaMemcpy(&bb, scal + kBb, sizeof(double), cudaMemcpyDeviceToHost));
+  if (!(bb > 0.0)) {
+    if (stats) *stats = out;
+    return 0;
+  }
+  out.status = 3;
+  for (int it = 0; it < max_iterations; ++it) {
+    symv_kernel<<<mg, 32 * rows_per_block>>>(n, A_, lda_, p, q, scal);
+    cg_update_kernel<<<eg, 256>>>(n, p, q, dscale_.get(), x, r, rs_.get(), scal);
+    double s2[2];  // pq, rr
+    GB_CUDA(cudaMemcpy(s2, scal + kPq, sizeof(s2), cudaMemcpyDeviceToHost));
+    ++out.refinements;
+    const double rel = std::sqrt(s2[1] / bb);
+    out.rel_residual = rel;
+    if (!(s2[0] > 0.0)) {
+      out.status = std::isfinite(s2[0]) ? 1 : 3;  // p . A p <= 0: not positive definite
+      break;
+    }
+    if (!std::isfinite(rel)) break;
+    if (rel <= tol) {
+      out.status = 0;
+      break;
+    }
+    trsv_kernel<<<1, kTrsvThreads, trsv_smem>>>(L_.get(), n_pad_, dinv_.get(), nt_, n, rs_.get(),
+                                                dscale_.get(), z_new);
+    cg_dots_kernel<<<eg, 256>>>(n, r, z_new, z_old, scal);
+    cg_dir_kernel<<<eg, 256>>>(n, z_new, p, scal, 0);
+    cg_rotate_kernel<<<1, 1>>>(scal);
+    std::swap(z_new, z_old);
+  }
+  GB_CUDA(cudaGetLastError());
+  if (stats) *stats = out;
+  return out.status;
+}
+
+}  // namespace gbba
+
+// ---------------------------------------------------------------------------
+// C ABI (include/gbba.h)
+extern "C" int gbba_dense_spd_solve(const double* a, int n, const double* b, double* x, double tol,
+                                    int max_refinements, gbba_dense_stats_t* stats) {
+  return gbba::guarded([&] {
+    if (!a || !b || !x || n < 0 || max_refinements < 1 || !(tol > 0.0))
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_dense_spd_solve: invalid argument");
+    gbba::DeviceArray<double> A, B, X;
+    A.upload(a, size_t(n) * n);
+    B.upload(b, size_t(n));
+    X.resize(size_t(std::max(n, 1)));
+    gbba::DenseSpdSolver solver;
+    GB_CUDA(cudaDeviceSynchronize());
+    const double t0 = gbba::seconds_now();
+    gbba::DenseSolveStats st;
+    st.status = solver.factor(A.get(), n, n);
+    GB_CUDA(cudaDeviceSynchronize());
+    const double t1 = gbba::seconds_now();
+    if (st.status == 0) solver.solve(B.get(), X.get(), tol, max_refinements, &st);
+    GB_CUDA(cudaDeviceSynchronize());
+    const double t2 = gbba::seconds_now();
+    X.download(x, size_t(n));
+    GB_CUDA(cudaDeviceSynchronize());
+    if (stats) {
+      stats->status = st.status;
+      stats->refinements = st.refinements;
+      stats->rel_residual = st.rel_residual;
+      stats->factor_seconds = t1 - t0;
+      stats->solve_seconds = t2 - t1;
+    }
+  });
+}
+
+extern "C" int gbba_dense_gemm_nt(const float* a, const float* b, float* c, int m, int n, int k) {
+  return gbba::guarded([&] {
+    if (!a || !b || !c || m <= 0 || n <= 0 || k <= 0 || m % 128 || n % 128 || k % 32)
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT,
+                           "gbba_dense_gemm_nt: m, n must be positive multiples of 128 and k of 32");
+    gbba::DeviceArray<float> A, B, C;
+    gbba::DeviceArray<int> status(1);
+    A.upload(a, size_t(m) * k);
+    B.upload(b, size_t(n) * k);
+    C.resize(size_t(m) * n);
+    status.zero();
+    gbba::tc_gemm_nt(A.get(), k, B.get(), k, C.get(), n, m, n, k, status.get());
+    int st = 0;
+    status.download(&st, 1);
+    C.download(c, size_t(m) * n);
+    GB_CUDA(cudaDeviceSynchronize());
+    if (st != 0) throw gbba::ApiError(GBBA_ERR_CUDA, "gbba_dense_gemm_nt: a device wait timed out");
+  });
+}

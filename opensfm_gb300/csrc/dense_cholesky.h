@@ -1,0 +1,56 @@
+// Dense symmetric positive definite solver for the reduced camera system.
+//
+// Ceres factors the reduced camera system S = U - W V^-1 W^T with a dense
+// (DENSE_SCHUR) or sparse (SPARSE_SCHUR) Cholesky factorization
+// (bundle_adjuster.cc:1159-1190; the choice in ba_helpers.cc:42-49).  Here
+// S is Jacobi-scaled, converted to FP32 and factored by a blocked
+// left-looking Cholesky whose block products run on the tensor cores
+// (tcgen05, TF32 operands, three products per term); FP64 iterative
+// refinement against the FP64 matrix then brings the solution to FP64
+// accuracy.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "device_buffer.h"
+
+namespace gbba {
+
+struct DenseSolveStats {
+  int status = 0;           // 0 solved, 1 not positive definite, 2 device wait timed out, 3 not converged
+  int refinements = 0;      // FP64 conjugate-gradient iterations (one FP64 matrix product each)
+  double rel_residual = 0;  // |D (b - A x)| / |D b| of the returned x, D = diag(A)^-1/2
+};
+
+class DenseSpdSolver {
+ public:
+  // Factors A: device FP64, n x n row-major with leading dimension lda.  The
+  // lower triangle is read and the upper triangle is overwritten with its
+  // mirror (the solve multiplies by the full matrix).  A must stay
+  // unchanged until the last solve().  Returns a DenseSolveStats status
+  // (0, 1 or 2).
+  int factor(double* A, int n, int lda);
+  // x = A^-1 b (device FP64 vectors of length n) to a relative scaled
+  // residual tol within max_iterations FP64 conjugate-gradient iterations
+  // preconditioned by the factor.
+  int solve(const double* b, double* x, double tol, int max_iterations, DenseSolveStats* stats);
+  int n() const { return n_; }
+  double shift() const { return shift_; }  // diagonal shift the factor needed (0 normally)
+
+ private:
+  int n_ = 0, nt_ = 0, n_pad_ = 0, lda_ = 0;
+  double shift_ = 0.0;
+  double* A_ = nullptr;
+  DeviceArray<float> L_, dinv_, rs_;
+  DeviceArray<double> dscale_, r_, z_, scal_;
+  DeviceArray<int> status_;
+};
+
+// C = A B^T on the tensor cores for row-major device FP32 matrices A (m x k,
+// leading dimension lda), B (n x k, ldb), C (m x n, ldc); m and n multiples
+// of 128, k a multiple of 32, leading dimensions multiples of 4.  status
+// (device) is set to 2 if a device wait timed out.
+void tc_gemm_nt(const float* A, int lda, const float* B, int ldb, float* C, int ldc, int m, int n, int k,
+                int* status);
+
+}  // namespace gbba

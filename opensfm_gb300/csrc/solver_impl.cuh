@@ -11,6 +11,8 @@
 #include <sstream>
 #include <vector>
 
+#include "dense_cholesky.h"
+#include "dense_schur.cuh"
 #include "device_buffer.h"
 #include "solver.h"
 #include "solver_kernels.cuh"
@@ -29,8 +31,12 @@ constexpr double kEps = 2.220446049250313e-16;
 constexpr double kRefineThreshold = 1e-4;
 constexpr double kRefineInnerTolerance = 1e-3;
 constexpr int kMaxRefinements = 4;
-// Mixed precision: PCG tolerance of the step that confirms convergence.
+// PCG tolerance of the step that confirms convergence of an inexact solve.
 constexpr double kConfirmTolerance = 1e-6;
+// Dense mode: relative residual of the solution, and the most FP64
+// conjugate-gradient iterations (preconditioned by the factor) per step.
+constexpr double kDenseTolerance = 1e-12;
+constexpr int kDenseMaxRefinements = 50;
 
 struct KernelConfig {
   int model;  // single model or kDyn
@@ -639,6 +645,7 @@ class DeviceSolver : public SolverBase {
   // ---- linear solve
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
   int run_pcg(const R* rhs, double bb, double tol, int max_it);
+  int solve_dense(double mu);
   // ---- IRLS
   double compute_weights(std::vector<std::string>& groups_report, int& proj_out, int& proj_total,
                          std::vector<std::pair<std::string, std::pair<int, int>>>& other);
@@ -669,6 +676,13 @@ class DeviceSolver : public SolverBase {
   int64_t refinements_ = 0;  // FP64 residual evaluations of iterative refinement
   int64_t confirmations_ = 0;  // convergence confirmations with a refined step (mixed)
   double pcg_tolerance_override_ = 0.0;  // > 0: PCG tolerance of the next steps
+  // dense mode: explicit reduced camera system over the n_dense_ optimised
+  // camera-side coordinates, factored by DenseSpdSolver
+  bool dense_ = false;
+  int n_dense_ = 0;
+  int64_t n_pairs_ = 0;
+  int64_t dense_failures_ = 0;  // factorizations that found the system not positive definite
+  DenseSpdSolver dense_solver_;
   std::vector<double> last_errors_, last_weights_;
 
   // device state
@@ -716,6 +730,10 @@ class DeviceSolver : public SolverBase {
   DeviceArray<int> d_group_dim_;
   DeviceArray<PointPriorDev> d_pp_;
   DeviceArray<double> d_pp_w_, d_pp_res_;
+  DeviceArray<int> d_dmap_, d_didx_;
+  DeviceArray<int2> d_pairs_;
+  DeviceArray<double> d_S_, d_WT_, d_bd_, d_xd_;
+  DeviceArray<double> d_V64_, d_Vinv64_, d_gp64_;  // FP64 point blocks of the dense path
 };
 
 // ---------------------------------------------------------------------------
@@ -863,6 +881,50 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
   d_rec_sm_.resize(size_t(n_planes_) * n_slots_);
   d_rec_sm_.zero();
+
+  // Dense mode: the reduced camera system is formed explicitly and factored
+  // when the linear solver type asks for an exact solve (Ceres' DENSE_*,
+  // SPARSE_SCHUR and SPARSE_NORMAL_CHOLESKY) and the optimised camera-side
+  // coordinates number at most opts.dense_max_unknowns; ITERATIVE_SCHUR,
+  // CGNR and larger systems use PCG on the implicit Schur product.
+  {
+    const std::string& ls = opts.linear_solver;
+    const bool exact = ls == "DENSE_SCHUR" || ls == "DENSE_QR" || ls == "DENSE_NORMAL_CHOLESKY" ||
+                       ls == "SPARSE_SCHUR" || ls == "SPARSE_NORMAL_CHOLESKY";
+    std::vector<int> dmap(cl_.n, -1);
+    n_dense_ = 0;
+    for (int j = 0; j < cl_.n; ++j)
+      if (cmask_[j]) dmap[j] = n_dense_++;
+    dense_ = exact && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
+    if (dense_) {
+      // pairs (o1 >= o2) of the observations of every point, as point-major
+      // slot indices
+      std::vector<int2> pairs;
+      int64_t s0 = 0;
+      while (s0 < n_obs_) {
+        const int p = P.observations[order[s0]].point;
+        int64_t s1 = s0 + 1;
+        while (s1 < n_obs_ && P.observations[order[s1]].point == p) ++s1;
+        for (int64_t a = s0; a < s1; ++a)
+          for (int64_t b = s0; b <= a; ++b) pairs.push_back(make_int2(int(a), int(b)));
+        s0 = s1;
+      }
+      n_pairs_ = int64_t(pairs.size());
+      const int W = 6 + kc_.cmax + (kc_.rig ? 6 : 0);
+      d_dmap_.upload(dmap);
+      d_pairs_.upload(pairs);
+      d_didx_.resize(size_t(n_slots_) * W);
+      d_WT_.resize(size_t(n_slots_) * 6 * W);
+      d_S_.resize(size_t(n_dense_) * n_dense_);
+      d_bd_.resize(n_dense_);
+      d_xd_.resize(n_dense_);
+      d_x64_.resize(cl_.n);
+      const size_t np1 = size_t(std::max<int64_t>(1, n_pt_));
+      d_V64_.resize(8 * np1);
+      d_Vinv64_.resize(8 * np1);
+      d_gp64_.resize(4 * np1);
+    }
+  }
 
   // shots / cameras / rigs
   std::vector<int> si(n_shots_), sr(n_shots_), sc(n_shots_);

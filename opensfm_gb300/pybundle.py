@@ -473,10 +473,12 @@ class BundleBatch:
 
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
-                        pcg_tolerance: Optional[float] = None) -> BundleAdjuster:
+                        pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path)."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
+    if linear_solver is not None:
+        ba.set_linear_solver_type(linear_solver)
     ba.set_irls_mode(irls)
     ba.set_max_num_iterations(max_iterations)
     if pcg_tolerance is not None:

@@ -5,7 +5,10 @@ within 1e-3 px.  FP64 runs use a tight PCG tolerance so their trajectory
 tracks the oracle's exact dense Schur solves; mixed-precision runs are held
 to the same converged-cost bar at a PCG tolerance of 1e-4, about what FP32
 conjugate gradients attain on these systems (tighter tolerances switch on
-FP64 iterative refinement, exercised by its own test).
+FP64 iterative refinement, exercised by its own test).  Runs use the PCG
+path (ITERATIVE_SCHUR) unless a test names the default SPARSE_SCHUR, which
+these system sizes solve by the dense tensor-core Cholesky
+(tests/test_gpu_dense.py covers that path on its own).
 """
 import numpy as np
 import pytest
@@ -22,19 +25,21 @@ def _rms_px(errors, width=1000):
     return float(np.sqrt((e ** 2).sum(1).mean()))
 
 
-def _run(scene, precision, **kw):
+def _run(scene, precision, linear_solver="ITERATIVE_SCHUR", **kw):
     pcg = kw.pop("pcg_tolerance", 1e-10 if precision == "fp64" else 1e-4)
-    ba = adjuster_from_scene(scene, precision=precision, pcg_tolerance=pcg, **kw)
+    ba = adjuster_from_scene(scene, precision=precision, pcg_tolerance=pcg, linear_solver=linear_solver, **kw)
     ba.run()
     errs, w, _ = ba.projection_results()
     return ba, errs, w
 
 
+@pytest.mark.parametrize("solver", ["ITERATIVE_SCHUR", "SPARSE_SCHUR"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_ring_huber_matches_oracle(precision):
+def test_ring_huber_matches_oracle(precision, solver):
     scene = syn.ring_scene(n_points=2000)
     ref = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=50, gps=False)
-    ba, errs, _ = _run(scene, precision, loss=("HuberLoss", 1.0), irls="none", max_iterations=50, gps=False)
+    ba, errs, _ = _run(scene, precision, linear_solver=solver, loss=("HuberLoss", 1.0), irls="none",
+                       max_iterations=50, gps=False)
     s = ba.summary()
     assert s["usable"]
     rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
@@ -48,21 +53,27 @@ def test_ring_huber_matches_oracle(precision):
     assert np.abs((errs[:, :2] - ref["errors"][:, :2]) * 1000).max() < 2e-2
 
 
+@pytest.mark.parametrize("solver", ["ITERATIVE_SCHUR", "SPARSE_SCHUR"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_ring_irls_mixture_matches_oracle(precision):
+def test_ring_irls_mixture_matches_oracle(precision, solver):
     scene = syn.ring_scene(n_points=2000, outlier_ratio=0.03, seed=5)
     ref = oracle.solve(scene, irls="mixture", max_iterations=100, gps=False)
-    ba, errs, w = _run(scene, precision, irls="mixture", max_iterations=100, gps=False)
+    ba, errs, w = _run(scene, precision, linear_solver=solver, irls="mixture", max_iterations=100, gps=False)
     s = ba.summary()
     rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
-    # IRLS reweights at states along the trajectory and stops on a
-    # log-likelihood test, so the final objective depends on the path: FP64
-    # tracks the oracle's path (1e-6); the mixed-precision path reweights at
-    # slightly different states (bar 1e-4).
-    assert rel < (1e-6 if precision == "fp64" else 1e-4), (s["final_cost"], ref["final_cost"])
-    assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < (1e-3 if precision == "fp64" else 1e-2)
+    # IRLS reweights at states along the trajectory and stops once the
+    # log-likelihood changes by less than 1e-3, so the final objective depends
+    # on the path.  The exact (dense) steps track the oracle's path in both
+    # precisions.  Inexact PCG steps reweight at slightly different states;
+    # in FP32 the atomics' summation order alone moves the end point by up to
+    # a few 1e-3 between runs.
+    bar = {("fp64", "SPARSE_SCHUR"): 1e-6, ("mixed", "SPARSE_SCHUR"): 1e-5,
+           ("fp64", "ITERATIVE_SCHUR"): 1e-6, ("mixed", "ITERATIVE_SCHUR"): 1e-2}[(precision, solver)]
+    assert rel < bar, (s["final_cost"], ref["final_cost"])
+    exact = precision == "fp64" or solver == "SPARSE_SCHUR"
+    assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < (1e-3 if exact else 5e-2)
     # the outliers are down-weighted the same way
-    assert np.abs(w - ref["weights"]).max() < (1e-3 if precision == "fp64" else 2e-2)
+    assert np.abs(w - ref["weights"]).max() < (1e-3 if exact else 1e-1)
     assert ba.irls_report()
 
 
@@ -80,20 +91,28 @@ def test_street_brown_soft_l1_outliers_not_worse_than_oracle():
     assert s["final_cost"] < 0.75 * s["initial_cost"]
 
 
-def test_street_brown_soft_l1_mixed_matches_oracle():
+@pytest.mark.parametrize("solver", ["ITERATIVE_SCHUR", "SPARSE_SCHUR"])
+def test_street_brown_soft_l1_mixed_matches_oracle(solver):
+    # Brown intrinsics shared by 40 shots, no priors: PCG converges slowly
+    # (hundreds of iterations per step) and its inexact steps stop the LM
+    # loop a little early, a few 1e-7 .. 1e-5 above the optimum depending on
+    # the run; the exact dense steps follow the oracle (3.5e-9 measured)
     scene = syn.street_scene(n_shots=40, n_points=3000, seed=11, outlier_ratio=0.0)
     ref = oracle.solve(scene, loss=("SoftLOneLoss", 1.0), irls="none", max_iterations=100, gps=False)
-    ba, errs, _ = _run(scene, "mixed", loss=("SoftLOneLoss", 1.0), irls="none", max_iterations=100, gps=False)
+    ba, errs, _ = _run(scene, "mixed", linear_solver=solver, loss=("SoftLOneLoss", 1.0), irls="none",
+                       max_iterations=100, gps=False)
     s = ba.summary()
     rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
-    assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
+    assert rel < (1e-6 if solver == "SPARSE_SCHUR" else 3e-5), (s["final_cost"], ref["final_cost"])
     assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < 1e-3
 
 
-def test_aerial_gps_utm_mixed_matches_oracle():
+@pytest.mark.parametrize("solver", ["ITERATIVE_SCHUR", "SPARSE_SCHUR"])
+def test_aerial_gps_utm_mixed_matches_oracle(solver):
     scene = syn.aerial_scene(seed=2, nx=8, ny=8, n_points=4000)
     ref = oracle.solve(scene, loss=("HuberLoss", 2.0), irls="none", max_iterations=60, gps=True)
-    ba, errs, _ = _run(scene, "mixed", loss=("HuberLoss", 2.0), irls="none", max_iterations=60, gps=True)
+    ba, errs, _ = _run(scene, "mixed", linear_solver=solver, loss=("HuberLoss", 2.0), irls="none",
+                       max_iterations=60, gps=True)
     s = ba.summary()
     rel = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
     assert rel < 1e-6, (s["final_cost"], ref["final_cost"])
