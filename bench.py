@@ -133,8 +133,8 @@ def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return {"hbm_gbs": d["hbm_gbs"], "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d.get("bf16_tflops", 1900.0), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
 def traffic_per_obs(kernel: str, precision: str):
@@ -280,6 +280,72 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
         "median_rel_cost_batch_vs_single_unconverged": float(np.median(rel[~both])) if (~both).any() else None,
         "mean_cost_reduction": float(np.mean(1.0 - batch_costs / init_costs)),
     })
+    return out
+
+
+def dense_benchmark(sizes=(1024, 2048, 4096), street_shots: int = 500, street_points: int = 200_000,
+                    max_iterations: int = 60, seed: int = 29) -> dict:
+    """Dense reduced-camera-system solver.
+
+    (1) gbba_dense_spd_solve on seeded SPD matrices (condition 1e4): device
+    time of the factorization (Jacobi scaling, FP32 conversion, tensor-core
+    blocked Cholesky) and of the FP64 CG solve, and the factorization's
+    algorithmic rate n^3/3 flop / s against the tensor roofline (TF32, taken
+    as half the measured bf16 rate: the nominal dense TF32 / bf16 ratio).
+    (2) The street workload (Brown cameras, soft-L1, outlier-free so that
+    every run ends at the same minimum): the exact dense steps (DENSE_SCHUR)
+    against PCG (ITERATIVE_SCHUR, tolerance 1e-3), FP64 and mixed; target =
+    the FP64 dense final cost x (1 + 1e-6)."""
+    from opensfm_gb300 import dense
+    from opensfm_gb300 import synthetic as syn
+    from opensfm_gb300.pybundle import adjuster_from_scene
+    peaks = measured_peaks()
+    tf32_peak = peaks["bf16_tflops"] / 2.0
+    out = {"spd": []}
+    rng = np.random.default_rng(seed)
+    for n in sizes:
+        q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        a = (q * np.geomspace(1.0, 1e4, n)) @ q.T
+        a = 0.5 * (a + a.T)
+        b = rng.standard_normal(n)
+        dense.spd_solve(a, b)  # warm-up (module load, kernel attributes)
+        best = None
+        for _ in range(3):
+            x, st = dense.spd_solve(a, b)
+            if best is None or st.factor_seconds < best.factor_seconds:
+                best = st
+        flops = n ** 3 / 3.0
+        out["spd"].append({
+            "n": n, "factor_ms": best.factor_seconds * 1e3, "solve_ms": best.solve_seconds * 1e3,
+            "cg_iterations": best.refinements, "scaled_residual": best.rel_residual, "status": best.status,
+            "factor_tflops": flops / best.factor_seconds / 1e12,
+            "roofline": {"bound": "tensor", "achieved": flops / best.factor_seconds / 1e12, "peak": tf32_peak,
+                         "unit": "TFLOP/s", "frac": flops / best.factor_seconds / 1e12 / tf32_peak,
+                         "peak_source": "measured bf16 / 2 (nominal TF32 rate)"}})
+    if street_shots <= 0:
+        return out
+    scene = syn.street_scene(n_shots=street_shots, n_points=street_points, seed=seed, outlier_ratio=0.0)
+    loss = ("SoftLOneLoss", 1.0)
+    out["street"] = {"n_shots": street_shots, "n_points": int(len(scene.points)),
+                     "n_observations": int(scene.n_observations), "loss": list(loss),
+                     "max_iterations": max_iterations}
+    runs = {}
+    for precision, solver in (("fp64", "DENSE_SCHUR"), ("mixed", "DENSE_SCHUR"), ("mixed", "ITERATIVE_SCHUR"),
+                              ("fp64", "ITERATIVE_SCHUR")):
+        ba = adjuster_from_scene(scene, precision=precision, loss=loss, irls="none", gps=False,
+                                 max_iterations=max_iterations, pcg_tolerance=1e-3, linear_solver=solver)
+        ba.run()
+        runs[(precision, solver)] = (ba.summary(), ba.trace())
+        del ba
+    target = runs[("fp64", "DENSE_SCHUR")][0]["final_cost"] * (1.0 + 1e-6)
+    out["street"]["target_cost"] = target
+    for (precision, solver), (s, tr) in runs.items():
+        hit = np.nonzero(tr[:, 1] <= target)[0]
+        out["street"][f"{precision}_{solver.lower()}"] = {
+            "time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None,
+            "iterations": s["iterations"], "final_cost": s["final_cost"], "solve_s": s["seconds"],
+            "linear_solver_s": s["linear_solver_seconds"], "linear_iterations": int(tr[:, 4].sum()),
+            "setup_s": s["setup_seconds"]}
     return out
 
 
@@ -493,6 +559,10 @@ def run_ours(args) -> None:
             ev.close()
             result["batched_local_ba"] = batch_benchmark(n_problems=args.batch_problems,
                                                          one_at_a_time=not args.batch_only)
+        if not args.no_dense:
+            ev.close()
+            result["dense_rcs"] = dense_benchmark(sizes=tuple(args.dense_sizes), street_shots=args.dense_street_shots,
+                                                  street_points=args.dense_street_points)
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -515,6 +585,10 @@ def main() -> None:
     ap.add_argument("--batch-problems", type=int, default=256)
     ap.add_argument("--batch-only", action="store_true", help="skip the one-at-a-time comparison")
     ap.add_argument("--autograd-observations", type=int, default=4_000_000)
+    ap.add_argument("--no-dense", action="store_true")
+    ap.add_argument("--dense-sizes", type=int, nargs="*", default=[1024, 2048, 4096])
+    ap.add_argument("--dense-street-shots", type=int, default=500, help="0: skip the street solves")
+    ap.add_argument("--dense-street-points", type=int, default=200_000)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
