@@ -283,8 +283,11 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
     return out
 
 
+DENSE_STREET_RUNS = ("fp64:DENSE_SCHUR", "mixed:DENSE_SCHUR", "mixed:ITERATIVE_SCHUR", "fp64:ITERATIVE_SCHUR")
+
+
 def dense_benchmark(sizes=(1024, 2048, 4096), street_shots: int = 500, street_points: int = 200_000,
-                    max_iterations: int = 60, seed: int = 29) -> dict:
+                    max_iterations: int = 60, seed: int = 29, runs=DENSE_STREET_RUNS) -> dict:
     """Dense reduced-camera-system solver.
 
     (1) gbba_dense_spd_solve on seeded SPD matrices (condition 1e4): device
@@ -329,17 +332,18 @@ def dense_benchmark(sizes=(1024, 2048, 4096), street_shots: int = 500, street_po
     out["street"] = {"n_shots": street_shots, "n_points": int(len(scene.points)),
                      "n_observations": int(scene.n_observations), "loss": list(loss),
                      "max_iterations": max_iterations}
-    runs = {}
-    for precision, solver in (("fp64", "DENSE_SCHUR"), ("mixed", "DENSE_SCHUR"), ("mixed", "ITERATIVE_SCHUR"),
-                              ("fp64", "ITERATIVE_SCHUR")):
+    results = {}
+    for spec in runs:
+        precision, solver = spec.split(":")
         ba = adjuster_from_scene(scene, precision=precision, loss=loss, irls="none", gps=False,
                                  max_iterations=max_iterations, pcg_tolerance=1e-3, linear_solver=solver)
         ba.run()
-        runs[(precision, solver)] = (ba.summary(), ba.trace())
+        results[(precision, solver)] = (ba.summary(), ba.trace())
         del ba
-    target = runs[("fp64", "DENSE_SCHUR")][0]["final_cost"] * (1.0 + 1e-6)
+    first = results[next(iter(results))][0]
+    target = results.get(("fp64", "DENSE_SCHUR"), (first,))[0]["final_cost"] * (1.0 + 1e-6)
     out["street"]["target_cost"] = target
-    for (precision, solver), (s, tr) in runs.items():
+    for (precision, solver), (s, tr) in results.items():
         hit = np.nonzero(tr[:, 1] <= target)[0]
         out["street"][f"{precision}_{solver.lower()}"] = {
             "time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None,
@@ -562,7 +566,8 @@ def run_ours(args) -> None:
         if not args.no_dense:
             ev.close()
             result["dense_rcs"] = dense_benchmark(sizes=tuple(args.dense_sizes), street_shots=args.dense_street_shots,
-                                                  street_points=args.dense_street_points)
+                                                  street_points=args.dense_street_points,
+                                                  runs=tuple(args.dense_street_runs))
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -589,6 +594,8 @@ def main() -> None:
     ap.add_argument("--dense-sizes", type=int, nargs="*", default=[1024, 2048, 4096])
     ap.add_argument("--dense-street-shots", type=int, default=500, help="0: skip the street solves")
     ap.add_argument("--dense-street-points", type=int, default=200_000)
+    ap.add_argument("--dense-street-runs", nargs="*", default=list(DENSE_STREET_RUNS),
+                    help="precision:LINEAR_SOLVER pairs of the street solves")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

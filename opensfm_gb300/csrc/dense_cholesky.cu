@@ -117,18 +117,22 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
   for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// Loads a 128 x 32 FP32 block (rows of `src`, columns k0..k0+31), splits it
-// into TF32 high and remainder parts and stores both in the 128-byte
-// swizzled K-major layout: row r at byte r * 128, its 16-byte chunk c at
-// position c ^ (r & 7).
-__device__ __forceinline__ void load_split(const float* src, int ld, int k0, uint8_t* hi, uint8_t* lo, int tid) {
-  float4 x[8];
+// A 128 x 32 FP32 block (rows of `src`, columns k0..k0+31) into registers:
+// eight 16-byte pieces per thread, rows of 128 bytes read by 8 consecutive
+// threads.
+__device__ __forceinline__ void load_block(const float* src, int ld, int k0, float4 (&x)[8], int tid) {
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const int f = tid + q * kGemmThreads;
     const int r = f >> 3, c = f & 7;
     x[q] = *reinterpret_cast<const float4*>(src + int64_t(r) * ld + k0 + c * 4);
   }
+}
+
+// Splits a block into TF32 high and remainder parts and stores both in the
+// 128-byte swizzled K-major layout: row r at byte r * 128, its 16-byte chunk
+// c at position c ^ (r & 7).
+__device__ __forceinline__ void split_store(const float4 (&x)[8], uint8_t* hi, uint8_t* lo, int tid) {
 #pragma unroll
   for (int q = 0; q < 8; ++q) {
     const int f = tid + q * kGemmThreads;
@@ -155,15 +159,19 @@ struct GemmArgs {
   int ldb;
   float* c;          // C tile (0, 0)
   int ldc;
-  const float* cin;  // mode 1: C = cin - A B^T (cin laid out as C), else null
+  const float* cin;  // C = cin - A B^T (cin laid out as C), else null
   int k;             // multiple of kKb, > 0
+  int k_chunk;       // K range of one CTA (blockIdx.z), a multiple of kKb
+  int subtract;      // 1: C -= A B^T with atomic adds (split K), 0: store
   int* status;
 };
 
-// One 128 x 128 tile of C = A B^T (or cin - A B^T) per CTA: tile row
-// blockIdx.x, tile column blockIdx.y.  A and C may alias (the in-place
-// triangular solve): every A row of the tile is read before the epilogue
-// writes C.
+// One 128 x 128 tile of C = A B^T (or cin - A B^T, or C -= A B^T) per CTA:
+// tile row blockIdx.x, tile column blockIdx.y, K range blockIdx.z.  A and C
+// may alias (the in-place triangular solve, a single K range): every A row of
+// the tile is read before the epilogue writes C.  The next stage's operands
+// are loaded into registers while the current stage is split, stored and
+// multiplied.
 __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g) {
   extern __shared__ uint8_t smem_raw[];
   __shared__ __align__(8) uint64_t bars[kStages];
@@ -186,13 +194,29 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g)
   tc_fence_after();
   const uint32_t tmem = tmem_holder;
 
-  const float* A = g.a + int64_t(blockIdx.x) * kTile * g.lda;
-  const float* B = g.b + int64_t(blockIdx.y) * kTile * g.ldb;
-  const int nkb = g.k / kKb;
+  const int k0 = int(blockIdx.z) * g.k_chunk;
+  const float* A = g.a + int64_t(blockIdx.x) * kTile * g.lda + k0;
+  const float* B = g.b + int64_t(blockIdx.y) * kTile * g.ldb + k0;
+  const int nkb = max(0, min(g.k_chunk, g.k - k0)) / kKb;
   bool ok = true;
   int committed = 0;  // stages whose products were issued
+  float4 na[8], nb[8];
+  if (nkb > 0) {
+    load_block(A, g.lda, 0, na, tid);
+    load_block(B, g.ldb, 0, nb, tid);
+  }
   for (int kb = 0; kb < nkb; ++kb) {
     const int s = kb & 1;
+    float4 ca[8], cb[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      ca[q] = na[q];
+      cb[q] = nb[q];
+    }
+    if (kb + 1 < nkb) {
+      load_block(A, g.lda, (kb + 1) * kKb, na, tid);
+      load_block(B, g.ldb, (kb + 1) * kKb, nb, tid);
+    }
     if (kb >= kStages) {
       // the products of stage kb - 2 have finished reading buffer s
       const bool w = mbar_wait(smem_u32(&bars[s]), uint32_t((kb >> 1) - 1) & 1u);
@@ -200,8 +224,8 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g)
       if (!ok) break;
     }
     uint8_t* st = smem + s * kStageBytes;
-    load_split(A, g.lda, kb * kKb, st, st + kOpBytes, tid);
-    load_split(B, g.ldb, kb * kKb, st + 2 * kOpBytes, st + 3 * kOpBytes, tid);
+    split_store(ca, st, st + kOpBytes, tid);
+    split_store(cb, st + 2 * kOpBytes, st + 3 * kOpBytes, tid);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
@@ -228,7 +252,7 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g)
     ok = (__syncthreads_and(w ? 1 : 0) != 0) && ok;
   }
   tc_fence_after();
-  if (ok && committed == nkb) {
+  if (ok && committed == nkb && nkb > 0) {
     const int row = warp * 32 + lane;
     float* C = g.c + int64_t(blockIdx.x) * kTile * g.ldc + int64_t(blockIdx.y) * kTile + int64_t(row) * g.ldc;
     const float* Cin =
@@ -238,17 +262,22 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g)
     for (int cc = 0; cc < kTile / 32; ++cc) {
       float v[32];
       tmem_ld32(tmem + (uint32_t(warp * 32) << 16) + uint32_t(cc * 32), v);
+      if (g.subtract) {
 #pragma unroll
-      for (int q = 0; q < 32; q += 4) {
-        float4 o = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
-        if (Cin) {
-          const float4 ci = *reinterpret_cast<const float4*>(Cin + cc * 32 + q);
-          o = make_float4(ci.x - o.x, ci.y - o.y, ci.z - o.z, ci.w - o.w);
+        for (int q = 0; q < 32; ++q) atomicAdd(C + cc * 32 + q, -v[q]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 32; q += 4) {
+          float4 o = make_float4(v[q], v[q + 1], v[q + 2], v[q + 3]);
+          if (Cin) {
+            const float4 ci = *reinterpret_cast<const float4*>(Cin + cc * 32 + q);
+            o = make_float4(ci.x - o.x, ci.y - o.y, ci.z - o.z, ci.w - o.w);
+          }
+          *reinterpret_cast<float4*>(C + cc * 32 + q) = o;
         }
-        *reinterpret_cast<float4*>(C + cc * 32 + q) = o;
       }
     }
-  } else if (tid == 0) {
+  } else if (nkb > 0 && tid == 0) {
     atomicExch(g.status, 2);
   }
   tc_fence_before();
@@ -260,19 +289,26 @@ __global__ void __launch_bounds__(kGemmThreads, 1) tc_gemm_nt_kernel(GemmArgs g)
 }
 
 // ---------------------------------------------------------------------------
-// Diagonal tile: L_kk = chol(A_kk) and Dinv_k = L_kk^-1, in shared memory.
+// Diagonal tile: L_kk = chol(A_kk) and Dinv_k = L_kk^-1, in shared memory,
+// in eight 16-column panels.  Per panel: one warp factors the 16 x 16
+// diagonal block (lane = row, warp-synchronous), one thread per row solves
+// the rows below it against that block, and all threads update the rest of
+// the tile.  The inverse: one warp per diagonal block, then the blocks below
+// the diagonal, block row by block row: X_ij = -X_ii sum_{j<=m<i} L_im X_mj.
 constexpr int kPotrfThreads = 512;
 constexpr int kLdS = kTile + 1;
-constexpr int kPotrfSmem = 2 * kTile * kLdS * 4 + kTile * 4;
+constexpr int kPanel = 16;
+constexpr int kPotrfSmem = (2 * kTile * kLdS + (kTile / kPanel - 1) * kPanel * kPanel) * 4;
 
 __global__ void __launch_bounds__(kPotrfThreads) potrf_tile_kernel(float* L, int ld, int k, float* dinv,
                                                                    int* status) {
   extern __shared__ float sm[];
-  float* a = sm;                  // the tile, then its factor (lower)
-  float* x = sm + kTile * kLdS;   // the inverse of the factor (lower)
-  float* rdiag = x + kTile * kLdS;
+  float* a = sm;                   // the tile, then its factor (lower)
+  float* x = a + kTile * kLdS;     // the inverse of the factor (lower)
+  float* tmp = x + kTile * kLdS;   // [3][32][32] partial sums of the inverse
   __shared__ int bad;
-  const int tid = threadIdx.x;
+  __shared__ float rdiag[kTile];  // 1 / L_jj
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   float* tile = L + int64_t(k) * kTile * ld + int64_t(k) * kTile;
   for (int t = tid; t < kTile * kTile; t += kPotrfThreads) {
     const int i = t >> 7, j = t & (kTile - 1);
@@ -281,42 +317,112 @@ __global__ void __launch_bounds__(kPotrfThreads) potrf_tile_kernel(float* L, int
   }
   if (tid == 0) bad = 0;
   __syncthreads();
-  // right-looking unblocked Cholesky of the lower triangle
-  for (int j = 0; j < kTile; ++j) {
-    if (tid == 0) {
-      float d = a[j * kLdS + j];
-      if (!(d > 0.f) || !isfinite(d)) {
-        bad = 1;
-        d = 1.f;
+  for (int p = 0; p < kTile / kPanel; ++p) {
+    const int c0 = kPanel * p;
+    if (warp == 0) {
+      // the diagonal block, warp-synchronous: lane = row (lanes beyond the
+      // panel only take part in the warp's collective steps)
+      const bool act = lane < kPanel;
+      const int i = c0 + (act ? lane : kPanel - 1);
+      for (int j = 0; j < kPanel; ++j) {
+        const int jj = c0 + j;
+        float d = a[jj * kLdS + jj];
+        if (!(d > 0.f) || !isfinite(d)) {
+          if (lane == 0) bad = 1;
+          d = 1.f;
+        }
+        // the factor only preconditions FP64 conjugate gradients: the fast
+        // reciprocal square root is accurate enough
+        const float inv = rsqrtf(d);
+        const float l = d * inv;
+        __syncwarp();
+        if (lane == j) {
+          a[jj * kLdS + jj] = l;
+          rdiag[jj] = inv;
+        }
+        if (act && lane > j) a[i * kLdS + jj] *= inv;
+        __syncwarp();
+        // all loads first (constant offsets, so they issue back to back),
+        // then the predicated updates of this lane's row
+        const float lij = a[i * kLdS + jj];
+        float lc[kPanel], ar[kPanel];
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c) {
+          lc[c] = a[(c0 + c) * kLdS + jj];
+          ar[c] = a[i * kLdS + c0 + c];
+        }
+#pragma unroll
+        for (int c = 0; c < kPanel; ++c)
+          if (act && c > j && c <= lane) a[i * kLdS + c0 + c] = ar[c] - lij * lc[c];
+        __syncwarp();
       }
-      const float l = sqrtf(d);
-      a[j * kLdS + j] = l;
-      rdiag[j] = 1.f / l;
     }
     __syncthreads();
-    const float inv = rdiag[j];
-    for (int i = j + 1 + tid; i < kTile; i += kPotrfThreads) a[i * kLdS + j] *= inv;
+    for (int i = c0 + kPanel + tid; i < kTile; i += kPotrfThreads) {
+      // row i of the panel in registers, solved against the diagonal block
+      float row[kPanel];
+#pragma unroll
+      for (int j = 0; j < kPanel; ++j) row[j] = a[i * kLdS + c0 + j];
+#pragma unroll
+      for (int j = 0; j < kPanel; ++j) {
+        float v = row[j];
+#pragma unroll
+        for (int m = 0; m < j; ++m) v -= row[m] * a[(c0 + j) * kLdS + c0 + m];
+        row[j] = v * rdiag[c0 + j];
+      }
+#pragma unroll
+      for (int j = 0; j < kPanel; ++j) a[i * kLdS + c0 + j] = row[j];
+    }
     __syncthreads();
-    for (int i = j + 1 + (tid >> 4); i < kTile; i += kPotrfThreads / 16) {
-      const float lij = a[i * kLdS + j];
-      for (int c = j + 1 + (tid & 15); c <= i; c += 16) a[i * kLdS + c] -= lij * a[c * kLdS + j];
+    const int r0 = c0 + kPanel;
+    for (int i = r0 + (tid >> 4); i < kTile; i += kPotrfThreads / 16) {
+      for (int c = r0 + (tid & 15); c <= i; c += 16) {
+        float v = 0.f;
+#pragma unroll 8
+        for (int m = 0; m < kPanel; ++m) v += a[i * kLdS + c0 + m] * a[c * kLdS + c0 + m];
+        a[i * kLdS + c] -= v;
+      }
     }
     __syncthreads();
   }
-  // X = L^-1 by forward substitution, four threads per column
-  {
-    const int c = tid >> 2, s = tid & 3;
-    for (int i = 0; i < kTile; ++i) {
-      float part = 0.f;
-      if (i >= c)
-        for (int m = c + s; m < i; m += 4) part += a[i * kLdS + m] * x[m * kLdS + c];
-      part += __shfl_xor_sync(0xffffffffu, part, 1);
-      part += __shfl_xor_sync(0xffffffffu, part, 2);
-      if (s == 0 && i >= c) x[i * kLdS + c] = ((i == c ? 1.f : 0.f) - part) * rdiag[i];
-      __syncwarp();
+  // inverse of the diagonal 32 x 32 blocks: warp w inverts block w, lane = column
+  if (warp < kTile / kPanel) {
+    // lane c holds column c of the block's inverse in registers
+    const int b0 = kPanel * warp, c = lane < kPanel ? lane : kPanel - 1;
+    float col[kPanel];
+#pragma unroll
+    for (int i = 0; i < kPanel; ++i) {
+      float v = i == c ? 1.f : 0.f;
+#pragma unroll
+      for (int m = 0; m < i; ++m) v -= a[(b0 + i) * kLdS + b0 + m] * col[m];
+      col[i] = i >= c ? v * rdiag[b0 + i] : 0.f;
+    }
+    if (lane < kPanel) {
+#pragma unroll
+      for (int i = 0; i < kPanel; ++i) x[(b0 + i) * kLdS + b0 + c] = col[i];
     }
   }
   __syncthreads();
+  for (int bi = 1; bi < kTile / kPanel; ++bi) {
+    for (int e = tid; e < bi * kPanel * kPanel; e += kPotrfThreads) {
+      const int j = e / (kPanel * kPanel), r = (e / kPanel) % kPanel, c = e % kPanel;
+      float v = 0.f;
+      for (int kk = j; kk < bi; ++kk)
+#pragma unroll 8
+        for (int m = 0; m < kPanel; ++m)
+          v += a[(kPanel * bi + r) * kLdS + kPanel * kk + m] * x[(kPanel * kk + m) * kLdS + kPanel * j + c];
+      tmp[e] = v;
+    }
+    __syncthreads();
+    for (int e = tid; e < bi * kPanel * kPanel; e += kPotrfThreads) {
+      const int j = e / (kPanel * kPanel), r = (e / kPanel) % kPanel, c = e % kPanel;
+      float v = 0.f;
+      for (int m = 0; m <= r; ++m)
+        v += x[(kPanel * bi + r) * kLdS + kPanel * bi + m] * tmp[j * kPanel * kPanel + m * kPanel + c];
+      x[(kPanel * bi + r) * kLdS + kPanel * j + c] = -v;
+    }
+    __syncthreads();
+  }
   float* dk = dinv + int64_t(k) * kTile * kTile;
   for (int t = tid; t < kTile * kTile; t += kPotrfThreads) {
     const int i = t >> 7, j = t & (kTile - 1);
@@ -371,66 +477,81 @@ __device__ __forceinline__ double warp_sum_d(double v) {
 }
 
 // ---------------------------------------------------------------------------
-// Triangular solves with the tiled factor (one CTA): v = (L L^T)^-1 rhs, then
-// z = D v.  Forward: y_k = Dinv_k (rhs_k - sum_{j<k} L_kj y_j); backward:
-// x_k = Dinv_k^T (y_k - sum_{j>k} L_jk^T x_j).
-constexpr int kTrsvThreads = 1024;
+// Triangular solves with the tiled factor, one launch per tile step with one
+// CTA per tile it touches.  Forward, step k: y_k = Dinv_k b_k (CTA 0 stores
+// it) and b_i -= L_ik y_k for i > k (CTA i - k).  Backward, step k: x_k =
+// Dinv_k^T y_k (CTA k stores it) and y_i -= L_ki^T x_k for i < k (CTA i).
+// Each CTA recomputes the 128-long diagonal product instead of waiting for
+// another CTA.
+constexpr int kTsThreads = 256;
 
-__global__ void __launch_bounds__(kTrsvThreads) trsv_kernel(const float* __restrict__ L, int ld,
-                                                            const float* __restrict__ dinv, int nt, int n,
-                                                            const float* __restrict__ rhs,
-                                                            const double* __restrict__ d, double* __restrict__ z) {
-  extern __shared__ float v[];  // nt * 128
-  __shared__ float t[kTile];
-  __shared__ float part[kTrsvThreads / kTile][kTile];
+__global__ void ts_init_kernel(int n, int n_pad, const float* __restrict__ rs, float* __restrict__ b) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n_pad) b[i] = i < n ? rs[i] : 0.f;
+}
+
+__global__ void __launch_bounds__(kTsThreads) fwd_step_kernel(const float* __restrict__ L, int ld,
+                                                              const float* __restrict__ dinv, int k,
+                                                              float* __restrict__ b, float* __restrict__ y) {
+  __shared__ __align__(16) float bk[kTile];
+  __shared__ __align__(16) float yk[kTile];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int np = nt * kTile;
-  for (int i = tid; i < np; i += kTrsvThreads) v[i] = i < n ? rhs[i] : 0.f;
+  if (tid < kTile) bk[tid] = b[k * kTile + tid];
   __syncthreads();
-  for (int k = 0; k < nt; ++k) {
-    for (int r = warp; r < kTile; r += kTrsvThreads / 32) {
-      const float* row = L + int64_t(k * kTile + r) * ld;
-      float s = 0.f;
-      for (int j = lane; j < k * kTile; j += 32) s += row[j] * v[j];
-      s = warp_sum_f(s);
-      if (lane == 0) t[r] = v[k * kTile + r] - s;
-    }
-    __syncthreads();
-    const float* dk = dinv + int64_t(k) * kTile * kTile;
-    for (int r = warp; r < kTile; r += kTrsvThreads / 32) {
-      float s = 0.f;
-      for (int j = lane; j <= r; j += 32) s += dk[r * kTile + j] * t[j];
-      s = warp_sum_f(s);
-      if (lane == 0) v[k * kTile + r] = s;
-    }
-    __syncthreads();
+  const float4 bv = reinterpret_cast<const float4*>(bk)[lane];
+  const float* D = dinv + int64_t(k) * kTile * kTile;
+  for (int r = warp; r < kTile; r += kTsThreads / 32) {
+    const float4 dv = reinterpret_cast<const float4*>(D + r * kTile)[lane];
+    const float s = warp_sum_f(dv.x * bv.x + dv.y * bv.y + dv.z * bv.z + dv.w * bv.w);
+    if (lane == 0) yk[r] = s;
   }
-  const int c = tid & (kTile - 1), g = tid >> 7;
-  constexpr int G = kTrsvThreads / kTile;
-  for (int k = nt - 1; k >= 0; --k) {
-    float s = 0.f;
-    for (int j = (k + 1) * kTile + g; j < np; j += G) s += L[int64_t(j) * ld + k * kTile + c] * v[j];
-    part[g][c] = s;
-    __syncthreads();
-    if (tid < kTile) {
-      float acc = 0.f;
-      for (int q = 0; q < G; ++q) acc += part[q][tid];
-      t[tid] = v[k * kTile + tid] - acc;
-    }
-    __syncthreads();
-    const float* dk = dinv + int64_t(k) * kTile * kTile;
-    float s2 = 0.f;
-    for (int r = g; r < kTile; r += G) s2 += dk[r * kTile + c] * t[r];  // zero above the diagonal
-    part[g][c] = s2;
-    __syncthreads();
-    if (tid < kTile) {
-      float acc = 0.f;
-      for (int q = 0; q < G; ++q) acc += part[q][tid];
-      v[k * kTile + tid] = acc;
-    }
-    __syncthreads();
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    if (tid < kTile) y[k * kTile + tid] = yk[tid];
+    return;
   }
-  for (int i = tid; i < n; i += kTrsvThreads) z[i] = d[i] * double(v[i]);
+  const int i = k + int(blockIdx.x);
+  const float4 yv = reinterpret_cast<const float4*>(yk)[lane];
+  for (int r = warp; r < kTile; r += kTsThreads / 32) {
+    const float4 lv = reinterpret_cast<const float4*>(L + int64_t(i * kTile + r) * ld + k * kTile)[lane];
+    const float s = warp_sum_f(lv.x * yv.x + lv.y * yv.y + lv.z * yv.z + lv.w * yv.w);
+    if (lane == 0) b[i * kTile + r] -= s;
+  }
+}
+
+__global__ void __launch_bounds__(kTsThreads) bwd_step_kernel(const float* __restrict__ L, int ld,
+                                                              const float* __restrict__ dinv, int k,
+                                                              float* __restrict__ y, float* __restrict__ xv) {
+  __shared__ float tk[kTile], xk[kTile], part[2][kTile];
+  const int tid = threadIdx.x, c = tid & (kTile - 1), h = tid >> 7;
+  if (tid < kTile) tk[tid] = y[k * kTile + tid];
+  __syncthreads();
+  const float* D = dinv + int64_t(k) * kTile * kTile;
+  float s = 0.f;
+#pragma unroll 8
+  for (int r = h * 64; r < h * 64 + 64; ++r) s += D[r * kTile + c] * tk[r];
+  part[h][c] = s;
+  __syncthreads();
+  if (tid < kTile) xk[tid] = part[0][tid] + part[1][tid];
+  __syncthreads();
+  const int i = int(blockIdx.x);
+  if (i == k) {
+    if (tid < kTile) xv[k * kTile + tid] = xk[tid];
+    return;
+  }
+  float s2 = 0.f;
+#pragma unroll 8
+  for (int r = h * 64; r < h * 64 + 64; ++r) s2 += L[int64_t(k * kTile + r) * ld + i * kTile + c] * xk[r];
+  part[h][c] = s2;
+  __syncthreads();
+  if (tid < kTile) y[i * kTile + tid] -= part[0][tid] + part[1][tid];
+}
+
+// z = D x (back to the unscaled unknowns, FP64)
+__global__ void ts_finish_kernel(int n, const double* __restrict__ d, const float* __restrict__ xv,
+                                 double* __restrict__ z) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) z[i] = d[i] * double(xv[i]);
 }
 
 // Flexible preconditioned conjugate gradients in FP64.  Scalars live on the
@@ -544,13 +665,21 @@ void set_smem(const void* f, int bytes) {
   GB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
 
-void launch_gemm(const GemmArgs& g, int tiles_m, int tiles_n) {
+void launch_gemm(const GemmArgs& g, int tiles_m, int tiles_n, int splits = 1) {
   static bool configured = false;
   if (!configured) {
     set_smem(reinterpret_cast<const void*>(tc_gemm_nt_kernel), kGemmSmem);
     configured = true;
   }
-  tc_gemm_nt_kernel<<<dim3(tiles_m, tiles_n), kGemmThreads, kGemmSmem>>>(g);
+  tc_gemm_nt_kernel<<<dim3(tiles_m, tiles_n, splits), kGemmThreads, kGemmSmem>>>(g);
+}
+
+// Splits K so that a launch fills about one wave of CTAs (152 SMs), with at
+// least four stages of 32 per CTA.
+int k_splits(int tiles, int k) {
+  const int by_sms = (152 + tiles - 1) / tiles;
+  const int by_k = std::max(1, k / (4 * kKb));
+  return std::max(1, std::min(by_sms, by_k));
 }
 
 double seconds_now() {
@@ -564,7 +693,7 @@ void tc_gemm_nt(const float* A, int lda, const float* B, int ldb, float* C, int 
                 int* status) {
   if (m % kTile || n % kTile || k % kKb || k <= 0 || lda % 4 || ldb % 4 || ldc % 4)
     throw std::invalid_argument("tc_gemm_nt: m, n must be multiples of 128, k a positive multiple of 32");
-  GemmArgs g{A, lda, B, ldb, C, ldc, nullptr, k, status};
+  GemmArgs g{A, lda, B, ldb, C, ldc, nullptr, k, k, 0, status};
   launch_gemm(g, m / kTile, n / kTile);
   GB_CUDA(cudaGetLastError());
 }
@@ -580,13 +709,13 @@ int DenseSpdSolver::factor(double* A, int n, int lda) {
   static bool configured = false;
   if (!configured) {
     set_smem(reinterpret_cast<const void*>(potrf_tile_kernel), kPotrfSmem);
-    set_smem(reinterpret_cast<const void*>(trsv_kernel), 64 * 1024);
     configured = true;
   }
-  if (n_pad_ > 64 * 1024 / 4) throw std::invalid_argument("dense solver: system larger than 16384 unknowns");
+  if (n_pad_ > 32768) throw std::invalid_argument("dense solver: system larger than 32768 unknowns");
   L_.resize(size_t(n_pad_) * n_pad_);
   dinv_.resize(size_t(nt_) * kTile * kTile);
   rs_.resize(n_pad_);
+  ts_.resize(3 * size_t(n_pad_));
   dscale_.resize(n_pad_);
   r_.resize(4 * size_t(n_pad_));  // r, p, q and the second preconditioned residual
   z_.resize(n_pad_);
@@ -608,15 +737,18 @@ int DenseSpdSolver::factor(double* A, int n, int lda) {
     for (int k = 0; k < nt_; ++k) {
       float* rowk = L + int64_t(k) * kTile * ld;
       if (k > 0) {
-        GemmArgs g{rowk, ld, rowk, ld, rowk + int64_t(k) * kTile, ld, rowk + int64_t(k) * kTile, k * kTile,
-                   status_.get() + 2};
-        launch_gemm(g, nt_ - k, 1);
+        // A_ik -= L_i,0:k L_k,0:k^T, K split across CTAs (atomic subtraction)
+        const int K = k * kTile;
+        const int splits = k_splits(nt_ - k, K);
+        const int chunk = (K / kKb + splits - 1) / splits * kKb;
+        GemmArgs g{rowk, ld, rowk, ld, rowk + int64_t(k) * kTile, ld, nullptr, K, chunk, 1, status_.get() + 2};
+        launch_gemm(g, nt_ - k, 1, (K + chunk - 1) / chunk);
       }
       potrf_tile_kernel<<<1, kPotrfThreads, kPotrfSmem>>>(L, ld, k, dinv_.get(), status_.get());
       if (k + 1 < nt_) {
         float* below = L + int64_t(k + 1) * kTile * ld + int64_t(k) * kTile;
-        GemmArgs g{below, ld, dinv_.get() + int64_t(k) * kTile * kTile, kTile, below, ld, nullptr, kTile,
-                   status_.get() + 2};
+        GemmArgs g{below, ld, dinv_.get() + int64_t(k) * kTile * kTile, kTile, below, ld, nullptr, kTile, kTile,
+                   0, status_.get() + 2};
         launch_gemm(g, nt_ - k - 1, 1);
       }
     }
@@ -646,11 +778,21 @@ int DenseSpdSolver::solve(const double* b, double* x, double tol, int max_iterat
   double* z_new = q + n_pad_;
   double* z_old = z_.get();
   double* scal = scal_.get();
-  const size_t trsv_smem = size_t(n_pad_) * sizeof(float);
+  float* tb = ts_.get();
+  float* ty = tb + n_pad_;
+  float* tx = ty + n_pad_;
+  // z = D (L L^T)^-1 rs, rs = fp32(D r)
+  auto precondition = [&](double* z) {
+    ts_init_kernel<<<(n_pad_ + 255) / 256, 256>>>(n, n_pad_, rs_.get(), tb);
+    for (int k = 0; k < nt_; ++k)
+      fwd_step_kernel<<<nt_ - k, kTsThreads>>>(L_.get(), n_pad_, dinv_.get(), k, tb, ty);
+    for (int k = nt_ - 1; k >= 0; --k)
+      bwd_step_kernel<<<k + 1, kTsThreads>>>(L_.get(), n_pad_, dinv_.get(), k, ty, tx);
+    ts_finish_kernel<<<eg, 256>>>(n, dscale_.get(), tx, z);
+  };
   scal_.zero();
   cg_init_kernel<<<eg, 256>>>(n, b, dscale_.get(), x, r, rs_.get(), scal);
-  trsv_kernel<<<1, kTrsvThreads, trsv_smem>>>(L_.get(), n_pad_, dinv_.get(), nt_, n, rs_.get(), dscale_.get(),
-                                              z_old);
+  precondition(z_old);
   cg_dots_kernel<<<eg, 256>>>(n, r, z_old, nullptr, scal);
   cg_dir_kernel<<<eg, 256>>>(n, z_old, p, scal, 1);
   cg_rotate_kernel<<<1, 1>>>(scal);
@@ -679,8 +821,7 @@ int DenseSpdSolver::solve(const double* b, double* x, double tol, int max_iterat
       out.status = 0;
       break;
     }
-    trsv_kernel<<<1, kTrsvThreads, trsv_smem>>>(L_.get(), n_pad_, dinv_.get(), nt_, n, rs_.get(),
-                                                dscale_.get(), z_new);
+    precondition(z_new);
     cg_dots_kernel<<<eg, 256>>>(n, r, z_new, z_old, scal);
     cg_dir_kernel<<<eg, 256>>>(n, z_new, p, scal, 0);
     cg_rotate_kernel<<<1, 1>>>(scal);

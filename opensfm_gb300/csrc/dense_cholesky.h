@@ -41,7 +41,7 @@ class DenseSpdSolver {
   int n_ = 0, nt_ = 0, n_pad_ = 0, lda_ = 0;
   double shift_ = 0.0;
   double* A_ = nullptr;
-  DeviceArray<float> L_, dinv_, rs_;
+  DeviceArray<float> L_, dinv_, rs_, ts_;
   DeviceArray<double> dscale_, r_, z_, scal_;
   DeviceArray<int> status_;
 };

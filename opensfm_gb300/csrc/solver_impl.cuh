@@ -732,6 +732,7 @@ class DeviceSolver : public SolverBase {
   DeviceArray<double> d_pp_w_, d_pp_res_;
   DeviceArray<int> d_dmap_, d_didx_;
   DeviceArray<int2> d_pairs_;
+  DeviceArray<int> d_pair_key_;
   DeviceArray<double> d_S_, d_WT_, d_bd_, d_xd_;
   DeviceArray<double> d_V64_, d_Vinv64_, d_gp64_;  // FP64 point blocks of the dense path
 };
@@ -898,23 +899,48 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     dense_ = exact && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
     if (dense_) {
       // pairs (o1 >= o2) of the observations of every point, as point-major
-      // slot indices
-      std::vector<int2> pairs;
-      int64_t s0 = 0;
-      while (s0 < n_obs_) {
-        const int p = P.observations[order[s0]].point;
-        int64_t s1 = s0 + 1;
-        while (s1 < n_obs_ && P.observations[order[s1]].point == p) ++s1;
-        for (int64_t a = s0; a < s1; ++a)
-          for (int64_t b = s0; b <= a; ++b) pairs.push_back(make_int2(int(a), int(b)));
-        s0 = s1;
+      // slot indices, sorted (stable counting sort) by the block of S they
+      // add to: key = (shot(o1) * n_shots + shot(o2)) * 2 + (o1 == o2)
+      const int64_t n_keys = int64_t(n_shots_) * n_shots_ * 2;
+      if (n_keys > int64_t(std::numeric_limits<int>::max()))
+        throw std::invalid_argument("dense mode: too many shots");
+      std::vector<int2> raw_pairs;
+      std::vector<int> raw_keys;
+      {
+        int64_t s0 = 0;
+        while (s0 < n_obs_) {
+          const int p = P.observations[order[s0]].point;
+          int64_t s1 = s0 + 1;
+          while (s1 < n_obs_ && P.observations[order[s1]].point == p) ++s1;
+          for (int64_t a = s0; a < s1; ++a) {
+            const int64_t sa = P.observations[order[a]].shot;
+            for (int64_t b = s0; b <= a; ++b) {
+              const int64_t sb = P.observations[order[b]].shot;
+              raw_pairs.push_back(make_int2(int(a), int(b)));
+              raw_keys.push_back(int((sa * n_shots_ + sb) * 2 + (a == b ? 1 : 0)));
+            }
+          }
+          s0 = s1;
+        }
       }
-      n_pairs_ = int64_t(pairs.size());
+      n_pairs_ = int64_t(raw_pairs.size());
+      std::vector<int64_t> kstart(static_cast<size_t>(n_keys) + 1, 0);
+      for (int k : raw_keys) ++kstart[size_t(k) + 1];
+      for (int64_t k = 0; k < n_keys; ++k) kstart[k + 1] += kstart[k];
+      std::vector<int2> sorted_pairs(static_cast<size_t>(n_pairs_));
+      std::vector<int> pair_key(static_cast<size_t>(n_pairs_));
+      for (size_t q = 0; q < raw_keys.size(); ++q) {
+        const int k = raw_keys[q];
+        const size_t dst = size_t(kstart[size_t(k)]++);
+        sorted_pairs.data()[dst] = raw_pairs.data()[q];
+        pair_key.data()[dst] = k;
+      }
+      d_pair_key_.upload(pair_key);
       const int W = 6 + kc_.cmax + (kc_.rig ? 6 : 0);
       d_dmap_.upload(dmap);
-      d_pairs_.upload(pairs);
+      d_pairs_.upload(sorted_pairs);
       d_didx_.resize(size_t(n_slots_) * W);
-      d_WT_.resize(size_t(n_slots_) * 6 * W);
+      d_WT_.resize(size_t(n_slots_) * 9 * W);  // dense_record<W>()
       d_S_.resize(size_t(n_dense_) * n_dense_);
       d_bd_.resize(n_dense_);
       d_xd_.resize(n_dense_);
