@@ -208,6 +208,20 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
             "pcg_iterations": int(tr[:, 4].sum()),
         }
     out["target_cost"] = target
+    # the same mixed solve with matrix-free passes (no stored Jacobian
+    # records: what a problem too large for the records would run)
+    ba = adjuster_from_scene(scene, precision="mixed", loss=loss, irls="none", max_iterations=max_iterations,
+                             pcg_tolerance=pcg_tolerance, gps=True, matrix_free=1)
+    ba.run()
+    s, tr = ba.summary(), ba.trace()
+    del ba
+    hit = np.nonzero(tr[:, 1] <= target)[0]
+    out["mixed_matrix_free"] = {
+        "time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None, "final_cost": s["final_cost"],
+        "iterations": s["iterations"], "solve_s": s["seconds"], "linear_solver_s": s["linear_solver_seconds"],
+        "pcg_iterations": int(tr[:, 4].sum()),
+        "pcg_iteration_ms": 1e3 * s["linear_solver_seconds"] / max(1, int(tr[:, 4].sum())),
+        "stored_pcg_iteration_ms": 1e3 * out["mixed"]["linear_solver_s"] / max(1, out["mixed"]["pcg_iterations"])}
     out["mixed_final_rel_to_fp64"] = abs(runs["mixed"]["summary"]["final_cost"] - c64) / c64
     tm, tf = out["mixed"]["time_to_target_s"], out["fp64"]["time_to_target_s"]
     out["speedup_mixed_vs_fp64"] = (tf / tm) if (tm and tf) else None

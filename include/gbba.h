@@ -289,6 +289,13 @@ int gbba_set_group_density_ratio(gbba_adjuster_t* h, const char* group, double r
 double gbba_get_group_density_ratio(const gbba_adjuster_t* h, const char* group);
 /* Relative residual at which the reduced-camera-system PCG stops. */
 int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance);
+/* Jacobian storage of the iterative solver.  0 (default): the residual +
+ * Jacobian records of a linearization are stored (two copies, about 224 B
+ * per observation for a perspective camera in mixed precision) when they
+ * fit in device memory, and otherwise evaluated again in every pass
+ * (matrix-free); 1: always matrix-free; -1: always stored.  The exact dense
+ * path always stores them. */
+int gbba_set_matrix_free(gbba_adjuster_t* h, int mode);
 
 /* BundleAdjuster::Run (bundle_adjuster.cc:670-1203). */
 int gbba_run(gbba_adjuster_t* h);

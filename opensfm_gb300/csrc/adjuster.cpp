@@ -415,6 +415,8 @@ std::string BundleAdjuster::FullReport() const {
      << summary_.setup_seconds << "\n";
   ss << "  Kernel launches      " << summary_.kernel_launches << "\n";
   ss << "  PCG refinements      " << summary_.pcg_refinements << " (FP64 residuals of the mixed-precision solve)\n";
+  ss << "  Jacobians            " << (summary_.matrix_free ? "matrix-free (evaluated in every pass)" : "stored")
+     << "\n";
   ss << "  Termination          " << summary_.termination << "\n";
   return ss.str();
 }

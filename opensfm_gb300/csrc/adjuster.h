@@ -58,6 +58,7 @@ class BundleAdjuster {
   void SetGroupDensityRatio(const std::string& g, double r) { group_ratio_[g] = r; }
   double GetGroupDensityRatio(const std::string& g) const;
   void SetPcgTolerance(double t) { opts_.pcg_tolerance = t; }
+  void SetMatrixFree(int mode) { opts_.matrix_free = mode; }
 
   void Run();
 

@@ -261,6 +261,13 @@ double gbba_get_group_density_ratio(const gbba_adjuster_t* h, const char* group)
   return v;
 }
 
+int gbba_set_matrix_free(gbba_adjuster_t* h, int mode) {
+  return guarded([&] {
+    if (mode < -1 || mode > 1) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "matrix-free mode must be -1, 0 or 1");
+    ba_of(h).SetMatrixFree(mode);
+  });
+}
+
 int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance) {
   return guarded([&] {
     if (!(tolerance > 0.0)) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "tolerance must be positive");

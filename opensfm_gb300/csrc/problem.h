@@ -88,6 +88,9 @@ struct SolverOptions {
   int precision = 1;          // 0 FP64, 1 mixed
   std::string linear_solver = "SPARSE_SCHUR";
   int dense_max_unknowns = 4096;  // dense reduced-camera Cholesky below this
+  // Jacobian records: 0 stored when they fit in device memory (else
+  // matrix-free), 1 always matrix-free, -1 always stored
+  int matrix_free = 0;
   double pcg_tolerance = 1e-3;    // relative residual of the reduced system
   int pcg_max_iterations = 500;
   bool compute_reprojection_errors = true;
@@ -137,6 +140,7 @@ struct SolveSummary {
   double setup_seconds = 0;  // slot sorts, uploads, device buffers
   int64_t kernel_launches = 0;
   int64_t pcg_refinements = 0;  // FP64 residual evaluations (mixed-precision iterative refinement)
+  bool matrix_free = false;      // the record passes evaluated the Jacobians instead of reading them
   std::string linear_solver;
   std::vector<IterationRecord> trace;
   std::vector<std::string> irls_lines;

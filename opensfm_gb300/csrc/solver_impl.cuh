@@ -17,12 +17,13 @@
 #include "solver.h"
 #include "solver_kernels.cuh"
 #include "solver_shot_major.cuh"
+#include "kernel_config.cuh"
+#include "record_passes.cuh"
 
 namespace gbba {
 
 namespace {
 
-constexpr int kDyn = -1;
 constexpr double kEps = 2.220446049250313e-16;
 // Iterative refinement of the mixed-precision linear solve: used when the
 // requested PCG tolerance is tighter than kRefineThreshold; every FP32 PCG
@@ -38,41 +39,9 @@ constexpr double kConfirmTolerance = 1e-6;
 constexpr double kDenseTolerance = 1e-12;
 constexpr int kDenseMaxRefinements = 50;
 
-struct KernelConfig {
-  int model;  // single model or kDyn
-  int nr;
-  int cmax;
-  bool rig;
-};
-
 template <int C>
 constexpr int tri_pad() {
   return TriSize<C>::kPad;
-}
-
-// Calls f.template run<M, NR, CMAX, RIG>() for a kernel configuration.
-template <typename F>
-void dispatch_config(const KernelConfig& k, F& f) {
-  if (k.model != kDyn) {
-    switch (k.model) {
-      case kPerspective: f.template run<kPerspective, 2, 3, false>(); return;
-      case kBrown: f.template run<kBrown, 2, 9, false>(); return;
-      case kFisheye: f.template run<kFisheye, 2, 3, false>(); return;
-      case kFisheyeOpencv: f.template run<kFisheyeOpencv, 2, 8, false>(); return;
-      case kFisheye62: f.template run<kFisheye62, 2, 12, false>(); return;
-      case kFisheye624: f.template run<kFisheye624, 2, 16, false>(); return;
-      case kDual: f.template run<kDual, 2, 4, false>(); return;
-      case kRadial: f.template run<kRadial, 2, 6, false>(); return;
-      case kSimpleRadial: f.template run<kSimpleRadial, 2, 5, false>(); return;
-    }
-  }
-  if (k.nr == 2) {
-    if (k.rig) f.template run<kDyn, 2, 16, true>();
-    else f.template run<kDyn, 2, 16, false>();
-  } else {
-    if (k.rig) f.template run<kDyn, 3, 16, true>();
-    else f.template run<kDyn, 3, 16, false>();
-  }
 }
 
 int slot_grid(int64_t n) {
@@ -80,6 +49,26 @@ int slot_grid(int64_t n) {
   return int(std::max<int64_t>(1, std::min<int64_t>(want, 152 * 8)));
 }
 int elem_grid(int64_t n, int block = 256) { return int(std::max<int64_t>(1, (n + block - 1) / block)); }
+
+// One of the record-reading passes (RecordPassArgs::Which) of the solver,
+// launched with stored records by dispatch_config(kc, f), or matrix-free by
+// launch_evaluated(kc, f) (DeviceSolver::record_pass picks).
+template <typename R>
+struct RecordPassLaunch : RecordPassArgs<R> {
+  using Args = RecordPassArgs<R>;
+  RecordPassLaunch(typename Args::Which w, const SolveView<R>& view, const ShotMajorView<R>& shot_major = {}) {
+    this->which = w;
+    this->v = view;
+    this->sm = shot_major;
+    this->grid = slot_grid(view.scene.n_slots);
+  }
+  template <int M, int NR, int CMAX, bool RIG>
+  void run() {
+    using L = RecordLayout<NR, CMAX, RIG>;
+    this->template launch<M, NR, CMAX, RIG>(
+        StoredRecords<R, planes_of<R>(L::kWidth)>{this->v.rec, this->sm.rec, this->v.stride});
+  }
+};
 
 // ---------------------------------------------------------------------------
 // Slot construction from the uploaded observations (point-major order given
@@ -646,6 +635,11 @@ class DeviceSolver : public SolverBase {
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
   int run_pcg(const R* rhs, double bb, double tol, int max_it);
   int solve_dense(double mu);
+  // launches a record pass with stored or evaluated records
+  void record_pass(RecordPassLaunch<R>& f) {
+    if (matrix_free_) launch_evaluated<R>(kc_, f);
+    else dispatch_config(kc_, f);
+  }
   // ---- IRLS
   double compute_weights(std::vector<std::string>& groups_report, int& proj_out, int& proj_total,
                          std::vector<std::pair<std::string, std::pair<int, int>>>& other);
@@ -678,6 +672,8 @@ class DeviceSolver : public SolverBase {
   double pcg_tolerance_override_ = 0.0;  // > 0: PCG tolerance of the next steps
   // dense mode: explicit reduced camera system over the n_dense_ optimised
   // camera-side coordinates, factored by DenseSpdSolver
+  // matrix-free: no stored records; every record pass evaluates them again
+  bool matrix_free_ = false;
   bool dense_ = false;
   int n_dense_ = 0;
   int64_t n_pairs_ = 0;
@@ -878,10 +874,6 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     d_resid_cand_.resize(4 * n_slots_);
     d_resid_cand_.zero();
   }
-  d_rec_.resize(size_t(n_planes_) * n_slots_);
-  d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
-  d_rec_sm_.resize(size_t(n_planes_) * n_slots_);
-  d_rec_sm_.zero();
 
   // Dense mode: the reduced camera system is formed explicitly and factored
   // when the linear solver type asks for an exact solve (Ceres' DENSE_*,
@@ -949,6 +941,29 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
       d_V64_.resize(8 * np1);
       d_Vinv64_.resize(8 * np1);
       d_gp64_.resize(4 * np1);
+    }
+  }
+
+  // Records: stored (two copies, point-major and shot-major) unless they
+  // would take more than 60% of the free device memory, or the caller asks
+  // for matrix-free passes.  The dense path reads stored records (its
+  // systems are small) and keeps them.
+  {
+    const size_t record_bytes = 2 * size_t(n_planes_) * size_t(n_slots_) * sizeof(V16);
+    size_t free_bytes = 0, total_bytes = 0;
+    GB_CUDA(cudaMemGetInfo(&free_bytes, &total_bytes));
+    if (opts.matrix_free > 0) matrix_free_ = true;
+    else if (opts.matrix_free < 0) matrix_free_ = false;
+    else matrix_free_ = double(record_bytes) > 0.6 * double(free_bytes);
+    if (dense_) matrix_free_ = false;
+    if (!matrix_free_) {
+      d_rec_.resize(size_t(n_planes_) * n_slots_);
+      d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
+      d_rec_sm_.resize(size_t(n_planes_) * n_slots_);
+      d_rec_sm_.zero();
+    } else {
+      d_rec_.release();
+      d_rec_sm_.release();
     }
   }
 
@@ -1229,13 +1244,10 @@ double DeviceSolver<R>::cost_pass(bool candidate, bool store_residuals) {
 template <typename R>
 struct LinearizeLaunch {
   SolveView<R> v;
-  ShotMajorView<R> sm;
   uint64_t mask;
   template <int M, int NR, int CMAX, bool RIG>
   void run() {
-    const int g = slot_grid(v.scene.n_slots);
-    linearize_kernel<R, M, NR, CMAX, RIG><<<g, 256>>>(v, mask);
-    permute_records_kernel<R, NR, CMAX, RIG><<<g, 256>>>(v, sm, mask);
+    linearize_kernel<R, M, NR, CMAX, RIG><<<slot_grid(v.scene.n_slots), 256>>>(v, mask);
   }
 };
 
@@ -1245,8 +1257,13 @@ void DeviceSolver<R>::linearize() {
   d_gp_.zero();
   d_gc_.zero();
   d_dc_.zero();
-  LinearizeLaunch<R> f{view(), sm_view(), plane_mask_};
+  LinearizeLaunch<R> f{view(), matrix_free_ ? uint64_t(0) : plane_mask_};
   dispatch_config(kc_, f);
+  // the camera-side gradient and column norms, summed in shot-major order
+  // (and, with stored records, the shot-major copy of the records)
+  RecordPassLaunch<R> p{RecordPassLaunch<R>::kPermute, view(), sm_view()};
+  p.plane_mask = matrix_free_ ? uint64_t(0) : plane_mask_;
+  record_pass(p);
   launches_ += 2;
   if (!point_priors_.empty()) {
     point_prior_linearize_kernel<R><<<elem_grid(int64_t(point_priors_.size())), 256>>>(

@@ -495,8 +495,8 @@ struct PrecondView {
 // A is the arithmetic of the product: the working precision R for the PCG
 // iterations, FP64 (on the same records) for the residual of iterative
 // refinement.
-template <typename R, typename A, int NR, int CMAX, bool RIG>
-__global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, const A* __restrict__ x,
+template <typename R, typename A, int NR, int CMAX, bool RIG, typename Src>
+__global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, Src recs, const A* __restrict__ x,
                                                                A* __restrict__ zbuf) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, c
     A u[3] = {A(0), A(0), A(0)};
     if (valid) {
       R rec_r[NP * VN];
-      load_record<R, NP>(v.rec, v.stride, i, rec_r);
+      recs.point_major(v, i, rec_r);
       A rec[NP * VN];
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
@@ -571,8 +571,8 @@ __device__ __forceinline__ void block_sum_add(double v, double* out) {
 }
 
 // Linear-model decrease  sum_o 0.5 (|f_o|^2 - |f_o + J_o delta|^2)  (FP64).
-template <typename R, int NR, int CMAX, bool RIG>
-__global__ void __launch_bounds__(256) model_change_kernel(SolveView<R> v, const R* __restrict__ dc_step,
+template <typename R, int NR, int CMAX, bool RIG, typename Src>
+__global__ void __launch_bounds__(256) model_change_kernel(SolveView<R> v, Src recs, const R* __restrict__ dc_step,
                                                            const R* __restrict__ dp, double* __restrict__ out) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(256) model_change_kernel(SolveView<R> v, const
     const int pt = s.obs_point[i];
     if (pt < 0) continue;
     R rec[NP * VN];
-    load_record<R, NP>(v.rec, v.stride, i, rec);
+    recs.point_major(v, i, rec);
     int inst, cam, rig;
     shot_indices(s, shot_of(s, i), inst, cam, rig);
     CamGather<R, CMAX> g;

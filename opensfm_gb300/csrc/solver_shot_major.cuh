@@ -155,9 +155,9 @@ struct CarryStage {
 // ---------------------------------------------------------------------------
 // Copies the point-major records into shot-major order and accumulates the
 // camera-side gradient J_c^T r and squared column norms of the linearization.
-template <typename R, int NR, int CMAX, bool RIG>
+template <typename R, int NR, int CMAX, bool RIG, typename Src>
 __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveView<R> v, ShotMajorView<R> sm,
-                                                                          uint64_t plane_mask) {
+                                                                          Src recs, uint64_t plane_mask) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
   constexpr int VN = Vec16<R>::kN;
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
     const bool valid = src >= 0;
     R rec[NP * VN];
     if (valid) {
-      load_record<R, NP>(v.rec, v.stride, src, rec);
+      recs.point_major(v, src, rec);
     } else {
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = R(0);
@@ -272,9 +272,9 @@ __global__ void __launch_bounds__(kShotMajorBlock) permute_records_kernel(SolveV
 
 // ---------------------------------------------------------------------------
 // Right-hand side sum_o J_c^T J_p V^-1 g_p and Schur-Jacobi blocks, shot-major.
-template <typename R, int NR, int CMAX, bool RIG>
+template <typename R, int NR, int CMAX, bool RIG, typename Src>
 __global__ void __launch_bounds__(kShotMajorBlock) schur_rhs_precond_sm_kernel(SolveView<R> v, ShotMajorView<R> sm,
-                                                                               double* __restrict__ rhs,
+                                                                               Src recs, double* __restrict__ rhs,
                                                                                PrecondView<R> pc) {
   using L = RecordLayout<NR, CMAX, RIG>;
   constexpr int NP = planes_of<R>(L::kWidth);
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_rhs_precond_sm_kernel(S
 #pragma unroll
     for (int q = 0; q < NR; ++q) e[q] = R(0);
     if (valid) {
-      load_record<R, NP>(sm.rec, v.stride, j, rec);
+      recs.shot_major(v, j, sm.src[j], rec);
       shot_indices(s, sm.shot[j], inst, cam, rig);
 #pragma unroll
       for (int k = 0; k < 6; ++k) Vi[k] = v.Vinv[8 * int64_t(pt) + k];
@@ -391,9 +391,9 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_rhs_precond_sm_kernel(S
 // Implicit Schur product, camera half, shot-major:
 //   y_c += J_c^T (J_c x_c - J_p V^-1 zbuf_p).
 // A is the arithmetic of the product (see schur_point_pass_kernel).
-template <typename R, typename A, int NR, int CMAX, bool RIG>
+template <typename R, typename A, int NR, int CMAX, bool RIG, typename Src>
 __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(SolveView<R> v, ShotMajorView<R> sm,
-                                                                               const A* __restrict__ x,
+                                                                               Src recs, const A* __restrict__ x,
                                                                                const A* __restrict__ zbuf,
                                                                                A* __restrict__ y) {
   using L = RecordLayout<NR, CMAX, RIG>;
@@ -417,7 +417,7 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
     int inst = 0, cam = 0, rig = -1;
     if (valid) {
       R rec_r[NP * VN];
-      load_record<R, NP>(sm.rec, v.stride, j, rec_r);
+      recs.shot_major(v, j, sm.src[j], rec_r);
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
       shot_indices(s, sm.shot[j], inst, cam, rig);

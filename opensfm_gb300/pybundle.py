@@ -75,6 +75,7 @@ def _declare(L) -> None:
         "gbba_set_group_density_ratio": ([_H, S, C.c_double], C.c_int),
         "gbba_get_group_density_ratio": ([_H, S], C.c_double),
         "gbba_set_pcg_tolerance": ([_H, C.c_double], C.c_int),
+        "gbba_set_matrix_free": ([_H, C.c_int], C.c_int),
         "gbba_run": ([_H], C.c_int),
         "gbba_get_camera": ([_H, S, C.POINTER(C.c_int), _D, C.c_int, C.POINTER(C.c_int)], C.c_int),
         "gbba_get_rig_instance_pose": ([_H, S, _D], C.c_int),
@@ -305,6 +306,11 @@ class BundleAdjuster:
     def set_pcg_tolerance(self, tolerance: float) -> None:
         self._check(self._L.gbba_set_pcg_tolerance(self._h, float(tolerance)))
 
+    def set_matrix_free(self, mode: int) -> None:
+        """0: store the Jacobian records when they fit in device memory (the
+        default), 1: evaluate them in every pass, -1: always store them."""
+        self._check(self._L.gbba_set_matrix_free(self._h, int(mode)))
+
     def set_max_num_iterations(self, n: int) -> None:
         self._check(self._L.gbba_set_max_num_iterations(self._h, int(n)))
 
@@ -473,10 +479,13 @@ class BundleBatch:
 
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
-                        pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None) -> BundleAdjuster:
+                        pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
+                        matrix_free: Optional[int] = None) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path)."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
+    if matrix_free is not None:
+        ba.set_matrix_free(matrix_free)
     if linear_solver is not None:
         ba.set_linear_solver_type(linear_solver)
     ba.set_irls_mode(irls)
