@@ -189,7 +189,10 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
         ba.run()
         wall = time.perf_counter() - t0
         s = ba.summary()
-        runs[precision] = {"trace": ba.trace(), "summary": s, "wall_s": wall}
+        # final poses [rx ry rz tx ty tz] and points, for the mixed-vs-FP64 errors
+        poses = np.array([ba.get_rig_instance_pose(str(i)).ba_data() for i in range(len(scene.rig_instance_poses))])
+        runs[precision] = {"trace": ba.trace(), "summary": s, "wall_s": wall, "points": ba.get_points(),
+                           "poses": poses}
         del ba
     c64 = runs["fp64"]["summary"]["final_cost"]
     target = c64 * (1.0 + 1e-6)
@@ -223,6 +226,15 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
         "pcg_iteration_ms": 1e3 * s["linear_solver_seconds"] / max(1, int(tr[:, 4].sum())),
         "stored_pcg_iteration_ms": 1e3 * out["mixed"]["linear_solver_s"] / max(1, out["mixed"]["pcg_iterations"])}
     out["mixed_final_rel_to_fp64"] = abs(runs["mixed"]["summary"]["final_cost"] - c64) / c64
+    # pose and point errors of the mixed solution against the FP64 one (the
+    # GPS priors fix the gauge, so the solutions are directly comparable)
+    dp = np.linalg.norm(runs["mixed"]["points"] - runs["fp64"]["points"], axis=1)
+    dc = np.linalg.norm(runs["mixed"]["poses"][:, 3:] - runs["fp64"]["poses"][:, 3:], axis=1)
+    dr = np.linalg.norm(runs["mixed"]["poses"][:, :3] - runs["fp64"]["poses"][:, :3], axis=1)
+    out["mixed_vs_fp64_solution"] = {
+        "point_rms_m": float(np.sqrt((dp ** 2).mean())), "point_max_m": float(dp.max()),
+        "centre_rms_m": float(np.sqrt((dc ** 2).mean())), "centre_max_m": float(dc.max()),
+        "rotation_rms_rad": float(np.sqrt((dr ** 2).mean())), "rotation_max_rad": float(dr.max())}
     tm, tf = out["mixed"]["time_to_target_s"], out["fp64"]["time_to_target_s"]
     out["speedup_mixed_vs_fp64"] = (tf / tm) if (tm and tf) else None
     return out
