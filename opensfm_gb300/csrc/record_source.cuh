@@ -22,6 +22,9 @@ namespace gbba {
 
 template <typename R, int NP>
 struct StoredRecords {
+  // every slot, padding included, has a record: the passes may load it
+  // before they know whether the slot is valid (one iteration ahead)
+  static constexpr bool kPrefetch = true;
   const typename Vec16<R>::type* pm;
   const typename Vec16<R>::type* sm;
   int64_t stride;
@@ -35,6 +38,7 @@ struct StoredRecords {
 
 template <typename R, int M, int NR, int CMAX, bool RIG>
 struct EvaluatedRecords {
+  static constexpr bool kPrefetch = false;  // padding slots cannot be evaluated
   __device__ __forceinline__ void point_major(const SolveView<R>& v, int64_t i, R* rec) const { eval(v, i, rec); }
   __device__ __forceinline__ void shot_major(const SolveView<R>& v, int64_t, int64_t src, R* rec) const {
     eval(v, src, rec);

@@ -503,19 +503,43 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, S
   constexpr int VN = Vec16<R>::kN;
   const SceneView<R>& s = v.scene;
   if (v.any_active && *v.any_active == 0) return;
-  GB_WARP_SLOT_LOOP(s.n_slots) {
+  const int lane = int(threadIdx.x & 31u);
+  const int64_t step = ((int64_t(gridDim.x) * blockDim.x) >> 5) * 32;
+  int64_t base = ((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * 32;
+  // Software pipeline: the point index, shot and (stored) record of the
+  // warp's next slot group are loaded while the current one is processed,
+  // so only the L2-resident gathers (shot geometry, x) stay on the
+  // iteration's critical path.
+  int pt_n = -1, sh_n = 0;
+  R rec_n[NP * VN];
+  if (base < s.n_slots) {
+    pt_n = s.obs_point[base + lane];
+    sh_n = s.obs[base + lane].shot;
+    if constexpr (Src::kPrefetch) recs.point_major(v, base + lane, rec_n);
+  }
+  for (; base < s.n_slots; base += step) {
     const int64_t i = base + lane;
-    const int pt = s.obs_point[i];
+    const int pt = pt_n;
+    const int sh = sh_n;
+    R rec_r[NP * VN];
+    if constexpr (Src::kPrefetch) {
+#pragma unroll
+      for (int k = 0; k < NP * VN; ++k) rec_r[k] = rec_n[k];
+    }
+    if (base + step < s.n_slots) {
+      pt_n = s.obs_point[base + step + lane];
+      sh_n = s.obs[base + step + lane].shot;
+      if constexpr (Src::kPrefetch) recs.point_major(v, base + step + lane, rec_n);
+    }
     const bool valid = pt >= 0 && slot_active(v, pt);
     A u[3] = {A(0), A(0), A(0)};
     if (valid) {
-      R rec_r[NP * VN];
-      recs.point_major(v, i, rec_r);
+      if constexpr (!Src::kPrefetch) recs.point_major(v, i, rec_r);
       A rec[NP * VN];
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
       int inst, cam, rig;
-      shot_indices(s, shot_of(s, i), inst, cam, rig);
+      shot_indices(s, sh, inst, cam, rig);
       CamGather<A, CMAX> g;
       gather_cam<A, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
       A t[NR];

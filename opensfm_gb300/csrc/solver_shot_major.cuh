@@ -408,19 +408,40 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
   KeyCarry<6, A, true> c_inst;
   KeyCarry<CMAX, A, carry_fits<A, CMAX>()> c_cam;
   KeyCarry<6, A, true> c_rig;
+  // Software pipeline (as in schur_point_pass_kernel): the next group's
+  // point, shot and stored record are loaded one iteration ahead.
+  int pt_n = -1, sh_n = 0;
+  R rec_n[NP * VN];
+  bool first = true;
   GB_WARP_CHUNK_LOOP(s.n_slots) {
     const int64_t j = base + lane;
-    const int pt = sm.point[j];
+    if (first) {
+      pt_n = sm.point[j];
+      sh_n = sm.shot[j];
+      if constexpr (Src::kPrefetch) recs.shot_major(v, j, 0, rec_n);
+      first = false;
+    }
+    const int pt = pt_n;
+    const int sh = sh_n;
+    R rec_r[NP * VN];
+    if constexpr (Src::kPrefetch) {
+#pragma unroll
+      for (int k = 0; k < NP * VN; ++k) rec_r[k] = rec_n[k];
+    }
+    if (base + 32 < g_end * 32) {
+      pt_n = sm.point[j + 32];
+      sh_n = sm.shot[j + 32];
+      if constexpr (Src::kPrefetch) recs.shot_major(v, j + 32, 0, rec_n);
+    }
     const bool valid = pt >= 0 && slot_active(v, pt);
     A rec[NP * VN];
     A e[NR];
     int inst = 0, cam = 0, rig = -1;
     if (valid) {
-      R rec_r[NP * VN];
-      recs.shot_major(v, j, sm.src[j], rec_r);
+      if constexpr (!Src::kPrefetch) recs.shot_major(v, j, sm.src[j], rec_r);
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
-      shot_indices(s, sm.shot[j], inst, cam, rig);
+      shot_indices(s, sh, inst, cam, rig);
       CamGather<A, CMAX> g;
       gather_cam<A, CMAX, RIG>(x, v.cl, inst, cam, rig, g);
       apply_cam<A, NR, CMAX, RIG>(rec, g, e);
