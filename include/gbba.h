@@ -379,6 +379,39 @@ typedef struct gbba_batch_summary {
 } gbba_batch_summary_t;
 int gbba_batch_get_summary(const gbba_batch_t* b, gbba_batch_summary_t* out);
 
+/* ---- Post-solve outlier selection
+ *
+ * The observation test of sfm::BAHelpers::RemoveOutliers
+ * (ba_helpers.cc:1847-1975), data-parallel on the device.  filter_type 0
+ * (FIXED) uses fixed_threshold; 1 (AUTO) computes it from all observations'
+ * 2D errors: componentwise medians m (the element of rank n/2), robust
+ * deviation s = 1.486 * median |e - m|, threshold = auto_ratio *
+ * |(m_x + s, m_y + s)|.  An observation is an outlier if |e|^2 >
+ * threshold^2 or its IRLS weight is below weight_threshold.  A point is
+ * removed if it loses an observation and keeps fewer than two.  Defaults
+ * of the reference's configuration: FIXED, 0.006, 3.0, 0.5. */
+typedef struct gbba_outlier_config {
+  int filter_type;
+  double fixed_threshold;
+  double auto_ratio;
+  double weight_threshold;
+} gbba_outlier_config_t;
+typedef struct gbba_outlier_result {
+  double threshold;
+  int64_t n_outliers;
+  int64_t n_removed_points;
+} gbba_outlier_result_t;
+/* errors: n rows of `stride` doubles (columns 0 and 1 are the 2D error),
+ * weights [n], obs_point [n] in [0, n_points); host buffers.  flags [n]
+ * (1: outlier) and point_removed [n_points] are written. */
+int gbba_find_outliers(const double* errors, int stride, const double* weights, const int32_t* obs_point, int64_t n,
+                       int64_t n_points, const gbba_outlier_config_t* config, uint8_t* flags, uint8_t* point_removed,
+                       gbba_outlier_result_t* result);
+/* The same on an adjuster's last solve (its reprojection errors and IRLS
+ * weights, observations and points in insertion order). */
+int gbba_adjuster_find_outliers(const gbba_adjuster_t* h, const gbba_outlier_config_t* config, uint8_t* flags,
+                                uint8_t* point_removed, gbba_outlier_result_t* result);
+
 /* ---- Dense reduced-camera-system solver
  *
  * The linear solver behind gbba_run's dense mode (linear solver types

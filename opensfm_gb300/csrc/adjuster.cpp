@@ -377,6 +377,12 @@ void BundleAdjuster::GetPointsBulk(int64_t first, int64_t n, double* xyz) const 
     for (int k = 0; k < 3; ++k) xyz[3 * i + k] = problem_.points[first + i].value[k];
 }
 
+std::vector<int32_t> BundleAdjuster::ObservationPoints() const {
+  std::vector<int32_t> out(problem_.observations.size());
+  for (size_t i = 0; i < out.size(); ++i) out[i] = int32_t(problem_.observations[i].point);
+  return out;
+}
+
 void BundleAdjuster::GetProjectionResults(int64_t n, double* errors, double* weights, int32_t* dims) const {
   if (n != int64_t(problem_.observations.size())) throw std::invalid_argument("wrong observation count");
   const bool have = has_run_ && errors_.size() == size_t(3 * n);

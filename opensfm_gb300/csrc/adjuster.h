@@ -80,6 +80,12 @@ class BundleAdjuster {
   int64_t NumPoints() const { return int64_t(problem_.points.size()); }
   void GetPointsBulk(int64_t first, int64_t n, double* xyz) const;
   void GetProjectionResults(int64_t n, double* errors, double* weights, int32_t* dims) const;
+  // observation point indices in insertion order (for the outlier selection)
+  std::vector<int32_t> ObservationPoints() const;
+  int64_t NumObservations() const { return int64_t(problem_.observations.size()); }
+  bool HasResults() const { return has_run_ && errors_.size() == 3 * problem_.observations.size(); }
+  const std::vector<double>& Errors() const { return errors_; }
+  const std::vector<double>& Weights() const { return weights_; }
   bool CovarianceValid() const { return covariance_valid_; }
   std::string BriefReport() const;
   std::string FullReport() const;

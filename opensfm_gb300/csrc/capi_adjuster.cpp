@@ -345,6 +345,20 @@ int gbba_get_projection_results(const gbba_adjuster_t* h, int64_t n, double* err
   });
 }
 
+int gbba_adjuster_find_outliers(const gbba_adjuster_t* h, const gbba_outlier_config_t* config, uint8_t* flags,
+                                uint8_t* point_removed, gbba_outlier_result_t* result) {
+  const gbba::BundleAdjuster* ba = nullptr;
+  int st = guarded([&] {
+    ba = &ba_of(h);
+    if (!ba->HasResults())
+      throw ApiError(GBBA_ERR_RUNTIME, "no reprojection errors: run the adjuster (with reprojection errors) first");
+  });
+  if (st != GBBA_OK) return st;
+  const std::vector<int32_t> pts = ba->ObservationPoints();
+  return gbba_find_outliers(ba->Errors().data(), 3, ba->Weights().data(), pts.data(), ba->NumObservations(),
+                            ba->NumPoints(), config, flags, point_removed, result);
+}
+
 int gbba_brief_report(const gbba_adjuster_t* h, char* buf, size_t len) {
   int n = 0;
   const int st = guarded([&] { n = copy_string(ba_of(h).BriefReport(), buf, len); });

@@ -289,6 +289,16 @@ class BundleAdjuster:
         self._check(self._L.gbba_get_projection_results(self._h, n, _dp(errs), _dp(w), dims.ctypes.data_as(_I32)))
         return errs, w, dims
 
+    def find_outliers(self, filter_type: str = "FIXED", fixed_threshold: float = 0.006, auto_ratio: float = 3.0,
+                      weight_threshold: float = 0.5):
+        """Outlier observations of the last solve, as sfm::BAHelpers::RemoveOutliers
+        selects them (ba_helpers.cc:1847-1975), computed on the device.  Returns
+        (threshold, outlier flags per observation, removed flags per point), both
+        in insertion order."""
+        from .outliers import adjuster_outliers
+        return adjuster_outliers(self, filter_type=filter_type, fixed_threshold=fixed_threshold,
+                                 auto_ratio=auto_ratio, weight_threshold=weight_threshold)
+
     def projection_results(self):
         """(errors [n, 3], weights [n], dims [n]) per observation in insertion order."""
         return self._projection_results()

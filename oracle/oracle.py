@@ -252,3 +252,37 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     return dict(cameras=out_cam, instances=out_inst, points=out_pts, weights=out_w, errors=out_err,
                 trace=trace[: R.trace_n].copy(), initial_cost=R.initial_cost, final_cost=R.final_cost,
                 iterations=R.iterations, successful=R.successful, termination=R.termination)
+
+
+def remove_outliers(errors, weights, obs_point, n_points, filter_type="FIXED", fixed_threshold=0.006,
+                    auto_ratio=3.0, weight_threshold=0.5):
+    """The observation test of sfm::BAHelpers::RemoveOutliers
+    (opensfm/src/lib/sfm/src/ba_helpers.cc:1847-1975) in numpy: the AUTO
+    threshold from the componentwise medians (element of rank n/2, as
+    std::nth_element at size()/2) and 1.486 x the median deviation norm
+    (:1875-1920); outliers by squared error or IRLS weight (:1928-1941);
+    points that lose an observation and keep fewer than two (:1958-1967).
+    Returns (threshold, outlier flags, removed-point flags)."""
+    e = np.asarray(errors, dtype=np.float64)[:, :2]
+    w = np.asarray(weights, dtype=np.float64)
+    pts = np.asarray(obs_point, dtype=np.int64)
+    threshold = 1.0
+    if filter_type == "FIXED":
+        threshold = float(fixed_threshold)
+    elif len(e):
+        mid = len(e) // 2
+        mx = np.partition(e[:, 0], mid)[mid]
+        my = np.partition(e[:, 1], mid)[mid]
+        dx = e[:, 0] - mx
+        dy = e[:, 1] - my
+        dev = np.sqrt(dx * dx + dy * dy)
+        robust_std = np.float64(1.486) * np.partition(dev, mid)[mid]
+        ax = mx + robust_std
+        ay = my + robust_std
+        threshold = float(np.float64(auto_ratio) * np.sqrt(ax * ax + ay * ay))
+    sq = e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1]
+    flags = (sq > np.float64(threshold) * np.float64(threshold)) | (w < weight_threshold)
+    counts = np.bincount(pts, minlength=n_points)
+    outs = np.bincount(pts[flags], minlength=n_points)
+    removed = (outs > 0) & (counts - outs < 2)
+    return threshold, flags, removed
