@@ -282,6 +282,15 @@ int gbba_set_rig_parameters_prior_sd(gbba_adjuster_t* h, double translation_sd, 
 int gbba_set_compute_reprojection_errors(gbba_adjuster_t* h, int v);
 int gbba_set_compute_covariances(gbba_adjuster_t* h, int v);
 int gbba_get_covariance_estimation_valid(const gbba_adjuster_t* h);
+/* The 6 x 6 row-major covariance of a rig instance's pose [rx ry rz tx ty tz]
+ * after a run with covariances on, as BundleAdjuster::ComputeCovariances
+ * stores it in the rig instance (bundle_adjuster.cc:1217-1287): the instance
+ * block of the inverse Gauss-Newton matrix at the final state (locked
+ * coordinates zero), computed when the reduced camera system has at most
+ * 4,096 optimised unknowns; otherwise, or if it is singular, the estimation
+ * is invalid and the reference's default (variances 1e-5 rotation, 1e-2
+ * translation) is stored. */
+int gbba_get_rig_instance_covariance(const gbba_adjuster_t* h, const char* id, double* out);
 int gbba_set_skip_initial_reweighting(gbba_adjuster_t* h, int v);
 int gbba_set_default_density_ratio(gbba_adjuster_t* h, double ratio);
 double gbba_get_default_density_ratio(const gbba_adjuster_t* h);

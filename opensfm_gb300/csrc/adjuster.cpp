@@ -290,6 +290,7 @@ double BundleAdjuster::GetGroupDensityRatio(const std::string& g) const {
 
 void BundleAdjuster::Run() {
   PrepareRun();
+  opts_.compute_covariances = compute_covariances_;
   auto solver = make_solver(opts_.precision);
   summary_ = solver->solve(problem_, opts_);
   if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
@@ -297,8 +298,29 @@ void BundleAdjuster::Run() {
     errors_.clear();
     weights_.clear();
   }
-  covariance_valid_ = false;  // covariance estimation is not implemented (the reference's failure fallback)
+  covariance_valid_ = false;
+  covariances_.clear();
+  if (compute_covariances_) {
+    std::vector<double> cov;
+    covariance_valid_ = summary_.termination != "FAILURE" && solver->covariances(cov) &&
+                        cov.size() == 36 * problem_.instances.size();
+    if (covariance_valid_) {
+      covariances_ = std::move(cov);
+    } else {
+      // the reference's fallback (bundle_adjuster.cc:1272-1286)
+      covariances_.assign(36 * problem_.instances.size(), 0.0);
+      for (size_t i = 0; i < problem_.instances.size(); ++i)
+        for (int k = 0; k < 6; ++k) covariances_[36 * i + 7 * k] = k < 3 ? 1e-5 : 1e-2;
+    }
+  }
   has_run_ = true;
+}
+
+void BundleAdjuster::GetRigInstanceCovariance(const std::string& id, double* out) const {
+  const auto it = instance_index_.find(id);
+  if (it == instance_index_.end()) throw std::runtime_error("Rig instance " + id + " doesn't exist.");
+  if (covariances_.empty()) throw std::runtime_error("no covariance: run with set_compute_covariances(true)");
+  for (int k = 0; k < 36; ++k) out[k] = covariances_[36 * size_t(it->second) + k];
 }
 
 void BundleAdjuster::SetBatchResult(const SolveSummary& s, std::vector<double> errors) {

@@ -87,6 +87,11 @@ class BundleAdjuster {
   const std::vector<double>& Errors() const { return errors_; }
   const std::vector<double>& Weights() const { return weights_; }
   bool CovarianceValid() const { return covariance_valid_; }
+  // The 6 x 6 covariance (row-major) of a rig instance's pose
+  // [rx ry rz tx ty tz] from the last run with covariances on: the computed
+  // block, or the reference's default (1e-5 rotation, 1e-2 translation
+  // variances) when the estimation failed.
+  void GetRigInstanceCovariance(const std::string& id, double* out) const;
   std::string BriefReport() const;
   std::string FullReport() const;
   std::string IrlsReport() const;
@@ -109,6 +114,7 @@ class BundleAdjuster {
   bool use_analytic_ = false;
   bool compute_covariances_ = false;
   bool covariance_valid_ = false;
+  std::vector<double> covariances_;  // [n_instances][36], empty until a run computes them
   std::string loss_name_ = "TrivialLoss";
   SolveSummary summary_;
   std::vector<double> errors_, weights_;

@@ -231,6 +231,13 @@ int gbba_set_compute_covariances(gbba_adjuster_t* h, int v) {
   return guarded([&] { ba_of(h).SetComputeCovariances(v != 0); });
 }
 
+int gbba_get_rig_instance_covariance(const gbba_adjuster_t* h, const char* id, double* out) {
+  return guarded([&] {
+    need(out, "out");
+    ba_of(h).GetRigInstanceCovariance(str(id), out);
+  });
+}
+
 int gbba_get_covariance_estimation_valid(const gbba_adjuster_t* h) {
   int v = 0;
   guarded([&] { v = ba_of(h).CovarianceValid() ? 1 : 0; });

@@ -91,6 +91,10 @@ struct SolverOptions {
   // Jacobian records: 0 stored when they fit in device memory (else
   // matrix-free), 1 always matrix-free, -1 always stored
   int matrix_free = 0;
+  // pose covariances of the final state (the 6 x 6 instance blocks of the
+  // inverse Gauss-Newton matrix); computed when the reduced camera system is
+  // dense-sized (dense_max_unknowns)
+  bool compute_covariances = false;
   double pcg_tolerance = 1e-3;    // relative residual of the reduced system
   int pcg_max_iterations = 500;
   bool compute_reprojection_errors = true;

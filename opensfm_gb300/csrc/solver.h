@@ -32,6 +32,12 @@ class SolverBase {
   // Per-observation unscaled residuals (std = 1) and IRLS weights of the
   // last solve, in the order of problem.observations.
   virtual void reprojection(std::vector<double>& errors /* n x 3 */, std::vector<double>& weights) = 0;
+  // Pose covariances of the rig instances ([n_instances][6][6]) when the
+  // options asked for them; false if they could not be computed.
+  virtual bool covariances(std::vector<double>& cov) {
+    cov.clear();
+    return false;
+  }
 };
 
 // Many independent problems solved together (batched local bundle

@@ -616,6 +616,10 @@ class DeviceSolver : public SolverBase {
     errors = last_errors_;
     weights = last_weights_;
   }
+  bool covariances(std::vector<double>& cov) override {
+    cov = cov_;
+    return cov_valid_;
+  }
 
  protected:
   // ---- setup
@@ -635,6 +639,8 @@ class DeviceSolver : public SolverBase {
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
   int run_pcg(const R* rhs, double bb, double tol, int max_it);
   int solve_dense(double mu);
+  void assemble_dense(double mu);
+  bool compute_covariances();
   // launches a record pass with stored or evaluated records
   void record_pass(RecordPassLaunch<R>& f) {
     if (matrix_free_) launch_evaluated<R>(kc_, f);
@@ -675,7 +681,11 @@ class DeviceSolver : public SolverBase {
   // matrix-free: no stored records; every record pass evaluates them again
   bool matrix_free_ = false;
   bool dense_ = false;
+  bool dense_ready_ = false;  // the dense structures exist (dense steps or covariances)
   int n_dense_ = 0;
+  std::vector<int> dmap_host_;
+  std::vector<double> cov_;  // [n_inst][6][6] pose covariances of the final state
+  bool cov_valid_ = false;
   int64_t n_pairs_ = 0;
   int64_t dense_failures_ = 0;  // factorizations that found the system not positive definite
   DenseSpdSolver dense_solver_;
@@ -889,7 +899,9 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     for (int j = 0; j < cl_.n; ++j)
       if (cmask_[j]) dmap[j] = n_dense_++;
     dense_ = exact && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
-    if (dense_) {
+    dense_ready_ = (dense_ || opts.compute_covariances) && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
+    dmap_host_ = dmap;
+    if (dense_ready_) {
       // pairs (o1 >= o2) of the observations of every point, as point-major
       // slot indices, sorted (stable counting sort) by the block of S they
       // add to: key = (shot(o1) * n_shots + shot(o2)) * 2 + (o1 == o2)
@@ -955,7 +967,7 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     if (opts.matrix_free > 0) matrix_free_ = true;
     else if (opts.matrix_free < 0) matrix_free_ = false;
     else matrix_free_ = double(record_bytes) > 0.6 * double(free_bytes);
-    if (dense_) matrix_free_ = false;
+    if (dense_ready_) matrix_free_ = false;
     if (!matrix_free_) {
       d_rec_.resize(size_t(n_planes_) * n_slots_);
       d_rec_.zero();  // planes skipped by plane_mask_ must read as zero

@@ -69,6 +69,7 @@ def _declare(L) -> None:
         "gbba_set_compute_reprojection_errors": ([_H, C.c_int], C.c_int),
         "gbba_set_compute_covariances": ([_H, C.c_int], C.c_int),
         "gbba_get_covariance_estimation_valid": ([_H], C.c_int),
+        "gbba_get_rig_instance_covariance": ([_H, S, _D], C.c_int),
         "gbba_set_skip_initial_reweighting": ([_H, C.c_int], C.c_int),
         "gbba_set_default_density_ratio": ([_H, C.c_double], C.c_int),
         "gbba_get_default_density_ratio": ([_H], C.c_double),
@@ -350,6 +351,12 @@ class BundleAdjuster:
     def get_covariance_estimation_valid(self) -> bool:
         return bool(self._L.gbba_get_covariance_estimation_valid(self._h))
 
+    def get_rig_instance_covariance(self, id: str) -> np.ndarray:
+        """6 x 6 covariance of the rig instance's pose [rx ry rz tx ty tz]."""
+        out = np.zeros((6, 6))
+        self._check(self._L.gbba_get_rig_instance_covariance(self._h, _b(id), _dp(out)))
+        return out
+
     def set_skip_initial_reweighting(self, v: bool) -> None:
         self._check(self._L.gbba_set_skip_initial_reweighting(self._h, int(v)))
 
@@ -490,12 +497,14 @@ class BundleBatch:
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
-                        matrix_free: Optional[int] = None) -> BundleAdjuster:
+                        matrix_free: Optional[int] = None, covariances: bool = False) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path)."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
     if matrix_free is not None:
         ba.set_matrix_free(matrix_free)
+    if covariances:
+        ba.set_compute_covariances(True)
     if linear_solver is not None:
         ba.set_linear_solver_type(linear_solver)
     ba.set_irls_mode(irls)
