@@ -20,11 +20,14 @@
 
 namespace gbba {
 
-template <typename R, int NP>
+template <typename R, int NP, bool PREFETCH = true>
 struct StoredRecords {
   // every slot, padding included, has a record: the passes may load it
-  // before they know whether the slot is valid (one iteration ahead)
-  static constexpr bool kPrefetch = true;
+  // before they know whether the slot is valid (one iteration ahead).  The
+  // batched solver turns this off: it reads only the records of problems
+  // still running, and the extra registers of the pipeline cost it more
+  // than they gain.
+  static constexpr bool kPrefetch = PREFETCH;
   const typename Vec16<R>::type* pm;
   const typename Vec16<R>::type* sm;
   int64_t stride;

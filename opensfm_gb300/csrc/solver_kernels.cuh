@@ -510,31 +510,34 @@ __global__ void __launch_bounds__(256) schur_point_pass_kernel(SolveView<R> v, S
   // warp's next slot group are loaded while the current one is processed,
   // so only the L2-resident gathers (shot geometry, x) stay on the
   // iteration's critical path.
+  // Batched solves skip the records of converged problems: there the record
+  // is loaded only for active slots, not ahead.
+  const bool prefetch = Src::kPrefetch && v.active == nullptr;
   int pt_n = -1, sh_n = 0;
   R rec_n[NP * VN];
   if (base < s.n_slots) {
     pt_n = s.obs_point[base + lane];
     sh_n = s.obs[base + lane].shot;
-    if constexpr (Src::kPrefetch) recs.point_major(v, base + lane, rec_n);
+    if (prefetch) recs.point_major(v, base + lane, rec_n);
   }
   for (; base < s.n_slots; base += step) {
     const int64_t i = base + lane;
     const int pt = pt_n;
     const int sh = sh_n;
     R rec_r[NP * VN];
-    if constexpr (Src::kPrefetch) {
+    if (prefetch) {
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec_r[k] = rec_n[k];
     }
     if (base + step < s.n_slots) {
       pt_n = s.obs_point[base + step + lane];
       sh_n = s.obs[base + step + lane].shot;
-      if constexpr (Src::kPrefetch) recs.point_major(v, base + step + lane, rec_n);
+      if (prefetch) recs.point_major(v, base + step + lane, rec_n);
     }
     const bool valid = pt >= 0 && slot_active(v, pt);
     A u[3] = {A(0), A(0), A(0)};
     if (valid) {
-      if constexpr (!Src::kPrefetch) recs.point_major(v, i, rec_r);
+      if (!prefetch) recs.point_major(v, i, rec_r);
       A rec[NP * VN];
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);

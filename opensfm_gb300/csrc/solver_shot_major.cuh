@@ -410,6 +410,8 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
   KeyCarry<6, A, true> c_rig;
   // Software pipeline (as in schur_point_pass_kernel): the next group's
   // point, shot and stored record are loaded one iteration ahead.
+  // (batched solves load records only for active slots, not ahead)
+  const bool prefetch = Src::kPrefetch && v.active == nullptr;
   int pt_n = -1, sh_n = 0;
   R rec_n[NP * VN];
   bool first = true;
@@ -418,27 +420,27 @@ __global__ void __launch_bounds__(kShotMajorBlock) schur_camera_pass_sm_kernel(S
     if (first) {
       pt_n = sm.point[j];
       sh_n = sm.shot[j];
-      if constexpr (Src::kPrefetch) recs.shot_major(v, j, 0, rec_n);
+      if (prefetch) recs.shot_major(v, j, 0, rec_n);
       first = false;
     }
     const int pt = pt_n;
     const int sh = sh_n;
     R rec_r[NP * VN];
-    if constexpr (Src::kPrefetch) {
+    if (prefetch) {
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec_r[k] = rec_n[k];
     }
     if (base + 32 < g_end * 32) {
       pt_n = sm.point[j + 32];
       sh_n = sm.shot[j + 32];
-      if constexpr (Src::kPrefetch) recs.shot_major(v, j + 32, 0, rec_n);
+      if (prefetch) recs.shot_major(v, j + 32, 0, rec_n);
     }
     const bool valid = pt >= 0 && slot_active(v, pt);
     A rec[NP * VN];
     A e[NR];
     int inst = 0, cam = 0, rig = -1;
     if (valid) {
-      if constexpr (!Src::kPrefetch) recs.shot_major(v, j, sm.src[j], rec_r);
+      if (!prefetch) recs.shot_major(v, j, sm.src[j], rec_r);
 #pragma unroll
       for (int k = 0; k < NP * VN; ++k) rec[k] = A(rec_r[k]);
       shot_indices(s, sh, inst, cam, rig);
