@@ -242,6 +242,31 @@ int gbba_add_rig_instance_position_prior(gbba_adjuster_t* h, const char* id, con
                                          const double* std_dev, const char* scale_group);
 /* AddPoint (bundle_adjuster.cc:246-258). */
 int gbba_add_point(gbba_adjuster_t* h, const char* id, const double* position, int constant);
+/* Absolute orientation constraints of a shot, each under CauchyLoss(1):
+ * BundleAdjuster::AddAbsoluteUpVector / Pan / Tilt / Roll
+ * (bundle_adjuster.cc:352-387, added to the problem at :1011-1082;
+ * residuals absolute_motion_errors.h:10-126).  The up vector is a direction
+ * in the camera frame that the shot rotation must take to world +z; the
+ * angles in radians.  Constraints with std_deviation <= 0 are ignored, as
+ * in the reference.  Evaluated on the host in FP64 (a few residuals per
+ * shot); IRLS reweights them in the groups UP, PAN, TILT and ROLL.  An
+ * unknown shot is GBBA_ERR_OUT_OF_RANGE here (the reference's shots_.at()
+ * throws std::out_of_range when Run adds the block). */
+int gbba_add_absolute_up_vector(gbba_adjuster_t* h, const char* shot_id, const double* up_vector,
+                                double std_deviation);
+int gbba_add_absolute_pan(gbba_adjuster_t* h, const char* shot_id, double angle, double std_deviation);
+int gbba_add_absolute_tilt(gbba_adjuster_t* h, const char* shot_id, double angle, double std_deviation);
+int gbba_add_absolute_roll(gbba_adjuster_t* h, const char* shot_id, double angle, double std_deviation);
+/* The scaled residuals (before the loss) of one orientation constraint and
+ * their Jacobian: the functors of absolute_motion_errors.h:10-126 at rig
+ * instance rotation `instance_rotation` and rig camera rotation
+ * `camera_rotation` (angle-axis; NULL: identity).  kind 0 up vector
+ * (target[0..2]), 1 pan, 2 tilt, 3 roll (target[0]).  Writes m = 3 (up
+ * vector) or 1 residuals and J[m][6] (d/d instance rotation, d/d rig camera
+ * rotation), and m to *n_residuals.  Host arithmetic only. */
+int gbba_orientation_residual(int kind, const double* target, double std_deviation,
+                              const double* instance_rotation, const double* camera_rotation, double* residuals,
+                              double* jacobian, int* n_residuals);
 /* AddPointPrior (bundle_adjuster.cc:260-272). */
 int gbba_add_point_prior(gbba_adjuster_t* h, const char* id, const double* position, const double* std_dev,
                          int has_altitude);

@@ -336,12 +336,41 @@ void BundleAdjuster::SetBatchResult(const SolveSummary& s, std::vector<double> e
   has_run_ = true;
 }
 
+void BundleAdjuster::AddOrientationConstraint(const std::string& shot_id, int kind, const double* value,
+                                              double std_deviation) {
+  if (kind < OrientationTerm::kUpVector || kind > OrientationTerm::kRoll)
+    throw std::invalid_argument("unknown orientation constraint kind");
+  if (shot_index_.find(shot_id) == shot_index_.end()) throw std::out_of_range("Shot " + shot_id + " doesn't exist.");
+  PendingOrientation o{shot_id, kind, {value[0], kind == OrientationTerm::kUpVector ? value[1] : 0.0,
+                                      kind == OrientationTerm::kUpVector ? value[2] : 0.0},
+                       std_deviation};
+  orientations_.push_back(o);
+}
+
 void BundleAdjuster::PrepareRun() {
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
   bool known = false;
   for (const char* s : kSolvers) known |= opts_.linear_solver == s;
   if (!known) throw std::runtime_error("Linear solver type " + opts_.linear_solver + " doesn't exist.");
+  problem_.orientation_terms.clear();
+  for (const PendingOrientation& o : orientations_) {
+    if (!(o.std_deviation > 0.0)) continue;
+    const Shot& sh = problem_.shots[shot_index_.at(o.shot)];
+    OrientationTerm t;
+    t.kind = o.kind;
+    t.instance = sh.instance;
+    t.rig_camera = sh.rig_camera;
+    t.scale = 1.0 / o.std_deviation;
+    if (o.kind == OrientationTerm::kUpVector) {
+      // UpVectorError normalizes the direction (absolute_motion_errors.h:11-14)
+      const double n = std::sqrt(o.value[0] * o.value[0] + o.value[1] * o.value[1] + o.value[2] * o.value[2]);
+      for (int k = 0; k < 3; ++k) t.target[k] = n > 0.0 ? o.value[k] / n : 0.0;
+    } else {
+      t.target[0] = o.value[0];
+    }
+    problem_.orientation_terms.push_back(t);
+  }
   // sigmas and usage flags at run time
   for (CameraBlock& c : problem_.cameras) camera_sigma(c);
   for (PoseBlock& r : problem_.rig_cameras) {
@@ -364,6 +393,8 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
+  static const char* kOrientationGroups[4] = {"UP", "PAN", "TILT", "ROLL"};
+  for (int k = 0; k < 4; ++k) problem_.ratio_orientation[k] = GetGroupDensityRatio(kOrientationGroups[k]);
 }
 
 int BundleAdjuster::GetCamera(const std::string& id, int* model, double* values, int cap) const {

@@ -29,6 +29,11 @@ class BundleAdjuster {
                                    const std::string& scale_group);
   int64_t AddPoint(const std::string& id, const double* p, bool constant);
   void AddPointPrior(const std::string& id, const double* p, const double* std_dev, bool has_altitude);
+  // Absolute orientation constraints of a shot (bundle_adjuster.cc:352-395):
+  // kind OrientationTerm::kUpVector (value = 3-vector) or kPan / kTilt /
+  // kRoll (value[0] = angle).  Constraints with std_deviation <= 0 are kept
+  // and ignored, as the reference adds only positive ones.
+  void AddOrientationConstraint(const std::string& shot_id, int kind, const double* value, double std_deviation);
   void AddPointProjectionObservation(const std::string& shot, const std::string& point, const double* obs,
                                      double std_dev, bool is_gcp);
   // index-based adders (the raw-pointer path of AddPointProjectionObservationRaw)
@@ -115,6 +120,13 @@ class BundleAdjuster {
   bool compute_covariances_ = false;
   bool covariance_valid_ = false;
   std::vector<double> covariances_;  // [n_instances][36], empty until a run computes them
+  struct PendingOrientation {
+    std::string shot;
+    int kind;
+    double value[3];
+    double std_deviation;
+  };
+  std::vector<PendingOrientation> orientations_;
   std::string loss_name_ = "TrivialLoss";
   SolveSummary summary_;
   std::vector<double> errors_, weights_;

@@ -118,6 +118,55 @@ int gbba_add_point(gbba_adjuster_t* h, const char* id, const double* position, i
   });
 }
 
+int gbba_add_absolute_up_vector(gbba_adjuster_t* h, const char* shot_id, const double* up_vector,
+                                double std_deviation) {
+  return guarded([&] {
+    need(up_vector, "up_vector");
+    ba_of(h).AddOrientationConstraint(str(shot_id), gbba::OrientationTerm::kUpVector, up_vector, std_deviation);
+  });
+}
+
+int gbba_orientation_residual(int kind, const double* target, double std_deviation,
+                              const double* instance_rotation, const double* camera_rotation, double* residuals,
+                              double* jacobian, int* n_residuals) {
+  return guarded([&] {
+    if (kind < 0 || kind > 3 || !target || !instance_rotation || !residuals || !jacobian || !n_residuals ||
+        !(std_deviation > 0.0))
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_orientation_residual: invalid argument");
+    gbba::OrientationTerm t;
+    t.kind = kind;
+    t.rig_camera = camera_rotation ? 0 : -1;
+    t.scale = 1.0 / std_deviation;
+    if (kind == gbba::OrientationTerm::kUpVector) {
+      const double n = std::sqrt(target[0] * target[0] + target[1] * target[1] + target[2] * target[2]);
+      if (!(n > 0.0)) throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_orientation_residual: zero up vector");
+      for (int k = 0; k < 3; ++k) t.target[k] = target[k] / n;
+    } else {
+      t.target[0] = target[0];
+    }
+    gbba::orient::D r[3];
+    const int m = gbba::orient::residuals(t, instance_rotation, camera_rotation, r);
+    for (int q = 0; q < m; ++q) {
+      residuals[q] = r[q].v;
+      for (int k = 0; k < 6; ++k) jacobian[6 * q + k] = r[q].d[k];
+    }
+    *n_residuals = m;
+  });
+}
+
+static int add_angle(gbba_adjuster_t* h, const char* shot_id, int kind, double angle, double std_deviation) {
+  return guarded([&] { ba_of(h).AddOrientationConstraint(str(shot_id), kind, &angle, std_deviation); });
+}
+int gbba_add_absolute_pan(gbba_adjuster_t* h, const char* shot_id, double angle, double std_deviation) {
+  return add_angle(h, shot_id, gbba::OrientationTerm::kPan, angle, std_deviation);
+}
+int gbba_add_absolute_tilt(gbba_adjuster_t* h, const char* shot_id, double angle, double std_deviation) {
+  return add_angle(h, shot_id, gbba::OrientationTerm::kTilt, angle, std_deviation);
+}
+int gbba_add_absolute_roll(gbba_adjuster_t* h, const char* shot_id, double angle, double std_deviation) {
+  return add_angle(h, shot_id, gbba::OrientationTerm::kRoll, angle, std_deviation);
+}
+
 int gbba_add_point_prior(gbba_adjuster_t* h, const char* id, const double* position, const double* std_dev,
                          int has_altitude) {
   return guarded([&] {

@@ -13,6 +13,8 @@
 // below hold one flag per parameter (1 = optimised).
 #pragma once
 
+#include "orientation_terms.h"
+
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -109,10 +111,13 @@ struct Problem {
   std::vector<Shot> shots;
   std::vector<PointBlock> points;
   std::vector<Observation> observations;
+  // absolute orientation constraints (up vector, pan, tilt, roll)
+  std::vector<OrientationTerm> orientation_terms;
   // IRLS density ratios: one per projection group (shot groups "PROJ_<shot>"
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
   double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
+  double ratio_orientation[4] = {1e-3, 1e-3, 1e-3, 1e-3};  // groups UP, PAN, TILT, ROLL
 };
 
 // One LM iteration as reported by the solver.

@@ -3,6 +3,8 @@
 // solver_mixed.cu.
 #pragma once
 #include <algorithm>
+#include <array>
+#include <map>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -13,6 +15,7 @@
 
 #include "dense_cholesky.h"
 #include "dense_schur.cuh"
+#include "host_blocks.cuh"
 #include "device_buffer.h"
 #include "solver.h"
 #include "solver_kernels.cuh"
@@ -632,9 +635,17 @@ class DeviceSolver : public SolverBase {
   double cost_pass(bool candidate, bool store_residuals);
   void linearize();
   void point_priors_linearize(bool candidate);
-  // ---- host priors
+  // ---- host priors and orientation constraints
   double prior_terms(const std::vector<double>& x, bool want_derivs);
+  // y += H x for the host-computed Gauss-Newton blocks
+  template <typename A>
+  void host_blocks_apply(const A* x, A* y) {
+    if (n_hblocks_ == 0) return;
+    host_block_spmv_kernel<A><<<(8 * n_hblocks_ + 255) / 256, 256>>>(n_hblocks_, d_hbase_.get(), d_hval_.get(), x, y);
+    ++launches_;
+  }
   double prior_model_change(const std::vector<double>& x, const std::vector<double>& dx);
+  int orientation_residuals(const OrientationTerm& t, const std::vector<double>& x, orient::D* r, int* coord) const;
   // ---- linear solve
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
   int run_pcg(const R* rhs, double bb, double tol, int max_it);
@@ -665,6 +676,12 @@ class DeviceSolver : public SolverBase {
   std::vector<double> xc_, xc_cand_;
   std::vector<uint8_t> cmask_;
   std::vector<double> pgrad_, pdiag_;
+  // orientation constraints: Gauss-Newton blocks (8 x 8, keyed by coordinate
+  // group bases) and their diagonal (for the LM damping)
+  std::map<std::pair<int, int>, std::array<double, 64>> hblocks_;
+  std::vector<double> hdiag_;
+  int n_hblocks_ = 0;
+  std::vector<double> orient_weight_;  // IRLS weight of every orientation term
   std::vector<int> group_count_, group_dim_;
   std::vector<double> group_ratio_;
   std::vector<double> prior_weight_cam_, prior_weight_rig_, prior_weight_gps_;
@@ -727,6 +744,9 @@ class DeviceSolver : public SolverBase {
   DeviceArray<R> d_rref_;
   DeviceArray<R> d_dc_, d_rhs_, d_cscale_, d_damp_;
   DeviceArray<double> d_pdiag_, d_pgrad_;
+  DeviceArray<double> d_pdamp_;  // pdiag + orientation-term diagonal: the LM diagonal of the host terms
+  DeviceArray<int2> d_hbase_;
+  DeviceArray<double> d_hval_;
   DeviceArray<R> d_x_, d_r_, d_z_, d_p_, d_y_;
   DeviceArray<R> d_tri_inst_, d_tri_rig_, d_tri_cam_, d_minv_inst_, d_minv_rig_, d_minv_cam_;
   DeviceArray<double> d_scal_;
@@ -1051,6 +1071,8 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   d_rhs64_.resize(cl_.n);
   d_pdiag_.resize(cl_.n);
   d_pgrad_.resize(cl_.n);
+  d_pdamp_.resize(cl_.n);
+  hdiag_.assign(cl_.n, 0.0);
   d_tri_inst_.resize(24 * std::max(1, n_inst_));
   d_tri_rig_.resize(24 * std::max(1, n_rig_));
   cam_tri_stride_ = (kc_.cmax * (kc_.cmax + 1) / 2 + 3) / 4 * 4;
@@ -1079,6 +1101,7 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   for (int i = 0; i < n_inst_; ++i)
     if (P.instances[i].has_position_prior) gps_inst_.push_back(i);
   prior_weight_gps_.assign(gps_inst_.size(), 1.0);
+  orient_weight_.assign(P.orientation_terms.size(), 1.0);
   point_priors_.clear();
   for (int64_t p = 0; p < n_pt_; ++p) {
     const PointBlock& b = P.points[p];
@@ -1287,6 +1310,20 @@ void DeviceSolver<R>::linearize() {
   prior_terms(xc_, true);
   d_pgrad_.upload(pgrad_);
   d_pdiag_.upload(pdiag_);
+  std::vector<double> pdamp(cl_.n);
+  for (int j = 0; j < cl_.n; ++j) pdamp[j] = pdiag_[j] + hdiag_[j];
+  d_pdamp_.upload(pdamp);
+  n_hblocks_ = int(hblocks_.size());
+  if (n_hblocks_) {
+    std::vector<int2> base;
+    std::vector<double> val;
+    for (const auto& kv : hblocks_) {
+      base.push_back(make_int2(kv.first.first, kv.first.second));
+      val.insert(val.end(), kv.second.begin(), kv.second.end());
+    }
+    d_hbase_.upload(base);
+    d_hval_.upload(val);
+  }
 }
 
 // Camera, rig-camera and GPS priors at camera-side state x (FP64, host).
@@ -1303,6 +1340,8 @@ double DeviceSolver<R>::prior_terms(const std::vector<double>& x, bool want_deri
   if (want_derivs) {
     std::fill(pgrad_.begin(), pgrad_.end(), 0.0);
     std::fill(pdiag_.begin(), pdiag_.end(), 0.0);
+    std::fill(hdiag_.begin(), hdiag_.end(), 0.0);
+    hblocks_.clear();
   }
   double cost = 0.0;
   for (int c = 0; c < n_cam_; ++c) {
@@ -1364,7 +1403,45 @@ double DeviceSolver<R>::prior_terms(const std::vector<double>& x, bool want_deri
       }
     }
   }
+  // absolute orientation constraints (Cauchy loss): J^T r and J^T J over the
+  // free rotation coordinates of the rig instance and rig camera
+  for (size_t q = 0; q < P.orientation_terms.size(); ++q) {
+    int coord[6];
+    orient::D r[3];
+    const int m = orientation_residuals(P.orientation_terms[q], x, r, coord);
+    cost += 0.5 * orient::cauchy_correct(m, r, orient_weight_[q]);
+    if (!want_derivs) continue;
+    for (int a = 0; a < 6; ++a) {
+      if (coord[a] < 0) continue;
+      double g = 0.0;
+      for (int q = 0; q < m; ++q) g += r[q].d[a] * r[q].v;
+      pgrad_[coord[a]] += g;
+      for (int b = 0; b < 6; ++b) {
+        if (coord[b] < 0) continue;
+        double h = 0.0;
+        for (int q = 0; q < m; ++q) h += r[q].d[a] * r[q].d[b];
+        const int ga = coord[a] & ~7, gb = coord[b] & ~7;
+        hblocks_[{ga, gb}][8 * (coord[a] - ga) + (coord[b] - gb)] += h;
+        if (a == b) hdiag_[coord[a]] += h;
+      }
+    }
+  }
   return cost;
+}
+
+// Residuals of an orientation term at camera-side state x, with derivatives
+// w.r.t. the instance rotation (slots 0..2) and the rig camera rotation
+// (3..5); coord[] maps the slots to free camera-side coordinates (-1: fixed).
+template <typename R>
+int DeviceSolver<R>::orientation_residuals(const OrientationTerm& t, const std::vector<double>& x, orient::D* r,
+                                           int* coord) const {
+  const bool rig = t.rig_camera >= 0;
+  const int ib = 8 * t.instance, rb = rig ? cl_.rig_base + 8 * t.rig_camera : -1;
+  for (int k = 0; k < 3; ++k) {
+    coord[k] = cmask_[ib + k] ? ib + k : -1;
+    coord[3 + k] = (rig && cmask_[rb + k]) ? rb + k : -1;
+  }
+  return orient::residuals(t, &x[ib], rig ? &x[rb] : nullptr, r);
 }
 
 // Linear-model decrease of the priors for a camera-side step dx.
@@ -1411,6 +1488,18 @@ double DeviceSolver<R>::prior_model_change(const std::vector<double>& x, const s
       if (!cmask_[j]) continue;
       const double scale = 1.0 / std::max(b.position_sigma[k], kEps);
       total += term(prior_weight_gps_[g], scale * (x[j] - prior[k]), scale, dx[j]);
+    }
+  }
+  for (size_t q = 0; q < P.orientation_terms.size(); ++q) {
+    int coord[6];
+    orient::D r[3];
+    const int m = orientation_residuals(P.orientation_terms[q], x, r, coord);
+    orient::cauchy_correct(m, r, orient_weight_[q]);
+    for (int q = 0; q < m; ++q) {
+      double jd = 0.0;
+      for (int a = 0; a < 6; ++a)
+        if (coord[a] >= 0) jd += r[q].d[a] * dx[coord[a]];
+      total += -0.5 * jd * (2.0 * r[q].v + jd);
     }
   }
   return total;

@@ -52,6 +52,11 @@ def _declare(L) -> None:
         "gbba_add_rig_instance_position_prior": ([_H, S, _D, _D, S], C.c_int),
         "gbba_add_point": ([_H, S, _D, C.c_int], C.c_int),
         "gbba_add_point_prior": ([_H, S, _D, _D, C.c_int], C.c_int),
+        "gbba_add_absolute_up_vector": ([_H, S, _D, C.c_double], C.c_int),
+        "gbba_add_absolute_pan": ([_H, S, C.c_double, C.c_double], C.c_int),
+        "gbba_add_absolute_tilt": ([_H, S, C.c_double, C.c_double], C.c_int),
+        "gbba_add_absolute_roll": ([_H, S, C.c_double, C.c_double], C.c_int),
+        "gbba_orientation_residual": ([C.c_int, _D, C.c_double, _D, _D, _D, _D, C.POINTER(C.c_int)], C.c_int),
         "gbba_add_point_projection_observation": ([_H, S, S, _D, C.c_double, C.c_int], C.c_int),
         "gbba_shot_index": ([_H, S], C.c_int64),
         "gbba_point_index": ([_H, S], C.c_int64),
@@ -290,6 +295,19 @@ class BundleAdjuster:
         self._check(self._L.gbba_get_projection_results(self._h, n, _dp(errs), _dp(w), dims.ctypes.data_as(_I32)))
         return errs, w, dims
 
+    def add_absolute_up_vector(self, shot_id: str, up_vector, std_deviation: float) -> None:
+        v = np.ascontiguousarray(up_vector, dtype=np.float64)
+        self._check(self._L.gbba_add_absolute_up_vector(self._h, _b(shot_id), _dp(v), float(std_deviation)))
+
+    def add_absolute_pan(self, shot_id: str, angle: float, std_deviation: float) -> None:
+        self._check(self._L.gbba_add_absolute_pan(self._h, _b(shot_id), float(angle), float(std_deviation)))
+
+    def add_absolute_tilt(self, shot_id: str, angle: float, std_deviation: float) -> None:
+        self._check(self._L.gbba_add_absolute_tilt(self._h, _b(shot_id), float(angle), float(std_deviation)))
+
+    def add_absolute_roll(self, shot_id: str, angle: float, std_deviation: float) -> None:
+        self._check(self._L.gbba_add_absolute_roll(self._h, _b(shot_id), float(angle), float(std_deviation)))
+
     def find_outliers(self, filter_type: str = "FIXED", fixed_threshold: float = 0.006, auto_ratio: float = 3.0,
                       weight_threshold: float = 0.5):
         """Outlier observations of the last solve, as sfm::BAHelpers::RemoveOutliers
@@ -417,10 +435,6 @@ class BundleAdjuster:
     add_common_position = _unsupported
     add_heatmap = _unsupported
     add_absolute_position_heatmap = _unsupported
-    add_absolute_up_vector = _unsupported
-    add_absolute_pan = _unsupported
-    add_absolute_tilt = _unsupported
-    add_absolute_roll = _unsupported
     add_linear_motion = _unsupported
     set_gauge_fix_shots = _unsupported
     add_reconstruction = _unsupported
@@ -494,6 +508,28 @@ class BundleBatch:
         return {k: getattr(s, k) for k, _ in BatchSummary._fields_}
 
 
+ORIENTATION_KINDS = {"up_vector": 0, "pan": 1, "tilt": 2, "roll": 3}
+
+
+def orientation_residual(kind: str, target, std_deviation: float, instance_rotation, camera_rotation=None):
+    """Scaled residuals (before the loss) and Jacobian [m][6] of one absolute
+    orientation constraint -- UpVectorError, PanAngleError, TiltAngleError
+    or RollAngleError (bundle/error/absolute_motion_errors.h:10-126) -- at
+    the given rig instance and rig camera rotations (angle-axis)."""
+    L = _lib.lib()
+    _declare(L)
+    t = np.zeros(3)
+    v = np.atleast_1d(np.asarray(target, dtype=np.float64))
+    t[: len(v)] = v
+    ri = np.ascontiguousarray(instance_rotation, dtype=np.float64)
+    rc = None if camera_rotation is None else np.ascontiguousarray(camera_rotation, dtype=np.float64)
+    r, J = np.zeros(3), np.zeros(18)
+    m = C.c_int(0)
+    _lib.check(L.gbba_orientation_residual(ORIENTATION_KINDS[kind], _dp(t), float(std_deviation), _dp(ri),
+                                           _dp(rc) if rc is not None else None, _dp(r), _dp(J), C.byref(m)))
+    return r[: m.value].copy(), J[: 6 * m.value].reshape(m.value, 6)
+
+
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
@@ -532,4 +568,4 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
     return ba
 
 
-__all__ = ["BundleAdjuster", "BundleBatch", "Point", "adjuster_from_scene"]
+__all__ = ["BundleAdjuster", "BundleBatch", "Point", "adjuster_from_scene", "orientation_residual"]

@@ -147,6 +147,7 @@ class _Problem(C.Structure):
         ("n_points", C.c_int64), ("points", D), ("point_free", U8), ("point_has_prior", U8), ("point_prior", D),
         ("point_sigma", D), ("point_has_altitude", U8),
         ("n_obs", C.c_int64), ("obs_shot", I32), ("obs_point", I32), ("obs_xy", D), ("obs_std", D), ("obs_gcp", U8),
+        ("n_orient", C.c_int32), ("orient_kind", I32), ("orient_shot", I32), ("orient_target", D), ("orient_std", D),
     ]
 
 
@@ -175,11 +176,34 @@ _LOG = {0: [0, 0, 1], 1: [0, 0, 0, 0, 0, 1, 1, 0, 0], 2: [0, 0, 1], 3: [0, 0, 0,
         9: [0, 1, 1, 0, 0]}
 
 
+ORIENTATION_KINDS = {"up_vector": 0, "pan": 1, "tilt": 2, "roll": 3}
+
+
+def orientation_residual(kind: str, target, std: float, instance_rotation, camera_rotation=None):
+    """Scaled residuals and Jacobian [m][6] of one absolute orientation
+    constraint (oracle/solver.cpp restatement)."""
+    L = lib()
+    f = L.oracle_orientation_residual
+    f.argtypes = [C.c_int, D, C.c_double, D, D, D, D]
+    f.restype = C.c_int
+    t = np.zeros(3)
+    v = np.atleast_1d(np.asarray(target, np.float64))
+    t[: len(v)] = v
+    ri = np.ascontiguousarray(instance_rotation, np.float64)
+    rc = None if camera_rotation is None else np.ascontiguousarray(camera_rotation, np.float64)
+    r, J = np.zeros(3), np.zeros(18)
+    m = f(ORIENTATION_KINDS[kind], _p(t), std, _p(ri), _p(rc), _p(r), _p(J))
+    return r[:m].copy(), J[: 6 * m].reshape(m, 6)
+
+
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
-          density_ratio=1e-3, skip_initial_reweighting=False, threads=None):
+          density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=()):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
-    Returns a dict with the final parameters, costs and the cost trace."""
+    ``orientation``: absolute orientation constraints, tuples (kind, shot,
+    value, std) with kind one of ORIENTATION_KINDS and value the up vector
+    or the angle.  Returns a dict with the final parameters, costs and the
+    cost trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
     L.oracle_solve.restype = C.c_int
@@ -223,8 +247,17 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     psig = np.ones((npt, 3))
     palt = np.ones(npt, np.uint8)
     gcp = np.zeros(scene.n_observations, np.uint8)
+    no = len(orientation)
+    o_kind = np.array([ORIENTATION_KINDS[o[0]] for o in orientation], np.int32).reshape(no)
+    o_shot = np.array([int(o[1]) for o in orientation], np.int32).reshape(no)
+    o_target = np.zeros((max(no, 1), 3))
+    for q, o in enumerate(orientation):
+        v = np.atleast_1d(np.asarray(o[2], np.float64))
+        o_target[q, : len(v)] = v
+    o_std = np.array([float(o[3]) for o in orientation], np.float64).reshape(no)
     keep = [cam_values, cam_sigma, cam_log, cam_free, inst, inst_free, has_gps, gps_pos, gps_std, rig, rig_free,
-            rig_used, rig_has_prior, rig_prior, rig_sigma, shot_rig, pts, pfree, phas, pprior, psig, palt, gcp]
+            rig_used, rig_has_prior, rig_prior, rig_sigma, shot_rig, pts, pfree, phas, pprior, psig, palt, gcp,
+            o_kind, o_shot, o_target, o_std]
     u8 = lambda a: a.ctypes.data_as(U8)  # noqa: E731
     i32 = lambda a: a.ctypes.data_as(I32)  # noqa: E731
     P = _Problem(nc, i32(scene.camera_projection), _p(cam_values), _p(cam_values.copy() if False else cam_values),
@@ -234,7 +267,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
                  ns, i32(scene.shot_rig_instance), i32(shot_rig), i32(scene.shot_camera),
                  npt, _p(pts), u8(pfree), u8(phas), _p(pprior), _p(psig), u8(palt),
                  scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
-                 _p(scene.obs_std), u8(gcp))
+                 _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std))
     loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
     O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
                  int(skip_initial_reweighting), threads or os.cpu_count() or 1)

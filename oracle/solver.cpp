@@ -75,6 +75,12 @@ struct OracleProblem {
   const double* obs_xy;
   const double* obs_std;
   const uint8_t* obs_gcp;
+  // absolute orientation constraints of shots
+  int32_t n_orient;
+  const int32_t* orient_kind;   // 0 up vector, 1 pan, 2 tilt, 3 roll
+  const int32_t* orient_shot;
+  const double* orient_target;  // [n][3]: the up vector, or the angle in [0]
+  const double* orient_std;
 };
 
 struct OracleOptions {
@@ -122,11 +128,111 @@ struct Mixture {
   double ll = 0.0;
 };
 
+// ---- absolute orientation constraints
+// UpVectorError, PanAngleError, TiltAngleError and RollAngleError
+// (bundle/error/absolute_motion_errors.h:10-126) on the shot rotation, the
+// rig instance rotation composed with the rig camera rotation
+// (bundle/error/position_functors.h:40-63).  Restated with rotation
+// matrices: R = R(instance) R(rig camera), and R e_x, R e_z are its first
+// and third columns.  Derivatives w.r.t. the two rotations (slots 0..2 and
+// 3..5) by forward-mode duals.
+using D6 = Dual<6>;
+
+D6 asin6(const D6& a) {
+  D6 r(std::asin(a.v));
+  const double k = 1.0 / std::sqrt(1.0 - a.v * a.v);
+  for (int i = 0; i < 6; ++i) r.d[i] = a.d[i] * k;
+  return r;
+}
+
+// Rodrigues: R = cos t I + sin t [k]x + (1 - cos t) k k^T, k = a / t
+void rotation_matrix(const D6* a, D6* M) {
+  const D6 t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+  if (t2.v > kEps) {
+    const D6 t = sqrt(t2);
+    const D6 k[3] = {a[0] / t, a[1] / t, a[2] / t};
+    const D6 c = cos(t), sn = sin(t), v = 1.0 - c;
+    M[0] = c + v * k[0] * k[0];
+    M[1] = v * k[0] * k[1] - sn * k[2];
+    M[2] = v * k[0] * k[2] + sn * k[1];
+    M[3] = v * k[1] * k[0] + sn * k[2];
+    M[4] = c + v * k[1] * k[1];
+    M[5] = v * k[1] * k[2] - sn * k[0];
+    M[6] = v * k[2] * k[0] - sn * k[1];
+    M[7] = v * k[2] * k[1] + sn * k[0];
+    M[8] = c + v * k[2] * k[2];
+  } else {
+    M[0] = D6(1.0), M[1] = -a[2], M[2] = a[1];
+    M[3] = a[2], M[4] = D6(1.0), M[5] = -a[0];
+    M[6] = -a[1], M[7] = a[0], M[8] = D6(1.0);
+  }
+}
+
+D6 wrap_angle(const D6& d) {
+  if (d.v > M_PI) return d - 2 * M_PI;
+  if (d.v < -M_PI) return d + 2 * M_PI;
+  return d;
+}
+
+// Scaled residuals (1 or 3) of one constraint; returns the count.
+int orientation_residual(int kind, const double* target, double std_dev, const double* ri, const double* rc,
+                         D6* r) {
+  D6 a[3], b[3], A[9], B[9], R[9];
+  for (int k = 0; k < 3; ++k) {
+    a[k] = D6::var(ri[k], k);
+    b[k] = D6::var(rc[k], 3 + k);
+  }
+  rotation_matrix(a, A);
+  rotation_matrix(b, B);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) R[3 * i + j] = A[3 * i] * B[j] + A[3 * i + 1] * B[3 + j] + A[3 * i + 2] * B[6 + j];
+  const double scale = 1.0 / std_dev;
+  const D6 z[3] = {R[2], R[5], R[8]}, x[3] = {R[0], R[3], R[6]};
+  if (kind == 0) {
+    const double n = std::sqrt(target[0] * target[0] + target[1] * target[1] + target[2] * target[2]);
+    const double u[3] = {target[0] / n, target[1] / n, target[2] / n};
+    for (int i = 0; i < 3; ++i) {
+      const D6 v = R[3 * i] * u[0] + R[3 * i + 1] * u[1] + R[3 * i + 2] * u[2];
+      r[i] = scale * (v - (i == 2 ? 1.0 : 0.0));
+    }
+    return 3;
+  }
+  if (kind == 1) {
+    if (std::fabs(z[0].v) < 1e-8 && std::fabs(z[1].v) < 1e-8) r[0] = D6(0.0);
+    else r[0] = scale * wrap_angle(atan2(z[0], z[1]) - target[0]);
+    return 1;
+  }
+  if (kind == 2) {
+    const D6 l = sqrt(z[0] * z[0] + z[1] * z[1]);
+    r[0] = scale * wrap_angle(-atan2(z[2], l) - target[0]);
+    return 1;
+  }
+  // roll: the angle of the camera x axis out of the horizontal plane
+  const double eps = 1e-5;
+  D6 h[2] = {z[1], -z[0]};
+  const D6 lh = sqrt(h[0] * h[0] + h[1] * h[1]);
+  if (lh.v < eps) {
+    r[0] = D6(0.0);
+    return 1;
+  }
+  h[0] = h[0] / lh;
+  h[1] = h[1] / lh;
+  // c = x cross (h0, h1, 0)
+  const D6 c[3] = {-x[2] * h[1], x[2] * h[0], x[0] * h[1] - x[1] * h[0]};
+  const D6 sin_roll = z[0] * c[0] + z[1] * c[1] + z[2] * c[2];
+  if (sin_roll.v <= -(1.0 - eps)) {
+    r[0] = D6(0.0);
+    return 1;
+  }
+  r[0] = scale * wrap_angle(asin6(sin_roll) - target[0]);
+  return 1;
+}
+
 struct Solver {
   const OracleProblem& P;
   const OracleOptions& O;
   Index idx;
-  std::vector<double> w_obs, w_cam, w_rig, w_gps, w_pp;
+  std::vector<double> w_obs, w_cam, w_rig, w_gps, w_pp, w_orient;
   std::vector<int> gps_list, pp_list;
   int threads;
 
@@ -155,6 +261,33 @@ struct Solver {
     for (int64_t p = 0; p < P.n_points; ++p)
       if (P.point_has_prior[p]) pp_list.push_back(int(p));
     w_pp.assign(pp_list.size(), 1.0);
+    w_orient.assign(std::max(0, P.n_orient), 1.0);
+  }
+
+  // Orientation constraint q at state s under CauchyLoss(1) and its IRLS
+  // weight: the residuals and Jacobian corrected by sqrt(w rho'(|r|^2))
+  // (rho'' < 0, so no second-order term), the compact columns of the two
+  // rotations (-1: fixed), and w rho(|r|^2) through *rho.
+  int orientation_term(const State& s, int q, D6* r, int* col, double* rho, double* raw = nullptr) const {
+    const int sh = P.orient_shot[q];
+    const int inst = P.shot_instance[sh], rc = P.shot_rig[sh];
+    const bool use_rig = rc >= 0 && P.rig_used[rc];
+    static const double zero[3] = {0, 0, 0};
+    const int m = orientation_residual(P.orient_kind[q], P.orient_target + 3 * q, P.orient_std[q], &s.inst[6 * inst],
+                                       use_rig ? &s.rig[6 * rc] : zero, r);
+    for (int k = 0; k < 3; ++k) {
+      col[k] = idx.inst[6 * inst + k];
+      col[3 + k] = use_rig ? idx.rig[6 * rc + k] : -1;
+    }
+    double sq = 0.0;
+    for (int a = 0; a < m; ++a) {
+      sq += r[a].v * r[a].v;
+      if (raw) raw[a] = r[a].v;
+    }
+    *rho = w_orient[q] * std::log1p(sq);
+    const double f = std::sqrt(w_orient[q] / (1.0 + sq));
+    for (int a = 0; a < m; ++a) r[a] = r[a] * f;
+    return m;
   }
 
   template <typename F>
@@ -225,6 +358,13 @@ struct Solver {
 
   double prior_cost(const State& s) const {
     double c = 0.0;
+    for (int q = 0; q < P.n_orient; ++q) {
+      D6 r[3];
+      int col[6];
+      double rho;
+      orientation_term(s, q, r, col, &rho);
+      c += 0.5 * rho;
+    }
     double r[16], J[16];
     for (int k = 0; k < P.n_cameras; ++k) {
       const int n = cam_prior(s, k, r, J);
@@ -385,6 +525,20 @@ struct Solver {
         const double sc = 1.0 / std::max(P.point_sigma[3 * p + k], kEps);
         gp[3 * p + k] += w_pp[q] * sc * sc * (s.pts[3 * p + k] - P.point_prior[3 * p + k]);
         V[9 * p + 4 * k] += w_pp[q] * sc * sc;
+      }
+    }
+    for (int q = 0; q < P.n_orient; ++q) {
+      D6 rr[3];
+      int col[6];
+      double rho;
+      const int m = orientation_term(s, q, rr, col, &rho);
+      for (int a = 0; a < 6; ++a) {
+        if (col[a] < 0) continue;
+        for (int t = 0; t < m; ++t) g[col[a]] += rr[t].d[a] * rr[t].v;
+        for (int b = 0; b < 6; ++b) {
+          if (col[b] < 0) continue;
+          for (int t = 0; t < m; ++t) U[size_t(col[a]) * n + col[b]] += rr[t].d[a] * rr[t].d[b];
+        }
       }
     }
   }
@@ -582,6 +736,18 @@ struct Solver {
         mc += term(w_pp[q], sc * (s.pts[3 * p + k] - P.point_prior[3 * p + k]), sc, dp[3 * p + k]);
       }
     }
+    for (int q = 0; q < P.n_orient; ++q) {
+      D6 rr[3];
+      int col[6];
+      double rho;
+      const int m = orientation_term(s, q, rr, col, &rho);
+      for (int t = 0; t < m; ++t) {
+        double jd = 0.0;
+        for (int a = 0; a < 6; ++a)
+          if (col[a] >= 0) jd += rr[t].d[a] * dc[col[a]];
+        mc += -0.5 * jd * (2.0 * rr[t].v + jd);
+      }
+    }
     return mc;
   }
 
@@ -746,6 +912,20 @@ struct Solver {
       }
       total += mixture(res, w, O.density_ratio);
     }
+    for (int kind = 0; kind < 4; ++kind) {  // groups UP, PAN, TILT, ROLL
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      for (int q = 0; q < P.n_orient; ++q) {
+        if (P.orient_kind[q] != kind) continue;
+        D6 rr[3];
+        int col[6];
+        double rho, raw[3];
+        const int m = orientation_term(s, q, rr, col, &rho, raw);
+        res.emplace_back(raw, raw + m);
+        w.push_back(&w_orient[q]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
     return total;
   }
 };
@@ -764,6 +944,20 @@ extern "C" double oracle_mixture_group(int k, int64_t n, const double* residuals
     w[i] = weights + i;
   }
   return Solver::mixture(res, w, density_ratio);
+}
+
+// One orientation constraint's scaled residuals and Jacobian [m][6]
+// (d/d instance rotation, d/d rig camera rotation); returns m.
+extern "C" int oracle_orientation_residual(int kind, const double* target, double std_dev, const double* ri,
+                                           const double* rc, double* r, double* J) {
+  static const double zero[3] = {0, 0, 0};
+  D6 d[3];
+  const int m = orientation_residual(kind, target, std_dev, ri, rc ? rc : zero, d);
+  for (int q = 0; q < m; ++q) {
+    r[q] = d[q].v;
+    for (int k = 0; k < 6; ++k) J[6 * q + k] = d[q].d[k];
+  }
+  return m;
 }
 
 extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, OracleResult* out) {

@@ -99,9 +99,23 @@ def test_density_ratio_settings(ba):
 
 def test_unsupported_constraints_raise(ba):
     with pytest.raises(NotImplementedError):
-        ba.add_absolute_up_vector("1", np.array([0, -1, 0]), 1)
+        ba.add_relative_rotation("a", "b", np.zeros(3))
     with pytest.raises(NotImplementedError):
         ba.add_linear_motion("a", "b", "c", 0.5, 1, 1)
+
+
+def test_orientation_constraint_on_unknown_shot_is_index_error(ba):
+    # the reference looks the shot up with shots_.at() when Run adds the
+    # block (bundle_adjuster.cc:1013-1082); here the lookup is at add time
+    with pytest.raises(IndexError):
+        ba.add_absolute_up_vector("1", np.array([0, -1, 0]), 1)
+    ba.add_rig_instance("1", pygeometry.Pose(), {"s1": "cam1"}, {"s1": "rig_cam1"}, False)
+    ba.add_absolute_up_vector("s1", np.array([0, -1, 0]), 1)
+    ba.add_absolute_pan("s1", 0.1, 1)
+    ba.add_absolute_tilt("s1", 0.1, 1)
+    ba.add_absolute_roll("s1", 0.1, 1)
+    with pytest.raises(IndexError):
+        ba.add_absolute_roll("s2", 0.1, 1)
 
 
 def test_camera_factories_parameter_order():
