@@ -267,6 +267,42 @@ int gbba_add_absolute_roll(gbba_adjuster_t* h, const char* shot_id, double angle
 int gbba_orientation_residual(int kind, const double* target, double std_deviation,
                               const double* instance_rotation, const double* camera_rotation, double* residuals,
                               double* jacobian, int* n_residuals);
+/* Constraints between shots, evaluated on the host in FP64 like the
+ * orientation constraints.  Unknown shots are GBBA_ERR_OUT_OF_RANGE when the
+ * constraint is added.
+ *   AddRelativeRotation (bundle_adjuster.cc:307-309, added at :912-956):
+ *     residual scale_matrix * log(R_ij R_i^T R_j) (RelativeRotationError,
+ *     relative_motion_errors.h:66-94); scale_matrix row-major 3 x 3, NULL
+ *     for the identity; under the relative-motion loss, IRLS group ROT.
+ *   AddCommonPosition (bundle_adjuster.cc:311-320, :958-999): the two shot
+ *     positions agree, horizontally within `margin`
+ *     (CommonPositionError, relative_motion_errors.h:96-126); TukeyLoss(1),
+ *     group POS.
+ *   AddLinearMotion (bundle_adjuster.cc:503-514, :1080-1138): shot1 at
+ *     fraction alpha between shot0 and shot2 in position and rotation
+ *     (LinearMotionError, motion_prior_errors.h:12-74); CauchyLoss(1),
+ *     group MOTION.
+ * SetRelativeMotionLossFunction (bundle_adjuster.cc:396-400): the loss of
+ * the relative rotations; an unknown name fails the run that needs it. */
+int gbba_add_relative_rotation(gbba_adjuster_t* h, const char* shot_i, const char* shot_j, const double* rotation,
+                               const double* scale_matrix);
+int gbba_add_common_position(gbba_adjuster_t* h, const char* shot_i, const char* shot_j, double margin,
+                             double std_deviation);
+int gbba_add_linear_motion(gbba_adjuster_t* h, const char* shot0, const char* shot1, const char* shot2,
+                           double alpha, double position_std_deviation, double orientation_std_deviation);
+int gbba_set_relative_motion_loss_function(gbba_adjuster_t* h, const char* name, double threshold);
+/* The scaled residuals (before the loss) of one constraint between shots
+ * and their Jacobian.  kind 0 relative rotation (params: rotation[3], then
+ * the row-major scale matrix [9]), 1 common position (params: margin,
+ * std_deviation), 2 linear motion (params: alpha, position std, orientation
+ * std).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
+ * cameras) for the n = 2 (3 for linear motion) shots, [rx ry rz tx ty tz]
+ * with t the position.  Writes m = 3 (6 for linear motion) residuals, J[m][36]
+ * (12 columns per shot: instance rotation, instance position, rig camera
+ * rotation, rig camera position) and m to *n_residuals.  Host arithmetic
+ * only. */
+int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
+                           const double* params, double* residuals, double* jacobian, int* n_residuals);
 /* AddPointPrior (bundle_adjuster.cc:260-272). */
 int gbba_add_point_prior(gbba_adjuster_t* h, const char* id, const double* position, const double* std_dev,
                          int has_altitude);

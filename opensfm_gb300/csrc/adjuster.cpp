@@ -347,6 +347,55 @@ void BundleAdjuster::AddOrientationConstraint(const std::string& shot_id, int ki
   orientations_.push_back(o);
 }
 
+void BundleAdjuster::AddRelativeRotation(const std::string& shot_i, const std::string& shot_j,
+                                         const double* rotation, const double* scale_matrix) {
+  PendingRelative r{};
+  r.kind = RelativeTerm::kRelativeRotation;
+  r.shots[0] = shot_i;
+  r.shots[1] = shot_j;
+  for (int k = 0; k < 3; ++k) r.rotation[k] = rotation[k];
+  for (int k = 0; k < 9; ++k) r.scale_matrix[k] = scale_matrix ? scale_matrix[k] : (k % 4 == 0 ? 1.0 : 0.0);
+  for (int k = 0; k < 2; ++k)
+    if (shot_index_.find(r.shots[k]) == shot_index_.end())
+      throw std::out_of_range("Shot " + r.shots[k] + " doesn't exist.");
+  relatives_.push_back(r);
+}
+
+void BundleAdjuster::AddCommonPosition(const std::string& shot_i, const std::string& shot_j, double margin,
+                                       double std_deviation) {
+  PendingRelative r{};
+  r.kind = RelativeTerm::kCommonPosition;
+  r.shots[0] = shot_i;
+  r.shots[1] = shot_j;
+  r.margin = margin;
+  r.std_deviation = std_deviation;
+  for (int k = 0; k < 2; ++k)
+    if (shot_index_.find(r.shots[k]) == shot_index_.end())
+      throw std::out_of_range("Shot " + r.shots[k] + " doesn't exist.");
+  relatives_.push_back(r);
+}
+
+void BundleAdjuster::AddLinearMotion(const std::string& shot0, const std::string& shot1, const std::string& shot2,
+                                     double alpha, double position_std_deviation, double orientation_std_deviation) {
+  PendingRelative r{};
+  r.kind = RelativeTerm::kLinearMotion;
+  r.shots[0] = shot0;
+  r.shots[1] = shot1;
+  r.shots[2] = shot2;
+  r.alpha = alpha;
+  r.position_std = position_std_deviation;
+  r.orientation_std = orientation_std_deviation;
+  for (int k = 0; k < 3; ++k)
+    if (shot_index_.find(r.shots[k]) == shot_index_.end())
+      throw std::out_of_range("Shot " + r.shots[k] + " doesn't exist.");
+  relatives_.push_back(r);
+}
+
+void BundleAdjuster::SetRelativeMotionLossFunction(const std::string& name, double threshold) {
+  relative_loss_name_ = name;
+  relative_loss_threshold_ = threshold;
+}
+
 void BundleAdjuster::PrepareRun() {
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
@@ -393,8 +442,49 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
-  static const char* kOrientationGroups[4] = {"UP", "PAN", "TILT", "ROLL"};
-  for (int k = 0; k < 4; ++k) problem_.ratio_orientation[k] = GetGroupDensityRatio(kOrientationGroups[k]);
+  static const char* kHostGroups[7] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION"};
+  for (int k = 0; k < 7; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
+  // constraints between shots, composed with the rig cameras that are
+  // optimised or not the identity (IsRigCameraUseful), as Run passes them
+  // (bundle_adjuster.cc:912-1138)
+  problem_.relative_terms.clear();
+  bool any_rotation = false;
+  for (const PendingRelative& p : relatives_) {
+    RelativeTerm t;
+    t.kind = p.kind;
+    t.n_shots = p.kind == RelativeTerm::kLinearMotion ? 3 : 2;
+    int rc[3] = {-1, -1, -1};
+    for (int k = 0; k < t.n_shots; ++k) {
+      const Shot& sh = problem_.shots[shot_index_.at(p.shots[k])];
+      t.instance[k] = sh.instance;
+      rc[k] = sh.rig_camera >= 0 && problem_.rig_cameras[sh.rig_camera].used ? sh.rig_camera : -1;
+      t.rig_camera[k] = rc[k];
+    }
+    if (p.kind == RelativeTerm::kLinearMotion && rc[2] >= 0 && (rc[2] == rc[0] || rc[2] == rc[1]))
+      t.rig_camera[2] = rc[0];  // LinearMotionError reads shot 0's rig camera then (bundle_adjuster.cc:1124-1134)
+    for (int k = 0; k < 3; ++k) t.rotation[k] = p.rotation[k];
+    for (int k = 0; k < 9; ++k) t.scale_matrix[k] = p.scale_matrix[k];
+    t.margin = p.margin;
+    t.scale = 1.0 / p.std_deviation;
+    t.alpha = p.alpha;
+    t.position_scale = 1.0 / p.position_std;
+    t.orientation_scale = 1.0 / p.orientation_std;
+    any_rotation |= p.kind == RelativeTerm::kRelativeRotation;
+    problem_.relative_terms.push_back(t);
+  }
+  if (any_rotation) {
+    // CreateLossFunction (bundle_adjuster.cc:485-499)
+    const std::string& n = relative_loss_name_;
+    int loss;
+    if (n == "TrivialLoss") loss = kLossTrivial;
+    else if (n == "HuberLoss") loss = kLossHuber;
+    else if (n == "SoftLOneLoss") loss = kLossSoftLOne;
+    else if (n == "CauchyLoss") loss = kLossCauchy;
+    else if (n == "ArctanLoss") loss = kLossArctan;
+    else throw std::runtime_error("ceres::LossFunction with name " + n + " not found.");
+    problem_.relative_loss = loss;
+    problem_.relative_loss_threshold = relative_loss_threshold_;
+  }
 }
 
 int BundleAdjuster::GetCamera(const std::string& id, int* model, double* values, int cap) const {

@@ -34,6 +34,18 @@ class BundleAdjuster {
   // kRoll (value[0] = angle).  Constraints with std_deviation <= 0 are kept
   // and ignored, as the reference adds only positive ones.
   void AddOrientationConstraint(const std::string& shot_id, int kind, const double* value, double std_deviation);
+  // Constraints between shots (bundle_adjuster.cc:303-320, 503-514): a
+  // relative rotation R_ij with a 3 x 3 scale matrix (null: identity), a
+  // common position within a horizontal margin, and linear motion of shot1
+  // between shot0 and shot2 at fraction alpha.
+  void AddRelativeRotation(const std::string& shot_i, const std::string& shot_j, const double* rotation,
+                           const double* scale_matrix);
+  void AddCommonPosition(const std::string& shot_i, const std::string& shot_j, double margin, double std_deviation);
+  void AddLinearMotion(const std::string& shot0, const std::string& shot1, const std::string& shot2, double alpha,
+                       double position_std_deviation, double orientation_std_deviation);
+  // the loss of the relative rotations (SetRelativeMotionLossFunction,
+  // bundle_adjuster.cc:396-400); the name is checked when a run needs it
+  void SetRelativeMotionLossFunction(const std::string& name, double threshold);
   void AddPointProjectionObservation(const std::string& shot, const std::string& point, const double* obs,
                                      double std_dev, bool is_gcp);
   // index-based adders (the raw-pointer path of AddPointProjectionObservationRaw)
@@ -127,6 +139,16 @@ class BundleAdjuster {
     double std_deviation;
   };
   std::vector<PendingOrientation> orientations_;
+  struct PendingRelative {
+    int kind;
+    std::string shots[3];
+    double rotation[3];
+    double scale_matrix[9];
+    double margin, std_deviation, alpha, position_std, orientation_std;
+  };
+  std::vector<PendingRelative> relatives_;
+  std::string relative_loss_name_ = "CauchyLoss";
+  double relative_loss_threshold_ = 1.0;
   std::string loss_name_ = "TrivialLoss";
   SolveSummary summary_;
   std::vector<double> errors_, weights_;

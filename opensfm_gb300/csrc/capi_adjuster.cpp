@@ -154,6 +154,66 @@ int gbba_orientation_residual(int kind, const double* target, double std_deviati
   });
 }
 
+int gbba_add_relative_rotation(gbba_adjuster_t* h, const char* shot_i, const char* shot_j, const double* rotation,
+                               const double* scale_matrix) {
+  return guarded([&] {
+    need(rotation, "rotation");
+    ba_of(h).AddRelativeRotation(str(shot_i), str(shot_j), rotation, scale_matrix);
+  });
+}
+
+int gbba_add_common_position(gbba_adjuster_t* h, const char* shot_i, const char* shot_j, double margin,
+                             double std_deviation) {
+  return guarded([&] { ba_of(h).AddCommonPosition(str(shot_i), str(shot_j), margin, std_deviation); });
+}
+
+int gbba_add_linear_motion(gbba_adjuster_t* h, const char* shot0, const char* shot1, const char* shot2,
+                           double alpha, double position_std_deviation, double orientation_std_deviation) {
+  return guarded([&] {
+    ba_of(h).AddLinearMotion(str(shot0), str(shot1), str(shot2), alpha, position_std_deviation,
+                             orientation_std_deviation);
+  });
+}
+
+int gbba_set_relative_motion_loss_function(gbba_adjuster_t* h, const char* name, double threshold) {
+  return guarded([&] { ba_of(h).SetRelativeMotionLossFunction(str(name), threshold); });
+}
+
+int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
+                           const double* params, double* residuals, double* jacobian, int* n_residuals) {
+  return guarded([&] {
+    if (kind < 0 || kind > 2 || !instance_poses || !params || !residuals || !jacobian || !n_residuals)
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_relative_residual: invalid argument");
+    gbba::RelativeTerm t;
+    t.kind = kind;
+    t.n_shots = kind == gbba::RelativeTerm::kLinearMotion ? 3 : 2;
+    if (kind == gbba::RelativeTerm::kRelativeRotation) {
+      for (int k = 0; k < 3; ++k) t.rotation[k] = params[k];
+      for (int k = 0; k < 9; ++k) t.scale_matrix[k] = params[3 + k];
+    } else if (kind == gbba::RelativeTerm::kCommonPosition) {
+      t.margin = params[0];
+      t.scale = 1.0 / params[1];
+    } else {
+      t.alpha = params[0];
+      t.position_scale = 1.0 / params[1];
+      t.orientation_scale = 1.0 / params[2];
+    }
+    const double* pi[3] = {nullptr, nullptr, nullptr};
+    const double* pc[3] = {nullptr, nullptr, nullptr};
+    for (int k = 0; k < t.n_shots; ++k) {
+      pi[k] = instance_poses + 6 * k;
+      pc[k] = rig_camera_poses ? rig_camera_poses + 6 * k : nullptr;
+    }
+    gbba::orient::Dual<36> r[6];
+    const int m = gbba::orient::relative_residuals<36>(t, pi, pc, r);
+    for (int q = 0; q < m; ++q) {
+      residuals[q] = r[q].v;
+      for (int k = 0; k < 36; ++k) jacobian[36 * q + k] = r[q].d[k];
+    }
+    *n_residuals = m;
+  });
+}
+
 static int add_angle(gbba_adjuster_t* h, const char* shot_id, int kind, double angle, double std_deviation) {
   return guarded([&] { ba_of(h).AddOrientationConstraint(str(shot_id), kind, &angle, std_deviation); });
 }

@@ -1,13 +1,28 @@
-// Absolute orientation constraints of a shot: up vector, pan, tilt and roll
-// (bundle/error/absolute_motion_errors.h: UpVectorError, PanAngleError,
-// TiltAngleError, RollAngleError), each under CauchyLoss(1) as
-// BundleAdjuster::Run adds them (bundle_adjuster.cc:1013-1082).  They depend
-// on the shot rotation, the rig instance rotation composed with the rig
-// camera rotation (position_functors.h:40-63).  A handful of residuals per
-// shot: evaluated on the host in FP64, with the Jacobian w.r.t. the two
-// rotations from forward-mode dual numbers.
+// Host constraint terms on shot poses, evaluated in FP64 with forward-mode
+// dual numbers: a handful of residuals per constrained shot (or pair or
+// triple of shots), far too few to be worth a kernel.  The solver adds
+// their Gauss-Newton blocks to the camera-side system on the device.
+//
+//   absolute orientation  UpVectorError, PanAngleError, TiltAngleError,
+//                         RollAngleError (bundle/error/absolute_motion_errors.h:
+//                         10-126) under CauchyLoss(1) (bundle_adjuster.cc:
+//                         1011-1082); derivatives w.r.t. the rig instance and
+//                         rig camera rotations.
+//   relative rotation     RelativeRotationError (relative_motion_errors.h:
+//                         66-94) under the relative-motion loss
+//                         (bundle_adjuster.cc:912-956).
+//   common position       CommonPositionError (relative_motion_errors.h:
+//                         96-126) under TukeyLoss(1) (bundle_adjuster.cc:
+//                         958-999).
+//   linear motion         LinearMotionError (motion_prior_errors.h:12-74)
+//                         under CauchyLoss(1) (bundle_adjuster.cc:1080-1138).
+//
+// Shot rotation and position compose the rig instance with the rig camera
+// as ShotRotationFunctor / ShotPositionFunctor do (position_functors.h:
+// 12-63).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <limits>
 
@@ -17,139 +32,181 @@ struct OrientationTerm {
   enum Kind { kUpVector = 0, kPan = 1, kTilt = 2, kRoll = 3 };
   int kind = kUpVector;
   int instance = 0;
-  int rig_camera = -1;         // the shot's rig camera (-1: none)
+  int rig_camera = -1;           // the shot's rig camera (-1: none)
   double target[3] = {0, 0, 0};  // up vector: the direction (normalized here); angles: target[0]
-  double scale = 1.0;          // 1 / std deviation
+  double scale = 1.0;            // 1 / std deviation
+};
+
+// Constraints between two or three shots.  Each shot contributes 12
+// derivative slots: instance rotation (0..2), instance position (3..5), rig
+// camera rotation (6..8), rig camera position (9..11).
+struct RelativeTerm {
+  enum Kind { kRelativeRotation = 0, kCommonPosition = 1, kLinearMotion = 2 };
+  int kind = kRelativeRotation;
+  int n_shots = 2;
+  int instance[3] = {0, 0, 0};
+  int rig_camera[3] = {-1, -1, -1};  // the rig camera used in the composition (-1: none)
+  double rotation[3] = {0, 0, 0};    // relative rotation R_ij
+  double scale_matrix[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  double margin = 0.0, scale = 1.0;  // common position: margin, 1 / std
+  double alpha = 0.0, position_scale = 1.0, orientation_scale = 1.0;  // linear motion
 };
 
 namespace orient {
 
-// Value and derivatives w.r.t. the instance rotation (0..2) and the rig
-// camera rotation (3..5).
-constexpr int kN = 6;
-struct D {
+// Value and derivatives w.r.t. N parameters.
+template <int N>
+struct Dual {
   double v = 0.0;
-  double d[kN] = {0, 0, 0, 0, 0, 0};
-  D() = default;
-  D(double x) : v(x) {}  // NOLINT: constants promote implicitly
+  double d[N] = {};
+  Dual() = default;
+  Dual(double x) : v(x) {}  // NOLINT: constants promote implicitly
 };
-inline D var(double x, int k) {
-  D r(x);
+template <int N>
+inline Dual<N> var(double x, int k) {
+  Dual<N> r(x);
   r.d[k] = 1.0;
   return r;
 }
-inline D operator+(const D& a, const D& b) {
-  D r(a.v + b.v);
-  for (int k = 0; k < kN; ++k) r.d[k] = a.d[k] + b.d[k];
+template <int N>
+inline Dual<N> operator+(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v + b.v);
+  for (int k = 0; k < N; ++k) r.d[k] = a.d[k] + b.d[k];
   return r;
 }
-inline D operator-(const D& a, const D& b) {
-  D r(a.v - b.v);
-  for (int k = 0; k < kN; ++k) r.d[k] = a.d[k] - b.d[k];
+template <int N>
+inline Dual<N> operator-(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v - b.v);
+  for (int k = 0; k < N; ++k) r.d[k] = a.d[k] - b.d[k];
   return r;
 }
-inline D operator-(const D& a) {
-  D r(-a.v);
-  for (int k = 0; k < kN; ++k) r.d[k] = -a.d[k];
+template <int N>
+inline Dual<N> operator-(const Dual<N>& a) {
+  Dual<N> r(-a.v);
+  for (int k = 0; k < N; ++k) r.d[k] = -a.d[k];
   return r;
 }
-inline D operator*(const D& a, const D& b) {
-  D r(a.v * b.v);
-  for (int k = 0; k < kN; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+template <int N>
+inline Dual<N> operator*(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v * b.v);
+  for (int k = 0; k < N; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
   return r;
 }
-inline D operator/(const D& a, const D& b) {
-  D r(a.v / b.v);
-  for (int k = 0; k < kN; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+template <int N>
+inline Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r(a.v / b.v);
+  for (int k = 0; k < N; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
   return r;
 }
 // f(a) with f'(a) = df
-inline D chain(const D& a, double f, double df) {
-  D r(f);
-  for (int k = 0; k < kN; ++k) r.d[k] = df * a.d[k];
+template <int N>
+inline Dual<N> chain(const Dual<N>& a, double f, double df) {
+  Dual<N> r(f);
+  for (int k = 0; k < N; ++k) r.d[k] = df * a.d[k];
   return r;
 }
-inline D sqrt(const D& a) {
+template <int N>
+inline Dual<N> sqrt(const Dual<N>& a) {
   const double s = std::sqrt(a.v);
   return chain(a, s, s > 0.0 ? 0.5 / s : 0.0);
 }
-inline D sin(const D& a) { return chain(a, std::sin(a.v), std::cos(a.v)); }
-inline D cos(const D& a) { return chain(a, std::cos(a.v), -std::sin(a.v)); }
-inline D asin(const D& a) { return chain(a, std::asin(a.v), 1.0 / std::sqrt(1.0 - a.v * a.v)); }
-inline D atan2(const D& y, const D& x) {
+template <int N>
+inline Dual<N> sin(const Dual<N>& a) { return chain(a, std::sin(a.v), std::cos(a.v)); }
+template <int N>
+inline Dual<N> cos(const Dual<N>& a) { return chain(a, std::cos(a.v), -std::sin(a.v)); }
+template <int N>
+inline Dual<N> asin(const Dual<N>& a) { return chain(a, std::asin(a.v), 1.0 / std::sqrt(1.0 - a.v * a.v)); }
+template <int N>
+inline Dual<N> abs(const Dual<N>& a) { return a.v < 0.0 ? -a : a; }
+template <int N>
+inline Dual<N> atan2(const Dual<N>& y, const Dual<N>& x) {
   // d atan2(y, x) = (x dy - y dx) / (x^2 + y^2)
   const double den = x.v * x.v + y.v * y.v;
-  D r(std::atan2(y.v, x.v));
-  for (int k = 0; k < kN; ++k) r.d[k] = den > 0.0 ? (x.v * y.d[k] - y.v * x.d[k]) / den : 0.0;
+  Dual<N> r(std::atan2(y.v, x.v));
+  for (int k = 0; k < N; ++k) r.d[k] = den > 0.0 ? (x.v * y.d[k] - y.v * x.d[k]) / den : 0.0;
   return r;
 }
 
 // Rotations as angle-axis vectors; quaternions scalar first.
-inline void aa_to_quat(const D* a, D* q) {
-  const D t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+template <int N>
+inline void aa_to_quat(const Dual<N>* a, Dual<N>* q) {
+  const Dual<N> t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
   if (t2.v > 0.0) {
-    const D t = sqrt(t2);
-    const D h = t * D(0.5);
-    const D k = sin(h) / t;
+    const Dual<N> t = sqrt(t2);
+    const Dual<N> h = t * Dual<N>(0.5);
+    const Dual<N> k = sin(h) / t;
     q[0] = cos(h);
     for (int i = 0; i < 3; ++i) q[1 + i] = a[i] * k;
   } else {
-    q[0] = D(1.0);
-    for (int i = 0; i < 3; ++i) q[1 + i] = a[i] * D(0.5);
+    q[0] = Dual<N>(1.0);
+    for (int i = 0; i < 3; ++i) q[1 + i] = a[i] * Dual<N>(0.5);
   }
 }
-inline void quat_mul(const D* a, const D* b, D* r) {
+template <int N>
+inline void quat_mul(const Dual<N>* a, const Dual<N>* b, Dual<N>* r) {
   r[0] = a[0] * b[0] - a[1] * b[1] - a[2] * b[2] - a[3] * b[3];
   r[1] = a[0] * b[1] + a[1] * b[0] + a[2] * b[3] - a[3] * b[2];
   r[2] = a[0] * b[2] - a[1] * b[3] + a[2] * b[0] + a[3] * b[1];
   r[3] = a[0] * b[3] + a[1] * b[2] - a[2] * b[1] + a[3] * b[0];
 }
-inline void quat_to_aa(const D* q, D* a) {
-  const D s2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
-  D k(2.0);
+template <int N>
+inline void quat_to_aa(const Dual<N>* q, Dual<N>* a) {
+  const Dual<N> s2 = q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+  Dual<N> k(2.0);
   if (s2.v > 0.0) {
-    const D s = sqrt(s2);
+    const Dual<N> s = sqrt(s2);
     // the angle of the shorter rotation
-    const D two_theta = q[0].v < 0.0 ? D(2.0) * atan2(-s, -q[0]) : D(2.0) * atan2(s, q[0]);
+    const Dual<N> two_theta = q[0].v < 0.0 ? Dual<N>(2.0) * atan2(-s, -q[0]) : Dual<N>(2.0) * atan2(s, q[0]);
     k = two_theta / s;
   }
   for (int i = 0; i < 3; ++i) a[i] = q[1 + i] * k;
 }
+// the angle-axis of R(a) R(b) (MultRotations, error_utils.h:14-24)
+template <int N>
+inline void compose(const Dual<N>* a, const Dual<N>* b, Dual<N>* out) {
+  Dual<N> qa[4], qb[4], q[4];
+  aa_to_quat(a, qa);
+  aa_to_quat(b, qb);
+  quat_mul(qa, qb, q);
+  quat_to_aa(q, out);
+}
 // R(a) p by the Rodrigues formula (first order for tiny angles)
-inline void rotate(const D* a, const D* p, D* out) {
-  const D t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+template <int N>
+inline void rotate(const Dual<N>* a, const Dual<N>* p, Dual<N>* out) {
+  const Dual<N> t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
   if (t2.v > std::numeric_limits<double>::epsilon()) {
-    const D t = sqrt(t2);
-    const D c = cos(t), s = sin(t);
-    const D w[3] = {a[0] / t, a[1] / t, a[2] / t};
-    const D wxp[3] = {w[1] * p[2] - w[2] * p[1], w[2] * p[0] - w[0] * p[2], w[0] * p[1] - w[1] * p[0]};
-    const D wp = w[0] * p[0] + w[1] * p[1] + w[2] * p[2];
-    const D f = wp * (D(1.0) - c);
+    const Dual<N> t = sqrt(t2);
+    const Dual<N> c = cos(t), s = sin(t);
+    const Dual<N> w[3] = {a[0] / t, a[1] / t, a[2] / t};
+    const Dual<N> wxp[3] = {w[1] * p[2] - w[2] * p[1], w[2] * p[0] - w[0] * p[2], w[0] * p[1] - w[1] * p[0]};
+    const Dual<N> wp = w[0] * p[0] + w[1] * p[1] + w[2] * p[2];
+    const Dual<N> f = wp * (Dual<N>(1.0) - c);
     for (int i = 0; i < 3; ++i) out[i] = p[i] * c + wxp[i] * s + w[i] * f;
   } else {
-    const D axp[3] = {a[1] * p[2] - a[2] * p[1], a[2] * p[0] - a[0] * p[2], a[0] * p[1] - a[1] * p[0]};
+    const Dual<N> axp[3] = {a[1] * p[2] - a[2] * p[1], a[2] * p[0] - a[0] * p[2], a[0] * p[1] - a[1] * p[0]};
     for (int i = 0; i < 3; ++i) out[i] = p[i] + axp[i];
   }
 }
-inline D angle_diff(const D& a, double b) {
-  const D d = a - D(b);
-  if (d.v > M_PI) return d - D(2 * M_PI);
-  if (d.v < -M_PI) return d + D(2 * M_PI);
+template <int N>
+inline Dual<N> angle_diff(const Dual<N>& a, double b) {
+  const Dual<N> d = a - Dual<N>(b);
+  if (d.v > M_PI) return d - Dual<N>(2 * M_PI);
+  if (d.v < -M_PI) return d + Dual<N>(2 * M_PI);
   return d;
 }
+
+// ---- absolute orientation: 6 slots (instance rotation, rig camera rotation)
+using D = Dual<6>;
 
 // Residuals of a term (1 or 3) at instance rotation ri and rig camera
 // rotation rc; returns the count.
 inline int residuals(const OrientationTerm& t, const double* ri, const double* rc, D* r) {
-  D a[3], b[3], qa[4], qb[4], q[4], R[3];
+  D a[3], b[3], R[3];
   for (int k = 0; k < 3; ++k) {
-    a[k] = var(ri[k], k);
-    b[k] = var(rc ? rc[k] : 0.0, 3 + k);
+    a[k] = var<6>(ri[k], k);
+    b[k] = var<6>(rc ? rc[k] : 0.0, 3 + k);
   }
-  aa_to_quat(a, qa);
-  aa_to_quat(b, qb);
-  quat_mul(qa, qb, q);
-  quat_to_aa(q, R);
+  compose(a, b, R);
   const D ex[3] = {D(1.0), D(0.0), D(0.0)};
   const D ez[3] = {D(0.0), D(0.0), D(1.0)};
   switch (t.kind) {
@@ -199,17 +256,184 @@ inline int residuals(const OrientationTerm& t, const double* ri, const double* r
   }
 }
 
-// Cauchy loss (a = 1) times the IRLS weight w, with the Gauss-Newton
-// correction Ceres applies when rho'' < 0: residual and Jacobian scaled by
-// sqrt(w rho'(s)).  Returns w rho(s).
-inline double cauchy_correct(int m, D* r, double w = 1.0) {
+// ---- relative terms: 12 slots per shot
+template <int N>
+struct ShotPose {
+  Dual<N> rotation[3];  // the shot rotation (instance composed with rig camera)
+  Dual<N> position[3];  // the shot position
+};
+
+// pose of shot k from instance pose pi[6] and rig camera pose pc[6] (null:
+// no rig camera), with slots 12k .. 12k + 11
+template <int N>
+inline ShotPose<N> shot_pose(int k, const double* pi, const double* pc) {
+  ShotPose<N> s;
+  Dual<N> ri[3], ti[3];
+  for (int i = 0; i < 3; ++i) {
+    ri[i] = var<N>(pi[i], 12 * k + i);
+    ti[i] = var<N>(pi[3 + i], 12 * k + 3 + i);
+  }
+  if (!pc) {
+    for (int i = 0; i < 3; ++i) {
+      s.rotation[i] = ri[i];
+      s.position[i] = ti[i];
+    }
+    return s;
+  }
+  Dual<N> rc[3], tc[3], off[3];
+  for (int i = 0; i < 3; ++i) {
+    rc[i] = var<N>(pc[i], 12 * k + 6 + i);
+    tc[i] = var<N>(pc[3 + i], 12 * k + 9 + i);
+  }
+  compose(ri, rc, s.rotation);
+  rotate(ri, tc, off);
+  for (int i = 0; i < 3; ++i) s.position[i] = ti[i] + off[i];
+  return s;
+}
+
+// Scaled residuals (3 or 6) of a relative term from the shots' instance
+// and rig camera poses (pc[k] null: no rig camera); returns the count.
+template <int N>
+inline int relative_residuals(const RelativeTerm& t, const double* const* pi, const double* const* pc,
+                              Dual<N>* r) {
+  ShotPose<N> s[3];
+  for (int k = 0; k < t.n_shots; ++k) s[k] = shot_pose<N>(k, pi[k], pc[k]);
+  switch (t.kind) {
+    case RelativeTerm::kRelativeRotation: {
+      // log(R_ij R_i^T R_j), then the scale matrix
+      Dual<N> rij[3], neg[3], tmp[3], e[3];
+      for (int i = 0; i < 3; ++i) {
+        rij[i] = Dual<N>(t.rotation[i]);
+        neg[i] = -s[0].rotation[i];
+      }
+      compose(rij, neg, tmp);
+      compose(tmp, s[1].rotation, e);
+      for (int i = 0; i < 3; ++i)
+        r[i] = Dual<N>(t.scale_matrix[3 * i]) * e[0] + Dual<N>(t.scale_matrix[3 * i + 1]) * e[1] +
+               Dual<N>(t.scale_matrix[3 * i + 2]) * e[2];
+      return 3;
+    }
+    case RelativeTerm::kCommonPosition: {
+      for (int i = 0; i < 3; ++i) {
+        Dual<N> e = s[0].position[i] - s[1].position[i];
+        if (i < 2) {
+          e = abs(e) - Dual<N>(t.margin);
+          if (e.v < 0.0) e = Dual<N>(0.0);
+        }
+        r[i] = Dual<N>(t.scale) * e;
+      }
+      return 3;
+    }
+    default: {  // linear motion: shot 1 between shots 0 and 2 at fraction alpha
+      Dual<N> d20[3], d10[3];
+      for (int i = 0; i < 3; ++i) {
+        d20[i] = s[2].position[i] - s[0].position[i];
+        d10[i] = s[1].position[i] - s[0].position[i];
+      }
+      const Dual<N> n20 = sqrt(d20[0] * d20[0] + d20[1] * d20[1] + d20[2] * d20[2]);
+      const Dual<N> n10 = sqrt(d10[0] * d10[0] + d10[1] * d10[1] + d10[2] * d10[2]);
+      for (int i = 0; i < 3; ++i) {
+        if (n20.v > 1e-15) r[i] = Dual<N>(t.position_scale) * (Dual<N>(t.alpha) - n10 / n20);
+        else r[i] = Dual<N>(t.position_scale) * (Dual<N>(t.alpha) * d20[i] - d10[i]);
+      }
+      Dual<N> neg0[3], neg1[3], a[3], b[3], e[3];
+      for (int i = 0; i < 3; ++i) {
+        neg0[i] = -s[0].rotation[i];
+        neg1[i] = -s[1].rotation[i];
+      }
+      compose(s[2].rotation, neg0, a);
+      for (int i = 0; i < 3; ++i) a[i] = Dual<N>(t.alpha) * a[i];
+      compose(s[0].rotation, neg1, b);
+      compose(a, b, e);
+      for (int i = 0; i < 3; ++i) r[3 + i] = Dual<N>(t.orientation_scale) * e[i];
+      return 6;
+    }
+  }
+}
+
+// ---- losses
+// rho(s) and its derivatives for the loss kinds of the projection loss
+// (0 trivial, 1 Huber, 2 soft-L1, 3 Cauchy, 4 arctan) and 5 Tukey, scale a
+// (Ceres' documented definitions).
+inline void loss_rho(int kind, double a, double s, double* rho) {
+  const double b = a * a;
+  switch (kind) {
+    case 1:
+      if (s > b) {
+        const double r = std::sqrt(s);
+        rho[0] = 2.0 * a * r - b;
+        rho[1] = std::max(std::numeric_limits<double>::min(), a / r);
+        rho[2] = -rho[1] / (2.0 * s);
+      } else {
+        rho[0] = s, rho[1] = 1.0, rho[2] = 0.0;
+      }
+      return;
+    case 2: {
+      const double sum = 1.0 + s / b, tmp = std::sqrt(sum);
+      rho[0] = 2.0 * b * (tmp - 1.0);
+      rho[1] = std::max(std::numeric_limits<double>::min(), 1.0 / tmp);
+      rho[2] = -(0.5 / b) * rho[1] / sum;
+      return;
+    }
+    case 3: {
+      const double sum = 1.0 + s / b, inv = 1.0 / sum;
+      rho[0] = b * std::log1p(s / b);
+      rho[1] = std::max(std::numeric_limits<double>::min(), inv);
+      rho[2] = -inv * inv / b;
+      return;
+    }
+    case 4: {
+      const double inv = 1.0 / (b + s * s);
+      rho[0] = a * std::atan2(s, a);
+      rho[1] = std::max(std::numeric_limits<double>::min(), b * inv);
+      rho[2] = -2.0 * s * b * inv * inv;
+      return;
+    }
+    case 5:
+      if (s <= b) {
+        const double v = 1.0 - s / b;
+        rho[0] = b / 3.0 * (1.0 - v * v * v);
+        rho[1] = v * v;
+        rho[2] = -2.0 * v / b;
+      } else {
+        rho[0] = b / 3.0, rho[1] = 0.0, rho[2] = 0.0;
+      }
+      return;
+    default:
+      rho[0] = s, rho[1] = 1.0, rho[2] = 0.0;
+  }
+}
+
+// Loss times the IRLS weight w with the residual/Jacobian correction Ceres
+// applies (Triggs et al.): r <- sqrt(rho') r / (1 - alpha), J <- sqrt(rho')
+// (J - alpha r r^T J / |r|^2), alpha from rho''; alpha = 0 when rho'' <= 0.
+// Returns w rho(|r|^2).
+template <int N>
+inline double loss_correct(int kind, double a, int m, Dual<N>* r, double w = 1.0) {
   double s = 0.0;
   for (int q = 0; q < m; ++q) s += r[q].v * r[q].v;
-  const double rho = std::log1p(s);
-  const double sq = std::sqrt(w / (1.0 + s));
-  for (int q = 0; q < m; ++q) r[q] = r[q] * D(sq);
-  return w * rho;
+  double rho[3];
+  loss_rho(kind, a, s, rho);
+  for (double& v : rho) v *= w;
+  const double sq1 = std::sqrt(rho[1]);
+  double rscale = sq1, alpha_s = 0.0;
+  if (s > 0.0 && rho[2] > 0.0) {
+    const double alpha = 1.0 - std::sqrt(1.0 + 2.0 * s * rho[2] / rho[1]);
+    rscale = sq1 / (1.0 - alpha);
+    alpha_s = alpha / s;
+  }
+  for (int k = 0; k < N; ++k) {
+    double rj = 0.0;
+    for (int q = 0; q < m; ++q) rj += r[q].v * r[q].d[k];
+    for (int q = 0; q < m; ++q) r[q].d[k] = sq1 * (r[q].d[k] - alpha_s * r[q].v * rj);
+  }
+  for (int q = 0; q < m; ++q) r[q].v *= rscale;
+  return rho[0];
 }
+
+// Cauchy loss (a = 1) times the IRLS weight w, the loss of the orientation
+// constraints.  Returns w rho(s).
+inline double cauchy_correct(int m, D* r, double w = 1.0) { return loss_correct<6>(3, 1.0, m, r, w); }
 
 }  // namespace orient
 }  // namespace gbba

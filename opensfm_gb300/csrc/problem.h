@@ -113,11 +113,14 @@ struct Problem {
   std::vector<Observation> observations;
   // absolute orientation constraints (up vector, pan, tilt, roll)
   std::vector<OrientationTerm> orientation_terms;
+  std::vector<RelativeTerm> relative_terms;
+  int relative_loss = 3;  // loss of the relative rotations (kinds as the projection loss), scale below
+  double relative_loss_threshold = 1.0;
   // IRLS density ratios: one per projection group (shot groups "PROJ_<shot>"
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
   double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
-  double ratio_orientation[4] = {1e-3, 1e-3, 1e-3, 1e-3};  // groups UP, PAN, TILT, ROLL
+  double ratio_host[7] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};  // UP, PAN, TILT, ROLL, ROT, POS, MOTION
 };
 
 // One LM iteration as reported by the solver.

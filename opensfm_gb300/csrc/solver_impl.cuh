@@ -533,6 +533,24 @@ void mixture_params(const std::vector<double>& cov_in, int k, double density_rat
   K = density_ratio / sq;
 }
 
+// One host constraint term linearized at a camera-side state: the residuals
+// and Jacobian after the loss correction (m rows, ns derivative slots), the
+// loss-free residuals the IRLS mixture reads, the free camera-side
+// coordinate of every slot (-1: fixed), and w rho(|r|^2).
+struct HostTermLin {
+  static constexpr int kMaxRows = 6, kMaxSlots = 36;
+  int m = 0, ns = 0;
+  double r[kMaxRows] = {}, raw[kMaxRows] = {};
+  double J[kMaxRows][kMaxSlots] = {};
+  int coord[kMaxSlots] = {};
+  double rho = 0.0;
+};
+
+// IRLS groups of the host constraint terms: UP, PAN, TILT, ROLL (by
+// orientation kind), ROT, POS, MOTION (by relative kind)
+constexpr int kHostGroups = 7;
+const char* const kHostGroupNames[kHostGroups] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION"};
+
 MixtureResult mixture_group(const std::vector<std::vector<double>>& res, std::vector<double>& weights,
                             double density_ratio) {
   MixtureResult out;
@@ -645,7 +663,10 @@ class DeviceSolver : public SolverBase {
     ++launches_;
   }
   double prior_model_change(const std::vector<double>& x, const std::vector<double>& dx);
-  int orientation_residuals(const OrientationTerm& t, const std::vector<double>& x, orient::D* r, int* coord) const;
+  // host constraint terms: the orientation terms, then the relative terms
+  int n_host_terms() const { return int(prob_->orientation_terms.size() + prob_->relative_terms.size()); }
+  int host_term_group(int q) const;
+  void host_term(int q, const std::vector<double>& x, HostTermLin& L) const;
   // ---- linear solve
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
   int run_pcg(const R* rhs, double bb, double tol, int max_it);
@@ -681,7 +702,7 @@ class DeviceSolver : public SolverBase {
   std::map<std::pair<int, int>, std::array<double, 64>> hblocks_;
   std::vector<double> hdiag_;
   int n_hblocks_ = 0;
-  std::vector<double> orient_weight_;  // IRLS weight of every orientation term
+  std::vector<double> host_weight_;  // IRLS weight of every host constraint term
   std::vector<int> group_count_, group_dim_;
   std::vector<double> group_ratio_;
   std::vector<double> prior_weight_cam_, prior_weight_rig_, prior_weight_gps_;
@@ -1101,7 +1122,7 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   for (int i = 0; i < n_inst_; ++i)
     if (P.instances[i].has_position_prior) gps_inst_.push_back(i);
   prior_weight_gps_.assign(gps_inst_.size(), 1.0);
-  orient_weight_.assign(P.orientation_terms.size(), 1.0);
+  host_weight_.assign(P.orientation_terms.size() + P.relative_terms.size(), 1.0);
   point_priors_.clear();
   for (int64_t p = 0; p < n_pt_; ++p) {
     const PointBlock& b = P.points[p];
@@ -1403,45 +1424,95 @@ double DeviceSolver<R>::prior_terms(const std::vector<double>& x, bool want_deri
       }
     }
   }
-  // absolute orientation constraints (Cauchy loss): J^T r and J^T J over the
-  // free rotation coordinates of the rig instance and rig camera
-  for (size_t q = 0; q < P.orientation_terms.size(); ++q) {
-    int coord[6];
-    orient::D r[3];
-    const int m = orientation_residuals(P.orientation_terms[q], x, r, coord);
-    cost += 0.5 * orient::cauchy_correct(m, r, orient_weight_[q]);
+  // host constraint terms: J^T r and J^T J over their free coordinates,
+  // as 8 x 8 blocks of the coordinate groups they couple
+  for (int q = 0; q < n_host_terms(); ++q) {
+    HostTermLin L;
+    host_term(q, x, L);
+    cost += 0.5 * L.rho;
     if (!want_derivs) continue;
-    for (int a = 0; a < 6; ++a) {
-      if (coord[a] < 0) continue;
+    for (int a = 0; a < L.ns; ++a) {
+      if (L.coord[a] < 0) continue;
       double g = 0.0;
-      for (int q = 0; q < m; ++q) g += r[q].d[a] * r[q].v;
-      pgrad_[coord[a]] += g;
-      for (int b = 0; b < 6; ++b) {
-        if (coord[b] < 0) continue;
+      for (int i = 0; i < L.m; ++i) g += L.J[i][a] * L.r[i];
+      pgrad_[L.coord[a]] += g;
+      for (int b = 0; b < L.ns; ++b) {
+        if (L.coord[b] < 0) continue;
         double h = 0.0;
-        for (int q = 0; q < m; ++q) h += r[q].d[a] * r[q].d[b];
-        const int ga = coord[a] & ~7, gb = coord[b] & ~7;
-        hblocks_[{ga, gb}][8 * (coord[a] - ga) + (coord[b] - gb)] += h;
-        if (a == b) hdiag_[coord[a]] += h;
+        for (int i = 0; i < L.m; ++i) h += L.J[i][a] * L.J[i][b];
+        const int ga = L.coord[a] & ~7, gb = L.coord[b] & ~7;
+        hblocks_[{ga, gb}][8 * (L.coord[a] - ga) + (L.coord[b] - gb)] += h;
+        if (L.coord[a] == L.coord[b]) hdiag_[L.coord[a]] += h;
       }
     }
   }
   return cost;
 }
 
-// Residuals of an orientation term at camera-side state x, with derivatives
-// w.r.t. the instance rotation (slots 0..2) and the rig camera rotation
-// (3..5); coord[] maps the slots to free camera-side coordinates (-1: fixed).
 template <typename R>
-int DeviceSolver<R>::orientation_residuals(const OrientationTerm& t, const std::vector<double>& x, orient::D* r,
-                                           int* coord) const {
-  const bool rig = t.rig_camera >= 0;
-  const int ib = 8 * t.instance, rb = rig ? cl_.rig_base + 8 * t.rig_camera : -1;
-  for (int k = 0; k < 3; ++k) {
-    coord[k] = cmask_[ib + k] ? ib + k : -1;
-    coord[3 + k] = (rig && cmask_[rb + k]) ? rb + k : -1;
+int DeviceSolver<R>::host_term_group(int q) const {
+  const int no = int(prob_->orientation_terms.size());
+  return q < no ? prob_->orientation_terms[q].kind : 4 + prob_->relative_terms[q - no].kind;
+}
+
+// Host term q at camera-side state x.  Orientation terms: slots 0..2 the
+// instance rotation, 3..5 the rig camera rotation.  Relative terms: 12
+// slots per shot (instance rotation, instance position, rig camera
+// rotation, rig camera position).  Slots of coordinates shared by several
+// shots map to the same coordinate and their derivatives add up.
+template <typename R>
+void DeviceSolver<R>::host_term(int q, const std::vector<double>& x, HostTermLin& L) const {
+  const Problem& P = *prob_;
+  const int no = int(P.orientation_terms.size());
+  const double w = host_weight_[q];
+  auto coord_of = [&](int j) { return cmask_[j] ? j : -1; };
+  if (q < no) {
+    const OrientationTerm& t = P.orientation_terms[q];
+    const bool rig = t.rig_camera >= 0;
+    const int ib = 8 * t.instance, rb = rig ? cl_.rig_base + 8 * t.rig_camera : -1;
+    for (int k = 0; k < 3; ++k) {
+      L.coord[k] = coord_of(ib + k);
+      L.coord[3 + k] = rig ? coord_of(rb + k) : -1;
+    }
+    orient::D r[3];
+    L.m = orient::residuals(t, &x[ib], rig ? &x[rb] : nullptr, r);
+    L.ns = 6;
+    for (int i = 0; i < L.m; ++i) L.raw[i] = r[i].v;
+    L.rho = orient::cauchy_correct(L.m, r, w);
+    for (int i = 0; i < L.m; ++i) {
+      L.r[i] = r[i].v;
+      for (int a = 0; a < 6; ++a) L.J[i][a] = r[i].d[a];
+    }
+    return;
   }
-  return orient::residuals(t, &x[ib], rig ? &x[rb] : nullptr, r);
+  const RelativeTerm& t = P.relative_terms[q - no];
+  constexpr int N = HostTermLin::kMaxSlots;
+  const double* pi[3] = {nullptr, nullptr, nullptr};
+  const double* pc[3] = {nullptr, nullptr, nullptr};
+  for (int k = 0; k < 3; ++k)
+    for (int a = 0; a < 12; ++a) L.coord[12 * k + a] = -1;
+  for (int k = 0; k < t.n_shots; ++k) {
+    const int ib = 8 * t.instance[k];
+    pi[k] = &x[ib];
+    for (int a = 0; a < 6; ++a) L.coord[12 * k + a] = coord_of(ib + a);
+    if (t.rig_camera[k] >= 0) {
+      const int rb = cl_.rig_base + 8 * t.rig_camera[k];
+      pc[k] = &x[rb];
+      for (int a = 0; a < 6; ++a) L.coord[12 * k + 6 + a] = coord_of(rb + a);
+    }
+  }
+  orient::Dual<N> r[6];
+  L.m = orient::relative_residuals<N>(t, pi, pc, r);
+  L.ns = N;
+  for (int i = 0; i < L.m; ++i) L.raw[i] = r[i].v;
+  static const int kLoss[3] = {-1, 5, 3};  // relative rotation: the relative-motion loss; Tukey(1); Cauchy(1)
+  const int loss = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss : kLoss[t.kind];
+  const double a = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss_threshold : 1.0;
+  L.rho = orient::loss_correct<N>(loss, a, L.m, r, w);
+  for (int i = 0; i < L.m; ++i) {
+    L.r[i] = r[i].v;
+    for (int k = 0; k < N; ++k) L.J[i][k] = r[i].d[k];
+  }
 }
 
 // Linear-model decrease of the priors for a camera-side step dx.
@@ -1490,16 +1561,14 @@ double DeviceSolver<R>::prior_model_change(const std::vector<double>& x, const s
       total += term(prior_weight_gps_[g], scale * (x[j] - prior[k]), scale, dx[j]);
     }
   }
-  for (size_t q = 0; q < P.orientation_terms.size(); ++q) {
-    int coord[6];
-    orient::D r[3];
-    const int m = orientation_residuals(P.orientation_terms[q], x, r, coord);
-    orient::cauchy_correct(m, r, orient_weight_[q]);
-    for (int q = 0; q < m; ++q) {
+  for (int q = 0; q < n_host_terms(); ++q) {
+    HostTermLin L;
+    host_term(q, x, L);
+    for (int i = 0; i < L.m; ++i) {
       double jd = 0.0;
-      for (int a = 0; a < 6; ++a)
-        if (coord[a] >= 0) jd += r[q].d[a] * dx[coord[a]];
-      total += -0.5 * jd * (2.0 * r[q].v + jd);
+      for (int a = 0; a < L.ns; ++a)
+        if (L.coord[a] >= 0) jd += L.J[i][a] * dx[L.coord[a]];
+      total += -0.5 * jd * (2.0 * L.r[i] + jd);
     }
   }
   return total;

@@ -57,6 +57,11 @@ def _declare(L) -> None:
         "gbba_add_absolute_tilt": ([_H, S, C.c_double, C.c_double], C.c_int),
         "gbba_add_absolute_roll": ([_H, S, C.c_double, C.c_double], C.c_int),
         "gbba_orientation_residual": ([C.c_int, _D, C.c_double, _D, _D, _D, _D, C.POINTER(C.c_int)], C.c_int),
+        "gbba_add_relative_rotation": ([_H, S, S, _D, _D], C.c_int),
+        "gbba_add_common_position": ([_H, S, S, C.c_double, C.c_double], C.c_int),
+        "gbba_add_linear_motion": ([_H, S, S, S, C.c_double, C.c_double, C.c_double], C.c_int),
+        "gbba_set_relative_motion_loss_function": ([_H, S, C.c_double], C.c_int),
+        "gbba_relative_residual": ([C.c_int, _D, _D, _D, _D, _D, C.POINTER(C.c_int)], C.c_int),
         "gbba_add_point_projection_observation": ([_H, S, S, _D, C.c_double, C.c_int], C.c_int),
         "gbba_shot_index": ([_H, S], C.c_int64),
         "gbba_point_index": ([_H, S], C.c_int64),
@@ -120,6 +125,20 @@ def _vec(x, n: int) -> np.ndarray:
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(_D)
+
+
+class RelativeRotation:
+    """bundle::RelativeRotation (bundle_adjuster.h:106-122): the rotation
+    R_ij between shots i and j (angle-axis) and a 3 x 3 scale matrix."""
+
+    def __init__(self, shot_i: str, shot_j: str, r) -> None:
+        self.shot_i = shot_i
+        self.shot_j = shot_j
+        self.r = np.asarray(r, dtype=np.float64).reshape(3).copy()
+        self.scale_matrix = np.eye(3)
+
+    def set_scale_matrix(self, s) -> None:
+        self.scale_matrix = np.asarray(s, dtype=np.float64).reshape(3, 3).copy()
 
 
 class Point:
@@ -308,6 +327,24 @@ class BundleAdjuster:
     def add_absolute_roll(self, shot_id: str, angle: float, std_deviation: float) -> None:
         self._check(self._L.gbba_add_absolute_roll(self._h, _b(shot_id), float(angle), float(std_deviation)))
 
+    def add_relative_rotation(self, rr: "RelativeRotation") -> None:
+        sm = np.ascontiguousarray(rr.scale_matrix, dtype=np.float64).reshape(9)
+        r = _vec(rr.r, 3)
+        self._check(self._L.gbba_add_relative_rotation(self._h, _b(rr.shot_i), _b(rr.shot_j), _dp(r), _dp(sm)))
+
+    def add_common_position(self, shot_i: str, shot_j: str, margin: float, std_deviation: float) -> None:
+        self._check(self._L.gbba_add_common_position(self._h, _b(shot_i), _b(shot_j), float(margin),
+                                                     float(std_deviation)))
+
+    def add_linear_motion(self, shot0: str, shot1: str, shot2: str, alpha: float, position_std_deviation: float,
+                          orientation_std_deviation: float) -> None:
+        self._check(self._L.gbba_add_linear_motion(self._h, _b(shot0), _b(shot1), _b(shot2), float(alpha),
+                                                   float(position_std_deviation),
+                                                   float(orientation_std_deviation)))
+
+    def set_relative_motion_loss_function(self, name: str, threshold: float) -> None:
+        self._check(self._L.gbba_set_relative_motion_loss_function(self._h, _b(name), float(threshold)))
+
     def find_outliers(self, filter_type: str = "FIXED", fixed_threshold: float = 0.006, auto_ratio: float = 3.0,
                       weight_threshold: float = 0.5):
         """Outlier observations of the last solve, as sfm::BAHelpers::RemoveOutliers
@@ -431,17 +468,13 @@ class BundleAdjuster:
         raise NotImplementedError("this constraint type is not implemented by the GPU bundle adjuster")
 
     add_relative_motion = _unsupported
-    add_relative_rotation = _unsupported
-    add_common_position = _unsupported
     add_heatmap = _unsupported
     add_absolute_position_heatmap = _unsupported
-    add_linear_motion = _unsupported
     set_gauge_fix_shots = _unsupported
     add_reconstruction = _unsupported
     add_reconstruction_instance = _unsupported
     set_scale_sharing = _unsupported
     get_reconstruction = _unsupported
-    set_relative_motion_loss_function = _unsupported
     set_adjust_absolute_position_std = _unsupported
 
 
@@ -530,6 +563,27 @@ def orientation_residual(kind: str, target, std_deviation: float, instance_rotat
     return r[: m.value].copy(), J[: 6 * m.value].reshape(m.value, 6)
 
 
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2}
+
+
+def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
+    """Scaled residuals (before the loss) and Jacobian [m][36] of one
+    constraint between shots -- RelativeRotationError, CommonPositionError
+    (relative_motion_errors.h:66-126) or LinearMotionError
+    (motion_prior_errors.h:12-74).  Poses [n][6] as [rx ry rz tx ty tz] with
+    t the position; params as gbba_relative_residual takes them."""
+    L = _lib.lib()
+    _declare(L)
+    pi = np.ascontiguousarray(instance_poses, dtype=np.float64)
+    pc = None if rig_camera_poses is None else np.ascontiguousarray(rig_camera_poses, dtype=np.float64)
+    prm = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
+    r, J = np.zeros(6), np.zeros(6 * 36)
+    m = C.c_int(0)
+    _lib.check(L.gbba_relative_residual(RELATIVE_KINDS[kind], _dp(pi), _dp(pc) if pc is not None else None,
+                                        _dp(prm), _dp(r), _dp(J), C.byref(m)))
+    return r[: m.value].copy(), J[: 36 * m.value].reshape(m.value, 36)
+
+
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
@@ -568,4 +622,5 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
     return ba
 
 
-__all__ = ["BundleAdjuster", "BundleBatch", "Point", "adjuster_from_scene", "orientation_residual"]
+__all__ = ["BundleAdjuster", "BundleBatch", "Point", "RelativeRotation", "adjuster_from_scene",
+           "orientation_residual", "relative_residual"]

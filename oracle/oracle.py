@@ -148,6 +148,8 @@ class _Problem(C.Structure):
         ("point_sigma", D), ("point_has_altitude", U8),
         ("n_obs", C.c_int64), ("obs_shot", I32), ("obs_point", I32), ("obs_xy", D), ("obs_std", D), ("obs_gcp", U8),
         ("n_orient", C.c_int32), ("orient_kind", I32), ("orient_shot", I32), ("orient_target", D), ("orient_std", D),
+        ("n_rel", C.c_int32), ("rel_kind", I32), ("rel_shots", I32), ("rel_params", D), ("rel_loss", C.c_int32),
+        ("rel_loss_threshold", C.c_double),
     ]
 
 
@@ -196,14 +198,38 @@ def orientation_residual(kind: str, target, std: float, instance_rotation, camer
     return r[:m].copy(), J[: 6 * m].reshape(m, 6)
 
 
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2}
+
+
+def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
+    """Scaled residuals and Jacobian [m][36] of one constraint between shots
+    (oracle/solver.cpp restatement)."""
+    L = lib()
+    f = L.oracle_relative_residual
+    f.argtypes = [C.c_int, D, D, D, D, D]
+    f.restype = C.c_int
+    pi = np.ascontiguousarray(instance_poses, np.float64)
+    pc = None if rig_camera_poses is None else np.ascontiguousarray(rig_camera_poses, np.float64)
+    prm = np.zeros(12)
+    v = np.asarray(params, np.float64).reshape(-1)
+    prm[: len(v)] = v
+    r, J = np.zeros(6), np.zeros(6 * 36)
+    m = f(RELATIVE_KINDS[kind], _p(pi), _p(pc), _p(prm), _p(r), _p(J))
+    return r[:m].copy(), J[: 36 * m].reshape(m, 36)
+
+
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
-          density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=()):
+          density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
+          relative_loss=("CauchyLoss", 1.0)):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
     value, std) with kind one of ORIENTATION_KINDS and value the up vector
-    or the angle.  Returns a dict with the final parameters, costs and the
-    cost trace."""
+    or the angle.  ``relative``: constraints between shots, tuples (kind,
+    shots, params) with kind one of RELATIVE_KINDS, shots the 2 (3 for
+    linear motion) shot indices and params as gbba_relative_residual takes
+    them; ``relative_loss`` the loss of the relative rotations.  Returns a
+    dict with the final parameters, costs and the cost trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
     L.oracle_solve.restype = C.c_int
@@ -255,9 +281,17 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
         v = np.atleast_1d(np.asarray(o[2], np.float64))
         o_target[q, : len(v)] = v
     o_std = np.array([float(o[3]) for o in orientation], np.float64).reshape(no)
+    nr = len(relative)
+    r_kind = np.array([RELATIVE_KINDS[c[0]] for c in relative], np.int32).reshape(nr)
+    r_shots = np.zeros((max(nr, 1), 3), np.int32)
+    r_params = np.zeros((max(nr, 1), 12))
+    for q, c in enumerate(relative):
+        r_shots[q, : len(c[1])] = c[1]
+        v = np.asarray(c[2], np.float64).reshape(-1)
+        r_params[q, : len(v)] = v
     keep = [cam_values, cam_sigma, cam_log, cam_free, inst, inst_free, has_gps, gps_pos, gps_std, rig, rig_free,
             rig_used, rig_has_prior, rig_prior, rig_sigma, shot_rig, pts, pfree, phas, pprior, psig, palt, gcp,
-            o_kind, o_shot, o_target, o_std]
+            o_kind, o_shot, o_target, o_std, r_kind, r_shots, r_params]
     u8 = lambda a: a.ctypes.data_as(U8)  # noqa: E731
     i32 = lambda a: a.ctypes.data_as(I32)  # noqa: E731
     P = _Problem(nc, i32(scene.camera_projection), _p(cam_values), _p(cam_values.copy() if False else cam_values),
@@ -267,7 +301,8 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
                  ns, i32(scene.shot_rig_instance), i32(shot_rig), i32(scene.shot_camera),
                  npt, _p(pts), u8(pfree), u8(phas), _p(pprior), _p(psig), u8(palt),
                  scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
-                 _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std))
+                 _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std),
+                 nr, i32(r_kind), i32(r_shots), _p(r_params), LOSSES[relative_loss[0]], float(relative_loss[1]))
     loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
     O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
                  int(skip_initial_reweighting), threads or os.cpu_count() or 1)

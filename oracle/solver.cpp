@@ -81,6 +81,13 @@ struct OracleProblem {
   const int32_t* orient_shot;
   const double* orient_target;  // [n][3]: the up vector, or the angle in [0]
   const double* orient_std;
+  // constraints between shots
+  int32_t n_rel;
+  const int32_t* rel_kind;     // 0 relative rotation, 1 common position, 2 linear motion
+  const int32_t* rel_shots;    // [n][3]
+  const double* rel_params;    // [n][12]: rotation[3] + scale matrix[9]; margin, std; alpha, position std, orientation std
+  int32_t rel_loss;            // loss of the relative rotations (projection loss kinds)
+  double rel_loss_threshold;
 };
 
 struct OracleOptions {
@@ -146,12 +153,13 @@ D6 asin6(const D6& a) {
 }
 
 // Rodrigues: R = cos t I + sin t [k]x + (1 - cos t) k k^T, k = a / t
-void rotation_matrix(const D6* a, D6* M) {
-  const D6 t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+template <class T>
+void rotation_matrix(const T* a, T* M) {
+  const T t2 = a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
   if (t2.v > kEps) {
-    const D6 t = sqrt(t2);
-    const D6 k[3] = {a[0] / t, a[1] / t, a[2] / t};
-    const D6 c = cos(t), sn = sin(t), v = 1.0 - c;
+    const T t = sqrt(t2);
+    const T k[3] = {a[0] / t, a[1] / t, a[2] / t};
+    const T c = cos(t), sn = sin(t), v = 1.0 - c;
     M[0] = c + v * k[0] * k[0];
     M[1] = v * k[0] * k[1] - sn * k[2];
     M[2] = v * k[0] * k[2] + sn * k[1];
@@ -162,13 +170,14 @@ void rotation_matrix(const D6* a, D6* M) {
     M[7] = v * k[2] * k[1] + sn * k[0];
     M[8] = c + v * k[2] * k[2];
   } else {
-    M[0] = D6(1.0), M[1] = -a[2], M[2] = a[1];
-    M[3] = a[2], M[4] = D6(1.0), M[5] = -a[0];
-    M[6] = -a[1], M[7] = a[0], M[8] = D6(1.0);
+    M[0] = T(1.0), M[1] = -a[2], M[2] = a[1];
+    M[3] = a[2], M[4] = T(1.0), M[5] = -a[0];
+    M[6] = -a[1], M[7] = a[0], M[8] = T(1.0);
   }
 }
 
-D6 wrap_angle(const D6& d) {
+template <class T>
+T wrap_angle(const T& d) {
   if (d.v > M_PI) return d - 2 * M_PI;
   if (d.v < -M_PI) return d + 2 * M_PI;
   return d;
@@ -228,11 +237,137 @@ int orientation_residual(int kind, const double* target, double std_dev, const d
   return 1;
 }
 
+// ---- constraints between shots
+// RelativeRotationError, CommonPositionError (relative_motion_errors.h:
+// 66-126) and LinearMotionError (motion_prior_errors.h:12-74) on the shot
+// poses (position_functors.h:12-63).  Restated with rotation matrices: the
+// shot rotation is R(instance) R(rig camera), its position the instance
+// position plus R(instance) times the rig camera position, and a composed
+// rotation's angle-axis is the matrix logarithm (atan2 of the skew part's
+// norm and the trace).  12 derivative slots per shot: instance rotation,
+// instance position, rig camera rotation, rig camera position.
+using D36 = Dual<36>;
+
+template <class T>
+void matmul3(const T* A, const T* B, T* C, bool transpose_b = false) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      T acc(0.0);
+      for (int k = 0; k < 3; ++k) acc = acc + A[3 * i + k] * (transpose_b ? B[3 * j + k] : B[3 * k + j]);
+      C[3 * i + j] = acc;
+    }
+}
+
+template <class T>
+void log_rotation(const T* M, T* a) {
+  const T v[3] = {(M[7] - M[5]) * 0.5, (M[2] - M[6]) * 0.5, (M[3] - M[1]) * 0.5};
+  const T c = (M[0] + M[4] + M[8] - 1.0) * 0.5;
+  const T s2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  T k(1.0);
+  if (s2.v > 1e-24) {
+    const T sn = sqrt(s2);
+    k = atan2(sn, c) / sn;
+  }
+  for (int i = 0; i < 3; ++i) a[i] = v[i] * k;
+}
+
+struct ShotFrame {
+  D36 R[9];
+  D36 p[3];
+};
+
+ShotFrame shot_frame(int k, const double* pi, const double* pc) {
+  ShotFrame f;
+  D36 ri[3], rc[3], tc[3], Ri[9], Rc[9];
+  for (int i = 0; i < 3; ++i) {
+    ri[i] = D36::var(pi[i], 12 * k + i);
+    f.p[i] = D36::var(pi[3 + i], 12 * k + 3 + i);
+    rc[i] = D36::var(pc ? pc[i] : 0.0, 12 * k + 6 + i);
+    tc[i] = D36::var(pc ? pc[3 + i] : 0.0, 12 * k + 9 + i);
+  }
+  rotation_matrix(ri, Ri);
+  if (!pc) {
+    for (int i = 0; i < 9; ++i) f.R[i] = Ri[i];
+    return f;
+  }
+  rotation_matrix(rc, Rc);
+  matmul3(Ri, Rc, f.R);
+  for (int i = 0; i < 3; ++i) f.p[i] = f.p[i] + Ri[3 * i] * tc[0] + Ri[3 * i + 1] * tc[1] + Ri[3 * i + 2] * tc[2];
+  return f;
+}
+
+int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r) {
+  const int n = kind == 2 ? 3 : 2;
+  ShotFrame f[3];
+  for (int k = 0; k < n; ++k) f[k] = shot_frame(k, pi[k], pc[k]);
+  if (kind == 0) {
+    D36 rij[3], Rij[9], T1[9], T2[9], e[3];
+    for (int i = 0; i < 3; ++i) rij[i] = D36(prm[i]);
+    rotation_matrix(rij, Rij);
+    matmul3(Rij, f[0].R, T1, true);  // R_ij R_i^T
+    matmul3(T1, f[1].R, T2);
+    log_rotation(T2, e);
+    for (int i = 0; i < 3; ++i) r[i] = e[0] * prm[3 + 3 * i] + e[1] * prm[4 + 3 * i] + e[2] * prm[5 + 3 * i];
+    return 3;
+  }
+  if (kind == 1) {
+    const double scale = 1.0 / prm[1];
+    for (int i = 0; i < 3; ++i) {
+      D36 e = f[0].p[i] - f[1].p[i];
+      if (i < 2) {
+        if (e.v < 0.0) e = -e;
+        e = e - prm[0];
+        if (e.v < 0.0) e = D36(0.0);
+      }
+      r[i] = e * scale;
+    }
+    return 3;
+  }
+  const double alpha = prm[0], ps = 1.0 / prm[1], os = 1.0 / prm[2];
+  D36 d20[3], d10[3];
+  for (int i = 0; i < 3; ++i) {
+    d20[i] = f[2].p[i] - f[0].p[i];
+    d10[i] = f[1].p[i] - f[0].p[i];
+  }
+  const D36 n20 = sqrt(d20[0] * d20[0] + d20[1] * d20[1] + d20[2] * d20[2]);
+  const D36 n10 = sqrt(d10[0] * d10[0] + d10[1] * d10[1] + d10[2] * d10[2]);
+  for (int i = 0; i < 3; ++i) r[i] = n20.v > 1e-15 ? (alpha - n10 / n20) * ps : (d20[i] * alpha - d10[i]) * ps;
+  D36 M20[9], M01[9], a[3], b[3], Ra[9], Rb[9], Rab[9], e[3];
+  matmul3(f[2].R, f[0].R, M20, true);  // R2 R0^T
+  matmul3(f[0].R, f[1].R, M01, true);  // R0 R1^T
+  log_rotation(M20, a);
+  log_rotation(M01, b);
+  for (int i = 0; i < 3; ++i) a[i] = a[i] * alpha;
+  rotation_matrix(a, Ra);
+  rotation_matrix(b, Rb);
+  matmul3(Ra, Rb, Rab);
+  log_rotation(Rab, e);
+  for (int i = 0; i < 3; ++i) r[3 + i] = e[i] * os;
+  return 6;
+}
+
+// rho of the losses, Tukey (kind 5) included (Ceres' documented forms)
+void loss_rho5(int kind, double a, double s, double* rho) {
+  if (kind != 5) {
+    loss_eval(kind, a, s, rho);
+    return;
+  }
+  const double b = a * a;
+  if (s <= b) {
+    const double v = 1.0 - s / b;
+    rho[0] = b / 3.0 * (1.0 - v * v * v);
+    rho[1] = v * v;
+    rho[2] = -2.0 * v / b;
+  } else {
+    rho[0] = b / 3.0, rho[1] = 0.0, rho[2] = 0.0;
+  }
+}
+
 struct Solver {
   const OracleProblem& P;
   const OracleOptions& O;
   Index idx;
-  std::vector<double> w_obs, w_cam, w_rig, w_gps, w_pp, w_orient;
+  std::vector<double> w_obs, w_cam, w_rig, w_gps, w_pp, w_orient, w_rel;
   std::vector<int> gps_list, pp_list;
   int threads;
 
@@ -262,6 +397,54 @@ struct Solver {
       if (P.point_has_prior[p]) pp_list.push_back(int(p));
     w_pp.assign(pp_list.size(), 1.0);
     w_orient.assign(std::max(0, P.n_orient), 1.0);
+    w_rel.assign(std::max(0, P.n_rel), 1.0);
+  }
+
+  // Constraint q between shots at state s: residuals and Jacobian after the
+  // loss correction (Triggs; alpha = 0 when rho'' <= 0) times the IRLS
+  // weight, the compact columns of the 36 slots, w rho through *rho and the
+  // raw residuals through raw.
+  int relative_term(const State& s, int q, D36* r, int* col, double* rho, double* raw = nullptr) const {
+    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : 2;
+    const double* pi[3] = {nullptr, nullptr, nullptr};
+    const double* pc[3] = {nullptr, nullptr, nullptr};
+    for (int a = 0; a < 36; ++a) col[a] = -1;
+    for (int k = 0; k < n; ++k) {
+      const int sh = P.rel_shots[3 * q + k];
+      const int inst = P.shot_instance[sh], rc = P.shot_rig[sh];
+      pi[k] = &s.inst[6 * inst];
+      for (int a = 0; a < 6; ++a) col[12 * k + a] = idx.inst[6 * inst + a];
+      if (rc >= 0 && P.rig_used[rc]) {
+        pc[k] = &s.rig[6 * rc];
+        for (int a = 0; a < 6; ++a) col[12 * k + 6 + a] = idx.rig[6 * rc + a];
+      }
+    }
+    const int m = relative_residual(kind, pi, pc, P.rel_params + 12 * q, r);
+    double sq = 0.0;
+    for (int a = 0; a < m; ++a) {
+      sq += r[a].v * r[a].v;
+      if (raw) raw[a] = r[a].v;
+    }
+    const int loss = kind == 0 ? P.rel_loss : (kind == 1 ? 5 : LOSS_CAUCHY);
+    const double la = kind == 0 ? P.rel_loss_threshold : 1.0;
+    double rh[3];
+    loss_rho5(loss, la, sq, rh);
+    for (double& v : rh) v *= w_rel[q];
+    *rho = rh[0];
+    const double sq1 = std::sqrt(rh[1]);
+    double rs = sq1, as = 0.0;
+    if (sq > 0.0 && rh[2] > 0.0) {
+      const double alpha = 1.0 - std::sqrt(1.0 + 2.0 * sq * rh[2] / rh[1]);
+      rs = sq1 / (1.0 - alpha);
+      as = alpha / sq;
+    }
+    for (int k = 0; k < 36; ++k) {
+      double rj = 0.0;
+      for (int a = 0; a < m; ++a) rj += r[a].v * r[a].d[k];
+      for (int a = 0; a < m; ++a) r[a].d[k] = sq1 * (r[a].d[k] - as * r[a].v * rj);
+    }
+    for (int a = 0; a < m; ++a) r[a].v *= rs;
+    return m;
   }
 
   // Orientation constraint q at state s under CauchyLoss(1) and its IRLS
@@ -358,6 +541,13 @@ struct Solver {
 
   double prior_cost(const State& s) const {
     double c = 0.0;
+    for (int q = 0; q < P.n_rel; ++q) {
+      D36 r[6];
+      int col[36];
+      double rho;
+      relative_term(s, q, r, col, &rho);
+      c += 0.5 * rho;
+    }
     for (int q = 0; q < P.n_orient; ++q) {
       D6 r[3];
       int col[6];
@@ -536,6 +726,20 @@ struct Solver {
         if (col[a] < 0) continue;
         for (int t = 0; t < m; ++t) g[col[a]] += rr[t].d[a] * rr[t].v;
         for (int b = 0; b < 6; ++b) {
+          if (col[b] < 0) continue;
+          for (int t = 0; t < m; ++t) U[size_t(col[a]) * n + col[b]] += rr[t].d[a] * rr[t].d[b];
+        }
+      }
+    }
+    for (int q = 0; q < P.n_rel; ++q) {
+      D36 rr[6];
+      int col[36];
+      double rho;
+      const int m = relative_term(s, q, rr, col, &rho);
+      for (int a = 0; a < 36; ++a) {
+        if (col[a] < 0) continue;
+        for (int t = 0; t < m; ++t) g[col[a]] += rr[t].d[a] * rr[t].v;
+        for (int b = 0; b < 36; ++b) {
           if (col[b] < 0) continue;
           for (int t = 0; t < m; ++t) U[size_t(col[a]) * n + col[b]] += rr[t].d[a] * rr[t].d[b];
         }
@@ -748,6 +952,18 @@ struct Solver {
         mc += -0.5 * jd * (2.0 * rr[t].v + jd);
       }
     }
+    for (int q = 0; q < P.n_rel; ++q) {
+      D36 rr[6];
+      int col[36];
+      double rho;
+      const int m = relative_term(s, q, rr, col, &rho);
+      for (int t = 0; t < m; ++t) {
+        double jd = 0.0;
+        for (int a = 0; a < 36; ++a)
+          if (col[a] >= 0) jd += rr[t].d[a] * dc[col[a]];
+        mc += -0.5 * jd * (2.0 * rr[t].v + jd);
+      }
+    }
     return mc;
   }
 
@@ -926,6 +1142,20 @@ struct Solver {
       }
       total += mixture(res, w, O.density_ratio);
     }
+    for (int kind = 0; kind < 3; ++kind) {  // groups ROT, POS, MOTION
+      std::vector<std::vector<double>> res;
+      std::vector<double*> w;
+      for (int q = 0; q < P.n_rel; ++q) {
+        if (P.rel_kind[q] != kind) continue;
+        D36 rr[6];
+        int col[36];
+        double rho, raw[6];
+        const int m = relative_term(s, q, rr, col, &rho, raw);
+        res.emplace_back(raw, raw + m);
+        w.push_back(&w_rel[q]);
+      }
+      total += mixture(res, w, O.density_ratio);
+    }
     return total;
   }
 };
@@ -956,6 +1186,27 @@ extern "C" int oracle_orientation_residual(int kind, const double* target, doubl
   for (int q = 0; q < m; ++q) {
     r[q] = d[q].v;
     for (int k = 0; k < 6; ++k) J[6 * q + k] = d[q].d[k];
+  }
+  return m;
+}
+
+// One constraint between shots: scaled residuals and Jacobian [m][36]
+// (kind and params as OracleProblem holds them; rig camera poses may be
+// null); returns m.
+extern "C" int oracle_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
+                                        const double* params, double* r, double* J) {
+  const int n = kind == 2 ? 3 : 2;
+  const double* pi[3] = {nullptr, nullptr, nullptr};
+  const double* pc[3] = {nullptr, nullptr, nullptr};
+  for (int k = 0; k < n; ++k) {
+    pi[k] = instance_poses + 6 * k;
+    pc[k] = rig_camera_poses ? rig_camera_poses + 6 * k : nullptr;
+  }
+  D36 d[6];
+  const int m = relative_residual(kind, pi, pc, params, d);
+  for (int q = 0; q < m; ++q) {
+    r[q] = d[q].v;
+    for (int k = 0; k < 36; ++k) J[36 * q + k] = d[q].d[k];
   }
   return m;
 }

@@ -1,0 +1,131 @@
+"""Constraints between shots -- relative rotations, common positions, linear
+motion -- in the GPU solve, against the FP64 CPU oracle.
+
+They are host terms of the camera-side system (bundle_adjuster.cc:
+912-999, 1080-1138) coupling two or three rig instances; the GPU solve adds
+their off-diagonal Gauss-Newton blocks to the implicit Schur product and
+the dense reduced camera system.  GPS priors fix the gauge (a common
+position is not invariant to the scale of the scene).  Bars as in
+test_gpu_solver.py.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+from opensfm_gb300 import pybundle, pygeometry
+from opensfm_gb300 import synthetic as syn
+from opensfm_gb300.pybundle import adjuster_from_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def _rot(a):
+    a = np.asarray(a, np.float64)
+    t = np.linalg.norm(a)
+    if t < 1e-300:
+        return np.eye(3)
+    k = a / t
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    return np.eye(3) + np.sin(t) * K + (1 - np.cos(t)) * K @ K
+
+
+def _log(M):
+    th = np.arccos(np.clip((np.trace(M) - 1) / 2, -1, 1))
+    return th / (2 * np.sin(th)) * np.array([M[2, 1] - M[1, 2], M[0, 2] - M[2, 0], M[1, 0] - M[0, 1]])
+
+
+def _scene_and_constraints(seed=13):
+    """Ring scene with GPS priors; relative rotations between neighbours
+    (0.005 rad noise, 0.01 rad std), common positions of opposite shots
+    (25 m horizontal margin: the heights are pulled together), linear
+    motion over consecutive triples."""
+    scene = syn.ring_scene(n_points=1500, seed=seed)
+    true = scene.extras["true_poses"]
+    rng = np.random.default_rng(4)
+    n = len(scene.shot_camera)
+    scene.extras["gps"] = np.ascontiguousarray(true[:, 3:] + rng.normal(0, 0.05, (n, 3)))
+    scene.extras["gps_std"] = np.full((n, 3), 0.1)
+    rel = []
+    for s in range(n):
+        t = (s + 1) % n
+        rij = -_log(_rot(true[s][:3]).T @ _rot(true[t][:3])) + rng.normal(0, 0.005, 3)
+        rel.append(("relative_rotation", (s, t), np.r_[rij, (np.eye(3) / 0.01).ravel()]))
+    for s in range(n // 2):
+        rel.append(("common_position", (s, s + n // 2), [25.0, 1.0]))
+    for s in range(n):
+        rel.append(("linear_motion", (s, (s + 1) % n, (s + 2) % n), [0.5, 0.1, 0.05]))
+    return scene, rel
+
+
+def _add(ba, rel):
+    for kind, shots, prm in rel:
+        sh = [str(s) for s in shots]
+        if kind == "relative_rotation":
+            rr = pybundle.RelativeRotation(sh[0], sh[1], prm[:3])
+            rr.set_scale_matrix(np.asarray(prm[3:]).reshape(3, 3))
+            ba.add_relative_rotation(rr)
+        elif kind == "common_position":
+            ba.add_common_position(sh[0], sh[1], prm[0], prm[1])
+        else:
+            ba.add_linear_motion(sh[0], sh[1], sh[2], prm[0], prm[1], prm[2])
+
+
+@pytest.mark.parametrize("solver", ["ITERATIVE_SCHUR", "SPARSE_SCHUR"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_relative_constraints_match_oracle(precision, solver):
+    scene, rel = _scene_and_constraints()
+    ref = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=100, gps=True, relative=rel)
+    free = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=100, gps=True)
+    assert ref["termination"] == 1
+    assert ref["final_cost"] > free["final_cost"] * 1.0005  # the constraints pull against the images
+    ba = adjuster_from_scene(scene, precision=precision, loss=("HuberLoss", 1.0), irls="none", max_iterations=100,
+                             gps=True, linear_solver=solver, pcg_tolerance=1e-10 if precision == "fp64" else 1e-4)
+    _add(ba, rel)
+    ba.run()
+    s = ba.summary()
+    assert s["usable"]
+    rel_err = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel_err < 1e-6, (s["final_cost"], ref["final_cost"])
+    got = np.stack([ba.get_rig_instance_pose(str(i)).rotation for i in range(len(scene.shot_camera))])
+    want = np.stack([pygeometry.Pose.from_ba_data(p).rotation for p in ref["instances"]])
+    np.testing.assert_allclose(got, want, atol=1e-4)
+
+
+@pytest.mark.parametrize("kind", ["relative_rotation", "common_position", "linear_motion"])
+def test_each_kind_matches_oracle(kind):
+    scene, rel = _scene_and_constraints(seed=21)
+    sub = [c for c in rel if c[0] == kind]
+    ref = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=100, gps=True, relative=sub)
+    ba = adjuster_from_scene(scene, precision="fp64", loss=("HuberLoss", 1.0), irls="none", max_iterations=100,
+                             gps=True, linear_solver="SPARSE_SCHUR")
+    _add(ba, sub)
+    ba.run()
+    s = ba.summary()
+    assert abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"] < 1e-6, (s["final_cost"], ref["final_cost"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_relative_irls_and_loss_match_oracle(precision):
+    # groups ROT (20), POS (10), MOTION (20) are reweighted; the relative
+    # rotations under SoftLOneLoss(2)
+    scene, rel = _scene_and_constraints()
+    ref = oracle.solve(scene, irls="mixture", max_iterations=100, gps=True, relative=rel,
+                       relative_loss=("SoftLOneLoss", 2.0))
+    ba = adjuster_from_scene(scene, precision=precision, irls="mixture", max_iterations=100, gps=True,
+                             linear_solver="SPARSE_SCHUR")
+    ba.set_relative_motion_loss_function("SoftLOneLoss", 2.0)
+    _add(ba, rel)
+    ba.run()
+    s = ba.summary()
+    assert s["usable"]
+    rel_err = abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+    assert rel_err < (1e-6 if precision == "fp64" else 1e-5), (s["final_cost"], ref["final_cost"])
+
+
+def test_unknown_relative_loss_fails_the_run():
+    scene, rel = _scene_and_constraints()
+    ba = adjuster_from_scene(scene, precision="fp64", irls="none", gps=True)
+    ba.set_relative_motion_loss_function("NoSuchLoss", 1.0)
+    _add(ba, rel[:1])
+    with pytest.raises(RuntimeError, match="NoSuchLoss"):
+        ba.run()

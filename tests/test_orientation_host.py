@@ -101,3 +101,71 @@ def test_degenerate_and_invalid():
         pybundle.orientation_residual("pan", 0.3, 0.0, np.zeros(3))
     with pytest.raises(pybundle._lib.GbbaError):
         pybundle.orientation_residual("up_vector", [0, 0, 0], 1.0, np.zeros(3))
+
+
+# ---- constraints between shots (relative_motion_errors.h:66-126,
+# motion_prior_errors.h:12-74)
+
+def _relative_cases(n_shots, seed):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(30):
+        poses = np.concatenate([rng.normal(size=(n_shots, 3)) * 0.8, rng.normal(size=(n_shots, 3)) * 3], axis=1)
+        rig = None
+        if i % 2:
+            rig = np.concatenate([rng.normal(size=(n_shots, 3)) * 0.3, rng.normal(size=(n_shots, 3))], axis=1)
+        out.append((poses, rig))
+    return out
+
+
+REL = [
+    ("relative_rotation", 2, lambda rng: np.concatenate([rng.normal(size=3) * 0.5,
+                                                         (np.eye(3) + 0.1 * rng.normal(size=(3, 3))).ravel()])),
+    ("common_position", 2, lambda rng: np.array([0.5, 0.2])),
+    ("linear_motion", 3, lambda rng: np.array([0.4, 0.3, 0.05])),
+]
+
+
+@pytest.mark.parametrize("kind,n_shots,make_params", REL)
+def test_relative_matches_oracle_and_finite_differences(kind, n_shots, make_params):
+    rng = np.random.default_rng(7)
+    for poses, rig in _relative_cases(n_shots, 3):
+        prm = make_params(rng)
+        r, J = pybundle.relative_residual(kind, poses, prm, rig)
+        ro, Jo = oracle.relative_residual(kind, poses, prm, rig)
+        np.testing.assert_allclose(r, ro, rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(J, Jo, rtol=1e-7, atol=1e-7)
+        # central differences of the library's residuals over every slot
+        x0 = np.concatenate([poses, np.zeros_like(poses) if rig is None else rig], axis=1)  # [n][12]
+        h = 1e-6
+        for k in range(n_shots):
+            for a in range(12 if rig is not None else 6):
+                xp, xm = x0.copy(), x0.copy()
+                xp[k, a] += h
+                xm[k, a] -= h
+                rp, _ = pybundle.relative_residual(kind, xp[:, :6], prm, xp[:, 6:] if rig is not None else None)
+                rm, _ = pybundle.relative_residual(kind, xm[:, :6], prm, xm[:, 6:] if rig is not None else None)
+                np.testing.assert_allclose((rp - rm) / (2 * h), J[:, 12 * k + a], rtol=1e-5, atol=2e-5)
+
+
+def test_relative_known_values():
+    # relative rotation: zero when R_ij R_i^T R_j = I, i.e. R_ij is the
+    # inverse of R_i^T R_j; common position: zero within the margin; linear
+    # motion:
+    # zero for shot 1 on the segment at fraction alpha with the rotation
+    # interpolated
+    rng = np.random.default_rng(9)
+    ri, rj = rng.normal(size=3) * 0.4, rng.normal(size=3) * 0.4
+    M = _rot(ri).T @ _rot(rj)
+    th = np.arccos(np.clip((np.trace(M) - 1) / 2, -1, 1))
+    rij = th / (2 * np.sin(th)) * np.array([M[2, 1] - M[1, 2], M[0, 2] - M[2, 0], M[1, 0] - M[0, 1]])
+    poses = np.array([np.r_[ri, 0, 0, 0], np.r_[rj, 1, 2, 3]])
+    r, _ = pybundle.relative_residual("relative_rotation", poses, np.r_[-rij, np.eye(3).ravel()])
+    np.testing.assert_allclose(r, 0, atol=1e-12)
+    poses = np.array([np.r_[0, 0, 0, 1.0, 2.0, 3.0], np.r_[0, 0, 0, 1.3, 1.8, 4.0]])
+    r, _ = pybundle.relative_residual("common_position", poses, [0.5, 0.25])
+    np.testing.assert_allclose(r, [0, 0, -4.0], atol=1e-12)
+    p0, p2 = np.array([0.0, 0, 0]), np.array([4.0, 2, -2])
+    poses = np.array([np.r_[0, 0, 0, p0], np.r_[0, 0, 0.25 * 0.8, 0.25 * p2], np.r_[0, 0, 0.8, p2]])
+    r, _ = pybundle.relative_residual("linear_motion", poses, [0.25, 1.0, 1.0])
+    np.testing.assert_allclose(r, 0, atol=1e-12)

@@ -99,9 +99,26 @@ def test_density_ratio_settings(ba):
 
 def test_unsupported_constraints_raise(ba):
     with pytest.raises(NotImplementedError):
-        ba.add_relative_rotation("a", "b", np.zeros(3))
+        ba.add_relative_motion(None)
     with pytest.raises(NotImplementedError):
-        ba.add_linear_motion("a", "b", "c", 0.5, 1, 1)
+        ba.set_gauge_fix_shots("a", "b")
+
+
+def test_relative_constraints_on_unknown_shots_are_index_errors(ba):
+    ba.add_rig_instance("1", pygeometry.Pose(), {"s1": "cam1"}, {"s1": "rig_cam1"}, False)
+    ba.add_rig_instance("2", pygeometry.Pose(), {"s2": "cam1"}, {"s2": "rig_cam1"}, False)
+    rr = pybundle.RelativeRotation("s1", "s2", [0.1, 0.0, 0.0])
+    rr.set_scale_matrix(2 * np.eye(3))
+    ba.add_relative_rotation(rr)
+    ba.add_common_position("s1", "s2", 0.5, 1.0)
+    ba.add_linear_motion("s1", "s2", "s1", 0.5, 1.0, 1.0)
+    ba.set_relative_motion_loss_function("HuberLoss", 1.0)
+    with pytest.raises(IndexError):
+        ba.add_relative_rotation(pybundle.RelativeRotation("s1", "nope", [0, 0, 0]))
+    with pytest.raises(IndexError):
+        ba.add_common_position("nope", "s2", 0.5, 1.0)
+    with pytest.raises(IndexError):
+        ba.add_linear_motion("s1", "s2", "nope", 0.5, 1.0, 1.0)
 
 
 def test_orientation_constraint_on_unknown_shot_is_index_error(ba):
