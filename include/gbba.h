@@ -291,13 +291,20 @@ int gbba_add_common_position(gbba_adjuster_t* h, const char* shot_i, const char*
 int gbba_add_linear_motion(gbba_adjuster_t* h, const char* shot0, const char* shot1, const char* shot2,
                            double alpha, double position_std_deviation, double orientation_std_deviation);
 int gbba_set_relative_motion_loss_function(gbba_adjuster_t* h, const char* name, double threshold);
+/* SetGaugeFixShots (bundle_adjuster.cc:389-394): the origin shot's rig
+ * instance becomes constant and a run adds log(|t1 - t2| / d) on the two
+ * shots' rig instance positions, d their distance when the run starts
+ * (TranslationPriorError, absolute_motion_errors.h:175-190; added at
+ * bundle_adjuster.cc:1140-1157), no loss, group GAUGE. */
+int gbba_set_gauge_fix_shots(gbba_adjuster_t* h, const char* shot_origin, const char* shot_scale);
 /* The scaled residuals (before the loss) of one constraint between shots
  * and their Jacobian.  kind 0 relative rotation (params: rotation[3], then
  * the row-major scale matrix [9]), 1 common position (params: margin,
  * std_deviation), 2 linear motion (params: alpha, position std, orientation
- * std).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
+ * std), 3 gauge scale (params: the distance; rig camera poses unused).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
  * cameras) for the n = 2 (3 for linear motion) shots, [rx ry rz tx ty tz]
- * with t the position.  Writes m = 3 (6 for linear motion) residuals, J[m][36]
+ * with t the position.  Writes m = 3 (6 for linear motion, 1 for the gauge
+ * scale) residuals, J[m][36]
  * (12 columns per shot: instance rotation, instance position, rig camera
  * rotation, rig camera position) and m to *n_residuals.  Host arithmetic
  * only. */

@@ -396,6 +396,16 @@ void BundleAdjuster::SetRelativeMotionLossFunction(const std::string& name, doub
   relative_loss_threshold_ = threshold;
 }
 
+void BundleAdjuster::SetGaugeFixShots(const std::string& shot_origin, const std::string& shot_scale) {
+  const auto it = shot_index_.find(shot_origin);
+  if (it == shot_index_.end()) throw std::out_of_range("Shot " + shot_origin + " doesn't exist.");
+  PoseBlock& inst = problem_.instances[problem_.shots[it->second].instance];
+  for (int k = 0; k < 6; ++k) inst.free_mask[k] = 0;
+  has_gauge_ = true;
+  gauge_shots_[0] = shot_origin;
+  gauge_shots_[1] = shot_scale;
+}
+
 void BundleAdjuster::PrepareRun() {
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
@@ -442,8 +452,8 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
-  static const char* kHostGroups[7] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION"};
-  for (int k = 0; k < 7; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
+  static const char* kHostGroups[8] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE"};
+  for (int k = 0; k < 8; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
   // constraints between shots, composed with the rig cameras that are
   // optimised or not the identity (IsRigCameraUseful), as Run passes them
   // (bundle_adjuster.cc:912-1138)
@@ -470,6 +480,20 @@ void BundleAdjuster::PrepareRun() {
     t.position_scale = 1.0 / p.position_std;
     t.orientation_scale = 1.0 / p.orientation_std;
     any_rotation |= p.kind == RelativeTerm::kRelativeRotation;
+    problem_.relative_terms.push_back(t);
+  }
+  if (has_gauge_) {
+    RelativeTerm t;
+    t.kind = RelativeTerm::kGaugeScale;
+    t.n_shots = 2;
+    for (int k = 0; k < 2; ++k) {
+      const auto it = shot_index_.find(gauge_shots_[k]);
+      if (it == shot_index_.end()) throw std::out_of_range("Shot " + gauge_shots_[k] + " doesn't exist.");
+      t.instance[k] = problem_.shots[it->second].instance;
+    }
+    const double* a = problem_.instances[t.instance[0]].value + 3;
+    const double* b = problem_.instances[t.instance[1]].value + 3;
+    t.distance = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
     problem_.relative_terms.push_back(t);
   }
   if (any_rotation) {

@@ -46,6 +46,11 @@ class BundleAdjuster {
   // the loss of the relative rotations (SetRelativeMotionLossFunction,
   // bundle_adjuster.cc:396-400); the name is checked when a run needs it
   void SetRelativeMotionLossFunction(const std::string& name, double threshold);
+  // SetGaugeFixShots (bundle_adjuster.cc:389-394): the origin shot's rig
+  // instance becomes constant; a run adds log(|t1 - t2| / d) between the
+  // two shots' rig instance positions, d their distance at the start of the
+  // run (:1140-1157).
+  void SetGaugeFixShots(const std::string& shot_origin, const std::string& shot_scale);
   void AddPointProjectionObservation(const std::string& shot, const std::string& point, const double* obs,
                                      double std_dev, bool is_gcp);
   // index-based adders (the raw-pointer path of AddPointProjectionObservationRaw)
@@ -148,6 +153,8 @@ class BundleAdjuster {
   };
   std::vector<PendingRelative> relatives_;
   std::string relative_loss_name_ = "CauchyLoss";
+  bool has_gauge_ = false;
+  std::string gauge_shots_[2];
   double relative_loss_threshold_ = 1.0;
   std::string loss_name_ = "TrivialLoss";
   SolveSummary summary_;

@@ -179,10 +179,14 @@ int gbba_set_relative_motion_loss_function(gbba_adjuster_t* h, const char* name,
   return guarded([&] { ba_of(h).SetRelativeMotionLossFunction(str(name), threshold); });
 }
 
+int gbba_set_gauge_fix_shots(gbba_adjuster_t* h, const char* shot_origin, const char* shot_scale) {
+  return guarded([&] { ba_of(h).SetGaugeFixShots(str(shot_origin), str(shot_scale)); });
+}
+
 int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                            const double* params, double* residuals, double* jacobian, int* n_residuals) {
   return guarded([&] {
-    if (kind < 0 || kind > 2 || !instance_poses || !params || !residuals || !jacobian || !n_residuals)
+    if (kind < 0 || kind > 3 || !instance_poses || !params || !residuals || !jacobian || !n_residuals)
       throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_relative_residual: invalid argument");
     gbba::RelativeTerm t;
     t.kind = kind;
@@ -193,6 +197,8 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
     } else if (kind == gbba::RelativeTerm::kCommonPosition) {
       t.margin = params[0];
       t.scale = 1.0 / params[1];
+    } else if (kind == gbba::RelativeTerm::kGaugeScale) {
+      t.distance = params[0];
     } else {
       t.alpha = params[0];
       t.position_scale = 1.0 / params[1];

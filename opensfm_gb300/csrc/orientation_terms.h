@@ -16,6 +16,9 @@
 //                         958-999).
 //   linear motion         LinearMotionError (motion_prior_errors.h:12-74)
 //                         under CauchyLoss(1) (bundle_adjuster.cc:1080-1138).
+//   gauge scale           TranslationPriorError (absolute_motion_errors.h:
+//                         175-190) between the two gauge shots' rig
+//                         instances, no loss (bundle_adjuster.cc:1140-1157).
 //
 // Shot rotation and position compose the rig instance with the rig camera
 // as ShotRotationFunctor / ShotPositionFunctor do (position_functors.h:
@@ -41,7 +44,7 @@ struct OrientationTerm {
 // derivative slots: instance rotation (0..2), instance position (3..5), rig
 // camera rotation (6..8), rig camera position (9..11).
 struct RelativeTerm {
-  enum Kind { kRelativeRotation = 0, kCommonPosition = 1, kLinearMotion = 2 };
+  enum Kind { kRelativeRotation = 0, kCommonPosition = 1, kLinearMotion = 2, kGaugeScale = 3 };
   int kind = kRelativeRotation;
   int n_shots = 2;
   int instance[3] = {0, 0, 0};
@@ -50,6 +53,7 @@ struct RelativeTerm {
   double scale_matrix[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
   double margin = 0.0, scale = 1.0;  // common position: margin, 1 / std
   double alpha = 0.0, position_scale = 1.0, orientation_scale = 1.0;  // linear motion
+  double distance = 1.0;  // gauge scale: the instances' distance at the start of the run
 };
 
 namespace orient {
@@ -323,6 +327,14 @@ inline int relative_residuals(const RelativeTerm& t, const double* const* pi, co
         r[i] = Dual<N>(t.scale) * e;
       }
       return 3;
+    }
+    case RelativeTerm::kGaugeScale: {
+      // log(|t_0 - t_1| / distance) on the rig instance positions alone
+      Dual<N> d[3];
+      for (int i = 0; i < 3; ++i) d[i] = var<N>(pi[0][3 + i], 3 + i) - var<N>(pi[1][3 + i], 15 + i);
+      const Dual<N> n = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      r[0] = chain(n, std::log(n.v / t.distance), 1.0 / n.v);
+      return 1;
     }
     default: {  // linear motion: shot 1 between shots 0 and 2 at fraction alpha
       Dual<N> d20[3], d10[3];

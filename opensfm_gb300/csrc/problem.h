@@ -120,7 +120,7 @@ struct Problem {
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
   double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
-  double ratio_host[7] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};  // UP, PAN, TILT, ROLL, ROT, POS, MOTION
+  double ratio_host[8] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};  // UP PAN TILT ROLL ROT POS MOTION GAUGE
 };
 
 // One LM iteration as reported by the solver.

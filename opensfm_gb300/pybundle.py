@@ -62,6 +62,7 @@ def _declare(L) -> None:
         "gbba_add_linear_motion": ([_H, S, S, S, C.c_double, C.c_double, C.c_double], C.c_int),
         "gbba_set_relative_motion_loss_function": ([_H, S, C.c_double], C.c_int),
         "gbba_relative_residual": ([C.c_int, _D, _D, _D, _D, _D, C.POINTER(C.c_int)], C.c_int),
+        "gbba_set_gauge_fix_shots": ([_H, S, S], C.c_int),
         "gbba_add_point_projection_observation": ([_H, S, S, _D, C.c_double, C.c_int], C.c_int),
         "gbba_shot_index": ([_H, S], C.c_int64),
         "gbba_point_index": ([_H, S], C.c_int64),
@@ -345,6 +346,9 @@ class BundleAdjuster:
     def set_relative_motion_loss_function(self, name: str, threshold: float) -> None:
         self._check(self._L.gbba_set_relative_motion_loss_function(self._h, _b(name), float(threshold)))
 
+    def set_gauge_fix_shots(self, shot_origin: str, shot_scale: str) -> None:
+        self._check(self._L.gbba_set_gauge_fix_shots(self._h, _b(shot_origin), _b(shot_scale)))
+
     def find_outliers(self, filter_type: str = "FIXED", fixed_threshold: float = 0.006, auto_ratio: float = 3.0,
                       weight_threshold: float = 0.5):
         """Outlier observations of the last solve, as sfm::BAHelpers::RemoveOutliers
@@ -470,7 +474,6 @@ class BundleAdjuster:
     add_relative_motion = _unsupported
     add_heatmap = _unsupported
     add_absolute_position_heatmap = _unsupported
-    set_gauge_fix_shots = _unsupported
     add_reconstruction = _unsupported
     add_reconstruction_instance = _unsupported
     set_scale_sharing = _unsupported
@@ -563,7 +566,7 @@ def orientation_residual(kind: str, target, std_deviation: float, instance_rotat
     return r[: m.value].copy(), J[: 6 * m.value].reshape(m.value, 6)
 
 
-RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2}
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3}
 
 
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):

@@ -198,7 +198,7 @@ def orientation_residual(kind: str, target, std: float, instance_rotation, camer
     return r[:m].copy(), J[: 6 * m].reshape(m, 6)
 
 
-RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2}
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3}
 
 
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
@@ -220,7 +220,7 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
 
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
           density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
-          relative_loss=("CauchyLoss", 1.0)):
+          relative_loss=("CauchyLoss", 1.0), gauge=None):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
@@ -228,7 +228,8 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     or the angle.  ``relative``: constraints between shots, tuples (kind,
     shots, params) with kind one of RELATIVE_KINDS, shots the 2 (3 for
     linear motion) shot indices and params as gbba_relative_residual takes
-    them; ``relative_loss`` the loss of the relative rotations.  Returns a
+    them; ``relative_loss`` the loss of the relative rotations.  ``gauge``:
+    (origin shot, scale shot) as set_gauge_fix_shots takes them.  Returns a
     dict with the final parameters, costs and the cost trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
@@ -281,6 +282,12 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
         v = np.atleast_1d(np.asarray(o[2], np.float64))
         o_target[q, : len(v)] = v
     o_std = np.array([float(o[3]) for o in orientation], np.float64).reshape(no)
+    relative = list(relative)
+    if gauge is not None:
+        i0, i1 = (int(scene.shot_rig_instance[int(g)]) for g in gauge)
+        inst_free[i0] = 0
+        relative.append(("gauge_scale", (int(gauge[0]), int(gauge[1])),
+                         [float(np.linalg.norm(inst[i0, 3:] - inst[i1, 3:]))]))
     nr = len(relative)
     r_kind = np.array([RELATIVE_KINDS[c[0]] for c in relative], np.int32).reshape(nr)
     r_shots = np.zeros((max(nr, 1), 3), np.int32)

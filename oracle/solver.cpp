@@ -297,6 +297,14 @@ ShotFrame shot_frame(int k, const double* pi, const double* pc) {
 }
 
 int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r) {
+  if (kind == 3) {
+    // TranslationPriorError (absolute_motion_errors.h:175-190) on the
+    // instance positions: log of the distance ratio
+    D36 d[3];
+    for (int i = 0; i < 3; ++i) d[i] = D36::var(pi[0][3 + i], 3 + i) - D36::var(pi[1][3 + i], 15 + i);
+    r[0] = log(sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) / prm[0]);
+    return 1;
+  }
   const int n = kind == 2 ? 3 : 2;
   ShotFrame f[3];
   for (int k = 0; k < n; ++k) f[k] = shot_frame(k, pi[k], pc[k]);
@@ -425,7 +433,8 @@ struct Solver {
       sq += r[a].v * r[a].v;
       if (raw) raw[a] = r[a].v;
     }
-    const int loss = kind == 0 ? P.rel_loss : (kind == 1 ? 5 : LOSS_CAUCHY);
+    static const int kLoss[4] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL};  // Tukey(1), Cauchy(1), none
+    const int loss = kind == 0 ? P.rel_loss : kLoss[kind];
     const double la = kind == 0 ? P.rel_loss_threshold : 1.0;
     double rh[3];
     loss_rho5(loss, la, sq, rh);
@@ -1142,7 +1151,7 @@ struct Solver {
       }
       total += mixture(res, w, O.density_ratio);
     }
-    for (int kind = 0; kind < 3; ++kind) {  // groups ROT, POS, MOTION
+    for (int kind = 0; kind < 4; ++kind) {  // groups ROT, POS, MOTION, GAUGE
       std::vector<std::vector<double>> res;
       std::vector<double*> w;
       for (int q = 0; q < P.n_rel; ++q) {

@@ -129,3 +129,27 @@ def test_unknown_relative_loss_fails_the_run():
     _add(ba, rel[:1])
     with pytest.raises(RuntimeError, match="NoSuchLoss"):
         ba.run()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gauge_fix_matches_oracle(precision):
+    # no GPS: the origin shot's instance is held and the distance to the
+    # scale shot's instance kept, which fixes all seven gauge freedoms
+    scene = syn.ring_scene(n_points=1500, seed=17)
+    ref = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=100, gps=False, gauge=(0, 10))
+    assert ref["termination"] == 1
+    ba = adjuster_from_scene(scene, precision=precision, loss=("HuberLoss", 1.0), irls="none", max_iterations=100,
+                             gps=False, linear_solver="SPARSE_SCHUR")
+    ba.set_gauge_fix_shots("0", "10")
+    ba.run()
+    s = ba.summary()
+    assert s["usable"]
+    assert abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"] < 1e-6, (s["final_cost"], ref["final_cost"])
+    p0 = ba.get_rig_instance_pose("0")
+    np.testing.assert_allclose(p0.rotation, pygeometry.Pose.from_ba_data(scene.rig_instance_poses[0]).rotation,
+                               atol=1e-12)
+    d0 = np.linalg.norm(scene.rig_instance_poses[0, 3:] - scene.rig_instance_poses[10, 3:])
+    d1 = np.linalg.norm(ba.get_rig_instance_pose("0").get_origin() - ba.get_rig_instance_pose("10").get_origin())
+    assert abs(d1 / d0 - 1) < 1e-3
+    # the gauge is fixed: the same points as the oracle
+    np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4 if precision == "fp64" else 1e-3)

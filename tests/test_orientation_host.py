@@ -123,6 +123,7 @@ REL = [
                                                          (np.eye(3) + 0.1 * rng.normal(size=(3, 3))).ravel()])),
     ("common_position", 2, lambda rng: np.array([0.5, 0.2])),
     ("linear_motion", 3, lambda rng: np.array([0.4, 0.3, 0.05])),
+    ("gauge_scale", 2, lambda rng: np.array([2.5])),
 ]
 
 
