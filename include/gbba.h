@@ -297,6 +297,25 @@ int gbba_set_relative_motion_loss_function(gbba_adjuster_t* h, const char* name,
  * (TranslationPriorError, absolute_motion_errors.h:175-190; added at
  * bundle_adjuster.cc:1140-1157), no loss, group GAUGE. */
 int gbba_set_gauge_fix_shots(gbba_adjuster_t* h, const char* shot_origin, const char* shot_scale);
+/* AddHeatmap (bundle_adjuster.cc:331-336): a cost grid of n values,
+ * row-major with `width` columns (n a multiple of width), `resolution`
+ * metres per cell; an id added again replaces its grid.
+ * AddAbsolutePositionHeatmap (:338-350, added at :1000-1009): the grid's
+ * bicubic (Catmull-Rom, border-clamped) value at the shot position,
+ * row = height / 2 - (y - y_offset) / resolution, column = width / 2 +
+ * (x - x_offset) / resolution, divided by std_deviation
+ * (HeatmapdCostFunctor, absolute_motion_errors.h:128-173); no loss, group
+ * HEATMAP.  Unknown shots or heatmap ids are GBBA_ERR_OUT_OF_RANGE. */
+int gbba_add_heatmap(gbba_adjuster_t* h, const char* heatmap_id, const double* data, int64_t n, int64_t width,
+                     double resolution);
+int gbba_add_absolute_position_heatmap(gbba_adjuster_t* h, const char* shot_id, const char* heatmap_id,
+                                       double x_offset, double y_offset, double std_deviation);
+/* The heatmap residual at instance pose [6] and rig camera pose [6] (NULL:
+ * none) and its Jacobian [12] (instance rotation, instance position, rig
+ * camera rotation, rig camera position).  Host arithmetic only. */
+int gbba_heatmap_residual(const double* grid, int64_t n, int64_t width, double resolution, double x_offset,
+                          double y_offset, double std_deviation, const double* instance_pose,
+                          const double* rig_camera_pose, double* residual, double* jacobian);
 /* The scaled residuals (before the loss) of one constraint between shots
  * and their Jacobian.  kind 0 relative rotation (params: rotation[3], then
  * the row-major scale matrix [9]), 1 common position (params: margin,

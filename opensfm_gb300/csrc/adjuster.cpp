@@ -406,6 +406,31 @@ void BundleAdjuster::SetGaugeFixShots(const std::string& shot_origin, const std:
   gauge_shots_[1] = shot_scale;
 }
 
+void BundleAdjuster::AddHeatmap(const std::string& id, const double* data, int64_t n, int64_t width,
+                                double resolution) {
+  if (width <= 0 || n < width || n % width != 0)
+    throw std::invalid_argument("heatmap " + id + ": size must be a positive multiple of the width");
+  Problem::Heatmap h;
+  h.data.assign(data, data + n);
+  h.width = int(width);
+  h.resolution = resolution;
+  const auto it = heatmap_index_.find(id);
+  if (it != heatmap_index_.end()) {
+    problem_.heatmaps[it->second] = std::move(h);  // the reference replaces the grid of an id
+  } else {
+    heatmap_index_[id] = int(problem_.heatmaps.size());
+    problem_.heatmaps.push_back(std::move(h));
+  }
+}
+
+void BundleAdjuster::AddAbsolutePositionHeatmap(const std::string& shot, const std::string& heatmap_id,
+                                                double x_offset, double y_offset, double std_deviation) {
+  if (shot_index_.find(shot) == shot_index_.end()) throw std::out_of_range("Shot " + shot + " doesn't exist.");
+  const auto it = heatmap_index_.find(heatmap_id);
+  if (it == heatmap_index_.end()) throw std::out_of_range("Heatmap " + heatmap_id + " doesn't exist.");
+  heatmap_terms_.push_back({shot, it->second, x_offset, y_offset, std_deviation});
+}
+
 void BundleAdjuster::PrepareRun() {
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
@@ -452,8 +477,8 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
-  static const char* kHostGroups[8] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE"};
-  for (int k = 0; k < 8; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
+  static const char* kHostGroups[9] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE", "HEATMAP"};
+  for (int k = 0; k < 9; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
   // constraints between shots, composed with the rig cameras that are
   // optimised or not the identity (IsRigCameraUseful), as Run passes them
   // (bundle_adjuster.cc:912-1138)
@@ -480,6 +505,25 @@ void BundleAdjuster::PrepareRun() {
     t.position_scale = 1.0 / p.position_std;
     t.orientation_scale = 1.0 / p.orientation_std;
     any_rotation |= p.kind == RelativeTerm::kRelativeRotation;
+    problem_.relative_terms.push_back(t);
+  }
+  for (const PendingHeatmap& p : heatmap_terms_) {
+    // the shot position always composes the rig camera (the functor gets
+    // its parameter block whether or not it is optimised)
+    const Shot& sh = problem_.shots[shot_index_.at(p.shot)];
+    const Problem::Heatmap& hm = problem_.heatmaps[p.heatmap];
+    RelativeTerm t;
+    t.kind = RelativeTerm::kHeatmap;
+    t.n_shots = 1;
+    t.instance[0] = sh.instance;
+    t.rig_camera[0] = sh.rig_camera;
+    t.grid.data = hm.data.data();
+    t.grid.width = hm.width;
+    t.grid.height = int(hm.data.size() / size_t(hm.width));
+    t.grid.resolution = hm.resolution;
+    t.x_offset = p.x_offset;
+    t.y_offset = p.y_offset;
+    t.scale = 1.0 / p.std_deviation;
     problem_.relative_terms.push_back(t);
   }
   if (has_gauge_) {

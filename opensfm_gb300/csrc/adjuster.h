@@ -51,6 +51,12 @@ class BundleAdjuster {
   // two shots' rig instance positions, d their distance at the start of the
   // run (:1140-1157).
   void SetGaugeFixShots(const std::string& shot_origin, const std::string& shot_scale);
+  // AddHeatmap / AddAbsolutePositionHeatmap (bundle_adjuster.cc:331-350):
+  // a cost grid (row-major, `width` columns, `resolution` metres per cell)
+  // and a shot's position looked up in it, centred at (x_offset, y_offset).
+  void AddHeatmap(const std::string& id, const double* data, int64_t n, int64_t width, double resolution);
+  void AddAbsolutePositionHeatmap(const std::string& shot, const std::string& heatmap_id, double x_offset,
+                                  double y_offset, double std_deviation);
   void AddPointProjectionObservation(const std::string& shot, const std::string& point, const double* obs,
                                      double std_dev, bool is_gcp);
   // index-based adders (the raw-pointer path of AddPointProjectionObservationRaw)
@@ -153,6 +159,13 @@ class BundleAdjuster {
   };
   std::vector<PendingRelative> relatives_;
   std::string relative_loss_name_ = "CauchyLoss";
+  std::unordered_map<std::string, int> heatmap_index_;
+  struct PendingHeatmap {
+    std::string shot;
+    int heatmap;
+    double x_offset, y_offset, std_deviation;
+  };
+  std::vector<PendingHeatmap> heatmap_terms_;
   bool has_gauge_ = false;
   std::string gauge_shots_[2];
   double relative_loss_threshold_ = 1.0;

@@ -183,6 +183,50 @@ int gbba_set_gauge_fix_shots(gbba_adjuster_t* h, const char* shot_origin, const 
   return guarded([&] { ba_of(h).SetGaugeFixShots(str(shot_origin), str(shot_scale)); });
 }
 
+int gbba_add_heatmap(gbba_adjuster_t* h, const char* heatmap_id, const double* data, int64_t n, int64_t width,
+                     double resolution) {
+  return guarded([&] {
+    need(data, "data");
+    try {
+      ba_of(h).AddHeatmap(str(heatmap_id), data, n, width, resolution);
+    } catch (const std::invalid_argument& e) {
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+    }
+  });
+}
+
+int gbba_add_absolute_position_heatmap(gbba_adjuster_t* h, const char* shot_id, const char* heatmap_id,
+                                       double x_offset, double y_offset, double std_deviation) {
+  return guarded([&] {
+    ba_of(h).AddAbsolutePositionHeatmap(str(shot_id), str(heatmap_id), x_offset, y_offset, std_deviation);
+  });
+}
+
+int gbba_heatmap_residual(const double* grid, int64_t n, int64_t width, double resolution, double x_offset,
+                          double y_offset, double std_deviation, const double* instance_pose,
+                          const double* rig_camera_pose, double* residual, double* jacobian) {
+  return guarded([&] {
+    if (!grid || width <= 0 || n < width || n % width != 0 || !instance_pose || !residual || !jacobian)
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_heatmap_residual: invalid argument");
+    gbba::RelativeTerm t;
+    t.kind = gbba::RelativeTerm::kHeatmap;
+    t.n_shots = 1;
+    t.grid.data = grid;
+    t.grid.width = int(width);
+    t.grid.height = int(n / width);
+    t.grid.resolution = resolution;
+    t.x_offset = x_offset;
+    t.y_offset = y_offset;
+    t.scale = 1.0 / std_deviation;
+    const double* pi[3] = {instance_pose, nullptr, nullptr};
+    const double* pc[3] = {rig_camera_pose, nullptr, nullptr};
+    gbba::orient::Dual<12> r[6];
+    gbba::orient::relative_residuals<12>(t, pi, pc, r);
+    residual[0] = r[0].v;
+    for (int k = 0; k < 12; ++k) jacobian[k] = r[0].d[k];
+  });
+}
+
 int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                            const double* params, double* residuals, double* jacobian, int* n_residuals) {
   return guarded([&] {

@@ -19,6 +19,10 @@
 //   gauge scale           TranslationPriorError (absolute_motion_errors.h:
 //                         175-190) between the two gauge shots' rig
 //                         instances, no loss (bundle_adjuster.cc:1140-1157).
+//   position heatmap      HeatmapdCostFunctor (absolute_motion_errors.h:
+//                         128-173): a bicubic lookup of a cost grid at the
+//                         shot's horizontal position, no loss
+//                         (bundle_adjuster.cc:1000-1009).
 //
 // Shot rotation and position compose the rig instance with the rig camera
 // as ShotRotationFunctor / ShotPositionFunctor do (position_functors.h:
@@ -40,11 +44,19 @@ struct OrientationTerm {
   double scale = 1.0;            // 1 / std deviation
 };
 
-// Constraints between two or three shots.  Each shot contributes 12
+// A cost grid of AddHeatmap (bundle_adjuster.cc:331-336): row-major values,
+// height = size / width rows, `resolution` metres per cell.
+struct HeatmapGrid {
+  const double* data = nullptr;
+  int width = 0, height = 0;
+  double resolution = 1.0;
+};
+
+// Constraints between two or three shots (one for a heatmap).  Each shot contributes 12
 // derivative slots: instance rotation (0..2), instance position (3..5), rig
 // camera rotation (6..8), rig camera position (9..11).
 struct RelativeTerm {
-  enum Kind { kRelativeRotation = 0, kCommonPosition = 1, kLinearMotion = 2, kGaugeScale = 3 };
+  enum Kind { kRelativeRotation = 0, kCommonPosition = 1, kLinearMotion = 2, kGaugeScale = 3, kHeatmap = 4 };
   int kind = kRelativeRotation;
   int n_shots = 2;
   int instance[3] = {0, 0, 0};
@@ -54,6 +66,8 @@ struct RelativeTerm {
   double margin = 0.0, scale = 1.0;  // common position: margin, 1 / std
   double alpha = 0.0, position_scale = 1.0, orientation_scale = 1.0;  // linear motion
   double distance = 1.0;  // gauge scale: the instances' distance at the start of the run
+  HeatmapGrid grid;       // heatmap: the grid, the offsets of its centre, scale = 1 / std
+  double x_offset = 0.0, y_offset = 0.0;
 };
 
 namespace orient {
@@ -295,6 +309,36 @@ inline ShotPose<N> shot_pose(int k, const double* pi, const double* pc) {
   return s;
 }
 
+// Cubic Hermite (Catmull-Rom) interpolation between p1 and p2 at x in
+// [0, 1] with tangents from the neighbours -- the spline of Ceres'
+// CubicInterpolator -- and its derivative.
+inline double catmull_rom(double p0, double p1, double p2, double p3, double x, double* df) {
+  const double a = 0.5 * (-p0 + 3.0 * p1 - 3.0 * p2 + p3);
+  const double b = 0.5 * (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3);
+  const double c = 0.5 * (-p0 + p2);
+  if (df) *df = c + x * (2.0 * b + 3.0 * a * x);
+  return p1 + x * (c + x * (b + x * a));
+}
+
+// Bicubic value of the grid at fractional (row, col), indices clamped to
+// the grid (Grid2D's border rule), with d/d row and d/d col.
+inline double bicubic(const HeatmapGrid& g, double r, double c, double* dfdr, double* dfdc) {
+  auto at = [&](int i, int j) {
+    i = std::min(std::max(i, 0), g.height - 1);
+    j = std::min(std::max(j, 0), g.width - 1);
+    return g.data[size_t(i) * g.width + j];
+  };
+  const int row = int(std::floor(r)), col = int(std::floor(c));
+  double f[4], df[4];
+  for (int k = 0; k < 4; ++k) {
+    const int i = row - 1 + k;
+    f[k] = catmull_rom(at(i, col - 1), at(i, col), at(i, col + 1), at(i, col + 2), c - col, &df[k]);
+  }
+  const double v = catmull_rom(f[0], f[1], f[2], f[3], r - row, dfdr);
+  *dfdc = catmull_rom(df[0], df[1], df[2], df[3], r - row, nullptr);
+  return v;
+}
+
 // Scaled residuals (3 or 6) of a relative term from the shots' instance
 // and rig camera poses (pc[k] null: no rig camera); returns the count.
 template <int N>
@@ -327,6 +371,19 @@ inline int relative_residuals(const RelativeTerm& t, const double* const* pi, co
         r[i] = Dual<N>(t.scale) * e;
       }
       return 3;
+    }
+    case RelativeTerm::kHeatmap: {
+      // grid row = height / 2 - (y - y_offset) / resolution, column = width
+      // / 2 + (x - x_offset) / resolution
+      const HeatmapGrid& g = t.grid;
+      const Dual<N> row = Dual<N>(0.5 * g.height) - (s[0].position[1] - Dual<N>(t.y_offset)) / Dual<N>(g.resolution);
+      const Dual<N> col = Dual<N>(0.5 * g.width) + (s[0].position[0] - Dual<N>(t.x_offset)) / Dual<N>(g.resolution);
+      double dfdr, dfdc;
+      const double v = bicubic(g, row.v, col.v, &dfdr, &dfdc);
+      Dual<N> f(v);
+      for (int k = 0; k < N; ++k) f.d[k] = dfdr * row.d[k] + dfdc * col.d[k];
+      r[0] = Dual<N>(t.scale) * f;
+      return 1;
     }
     case RelativeTerm::kGaugeScale: {
       // log(|t_0 - t_1| / distance) on the rig instance positions alone

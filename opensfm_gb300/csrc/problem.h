@@ -120,7 +120,15 @@ struct Problem {
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
   double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
-  double ratio_host[8] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};  // UP PAN TILT ROLL ROT POS MOTION GAUGE
+  // UP PAN TILT ROLL ROT POS MOTION GAUGE HEATMAP
+  double ratio_host[9] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};
+  // AddHeatmap grids (the relative terms of kind kHeatmap point into them)
+  struct Heatmap {
+    std::vector<double> data;
+    int width = 0;
+    double resolution = 1.0;
+  };
+  std::vector<Heatmap> heatmaps;
 };
 
 // One LM iteration as reported by the solver.

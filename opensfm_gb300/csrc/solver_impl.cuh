@@ -547,9 +547,10 @@ struct HostTermLin {
 };
 
 // IRLS groups of the host constraint terms: UP, PAN, TILT, ROLL (by
-// orientation kind), ROT, POS, MOTION, GAUGE (by relative kind)
-constexpr int kHostGroups = 8;
-const char* const kHostGroupNames[kHostGroups] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE"};
+// orientation kind), ROT, POS, MOTION, GAUGE, HEATMAP (by relative kind)
+constexpr int kHostGroups = 9;
+const char* const kHostGroupNames[kHostGroups] = {"UP",  "PAN",    "TILT",  "ROLL",   "ROT",
+                                                  "POS", "MOTION", "GAUGE", "HEATMAP"};
 
 MixtureResult mixture_group(const std::vector<std::vector<double>>& res, std::vector<double>& weights,
                             double density_ratio) {
@@ -1505,8 +1506,8 @@ void DeviceSolver<R>::host_term(int q, const std::vector<double>& x, HostTermLin
   L.m = orient::relative_residuals<N>(t, pi, pc, r);
   L.ns = N;
   for (int i = 0; i < L.m; ++i) L.raw[i] = r[i].v;
-  // relative rotation: the relative-motion loss; Tukey(1); Cauchy(1); none
-  static const int kLoss[4] = {-1, 5, 3, 0};
+  // relative rotation: the relative-motion loss; Tukey(1); Cauchy(1); none; none
+  static const int kLoss[5] = {-1, 5, 3, 0, 0};
   const int loss = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss : kLoss[t.kind];
   const double a = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss_threshold : 1.0;
   L.rho = orient::loss_correct<N>(loss, a, L.m, r, w);

@@ -63,6 +63,10 @@ def _declare(L) -> None:
         "gbba_set_relative_motion_loss_function": ([_H, S, C.c_double], C.c_int),
         "gbba_relative_residual": ([C.c_int, _D, _D, _D, _D, _D, C.POINTER(C.c_int)], C.c_int),
         "gbba_set_gauge_fix_shots": ([_H, S, S], C.c_int),
+        "gbba_add_heatmap": ([_H, S, _D, C.c_int64, C.c_int64, C.c_double], C.c_int),
+        "gbba_add_absolute_position_heatmap": ([_H, S, S, C.c_double, C.c_double, C.c_double], C.c_int),
+        "gbba_heatmap_residual": ([_D, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double, _D, _D,
+                                   _D, _D], C.c_int),
         "gbba_add_point_projection_observation": ([_H, S, S, _D, C.c_double, C.c_int], C.c_int),
         "gbba_shot_index": ([_H, S], C.c_int64),
         "gbba_point_index": ([_H, S], C.c_int64),
@@ -346,6 +350,17 @@ class BundleAdjuster:
     def set_relative_motion_loss_function(self, name: str, threshold: float) -> None:
         self._check(self._L.gbba_set_relative_motion_loss_function(self._h, _b(name), float(threshold)))
 
+    def add_heatmap(self, heatmap_id: str, in_heatmap, in_width: int, resolution: float) -> None:
+        d = np.ascontiguousarray(np.asarray(in_heatmap, dtype=np.float64).reshape(-1))
+        self._check(self._L.gbba_add_heatmap(self._h, _b(heatmap_id), _dp(d), d.size, int(in_width),
+                                             float(resolution)))
+
+    def add_absolute_position_heatmap(self, shot_id: str, heatmap_id: str, x_offset: float, y_offset: float,
+                                      std_deviation: float) -> None:
+        self._check(self._L.gbba_add_absolute_position_heatmap(self._h, _b(shot_id), _b(heatmap_id),
+                                                               float(x_offset), float(y_offset),
+                                                               float(std_deviation)))
+
     def set_gauge_fix_shots(self, shot_origin: str, shot_scale: str) -> None:
         self._check(self._L.gbba_set_gauge_fix_shots(self._h, _b(shot_origin), _b(shot_scale)))
 
@@ -472,8 +487,6 @@ class BundleAdjuster:
         raise NotImplementedError("this constraint type is not implemented by the GPU bundle adjuster")
 
     add_relative_motion = _unsupported
-    add_heatmap = _unsupported
-    add_absolute_position_heatmap = _unsupported
     add_reconstruction = _unsupported
     add_reconstruction_instance = _unsupported
     set_scale_sharing = _unsupported
@@ -587,6 +600,22 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
     return r[: m.value].copy(), J[: 36 * m.value].reshape(m.value, 36)
 
 
+def heatmap_residual(grid, width: int, resolution: float, x_offset: float, y_offset: float, std_deviation: float,
+                     instance_pose, rig_camera_pose=None):
+    """HeatmapdCostFunctor (absolute_motion_errors.h:128-173): the residual
+    and its Jacobian [12] at the given instance and rig camera poses."""
+    L = _lib.lib()
+    _declare(L)
+    g = np.ascontiguousarray(np.asarray(grid, dtype=np.float64).reshape(-1))
+    pi = np.ascontiguousarray(instance_pose, dtype=np.float64)
+    pc = None if rig_camera_pose is None else np.ascontiguousarray(rig_camera_pose, dtype=np.float64)
+    r, J = np.zeros(1), np.zeros(12)
+    _lib.check(L.gbba_heatmap_residual(_dp(g), g.size, int(width), float(resolution), float(x_offset),
+                                       float(y_offset), float(std_deviation), _dp(pi),
+                                       _dp(pc) if pc is not None else None, _dp(r), _dp(J)))
+    return float(r[0]), J
+
+
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
@@ -626,4 +655,4 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
 
 
 __all__ = ["BundleAdjuster", "BundleBatch", "Point", "RelativeRotation", "adjuster_from_scene",
-           "orientation_residual", "relative_residual"]
+           "heatmap_residual", "orientation_residual", "relative_residual"]

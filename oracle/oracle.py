@@ -149,7 +149,8 @@ class _Problem(C.Structure):
         ("n_obs", C.c_int64), ("obs_shot", I32), ("obs_point", I32), ("obs_xy", D), ("obs_std", D), ("obs_gcp", U8),
         ("n_orient", C.c_int32), ("orient_kind", I32), ("orient_shot", I32), ("orient_target", D), ("orient_std", D),
         ("n_rel", C.c_int32), ("rel_kind", I32), ("rel_shots", I32), ("rel_params", D), ("rel_loss", C.c_int32),
-        ("rel_loss_threshold", C.c_double),
+        ("rel_loss_threshold", C.c_double), ("heat_grid", D), ("heat_n", C.c_int64), ("heat_width", C.c_int32),
+        ("heat_resolution", C.c_double),
     ]
 
 
@@ -198,7 +199,22 @@ def orientation_residual(kind: str, target, std: float, instance_rotation, camer
     return r[:m].copy(), J[: 6 * m].reshape(m, 6)
 
 
-RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3}
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3, "heatmap": 4}
+
+
+def heatmap_residual(grid, width, resolution, x_offset, y_offset, std, instance_pose, rig_camera_pose=None):
+    """Heatmap residual and Jacobian [12] (oracle/solver.cpp restatement)."""
+    L = lib()
+    f = L.oracle_heatmap_residual
+    f.argtypes = [D, C.c_int64, C.c_int, C.c_double, D, D, D, D]
+    f.restype = C.c_double
+    g = np.ascontiguousarray(np.asarray(grid, np.float64).reshape(-1))
+    prm = np.array([x_offset, y_offset, std], np.float64)
+    pi = np.ascontiguousarray(instance_pose, np.float64)
+    pc = None if rig_camera_pose is None else np.ascontiguousarray(rig_camera_pose, np.float64)
+    J = np.zeros(12)
+    r = f(_p(g), g.size, int(width), float(resolution), _p(prm), _p(pi), _p(pc), _p(J))
+    return r, J
 
 
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
@@ -220,7 +236,7 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
 
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
           density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
-          relative_loss=("CauchyLoss", 1.0), gauge=None):
+          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
@@ -229,8 +245,11 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     shots, params) with kind one of RELATIVE_KINDS, shots the 2 (3 for
     linear motion) shot indices and params as gbba_relative_residual takes
     them; ``relative_loss`` the loss of the relative rotations.  ``gauge``:
-    (origin shot, scale shot) as set_gauge_fix_shots takes them.  Returns a
-    dict with the final parameters, costs and the cost trace."""
+    (origin shot, scale shot) as set_gauge_fix_shots takes them.
+    ``heatmap``: (grid, width, resolution), the grid of the ``relative``
+    entries of kind "heatmap" (shots (s,), params (x_offset, y_offset,
+    std)).  Returns a dict with the final parameters, costs and the cost
+    trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
     L.oracle_solve.restype = C.c_int
@@ -299,6 +318,12 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     keep = [cam_values, cam_sigma, cam_log, cam_free, inst, inst_free, has_gps, gps_pos, gps_std, rig, rig_free,
             rig_used, rig_has_prior, rig_prior, rig_sigma, shot_rig, pts, pfree, phas, pprior, psig, palt, gcp,
             o_kind, o_shot, o_target, o_std, r_kind, r_shots, r_params]
+    if heatmap is not None:
+        h_grid = np.ascontiguousarray(np.asarray(heatmap[0], np.float64).reshape(-1))
+        h_width, h_res = int(heatmap[1]), float(heatmap[2])
+    else:
+        h_grid, h_width, h_res = np.zeros(1), 1, 1.0
+    keep.append(h_grid)
     u8 = lambda a: a.ctypes.data_as(U8)  # noqa: E731
     i32 = lambda a: a.ctypes.data_as(I32)  # noqa: E731
     P = _Problem(nc, i32(scene.camera_projection), _p(cam_values), _p(cam_values.copy() if False else cam_values),
@@ -309,7 +334,8 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
                  npt, _p(pts), u8(pfree), u8(phas), _p(pprior), _p(psig), u8(palt),
                  scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
                  _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std),
-                 nr, i32(r_kind), i32(r_shots), _p(r_params), LOSSES[relative_loss[0]], float(relative_loss[1]))
+                 nr, i32(r_kind), i32(r_shots), _p(r_params), LOSSES[relative_loss[0]], float(relative_loss[1]),
+                 _p(h_grid), h_grid.size, h_width, h_res)
     loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
     O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
                  int(skip_initial_reweighting), threads or os.cpu_count() or 1)

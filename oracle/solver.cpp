@@ -88,6 +88,11 @@ struct OracleProblem {
   const double* rel_params;    // [n][12]: rotation[3] + scale matrix[9]; margin, std; alpha, position std, orientation std
   int32_t rel_loss;            // loss of the relative rotations (projection loss kinds)
   double rel_loss_threshold;
+  // the heatmap of the kind-4 constraints (params: x offset, y offset, std)
+  const double* heat_grid;
+  int64_t heat_n;
+  int32_t heat_width;
+  double heat_resolution;
 };
 
 struct OracleOptions {
@@ -296,7 +301,62 @@ ShotFrame shot_frame(int k, const double* pi, const double* pc) {
   return f;
 }
 
-int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r) {
+// ---- position heatmap (HeatmapdCostFunctor, absolute_motion_errors.h:
+// 128-173): bicubic convolution of the grid with the Catmull-Rom kernel
+// (Keys, a = -1/2) as four weights per axis, indices clamped to the grid.
+struct HeatGrid {
+  const double* data;
+  int64_t n;
+  int width;
+  double resolution;
+};
+
+void keys_weights(double t, double* w, double* dw) {
+  const double t2 = t * t, t3 = t2 * t;
+  w[0] = 0.5 * (-t3 + 2.0 * t2 - t);
+  w[1] = 0.5 * (3.0 * t3 - 5.0 * t2 + 2.0);
+  w[2] = 0.5 * (-3.0 * t3 + 4.0 * t2 + t);
+  w[3] = 0.5 * (t3 - t2);
+  dw[0] = 0.5 * (-3.0 * t2 + 4.0 * t - 1.0);
+  dw[1] = 0.5 * (9.0 * t2 - 10.0 * t);
+  dw[2] = 0.5 * (-9.0 * t2 + 8.0 * t + 1.0);
+  dw[3] = 0.5 * (3.0 * t2 - 2.0 * t);
+}
+
+double heat_value(const HeatGrid& g, double r, double c, double* fr, double* fc) {
+  const int height = int(g.n / g.width);
+  const double r0 = std::floor(r), c0 = std::floor(c);
+  double wr[4], dwr[4], wc[4], dwc[4];
+  keys_weights(r - r0, wr, dwr);
+  keys_weights(c - c0, wc, dwc);
+  double f = 0.0;
+  *fr = *fc = 0.0;
+  for (int i = 0; i < 4; ++i) {
+    const int ri = std::min(std::max(int(r0) - 1 + i, 0), height - 1);
+    for (int j = 0; j < 4; ++j) {
+      const int cj = std::min(std::max(int(c0) - 1 + j, 0), g.width - 1);
+      const double v = g.data[int64_t(ri) * g.width + cj];
+      f += wr[i] * wc[j] * v;
+      *fr += dwr[i] * wc[j] * v;
+      *fc += wr[i] * dwc[j] * v;
+    }
+  }
+  return f;
+}
+
+int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r,
+                      const HeatGrid* grid = nullptr) {
+  if (kind == 4) {
+    const ShotFrame f = shot_frame(0, pi[0], pc[0]);
+    const int height = int(grid->n / grid->width);
+    const D36 row = (f.p[1] - prm[1]) * (-1.0 / grid->resolution) + 0.5 * height;
+    const D36 col = (f.p[0] - prm[0]) * (1.0 / grid->resolution) + 0.5 * grid->width;
+    double fr, fc;
+    D36 v(heat_value(*grid, row.v, col.v, &fr, &fc));
+    for (int k = 0; k < 36; ++k) v.d[k] = fr * row.d[k] + fc * col.d[k];
+    r[0] = v * (1.0 / prm[2]);
+    return 1;
+  }
   if (kind == 3) {
     // TranslationPriorError (absolute_motion_errors.h:175-190) on the
     // instance positions: log of the distance ratio
@@ -413,7 +473,7 @@ struct Solver {
   // weight, the compact columns of the 36 slots, w rho through *rho and the
   // raw residuals through raw.
   int relative_term(const State& s, int q, D36* r, int* col, double* rho, double* raw = nullptr) const {
-    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : 2;
+    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : (kind == 4 ? 1 : 2);
     const double* pi[3] = {nullptr, nullptr, nullptr};
     const double* pc[3] = {nullptr, nullptr, nullptr};
     for (int a = 0; a < 36; ++a) col[a] = -1;
@@ -422,18 +482,20 @@ struct Solver {
       const int inst = P.shot_instance[sh], rc = P.shot_rig[sh];
       pi[k] = &s.inst[6 * inst];
       for (int a = 0; a < 6; ++a) col[12 * k + a] = idx.inst[6 * inst + a];
-      if (rc >= 0 && P.rig_used[rc]) {
+      // the heatmap functor always composes the rig camera
+      if (rc >= 0 && (P.rig_used[rc] || kind == 4)) {
         pc[k] = &s.rig[6 * rc];
         for (int a = 0; a < 6; ++a) col[12 * k + 6 + a] = idx.rig[6 * rc + a];
       }
     }
-    const int m = relative_residual(kind, pi, pc, P.rel_params + 12 * q, r);
+    const HeatGrid grid{P.heat_grid, P.heat_n, P.heat_width, P.heat_resolution};
+    const int m = relative_residual(kind, pi, pc, P.rel_params + 12 * q, r, &grid);
     double sq = 0.0;
     for (int a = 0; a < m; ++a) {
       sq += r[a].v * r[a].v;
       if (raw) raw[a] = r[a].v;
     }
-    static const int kLoss[4] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL};  // Tukey(1), Cauchy(1), none
+    static const int kLoss[5] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL};  // Tukey(1), Cauchy(1), none
     const int loss = kind == 0 ? P.rel_loss : kLoss[kind];
     const double la = kind == 0 ? P.rel_loss_threshold : 1.0;
     double rh[3];
@@ -1151,7 +1213,7 @@ struct Solver {
       }
       total += mixture(res, w, O.density_ratio);
     }
-    for (int kind = 0; kind < 4; ++kind) {  // groups ROT, POS, MOTION, GAUGE
+    for (int kind = 0; kind < 5; ++kind) {  // groups ROT, POS, MOTION, GAUGE, HEATMAP
       std::vector<std::vector<double>> res;
       std::vector<double*> w;
       for (int q = 0; q < P.n_rel; ++q) {
@@ -1218,6 +1280,20 @@ extern "C" int oracle_relative_residual(int kind, const double* instance_poses, 
     for (int k = 0; k < 36; ++k) J[36 * q + k] = d[q].d[k];
   }
   return m;
+}
+
+// The heatmap residual and its Jacobian [12] at one instance pose and rig
+// camera pose (null: none).
+extern "C" double oracle_heatmap_residual(const double* grid, int64_t n, int width, double resolution,
+                                          const double* params, const double* instance_pose,
+                                          const double* rig_camera_pose, double* J) {
+  const HeatGrid g{grid, n, width, resolution};
+  const double* pi[3] = {instance_pose, nullptr, nullptr};
+  const double* pc[3] = {rig_camera_pose, nullptr, nullptr};
+  D36 r[6];
+  relative_residual(4, pi, pc, params, r, &g);
+  for (int k = 0; k < 12; ++k) J[k] = r[0].d[k];
+  return r[0].v;
 }
 
 extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, OracleResult* out) {

@@ -153,3 +153,63 @@ def test_gauge_fix_matches_oracle(precision):
     assert abs(d1 / d0 - 1) < 1e-3
     # the gauge is fixed: the same points as the oracle
     np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4 if precision == "fp64" else 1e-3)
+
+
+def _bell(size, r, mu_x, mu_y):
+    # the cost surface of test_bundle.py:675-693: 1 - a normalised Gaussian
+    x, y = np.meshgrid(np.linspace(-r, r, size), np.linspace(r, -r, size))
+    z = np.exp(-((x - mu_x) ** 2 / (2 * (r / 2) ** 2) + (y - mu_y) ** 2 / (2 * (r / 2) ** 2)))
+    return 1 - z / z.max()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_heatmap_singletons(precision):
+    # test_bundle.py:650-735 without the reconstruction bookkeeping (its
+    # scales enter only relative motions): three shots pulled to the bell's
+    # minimum shifted by their offsets
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    ba.set_skip_initial_reweighting(True)
+    cam = pygeometry.Camera.create_perspective(1.0, 0.0, 0.0)
+    ba.add_camera("cam1", cam, cam, True)
+    ba.add_rig_camera("rig_cam1", pygeometry.Pose(), pygeometry.Pose(), True)
+    for i in range(3):
+        ba.add_rig_instance(str(i + 1), pygeometry.Pose(np.zeros(3), np.zeros(3)), {str(i + 1): "cam1"},
+                            {str(i + 1): "rig_cam1"}, False)
+    hmap_x, hmap_y, size, rad = 1, -1, 101, 10
+    res = 2 * rad / (size - 1)
+    ba.add_heatmap("hmap1", _bell(size, rad, hmap_x, hmap_y).flatten().tolist(), size, res)
+    offsets = [(2, 0), (0, 2), (-2, 0)]
+    for i, (xo, yo) in enumerate(offsets):
+        ba.add_absolute_position_heatmap(str(i + 1), "hmap1", xo, yo, 1.0)
+    ba.run()
+    for i, (xo, yo) in enumerate(offsets):
+        s = ba.get_rig_instance_pose(str(i + 1))
+        assert np.allclose(-s.translation, [xo + hmap_x, yo + hmap_y, 0], atol=res), s.translation
+
+
+@pytest.mark.parametrize("solver", ["ITERATIVE_SCHUR", "SPARSE_SCHUR"])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_ring_heatmap_matches_oracle(precision, solver):
+    # every shot looked up in one 30 m bell grid, offset so that its minimum
+    # sits 1.2 m from the shot's true horizontal position (std 2 mm: the
+    # pull is felt); GPS priors hold the height
+    scene, _ = _scene_and_constraints(seed=23)
+    true = scene.extras["true_poses"]
+    size, rad = 121, 15.0
+    res = 2 * rad / (size - 1)
+    grid = _bell(size, rad, 0.0, 0.0)
+    rel = [("heatmap", (s,), [true[s, 3] + 1.0, true[s, 4] - 0.7, 0.002]) for s in range(len(scene.shot_camera))]
+    ref = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=100, gps=True, relative=rel,
+                       heatmap=(grid, size, res))
+    free = oracle.solve(scene, loss=("HuberLoss", 1.0), irls="none", max_iterations=100, gps=True)
+    assert ref["termination"] == 1 and ref["final_cost"] > free["final_cost"] * 1.001
+    ba = adjuster_from_scene(scene, precision=precision, loss=("HuberLoss", 1.0), irls="none", max_iterations=100,
+                             gps=True, linear_solver=solver, pcg_tolerance=1e-10 if precision == "fp64" else 1e-4)
+    ba.add_heatmap("bell", grid.ravel(), size, res)
+    for _, (s,), (xo, yo, std) in rel:
+        ba.add_absolute_position_heatmap(str(s), "bell", xo, yo, std)
+    ba.run()
+    s = ba.summary()
+    assert s["usable"]
+    assert abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"] < 1e-6, (s["final_cost"], ref["final_cost"])

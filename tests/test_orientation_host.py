@@ -170,3 +170,48 @@ def test_relative_known_values():
     poses = np.array([np.r_[0, 0, 0, p0], np.r_[0, 0, 0.25 * 0.8, 0.25 * p2], np.r_[0, 0, 0.8, p2]])
     r, _ = pybundle.relative_residual("linear_motion", poses, [0.25, 1.0, 1.0])
     np.testing.assert_allclose(r, 0, atol=1e-12)
+
+
+def _bell(size, r, mu_x, mu_y):
+    # the cost surface of test_bundle.py:675-693: 1 - a normalised Gaussian
+    x, y = np.meshgrid(np.linspace(-r, r, size), np.linspace(r, -r, size))
+    z = np.exp(-((x - mu_x) ** 2 / (2 * (r / 2) ** 2) + (y - mu_y) ** 2 / (2 * (r / 2) ** 2)))
+    return 1 - z / z.max()
+
+
+def test_heatmap_matches_oracle_and_finite_differences():
+    size, rad = 41, 10.0
+    res = 2 * rad / (size - 1)
+    grid = _bell(size, rad, 1.0, -1.0)
+    rng = np.random.default_rng(2)
+    for i in range(40):
+        pose = np.r_[rng.normal(size=3) * 0.5, rng.uniform(-13, 13, 2), rng.normal()]
+        rig = None if i % 2 else np.r_[rng.normal(size=3) * 0.3, rng.normal(size=3)]
+        xo, yo, std = rng.normal(size=2).tolist() + [0.7]
+        r, J = pybundle.heatmap_residual(grid, size, res, xo, yo, std, pose, rig)
+        ro, Jo = oracle.heatmap_residual(grid, size, res, xo, yo, std, pose, rig)
+        assert abs(r - ro) < 1e-12
+        np.testing.assert_allclose(J, Jo, atol=1e-10)
+        h = 1e-6
+        x0 = np.r_[pose, np.zeros(6) if rig is None else rig]
+        for k in range(12 if rig is not None else 6):
+            xp, xm = x0.copy(), x0.copy()
+            xp[k] += h
+            xm[k] -= h
+            rp, _ = pybundle.heatmap_residual(grid, size, res, xo, yo, std, xp[:6], xp[6:] if rig is not None else None)
+            rm, _ = pybundle.heatmap_residual(grid, size, res, xo, yo, std, xm[:6], xm[6:] if rig is not None else None)
+            if abs(rp - rm) > 0:  # the spline is C1: central differences agree except across clamped borders
+                assert abs((rp - rm) / (2 * h) - J[k]) < 1e-4, (k, (rp - rm) / (2 * h), J[k])
+
+
+def test_heatmap_interpolates_grid_nodes():
+    # at a node the spline returns the node's value
+    grid = np.arange(35, dtype=np.float64).reshape(5, 7) ** 1.5
+    res = 0.5
+    for i in range(1, 4):
+        for j in range(1, 6):
+            # row = height / 2 - y / res, col = width / 2 + x / res
+            x = (j - 3.5) * res
+            y = (2.5 - i) * res
+            r, _ = pybundle.heatmap_residual(grid, 7, res, 0.0, 0.0, 1.0, np.r_[0, 0, 0, x, y, 0])
+            assert abs(r - grid[i, j]) < 1e-12

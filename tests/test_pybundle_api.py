@@ -101,7 +101,7 @@ def test_unsupported_constraints_raise(ba):
     with pytest.raises(NotImplementedError):
         ba.add_relative_motion(None)
     with pytest.raises(NotImplementedError):
-        ba.add_heatmap("h", [0.0] * 4, 2, 1.0)
+        ba.add_reconstruction("r", False)
     # the gauge fix looks the origin shot up at once (bundle_adjuster.cc:391)
     with pytest.raises(IndexError):
         ba.set_gauge_fix_shots("a", "b")
