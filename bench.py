@@ -379,6 +379,80 @@ def dense_benchmark(sizes=(1024, 2048, 4096), street_shots: int = 500, street_po
     return out
 
 
+def outlier_benchmark(n_obs: int, seed: int = 31, reps: int = 3) -> dict:
+    """Post-solve outlier selection (the observation test of
+    sfm::BAHelpers::RemoveOutliers) on n_obs seeded 2D errors (1 mm Gaussian
+    on a unit-width image plus 2% uniform outliers), IRLS weights and point
+    indices (6 observations per point on average), FIXED and AUTO
+    thresholds.  e2e: the C-ABI call on host buffers (errors upload
+    included); device: the CUDA-event span from the inputs resident to the
+    flags written.  Algorithmic bytes per observation: the 2D error (16 B),
+    the weight (8 B), the point index (4 B) and the flag (1 B), plus one
+    byte per point; the AUTO threshold reads the errors again for three
+    exact radix selections (six 11-bit digit passes each).  CPU baseline:
+    the oracle's numpy restatement on the same arrays."""
+    from opensfm_gb300 import outliers
+    from oracle import oracle
+    rng = np.random.default_rng(seed)
+    n_points = max(1, n_obs // 6)
+    err = rng.normal(0.0, 1e-3, (n_obs, 3))
+    bad = rng.random(n_obs) < 0.02
+    err[bad, :2] = rng.uniform(-0.05, 0.05, (int(bad.sum()), 2))
+    w = rng.uniform(0.3, 1.0, n_obs)
+    pts = rng.integers(0, n_points, n_obs).astype(np.int32)
+    peaks = measured_peaks()
+    algo = 29.0 * n_obs + n_points
+    out = {"n_observations": n_obs, "n_points": n_points, "algorithmic_bytes": int(algo)}
+    for mode in ("FIXED", "AUTO"):
+        outliers.find_outliers(err, w, pts, n_points, filter_type=mode)  # warm-up
+        best, best_dev, st = None, None, {}
+        for _ in range(reps):
+            st = {}
+            t0 = time.perf_counter()
+            thr, flags, removed = outliers.find_outliers(err, w, pts, n_points, stats=st, filter_type=mode)
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+            best_dev = st["device_seconds"] if best_dev is None else min(best_dev, st["device_seconds"])
+        t0 = time.perf_counter()
+        rthr, rflags, rremoved = oracle.remove_outliers(err, w, pts, n_points, filter_type=mode)
+        cpu = time.perf_counter() - t0
+        achieved = algo / best_dev / 1e9
+        out[mode.lower()] = {
+            "e2e_ms": best * 1e3, "device_ms": best_dev * 1e3, "threshold": thr, "n_outliers": st["n_outliers"],
+            "n_removed_points": st["n_removed_points"],
+            "matches_oracle": bool(thr == rthr and np.array_equal(flags, rflags) and np.array_equal(removed, rremoved)),
+            "cpu_baseline": {"seconds": cpu, "kind": "port", "cores": 1, "sample": "the same arrays (numpy)"},
+            "e2e_speedup_vs_cpu": cpu / best,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "peak_source": peaks["source"]}}
+    return out
+
+
+def covariance_benchmark(street_shots: int = 500, street_points: int = 200_000, seed: int = 29,
+                         max_iterations: int = 60) -> dict:
+    """Pose covariances (set_compute_covariances) on the street workload:
+    the same FP64 dense solve with and without them; the difference is the
+    covariance time (the undamped reduced camera system assembled and
+    factored once, then 6 FP64 CG columns of its inverse per instance)."""
+    from opensfm_gb300 import synthetic as syn
+    from opensfm_gb300.pybundle import adjuster_from_scene
+    scene = syn.street_scene(n_shots=street_shots, n_points=street_points, seed=seed, outlier_ratio=0.0)
+    times = {}
+    valid = None
+    for cov in (False, True):
+        ba = adjuster_from_scene(scene, precision="fp64", loss=("SoftLOneLoss", 1.0), irls="none", gps=False,
+                                 max_iterations=max_iterations, linear_solver="DENSE_SCHUR", covariances=cov)
+        t0 = time.perf_counter()
+        ba.run()
+        times[cov] = time.perf_counter() - t0
+        if cov:
+            valid = bool(ba.get_covariance_estimation_valid())
+        del ba
+    return {"n_shots": street_shots, "n_instances": street_shots, "solve_s": times[False],
+            "solve_with_covariances_s": times[True], "covariance_s": times[True] - times[False],
+            "valid": valid}
+
+
 def autograd_benchmark(n_obs: int = 4_000_000, steps: int = 5, seed: int = 17) -> dict:
     """Differentiable projection operator over n_obs observations: forward +
     backward (gradients for intrinsics, poses and points) for Brown and
@@ -594,6 +668,12 @@ def run_ours(args) -> None:
             result["dense_rcs"] = dense_benchmark(sizes=tuple(args.dense_sizes), street_shots=args.dense_street_shots,
                                                   street_points=args.dense_street_points,
                                                   runs=tuple(args.dense_street_runs))
+        if not args.no_outliers:
+            ev.close()
+            result["outlier_selection"] = outlier_benchmark(args.outlier_observations or n_obs)
+        if not args.no_covariance:
+            ev.close()
+            result["covariances"] = covariance_benchmark(street_shots=args.covariance_shots)
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -617,6 +697,10 @@ def main() -> None:
     ap.add_argument("--batch-only", action="store_true", help="skip the one-at-a-time comparison")
     ap.add_argument("--autograd-observations", type=int, default=4_000_000)
     ap.add_argument("--no-dense", action="store_true")
+    ap.add_argument("--no-outliers", action="store_true")
+    ap.add_argument("--outlier-observations", type=int, default=0, help="0: the workload's observation count")
+    ap.add_argument("--no-covariance", action="store_true")
+    ap.add_argument("--covariance-shots", type=int, default=500)
     ap.add_argument("--dense-sizes", type=int, nargs="*", default=[1024, 2048, 4096])
     ap.add_argument("--dense-street-shots", type=int, default=500, help="0: skip the street solves")
     ap.add_argument("--dense-street-points", type=int, default=200_000)

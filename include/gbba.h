@@ -496,6 +496,7 @@ typedef struct gbba_outlier_result {
   double threshold;
   int64_t n_outliers;
   int64_t n_removed_points;
+  double device_seconds; /* stream time from the inputs resident to the flags written (host scans included) */
 } gbba_outlier_result_t;
 /* errors: n rows of `stride` doubles (columns 0 and 1 are the 2D error),
  * weights [n], obs_point [n] in [0, n_points); host buffers.  flags [n]

@@ -162,6 +162,9 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
   e.upload(errors, size_t(n) * stride);
   w.upload(weights, size_t(n));
   op.upload(obs_point, size_t(n));
+  cudaEvent_t ev[2];
+  for (cudaEvent_t& x : ev) GB_CUDA(cudaEventCreate(&x));
+  GB_CUDA(cudaEventRecord(ev[0]));
   double threshold = 1.0;
   if (cfg.filter_type == 0) {
     threshold = cfg.fixed_threshold;
@@ -191,13 +194,18 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
     removed_kernel<<<int((n_points + 255) / 256), 256>>>(n_points, pobs.get(), pout.get(), rem.get(),
                                                          counts.get() + 1);
   GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaEventRecord(ev[1]));
   unsigned long long c[2];
   counts.download(c, 2);
   f.download(flags, size_t(n));
   if (n_points > 0) rem.download(point_removed, size_t(n_points));
   GB_CUDA(cudaDeviceSynchronize());
+  float ms = 0.0f;
+  GB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+  for (cudaEvent_t& x : ev) GB_CUDA(cudaEventDestroy(x));
   res.n_outliers = int64_t(c[0]);
   res.n_removed_points = int64_t(c[1]);
+  res.device_seconds = 1e-3 * double(ms);
   return res;
 }
 
@@ -227,6 +235,7 @@ extern "C" int gbba_find_outliers(const double* errors, int stride, const double
       result->threshold = r.threshold;
       result->n_outliers = r.n_outliers;
       result->n_removed_points = r.n_removed_points;
+      result->device_seconds = r.device_seconds;
     }
   });
 }

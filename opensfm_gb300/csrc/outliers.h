@@ -18,6 +18,7 @@ struct OutlierResult {
   double threshold = 1.0;
   int64_t n_outliers = 0;
   int64_t n_removed_points = 0;
+  double device_seconds = 0.0;  // CUDA-event span of the selection (inputs resident to flags written)
 };
 
 // errors: n rows of `stride` doubles (the first two are the 2D reprojection

@@ -17,7 +17,8 @@ class OutlierConfig(C.Structure):
 
 
 class OutlierResult(C.Structure):
-    _fields_ = [("threshold", C.c_double), ("n_outliers", C.c_int64), ("n_removed_points", C.c_int64)]
+    _fields_ = [("threshold", C.c_double), ("n_outliers", C.c_int64), ("n_removed_points", C.c_int64),
+                ("device_seconds", C.c_double)]
 
 
 _FILTERS = {"FIXED": 0, "AUTO": 1}
@@ -44,8 +45,9 @@ def config(filter_type: str = "FIXED", fixed_threshold: float = 0.006, auto_rati
     return OutlierConfig(_FILTERS[filter_type], fixed_threshold, auto_ratio, weight_threshold)
 
 
-def find_outliers(errors, weights, obs_point, n_points: int, **cfg):
-    """Returns (threshold, outlier flags [n], removed-point flags [n_points])."""
+def find_outliers(errors, weights, obs_point, n_points: int, stats: dict | None = None, **cfg):
+    """Returns (threshold, outlier flags [n], removed-point flags [n_points]).
+    ``stats``, when given, receives the counts and the device time."""
     e = np.ascontiguousarray(errors, dtype=np.float64)
     w = np.ascontiguousarray(weights, dtype=np.float64)
     p = np.ascontiguousarray(obs_point, dtype=np.int32)
@@ -61,6 +63,9 @@ def find_outliers(errors, weights, obs_point, n_points: int, **cfg):
     _lib.check(_L().gbba_find_outliers(e.ctypes.data_as(D), e.shape[1], w.ctypes.data_as(D),
                                        p.ctypes.data_as(C.POINTER(C.c_int32)), n, n_points, C.byref(c),
                                        flags.ctypes.data_as(U8), removed.ctypes.data_as(U8), C.byref(res)))
+    if stats is not None:
+        stats.update(n_outliers=int(res.n_outliers), n_removed_points=int(res.n_removed_points),
+                     device_seconds=float(res.device_seconds))
     return res.threshold, flags.astype(bool), removed[:n_points].astype(bool)
 
 
