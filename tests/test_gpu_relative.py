@@ -148,9 +148,13 @@ def test_gauge_fix_matches_oracle(precision):
     p0 = ba.get_rig_instance_pose("0")
     np.testing.assert_allclose(p0.rotation, pygeometry.Pose.from_ba_data(scene.rig_instance_poses[0]).rotation,
                                atol=1e-12)
+    # the scale is held by a weak term (log of the distance ratio, unit
+    # weight): the run stops on the function tolerance with the ratio a
+    # little off 1, where the oracle stops too
     d0 = np.linalg.norm(scene.rig_instance_poses[0, 3:] - scene.rig_instance_poses[10, 3:])
     d1 = np.linalg.norm(ba.get_rig_instance_pose("0").get_origin() - ba.get_rig_instance_pose("10").get_origin())
-    assert abs(d1 / d0 - 1) < 1e-3
+    d_ref = np.linalg.norm(ref["instances"][0, 3:] - ref["instances"][10, 3:])
+    assert abs(d1 / d0 - 1) < 5e-3 and abs(d1 / d_ref - 1) < 1e-4, (d0, d1, d_ref)
     # the gauge is fixed: the same points as the oracle
     np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4 if precision == "fp64" else 1e-3)
 
