@@ -430,17 +430,24 @@ def outlier_benchmark(n_obs: int, seed: int = 31, reps: int = 3) -> dict:
 
 def covariance_benchmark(street_shots: int = 500, street_points: int = 200_000, seed: int = 29,
                          max_iterations: int = 60) -> dict:
-    """Pose covariances (set_compute_covariances) on the street workload:
-    the same FP64 dense solve with and without them; the difference is the
-    covariance time (the undamped reduced camera system assembled and
-    factored once, then 6 FP64 CG columns of its inverse per instance)."""
+    """Pose covariances (set_compute_covariances) on the street workload
+    with GPS priors on every shot (5 cm noise and std: they fix the gauge,
+    without which the reduced camera system is singular and the reference's
+    default covariances are returned): the same FP64 dense solve with and
+    without them; the difference is the covariance time (the undamped
+    reduced camera system assembled and factored once, then 6 FP64 CG
+    columns of its inverse per instance)."""
     from opensfm_gb300 import synthetic as syn
     from opensfm_gb300.pybundle import adjuster_from_scene
     scene = syn.street_scene(n_shots=street_shots, n_points=street_points, seed=seed, outlier_ratio=0.0)
+    rng = np.random.default_rng(seed + 1)
+    centres = scene.extras["true_poses"][:, 3:]
+    scene.extras["gps"] = np.ascontiguousarray(centres + rng.normal(0.0, 0.05, centres.shape))
+    scene.extras["gps_std"] = np.full(centres.shape, 0.05)
     times = {}
     valid = None
     for cov in (False, True):
-        ba = adjuster_from_scene(scene, precision="fp64", loss=("SoftLOneLoss", 1.0), irls="none", gps=False,
+        ba = adjuster_from_scene(scene, precision="fp64", loss=("SoftLOneLoss", 1.0), irls="none", gps=True,
                                  max_iterations=max_iterations, linear_solver="DENSE_SCHUR", covariances=cov)
         t0 = time.perf_counter()
         ba.run()

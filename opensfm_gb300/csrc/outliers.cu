@@ -11,8 +11,10 @@
 //
 // The medians are exact: a radix selection over the FP64 bit patterns
 // (mapped to order-preserving unsigned keys, 11-bit digits, one histogram
-// pass per digit) returns the element of the requested rank, so the
-// threshold is the one a sort would give.  Products and sums that decide a
+// pass per digit for both error columns at once, the digit found by a
+// one-block scan on the device) returns the element of the requested rank,
+// so the threshold is the one a sort would give.  The whole selection runs
+// on the stream without a host synchronization.  Products and sums that decide a
 // comparison are rounded without contraction (__dmul_rn / __dadd_rn), as
 // the host computes them.
 #include <cuda_runtime.h>
@@ -36,67 +38,124 @@ __device__ __forceinline__ uint64_t order_key(double v) {
   return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
 }
 
-double key_value(uint64_t k) {
+__device__ __forceinline__ double key_to_double(uint64_t k) {
   const uint64_t b = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
-  double v;
-  std::memcpy(&v, &b, sizeof(v));
-  return v;
+  return __longlong_as_double(static_cast<long long>(b));
 }
 
-// Histogram of one digit of the keys of v[i * stride] whose higher bits
-// match the selected prefix.
-__global__ void digit_histogram_kernel(int64_t n, const double* __restrict__ v, int stride, uint64_t prefix,
-                                       uint64_t prefix_mask, int shift, uint32_t digit_mask,
+// Radix selection state of one column: the digits fixed so far (prefix
+// under mask) and the rank still sought among the keys that match them.
+struct SelectState {
+  unsigned long long prefix, mask;
+  long long rank;
+};
+
+// Histogram of one digit of the keys of column c (c < n_cols <= 2) of
+// v[i * stride + c] whose higher digits match the column's prefix.
+__global__ void digit_histogram_kernel(int64_t n, const double* __restrict__ v, int stride, int n_cols,
+                                       const SelectState* __restrict__ st, int shift, uint32_t digit_mask,
                                        unsigned* __restrict__ hist) {
-  __shared__ unsigned h[kBins];
-  for (int b = threadIdx.x; b < kBins; b += blockDim.x) h[b] = 0u;
+  __shared__ unsigned h[2][kBins];
+  for (int b = threadIdx.x; b < n_cols * kBins; b += blockDim.x) h[b / kBins][b % kBins] = 0u;
   __syncthreads();
+  const uint64_t p0 = st[0].prefix, m0 = st[0].mask;
+  const uint64_t p1 = n_cols > 1 ? st[1].prefix : 0, m1 = n_cols > 1 ? st[1].mask : 0;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
-    const uint64_t k = order_key(v[i * stride]);
-    if ((k & prefix_mask) == prefix) atomicAdd(&h[uint32_t(k >> shift) & digit_mask], 1u);
+    const uint64_t k0 = order_key(v[i * stride]);
+    if ((k0 & m0) == p0) atomicAdd(&h[0][uint32_t(k0 >> shift) & digit_mask], 1u);
+    if (n_cols > 1) {
+      const uint64_t k1 = order_key(v[i * stride + 1]);
+      if ((k1 & m1) == p1) atomicAdd(&h[1][uint32_t(k1 >> shift) & digit_mask], 1u);
+    }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < kBins; b += blockDim.x)
-    if (h[b]) atomicAdd(&hist[b], h[b]);
+  for (int b = threadIdx.x; b < n_cols * kBins; b += blockDim.x)
+    if (h[b / kBins][b % kBins]) atomicAdd(&hist[b], h[b / kBins][b % kBins]);
 }
 
-// |e_i - m| for the 2D errors.
-__global__ void deviation_kernel(int64_t n, const double* __restrict__ e, int stride, double mx, double my,
-                                 double* __restrict__ dev) {
+// The digit of the sought rank in each column's histogram, appended to the
+// column's prefix (one thread per column; 2048 bins).
+__global__ void digit_select_kernel(int n_cols, const unsigned* __restrict__ hist, SelectState* __restrict__ st,
+                                    int shift, uint32_t digit_mask) {
+  const int c = threadIdx.x;
+  if (c >= n_cols) return;
+  const long long rank = st[c].rank;
+  long long cum = 0;
+  uint32_t digit = 0;
+  for (uint32_t b = 0; b <= digit_mask; ++b) {
+    const long long h = hist[c * kBins + b];
+    if (cum + h > rank) {
+      digit = b;
+      break;
+    }
+    cum += h;
+  }
+  st[c].rank = rank - cum;
+  st[c].prefix |= static_cast<unsigned long long>(digit) << shift;
+  st[c].mask |= static_cast<unsigned long long>(digit_mask) << shift;
+}
+
+// |e_i - m| for the 2D errors, m the selected medians.
+__global__ void deviation_kernel(int64_t n, const double* __restrict__ e, int stride,
+                                 const SelectState* __restrict__ st, double* __restrict__ dev) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  const double mx = key_to_double(st[0].prefix), my = key_to_double(st[1].prefix);
   const double dx = __dadd_rn(e[i * stride], -mx);
   const double dy = __dadd_rn(e[i * stride + 1], -my);
   dev[i] = sqrt(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
 }
 
-// Outlier flags and per-point counts of observations and outliers.
+// AUTO threshold = ratio * |(m_x + s, m_y + s)|, s = 1.486 * the median
+// deviation; writes the threshold and its square.
+__global__ void auto_threshold_kernel(const SelectState* __restrict__ st, double ratio, double* __restrict__ thr) {
+  const double mx = key_to_double(st[0].prefix), my = key_to_double(st[1].prefix);
+  const double robust_std = __dmul_rn(1.486, key_to_double(st[2].prefix));
+  const double ax = __dadd_rn(mx, robust_std), ay = __dadd_rn(my, robust_std);
+  const double t = __dmul_rn(ratio, sqrt(__dadd_rn(__dmul_rn(ax, ax), __dmul_rn(ay, ay))));
+  thr[0] = t;
+  thr[1] = __dmul_rn(t, t);
+}
+
+// Adds the warp's count of `pred` to *counter with one atomic (every lane
+// of the warp calls it).
+__device__ __forceinline__ void warp_count(bool pred, unsigned long long* counter) {
+  const unsigned m = __ballot_sync(0xffffffffu, pred);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(counter, static_cast<unsigned long long>(__popc(m)));
+}
+
+// Outlier flags and per-point counts of observations and outliers.  The
+// total is counted per warp: one atomic on the shared counter per warp
+// rather than one per outlier.
 __global__ void flag_kernel(int64_t n, const double* __restrict__ e, int stride, const double* __restrict__ w,
-                            const int32_t* __restrict__ obs_point, double thr_sqr, double weight_threshold,
-                            uint8_t* __restrict__ flags, unsigned* __restrict__ point_obs,
+                            const int32_t* __restrict__ obs_point, const double* __restrict__ thr,
+                            double weight_threshold, uint8_t* __restrict__ flags, unsigned* __restrict__ point_obs,
                             unsigned* __restrict__ point_out, unsigned long long* __restrict__ n_out) {
   const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double x = e[i * stride], y = e[i * stride + 1];
-  const double sq = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
-  const bool out = sq > thr_sqr || w[i] < weight_threshold;
-  flags[i] = out ? 1 : 0;
-  const int p = obs_point[i];
-  atomicAdd(&point_obs[p], 1u);
-  if (out) {
-    atomicAdd(&point_out[p], 1u);
-    atomicAdd(n_out, 1ull);
+  const double thr_sqr = thr[1];
+  bool out = false;
+  if (i < n) {
+    const double x = e[i * stride], y = e[i * stride + 1];
+    const double sq = __dadd_rn(__dmul_rn(x, x), __dmul_rn(y, y));
+    out = sq > thr_sqr || w[i] < weight_threshold;
+    flags[i] = out ? 1 : 0;
+    const int p = obs_point[i];
+    atomicAdd(&point_obs[p], 1u);
+    if (out) atomicAdd(&point_out[p], 1u);
   }
+  warp_count(out, n_out);
 }
 
 __global__ void removed_kernel(int64_t n_points, const unsigned* __restrict__ point_obs,
                                const unsigned* __restrict__ point_out, uint8_t* __restrict__ removed,
                                unsigned long long* __restrict__ n_removed) {
   const int64_t p = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (p >= n_points) return;
-  const bool r = point_out[p] > 0 && point_obs[p] - point_out[p] < 2;
-  removed[p] = r ? 1 : 0;
-  if (r) atomicAdd(n_removed, 1ull);
+  bool r = false;
+  if (p < n_points) {
+    r = point_out[p] > 0 && point_obs[p] - point_out[p] < 2;
+    removed[p] = r ? 1 : 0;
+  }
+  warp_count(r, n_removed);
 }
 
 // Host arithmetic rounded operation by operation (no fused multiply-add
@@ -105,44 +164,27 @@ double mul_rn(double a, double b) {
   volatile double r = a * b;
   return r;
 }
-double add_rn(double a, double b) {
-  volatile double r = a + b;
-  return r;
-}
 
 int grid_for(int64_t n, int block = 256, int cap = 152 * 8) {
   return int(std::max<int64_t>(1, std::min<int64_t>(cap, (n + block - 1) / block)));
 }
 
-// The element of rank `rank` (0-based, ascending) of v[i * stride], i < n.
-double select_rank(const double* v, int stride, int64_t n, int64_t rank, DeviceArray<unsigned>& hist) {
-  uint64_t prefix = 0, mask = 0;
-  std::vector<unsigned> h(kBins);
+// Radix selection of the element of rank st[c].rank (0-based, ascending)
+// of each column c < n_cols of v[i * stride + c], i < n: six passes of an
+// 11-bit digit, each a histogram and a one-block scan on the device, no
+// host synchronization.  The selected keys are left in st[c].prefix.
+void select_ranks(const double* v, int stride, int n_cols, int64_t n, SelectState* st, DeviceArray<unsigned>& hist) {
   int top = 64;
   while (top > 0) {
     const int width = top >= kDigitBits ? kDigitBits : top;
     const int shift = top - width;
     const uint32_t dmask = (1u << width) - 1u;
     hist.zero();
-    digit_histogram_kernel<<<grid_for(n), 256>>>(n, v, stride, prefix, mask, shift, dmask, hist.get());
+    digit_histogram_kernel<<<grid_for(n), 256>>>(n, v, stride, n_cols, st, shift, dmask, hist.get());
+    digit_select_kernel<<<1, 32>>>(n_cols, hist.get(), st, shift, dmask);
     GB_CUDA(cudaGetLastError());
-    hist.download(h.data(), kBins);
-    GB_CUDA(cudaDeviceSynchronize());
-    int64_t cum = 0;
-    uint32_t digit = 0;
-    for (uint32_t b = 0; b <= dmask; ++b) {
-      if (cum + int64_t(h[b]) > rank) {
-        digit = b;
-        break;
-      }
-      cum += h[b];
-    }
-    rank -= cum;
-    prefix |= uint64_t(digit) << shift;
-    mask |= uint64_t(dmask) << shift;
     top = shift;
   }
-  return key_value(prefix);
 }
 
 }  // namespace
@@ -165,22 +207,26 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
   cudaEvent_t ev[2];
   for (cudaEvent_t& x : ev) GB_CUDA(cudaEventCreate(&x));
   GB_CUDA(cudaEventRecord(ev[0]));
-  double threshold = 1.0;
+  DeviceArray<double> thr(2);
   if (cfg.filter_type == 0) {
-    threshold = cfg.fixed_threshold;
+    const double t[2] = {cfg.fixed_threshold, mul_rn(cfg.fixed_threshold, cfg.fixed_threshold)};
+    thr.upload(t, 2);
   } else {
-    DeviceArray<unsigned> hist(kBins);
-    const int64_t mid = n / 2;
-    const double mx = select_rank(e.get(), stride, n, mid, hist);
-    const double my = select_rank(e.get() + 1, stride, n, mid, hist);
+    // medians of the two error columns (one pass per digit for both), then
+    // the median deviation, all on the device
+    DeviceArray<unsigned> hist(2 * kBins);
+    DeviceArray<SelectState> st(3);
+    const long long mid = static_cast<long long>(n / 2);
+    const SelectState init[3] = {{0ull, 0ull, mid}, {0ull, 0ull, mid}, {0ull, 0ull, mid}};
+    st.upload(init, 3);
+    select_ranks(e.get(), stride, 2, n, st.get(), hist);
     dev.resize(size_t(n));
-    deviation_kernel<<<int((n + 255) / 256), 256>>>(n, e.get(), stride, mx, my, dev.get());
+    deviation_kernel<<<int((n + 255) / 256), 256>>>(n, e.get(), stride, st.get(), dev.get());
     GB_CUDA(cudaGetLastError());
-    const double robust_std = mul_rn(1.486, select_rank(dev.get(), 1, n, mid, hist));
-    const double ax = add_rn(mx, robust_std), ay = add_rn(my, robust_std);
-    threshold = mul_rn(cfg.auto_ratio, std::sqrt(add_rn(mul_rn(ax, ax), mul_rn(ay, ay))));
+    select_ranks(dev.get(), 1, 1, n, st.get() + 2, hist);
+    auto_threshold_kernel<<<1, 1>>>(st.get(), cfg.auto_ratio, thr.get());
+    GB_CUDA(cudaGetLastError());
   }
-  res.threshold = threshold;
   DeviceArray<uint8_t> f{static_cast<size_t>(n)}, rem{static_cast<size_t>(std::max<int64_t>(1, n_points))};
   DeviceArray<unsigned> pobs{static_cast<size_t>(std::max<int64_t>(1, n_points))},
       pout{static_cast<size_t>(std::max<int64_t>(1, n_points))};
@@ -188,21 +234,24 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
   pobs.zero();
   pout.zero();
   counts.zero();
-  flag_kernel<<<int((n + 255) / 256), 256>>>(n, e.get(), stride, w.get(), op.get(), mul_rn(threshold, threshold),
-                                             cfg.weight_threshold, f.get(), pobs.get(), pout.get(), counts.get());
+  flag_kernel<<<int((n + 255) / 256), 256>>>(n, e.get(), stride, w.get(), op.get(), thr.get(), cfg.weight_threshold,
+                                             f.get(), pobs.get(), pout.get(), counts.get());
   if (n_points > 0)
     removed_kernel<<<int((n_points + 255) / 256), 256>>>(n_points, pobs.get(), pout.get(), rem.get(),
                                                          counts.get() + 1);
   GB_CUDA(cudaGetLastError());
   GB_CUDA(cudaEventRecord(ev[1]));
   unsigned long long c[2];
+  double t[2];
   counts.download(c, 2);
+  thr.download(t, 2);
   f.download(flags, size_t(n));
   if (n_points > 0) rem.download(point_removed, size_t(n_points));
   GB_CUDA(cudaDeviceSynchronize());
   float ms = 0.0f;
   GB_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
   for (cudaEvent_t& x : ev) GB_CUDA(cudaEventDestroy(x));
+  res.threshold = t[0];
   res.n_outliers = int64_t(c[0]);
   res.n_removed_points = int64_t(c[1]);
   res.device_seconds = 1e-3 * double(ms);

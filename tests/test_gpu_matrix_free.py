@@ -50,8 +50,9 @@ def test_matrix_free_matches_stored(kind, precision):
     bar = 1e-10 if precision == "fp64" else (3e-5 if kind == "street" else 1e-6)
     assert abs(a - b) / a < bar, (a, b)
     if precision == "fp64":
-        # the same trajectory: the same step sequence
-        np.testing.assert_allclose(stored.trace()[:, 1], free.trace()[:, 1], rtol=1e-9)
+        # the same trajectory: the same step sequence (FP64 atomics sum in
+        # a different order in the two paths: costs agree to ~1e-9)
+        np.testing.assert_allclose(stored.trace()[:, 1], free.trace()[:, 1], rtol=1e-8)
 
 
 def test_auto_mode_stores_records_that_fit():
