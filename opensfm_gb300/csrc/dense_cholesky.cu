@@ -661,6 +661,233 @@ __global__ void cg_rotate_kernel(double* scal) {
   scal[kRzMix] = 0.0;
 }
 
+// ---- batched columns (inverse_columns): K right-hand sides in lockstep,
+// vectors stored [n_pad][K] row-major so that a warp reads one row's K
+// values.  Per-column scalars at mscal[c * kNumScal + ...].
+constexpr int kRhs = DenseSpdSolver::kInverseBatch;
+
+// Adds v to out[c] for the column c of each thread: a shared-memory sum per
+// block, then one global atomic per column.
+__device__ __forceinline__ void column_add(double v, int c, int K, double* out, int which) {
+  __shared__ double cs[kRhs];
+  if (threadIdx.x < kRhs) cs[threadIdx.x] = 0.0;
+  __syncthreads();
+  if (c >= 0 && v != 0.0) atomicAdd(&cs[c], v);
+  __syncthreads();
+  if (threadIdx.x < K && cs[threadIdx.x] != 0.0) atomicAdd(&out[threadIdx.x * kNumScal + which], cs[threadIdx.x]);
+}
+
+// x = 0, r = e_{unit[c]}, rs = fp32(D r) (rows n .. n_pad - 1 zero), bb = |D e|^2
+__global__ void mcg_init_kernel(int n, int n_pad, int K, const int* __restrict__ unit, const double* __restrict__ d,
+                                double* __restrict__ X, double* __restrict__ R, float* __restrict__ RS,
+                                double* __restrict__ scal) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n_pad) * K) return;
+  const int i = int(t / K), c = int(t % K);
+  const double b = (i < n && i == unit[c]) ? 1.0 : 0.0;
+  X[t] = 0.0;
+  R[t] = b;
+  RS[t] = i < n ? float(d[i] * b) : 0.f;
+  if (b != 0.0) scal[c * kNumScal + kBb] = d[i] * d[i];
+}
+
+// Forward step k of the triangular solve with K right-hand sides:
+// Y_k = Dinv_k B_k (CTA 0 stores it), B_i -= L_ik Y_k for i > k.
+__global__ void __launch_bounds__(kTsThreads) mfwd_step_kernel(const float* __restrict__ L, int ld,
+                                                               const float* __restrict__ dinv, int k, int K,
+                                                               float* __restrict__ B, float* __restrict__ Y) {
+  __shared__ float bk[kTile * kRhs], yk[kTile * kRhs];
+  const int tid = threadIdx.x, tk = kTile * K;
+  for (int e = tid; e < tk; e += kTsThreads) bk[e] = B[int64_t(k) * kTile * K + e];
+  __syncthreads();
+  const float* D = dinv + int64_t(k) * kTile * kTile;
+  for (int e = tid; e < tk; e += kTsThreads) {
+    const int r = e / K, c = e - r * K;
+    const float* dr = D + r * kTile;
+    float s = 0.f;
+#pragma unroll 8
+    for (int j = 0; j < kTile; ++j) s += dr[j] * bk[j * K + c];
+    yk[e] = s;
+  }
+  __syncthreads();
+  if (blockIdx.x == 0) {
+    for (int e = tid; e < tk; e += kTsThreads) Y[int64_t(k) * kTile * K + e] = yk[e];
+    return;
+  }
+  const int i = k + int(blockIdx.x);
+  for (int e = tid; e < tk; e += kTsThreads) {
+    const int r = e / K, c = e - r * K;
+    const float* lr = L + int64_t(i * kTile + r) * ld + k * kTile;
+    float s = 0.f;
+#pragma unroll 8
+    for (int j = 0; j < kTile; ++j) s += lr[j] * yk[j * K + c];
+    B[(int64_t(i) * kTile + r) * K + c] -= s;
+  }
+}
+
+// Backward step k: X_k = Dinv_k^T Y_k (CTA k stores it), Y_i -= L_ki^T X_k
+// for i < k.
+__global__ void __launch_bounds__(kTsThreads) mbwd_step_kernel(const float* __restrict__ L, int ld,
+                                                               const float* __restrict__ dinv, int k, int K,
+                                                               float* __restrict__ Y, float* __restrict__ X) {
+  __shared__ float tk_[kTile * kRhs], xk[kTile * kRhs];
+  const int tid = threadIdx.x, tk = kTile * K;
+  for (int e = tid; e < tk; e += kTsThreads) tk_[e] = Y[int64_t(k) * kTile * K + e];
+  __syncthreads();
+  const float* D = dinv + int64_t(k) * kTile * kTile;
+  for (int e = tid; e < tk; e += kTsThreads) {
+    const int r = e / K, c = e - r * K;
+    float s = 0.f;
+#pragma unroll 8
+    for (int j = 0; j < kTile; ++j) s += D[j * kTile + r] * tk_[j * K + c];
+    xk[e] = s;
+  }
+  __syncthreads();
+  const int i = int(blockIdx.x);
+  if (i == k) {
+    for (int e = tid; e < tk; e += kTsThreads) X[int64_t(k) * kTile * K + e] = xk[e];
+    return;
+  }
+  for (int e = tid; e < tk; e += kTsThreads) {
+    const int r = e / K, c = e - r * K;
+    float s = 0.f;
+#pragma unroll 8
+    for (int j = 0; j < kTile; ++j) s += L[int64_t(k * kTile + j) * ld + i * kTile + r] * xk[j * K + c];
+    Y[(int64_t(i) * kTile + r) * K + c] -= s;
+  }
+}
+
+// Z = D X (FP64, rows < n)
+__global__ void mts_finish_kernel(int n, int K, const double* __restrict__ d, const float* __restrict__ X,
+                                  double* __restrict__ Z) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n) * K) return;
+  Z[t] = d[t / K] * double(X[t]);
+}
+
+// Q += A P over the column range of blockIdx.y (two halves, so that about
+// 2 n / 32 CTAs share the FP64 pipes), and pq += P.Q per column.  32 rows x
+// K columns per CTA; thread (row r = tid / 8, columns 4 (tid % 8) .. + 3).
+constexpr int kSymmRows = 32, kSymmK = 32;
+__global__ void __launch_bounds__(256) msymm_kernel(int n, int K, const double* __restrict__ A, int lda,
+                                                    const double* __restrict__ P, double* __restrict__ Q,
+                                                    double* __restrict__ scal) {
+  __shared__ double As[kSymmRows][kSymmK + 1];
+  __shared__ double Ps[kSymmK][kRhs];
+  const int tid = threadIdx.x, r = tid >> 3, cg = (tid & 7) * 4;
+  const int row0 = blockIdx.x * kSymmRows;
+  const int half = (n + 1) / 2;
+  const int j_begin = blockIdx.y == 0 ? 0 : half, j_end = blockIdx.y == 0 ? half : n;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int j0 = j_begin; j0 < j_end; j0 += kSymmK) {
+    for (int e = tid; e < kSymmRows * kSymmK; e += 256) {
+      const int rr = e / kSymmK, jj = e % kSymmK;
+      const int gi = row0 + rr, gj = j0 + jj;
+      As[rr][jj] = (gi < n && gj < j_end) ? A[int64_t(gi) * lda + gj] : 0.0;
+    }
+    for (int e = tid; e < kSymmK * kRhs; e += 256) {
+      const int jj = e / kRhs, c = e % kRhs;
+      const int gj = j0 + jj;
+      Ps[jj][c] = (gj < j_end && c < K) ? P[int64_t(gj) * K + c] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int jj = 0; jj < kSymmK; ++jj) {
+      const double a = As[r][jj];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[q] += a * Ps[jj][cg + q];
+    }
+    __syncthreads();
+  }
+  const int gi = row0 + r;
+  double pq[4] = {0.0, 0.0, 0.0, 0.0};
+  if (gi < n) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = cg + q;
+      if (c < K) {
+        atomicAdd(&Q[int64_t(gi) * K + c], acc[q]);
+        pq[q] = acc[q] * P[int64_t(gi) * K + c];
+      }
+    }
+  }
+  __shared__ double cs[kRhs];
+  if (tid < kRhs) cs[tid] = 0.0;
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    if (pq[q] != 0.0) atomicAdd(&cs[cg + q], pq[q]);
+  __syncthreads();
+  if (tid < K && cs[tid] != 0.0) atomicAdd(&scal[tid * kNumScal + kPq], cs[tid]);
+}
+
+// alpha_c = rz_c / pq_c; X += alpha P; R -= alpha Q; RS = fp32(D R); rr += |D R|^2
+__global__ void mcg_update_kernel(int n, int K, const double* __restrict__ P, const double* __restrict__ Q,
+                                  const double* __restrict__ d, double* __restrict__ X, double* __restrict__ R,
+                                  float* __restrict__ RS, double* __restrict__ scal) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = -1;
+  double e = 0.0;
+  if (t < int64_t(n) * K) {
+    c = int(t % K);
+    const double pq = scal[c * kNumScal + kPq];
+    const double alpha = pq > 0.0 ? scal[c * kNumScal + kRz] / pq : 0.0;
+    X[t] += alpha * P[t];
+    const double v = R[t] - alpha * Q[t];
+    R[t] = v;
+    const double sv = d[t / K] * v;
+    RS[t] = float(sv);
+    e = sv * sv;
+  }
+  column_add(e, c, K, scal, kRr);
+}
+
+// rz_new += R.Z_new, rz_mix += R.Z_old per column (Z_old null: first direction)
+__global__ void mcg_dots_kernel(int n, int K, const double* __restrict__ R, const double* __restrict__ Zn,
+                                const double* __restrict__ Zo, double* __restrict__ scal) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  int c = -1;
+  double a = 0.0, b = 0.0;
+  if (t < int64_t(n) * K) {
+    c = int(t % K);
+    a = R[t] * Zn[t];
+    if (Zo) b = R[t] * Zo[t];
+  }
+  column_add(a, c, K, scal, kRzNew);
+  if (Zo) column_add(b, c, K, scal, kRzMix);
+}
+
+// P = Z + beta_c P (beta = 0 on the first direction)
+__global__ void mcg_dir_kernel(int n, int K, const double* __restrict__ Z, double* __restrict__ P,
+                               const double* __restrict__ scal, int first) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n) * K) return;
+  const int c = int(t % K);
+  const double rz = scal[c * kNumScal + kRz];
+  const double beta = first || !(rz != 0.0) ? 0.0 : (scal[c * kNumScal + kRzNew] - scal[c * kNumScal + kRzMix]) / rz;
+  P[t] = Z[t] + beta * P[t];
+}
+
+__global__ void mcg_rotate_kernel(int K, double* scal) {
+  const int c = threadIdx.x;
+  if (c >= K) return;
+  double* s = scal + c * kNumScal;
+  s[kRz] = s[kRzNew];
+  s[kPq] = 0.0;
+  s[kRr] = 0.0;
+  s[kRzNew] = 0.0;
+  s[kRzMix] = 0.0;
+}
+
+// out[6 c + k] = X[gather[6 c + k], c] (-1: 0)
+__global__ void mgather_kernel(int K, const int* __restrict__ gather, const double* __restrict__ X,
+                               double* __restrict__ out) {
+  const int t = threadIdx.x;
+  if (t >= 6 * K) return;
+  const int c = t / 6, g = gather[t];
+  out[t] = g >= 0 ? X[int64_t(g) * K + c] : 0.0;
+}
+
 void set_smem(const void* f, int bytes) {
   GB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
 }
@@ -830,6 +1057,88 @@ int DenseSpdSolver::solve(const double* b, double* x, double tol, int max_iterat
   GB_CUDA(cudaGetLastError());
   if (stats) *stats = out;
   return out.status;
+}
+
+int DenseSpdSolver::inverse_columns(const int* unit, int m, const int* gather, double* out, double tol,
+                                    int max_iterations) {
+  if (n_ <= 0 || m <= 0) return 0;
+  const int n = n_;
+  const size_t nk = size_t(n_pad_) * kRhs;
+  mv_.resize(6 * nk);
+  mts_.resize(4 * nk);
+  mscal_.resize(size_t(kRhs) * kNumScal);
+  mout_.resize(6 * kRhs);
+  munit_.resize(kRhs);
+  mgather_.resize(6 * kRhs);
+  int failed = 0;
+  std::vector<double> s2(size_t(kRhs) * kNumScal), bb(kRhs);
+  for (int c0 = 0; c0 < m && !failed; c0 += kRhs) {
+    const int K = std::min(kRhs, m - c0);
+    const size_t vk = size_t(n_pad_) * K;
+    double* X = mv_.get();
+    double* R = X + vk;
+    double* P = R + vk;
+    double* Q = P + vk;
+    double* Zn = Q + vk;
+    double* Zo = Zn + vk;
+    float* RS = mts_.get();
+    float* TB = RS + vk;
+    float* TY = TB + vk;
+    float* TX = TY + vk;
+    double* scal = mscal_.get();
+    munit_.upload(unit + c0, K);
+    mgather_.upload(gather + 6 * size_t(c0), 6 * size_t(K));
+    const int ge = int((int64_t(n_pad_) * K + 255) / 256);
+    const int gn = int((int64_t(n) * K + 255) / 256);
+    // Z = D (L L^T)^-1 RS, K columns
+    auto precondition = [&](double* Z) {
+      GB_CUDA(cudaMemcpyAsync(TB, RS, vk * sizeof(float), cudaMemcpyDeviceToDevice));
+      for (int k = 0; k < nt_; ++k)
+        mfwd_step_kernel<<<nt_ - k, kTsThreads>>>(L_.get(), n_pad_, dinv_.get(), k, K, TB, TY);
+      for (int k = nt_ - 1; k >= 0; --k)
+        mbwd_step_kernel<<<k + 1, kTsThreads>>>(L_.get(), n_pad_, dinv_.get(), k, K, TY, TX);
+      mts_finish_kernel<<<gn, 256>>>(n, K, dscale_.get(), TX, Z);
+    };
+    mscal_.zero();
+    mcg_init_kernel<<<ge, 256>>>(n, n_pad_, K, munit_.get(), dscale_.get(), X, R, RS, scal);
+    precondition(Zo);
+    mcg_dots_kernel<<<gn, 256>>>(n, K, R, Zo, nullptr, scal);
+    mcg_dir_kernel<<<gn, 256>>>(n, K, Zo, P, scal, 1);
+    GB_CUDA(cudaMemcpy(s2.data(), scal, sizeof(double) * K * kNumScal, cudaMemcpyDeviceToHost));
+    for (int c = 0; c < K; ++c) bb[c] = s2[c * kNumScal + kBb];
+    mcg_rotate_kernel<<<1, kRhs>>>(K, scal);
+    GB_CUDA(cudaGetLastError());
+    bool done = false;
+    for (int it = 0; it < max_iterations && !done; ++it) {
+      GB_CUDA(cudaMemsetAsync(Q, 0, vk * sizeof(double)));
+      msymm_kernel<<<dim3((n + kSymmRows - 1) / kSymmRows, 2), 256>>>(n, K, A_, lda_, P, Q, scal);
+      mcg_update_kernel<<<gn, 256>>>(n, K, P, Q, dscale_.get(), X, R, RS, scal);
+      GB_CUDA(cudaMemcpy(s2.data(), scal, sizeof(double) * K * kNumScal, cudaMemcpyDeviceToHost));
+      done = true;
+      for (int c = 0; c < K; ++c) {
+        const double pq = s2[c * kNumScal + kPq], rr = s2[c * kNumScal + kRr];
+        const double rel = bb[c] > 0.0 ? std::sqrt(rr / bb[c]) : 0.0;
+        if (!std::isfinite(rel)) failed = 1;
+        if (rel > tol) {
+          done = false;
+          if (!(pq > 0.0)) failed = 1;  // p . A p <= 0 before convergence: not positive definite
+        }
+      }
+      if (failed) break;
+      if (done) break;
+      precondition(Zn);
+      mcg_dots_kernel<<<gn, 256>>>(n, K, R, Zn, Zo, scal);
+      mcg_dir_kernel<<<gn, 256>>>(n, K, Zn, P, scal, 0);
+      mcg_rotate_kernel<<<1, kRhs>>>(K, scal);
+      std::swap(Zn, Zo);
+    }
+    if (!done) failed = 1;
+    mgather_kernel<<<1, 6 * kRhs>>>(K, mgather_.get(), X, mout_.get());
+    GB_CUDA(cudaGetLastError());
+    mout_.download(out + 6 * size_t(c0), 6 * size_t(K));
+    GB_CUDA(cudaDeviceSynchronize());
+  }
+  return failed;
 }
 
 }  // namespace gbba

@@ -34,6 +34,14 @@ class DenseSpdSolver {
   // residual tol within max_iterations FP64 conjugate-gradient iterations
   // preconditioned by the factor.
   int solve(const double* b, double* x, double tol, int max_iterations, DenseSolveStats* stats);
+  // Columns of A^-1, up to kInverseBatch at a time by conjugate gradients
+  // in lockstep (FP64, preconditioned by the factor, every column to the
+  // relative scaled residual tol): column c solves A x = e_{unit[c]} and
+  // returns x at the dense indices gather[6 c .. 6 c + 5] (-1: 0) in
+  // out[6 c .. 6 c + 5].  Host arrays of m columns.  Returns 0, or 1 when a
+  // column met p.Ap <= 0 or did not converge within max_iterations.
+  static constexpr int kInverseBatch = 32;
+  int inverse_columns(const int* unit, int m, const int* gather, double* out, double tol, int max_iterations);
   int n() const { return n_; }
   double shift() const { return shift_; }  // diagonal shift the factor needed (0 normally)
 
@@ -44,6 +52,11 @@ class DenseSpdSolver {
   DeviceArray<float> L_, dinv_, rs_, ts_;
   DeviceArray<double> dscale_, r_, z_, scal_;
   DeviceArray<int> status_;
+  // batched columns: FP64 x, r, p, q, z_new, z_old and FP32 rs, b, y, x, all
+  // [n_pad][kInverseBatch] row-major, per-column scalars, index tables
+  DeviceArray<double> mv_, mscal_, mout_;
+  DeviceArray<float> mts_;
+  DeviceArray<int> munit_, mgather_;
 };
 
 // C = A B^T on the tensor cores for row-major device FP32 matrices A (m x k,

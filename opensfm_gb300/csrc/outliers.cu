@@ -74,25 +74,57 @@ __global__ void digit_histogram_kernel(int64_t n, const double* __restrict__ v, 
 }
 
 // The digit of the sought rank in each column's histogram, appended to the
-// column's prefix (one thread per column; 2048 bins).
-__global__ void digit_select_kernel(int n_cols, const unsigned* __restrict__ hist, SelectState* __restrict__ st,
-                                    int shift, uint32_t digit_mask) {
-  const int c = threadIdx.x;
-  if (c >= n_cols) return;
-  const long long rank = st[c].rank;
-  long long cum = 0;
-  uint32_t digit = 0;
-  for (uint32_t b = 0; b <= digit_mask; ++b) {
-    const long long h = hist[c * kBins + b];
-    if (cum + h > rank) {
-      digit = b;
-      break;
-    }
-    cum += h;
+// column's prefix: one block of 256 threads per column, 8 bins a thread, a
+// block-wide exclusive scan of the thread sums; the thread whose bins hold
+// the rank writes the digit.
+constexpr int kSelectThreads = 256;
+constexpr int kBinsPerThread = kBins / kSelectThreads;
+
+__global__ void __launch_bounds__(kSelectThreads)
+    digit_select_kernel(const unsigned* __restrict__ hist, SelectState* __restrict__ st, int shift,
+                        uint32_t digit_mask) {
+  const int c = blockIdx.x, t = threadIdx.x;
+  const long long rank = st[c].rank;  // read by every thread before the writer's update
+  const unsigned* hc = hist + c * kBins;
+  long long local[kBinsPerThread];
+  long long sum = 0;
+#pragma unroll
+  for (int k = 0; k < kBinsPerThread; ++k) {
+    local[k] = hc[t * kBinsPerThread + k];
+    sum += local[k];
   }
-  st[c].rank = rank - cum;
-  st[c].prefix |= static_cast<unsigned long long>(digit) << shift;
-  st[c].mask |= static_cast<unsigned long long>(digit_mask) << shift;
+  long long incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long v = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((t & 31) >= o) incl += v;
+  }
+  __shared__ long long warp_sums[kSelectThreads / 32];
+  if ((t & 31) == 31) warp_sums[t >> 5] = incl;
+  __syncthreads();
+  long long excl = incl - sum;
+  for (int w = 0; w < (t >> 5); ++w) excl += warp_sums[w];
+  long long total = 0;
+  for (int w = 0; w < kSelectThreads / 32; ++w) total += warp_sums[w];
+  int digit = -1;
+  long long cum = excl;
+  if (excl <= rank && rank < excl + sum) {
+    for (int k = 0; k < kBinsPerThread; ++k) {
+      if (cum + local[k] > rank) {
+        digit = t * kBinsPerThread + k;
+        break;
+      }
+      cum += local[k];
+    }
+  } else if (t == kSelectThreads - 1 && rank >= total) {
+    digit = 0;  // no key of that rank (cannot happen for rank < n): digit 0, as a sequential scan leaves it
+    cum = total;
+  }
+  if (digit >= 0) {
+    st[c].rank = rank - cum;
+    st[c].prefix |= static_cast<unsigned long long>(uint32_t(digit) & digit_mask) << shift;
+    st[c].mask |= static_cast<unsigned long long>(digit_mask) << shift;
+  }
 }
 
 // |e_i - m| for the 2D errors, m the selected medians.
@@ -181,7 +213,7 @@ void select_ranks(const double* v, int stride, int n_cols, int64_t n, SelectStat
     const uint32_t dmask = (1u << width) - 1u;
     hist.zero();
     digit_histogram_kernel<<<grid_for(n), 256>>>(n, v, stride, n_cols, st, shift, dmask, hist.get());
-    digit_select_kernel<<<1, 32>>>(n_cols, hist.get(), st, shift, dmask);
+    digit_select_kernel<<<n_cols, kSelectThreads>>>(hist.get(), st, shift, dmask);
     GB_CUDA(cudaGetLastError());
     top = shift;
   }
