@@ -691,70 +691,133 @@ __global__ void mcg_init_kernel(int n, int n_pad, int K, const int* __restrict__
   if (b != 0.0) scal[c * kNumScal + kBb] = d[i] * d[i];
 }
 
-// Forward step k of the triangular solve with K right-hand sides:
-// Y_k = Dinv_k B_k (CTA 0 stores it), B_i -= L_ik Y_k for i > k.
-__global__ void __launch_bounds__(kTsThreads) mfwd_step_kernel(const float* __restrict__ L, int ld,
-                                                               const float* __restrict__ dinv, int k, int K,
-                                                               float* __restrict__ B, float* __restrict__ Y) {
-  __shared__ float bk[kTile * kRhs], yk[kTile * kRhs];
-  const int tid = threadIdx.x, tk = kTile * K;
-  for (int e = tid; e < tk; e += kTsThreads) bk[e] = B[int64_t(k) * kTile * K + e];
-  __syncthreads();
-  const float* D = dinv + int64_t(k) * kTile * kTile;
-  for (int e = tid; e < tk; e += kTsThreads) {
-    const int r = e / K, c = e - r * K;
-    const float* dr = D + r * kTile;
-    float s = 0.f;
-#pragma unroll 8
-    for (int j = 0; j < kTile; ++j) s += dr[j] * bk[j * K + c];
-    yk[e] = s;
-  }
-  __syncthreads();
-  if (blockIdx.x == 0) {
-    for (int e = tid; e < tk; e += kTsThreads) Y[int64_t(k) * kTile * K + e] = yk[e];
-    return;
-  }
-  const int i = k + int(blockIdx.x);
-  for (int e = tid; e < tk; e += kTsThreads) {
-    const int r = e / K, c = e - r * K;
-    const float* lr = L + int64_t(i * kTile + r) * ld + k * kTile;
-    float s = 0.f;
-#pragma unroll 8
-    for (int j = 0; j < kTile; ++j) s += lr[j] * yk[j * K + c];
-    B[(int64_t(i) * kTile + r) * K + c] -= s;
+// Triangular steps with K <= 32 right-hand sides.  A CTA stages a 128 x 128
+// factor tile in shared memory (Ms[j][r], rows padded to 132 floats) and the
+// 128 x 32 right-hand block (Vs[j][c]); thread (tr, tc) = (tid / 8, tid % 8)
+// computes the 4 x 4 outputs Out[4 tr + a][4 tc + b] = sum_j Ms[j][4 tr + a]
+// Vs[j][4 tc + b] from float4 reads.  Columns c >= K are zero.
+constexpr int kMsLd = kTile + 4;
+constexpr int kMsteps = (kTile * kMsLd + 2 * kTile * kRhs) * int(sizeof(float));  // dynamic shared bytes
+
+// Ms[j][r] = M[r][j] (transpose) or M[j][r], M a 128 x 128 tile at m with
+// leading dimension ld
+__device__ __forceinline__ void load_tile(float* Ms, const float* __restrict__ m, int64_t ld, bool transpose) {
+  for (int e = threadIdx.x; e < kTile * kTile / 4; e += kTsThreads) {
+    const int row = e / (kTile / 4), col = (e % (kTile / 4)) * 4;
+    const float4 v = *reinterpret_cast<const float4*>(m + row * ld + col);
+    if (transpose) {
+      Ms[(col + 0) * kMsLd + row] = v.x;
+      Ms[(col + 1) * kMsLd + row] = v.y;
+      Ms[(col + 2) * kMsLd + row] = v.z;
+      Ms[(col + 3) * kMsLd + row] = v.w;
+    } else {
+      *reinterpret_cast<float4*>(Ms + row * kMsLd + col) = v;
+    }
   }
 }
 
+// Vs[j][c] = V[j * K + c] for c < K, else 0 (128 rows)
+__device__ __forceinline__ void load_rhs(float* Vs, const float* __restrict__ v, int K) {
+  for (int e = threadIdx.x; e < kTile * kRhs; e += kTsThreads) {
+    const int j = e / kRhs, c = e % kRhs;
+    Vs[e] = c < K ? v[int64_t(j) * K + c] : 0.f;
+  }
+}
+
+__device__ __forceinline__ void tile_product(const float* Ms, const float* Vs, float (&acc)[4][4]) {
+  const int r0 = (threadIdx.x >> 3) * 4, c0 = (threadIdx.x & 7) * 4;
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.f;
+#pragma unroll 8
+  for (int j = 0; j < kTile; ++j) {
+    const float4 m = *reinterpret_cast<const float4*>(Ms + j * kMsLd + r0);
+    const float4 v = *reinterpret_cast<const float4*>(Vs + j * kRhs + c0);
+    const float mv[4] = {m.x, m.y, m.z, m.w}, vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) acc[a][b] += mv[a] * vv[b];
+  }
+}
+
+// Forward step k: Y_k = Dinv_k B_k (CTA 0 stores it), B_i -= L_ik Y_k for
+// i = k + blockIdx.x > k.
+__global__ void __launch_bounds__(kTsThreads) mfwd_step_kernel(const float* __restrict__ L, int ld,
+                                                               const float* __restrict__ dinv, int k, int K,
+                                                               float* __restrict__ B, float* __restrict__ Y) {
+  extern __shared__ __align__(16) float msm[];
+  float* Ms = msm;
+  float* Vs = Ms + kTile * kMsLd;
+  float* Os = Vs + kTile * kRhs;
+  const int r0 = (threadIdx.x >> 3) * 4, c0 = (threadIdx.x & 7) * 4;
+  load_tile(Ms, dinv + int64_t(k) * kTile * kTile, kTile, true);
+  load_rhs(Vs, B + int64_t(k) * kTile * K, K);
+  __syncthreads();
+  float acc[4][4];
+  tile_product(Ms, Vs, acc);
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) Os[(r0 + a) * kRhs + c0 + b] = acc[a][b];
+  if (blockIdx.x == 0) {
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (c0 + b < K) Y[(int64_t(k) * kTile + r0 + a) * K + c0 + b] = acc[a][b];
+    return;
+  }
+  const int i = k + int(blockIdx.x);
+  __syncthreads();  // Ms free, Os complete
+  load_tile(Ms, L + int64_t(i) * kTile * ld + int64_t(k) * kTile, ld, true);
+  __syncthreads();
+  tile_product(Ms, Os, acc);
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      if (c0 + b < K) B[(int64_t(i) * kTile + r0 + a) * K + c0 + b] -= acc[a][b];
+}
+
 // Backward step k: X_k = Dinv_k^T Y_k (CTA k stores it), Y_i -= L_ki^T X_k
-// for i < k.
+// for i = blockIdx.x < k.
 __global__ void __launch_bounds__(kTsThreads) mbwd_step_kernel(const float* __restrict__ L, int ld,
                                                                const float* __restrict__ dinv, int k, int K,
                                                                float* __restrict__ Y, float* __restrict__ X) {
-  __shared__ float tk_[kTile * kRhs], xk[kTile * kRhs];
-  const int tid = threadIdx.x, tk = kTile * K;
-  for (int e = tid; e < tk; e += kTsThreads) tk_[e] = Y[int64_t(k) * kTile * K + e];
+  extern __shared__ __align__(16) float msm[];
+  float* Ms = msm;
+  float* Vs = Ms + kTile * kMsLd;
+  float* Os = Vs + kTile * kRhs;
+  const int r0 = (threadIdx.x >> 3) * 4, c0 = (threadIdx.x & 7) * 4;
+  load_tile(Ms, dinv + int64_t(k) * kTile * kTile, kTile, false);
+  load_rhs(Vs, Y + int64_t(k) * kTile * K, K);
   __syncthreads();
-  const float* D = dinv + int64_t(k) * kTile * kTile;
-  for (int e = tid; e < tk; e += kTsThreads) {
-    const int r = e / K, c = e - r * K;
-    float s = 0.f;
-#pragma unroll 8
-    for (int j = 0; j < kTile; ++j) s += D[j * kTile + r] * tk_[j * K + c];
-    xk[e] = s;
-  }
-  __syncthreads();
+  float acc[4][4];
+  tile_product(Ms, Vs, acc);
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) Os[(r0 + a) * kRhs + c0 + b] = acc[a][b];
   const int i = int(blockIdx.x);
   if (i == k) {
-    for (int e = tid; e < tk; e += kTsThreads) X[int64_t(k) * kTile * K + e] = xk[e];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+        if (c0 + b < K) X[(int64_t(k) * kTile + r0 + a) * K + c0 + b] = acc[a][b];
     return;
   }
-  for (int e = tid; e < tk; e += kTsThreads) {
-    const int r = e / K, c = e - r * K;
-    float s = 0.f;
-#pragma unroll 8
-    for (int j = 0; j < kTile; ++j) s += L[int64_t(k * kTile + j) * ld + i * kTile + r] * xk[j * K + c];
-    Y[(int64_t(i) * kTile + r) * K + c] -= s;
-  }
+  __syncthreads();
+  load_tile(Ms, L + int64_t(k) * kTile * ld + int64_t(i) * kTile, ld, false);
+  __syncthreads();
+  tile_product(Ms, Os, acc);
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      if (c0 + b < K) Y[(int64_t(i) * kTile + r0 + a) * K + c0 + b] -= acc[a][b];
 }
 
 // Z = D X (FP64, rows < n)
@@ -1070,6 +1133,12 @@ int DenseSpdSolver::inverse_columns(const int* unit, int m, const int* gather, d
   mout_.resize(6 * kRhs);
   munit_.resize(kRhs);
   mgather_.resize(6 * kRhs);
+  static bool configured = false;
+  if (!configured) {
+    set_smem(reinterpret_cast<const void*>(mfwd_step_kernel), kMsteps);
+    set_smem(reinterpret_cast<const void*>(mbwd_step_kernel), kMsteps);
+    configured = true;
+  }
   int failed = 0;
   std::vector<double> s2(size_t(kRhs) * kNumScal), bb(kRhs);
   for (int c0 = 0; c0 < m && !failed; c0 += kRhs) {
@@ -1094,9 +1163,9 @@ int DenseSpdSolver::inverse_columns(const int* unit, int m, const int* gather, d
     auto precondition = [&](double* Z) {
       GB_CUDA(cudaMemcpyAsync(TB, RS, vk * sizeof(float), cudaMemcpyDeviceToDevice));
       for (int k = 0; k < nt_; ++k)
-        mfwd_step_kernel<<<nt_ - k, kTsThreads>>>(L_.get(), n_pad_, dinv_.get(), k, K, TB, TY);
+        mfwd_step_kernel<<<nt_ - k, kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, K, TB, TY);
       for (int k = nt_ - 1; k >= 0; --k)
-        mbwd_step_kernel<<<k + 1, kTsThreads>>>(L_.get(), n_pad_, dinv_.get(), k, K, TY, TX);
+        mbwd_step_kernel<<<k + 1, kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, K, TY, TX);
       mts_finish_kernel<<<gn, 256>>>(n, K, dscale_.get(), TX, Z);
     };
     mscal_.zero();
