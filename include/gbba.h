@@ -316,14 +316,40 @@ int gbba_add_absolute_position_heatmap(gbba_adjuster_t* h, const char* shot_id, 
 int gbba_heatmap_residual(const double* grid, int64_t n, int64_t width, double resolution, double x_offset,
                           double y_offset, double std_deviation, const double* instance_pose,
                           const double* rig_camera_pose, double* residual, double* jacobian);
+/* Reconstructions (bundle_adjuster.cc:219-244): AddReconstruction,
+ * AddReconstructionInstance (an unknown reconstruction id is ignored, as in
+ * the reference), SetScaleSharing (one scale for the whole reconstruction:
+ * its first instance's in id order), and Reconstruction::GetScale after a
+ * run (the shared scale, or the instance's).  The scales are unknowns of the
+ * relative motions only; the reference's lower bound 0 is not enforced. */
+int gbba_add_reconstruction(gbba_adjuster_t* h, const char* id, int constant);
+int gbba_add_reconstruction_instance(gbba_adjuster_t* h, const char* reconstruction_id, double scale,
+                                     const char* instance_id);
+int gbba_set_scale_sharing(gbba_adjuster_t* h, const char* id, int share);
+int gbba_get_reconstruction_scale(const gbba_adjuster_t* h, const char* reconstruction_id, const char* instance_id,
+                                  double* scale);
+/* 1 when the reconstruction exists, else 0 (-1: invalid handle). */
+int gbba_has_reconstruction(const gbba_adjuster_t* h, const char* reconstruction_id);
+/* AddRelativeMotion (bundle_adjuster.cc:303-305, added at :872-910): the
+ * motion [rx ry rz tx ty tz scale] from rig instance i to j with a 7 x 7
+ * row-major scale matrix (NULL: identity), under the relative-motion loss
+ * at threshold x robust_multiplier, IRLS group REL (RelativeMotionError,
+ * relative_motion_errors.h:13-64).  Both instances must belong to a
+ * reconstruction when the run starts (else GBBA_ERR_OUT_OF_RANGE). */
+int gbba_add_relative_motion(gbba_adjuster_t* h, const char* instance_i, const char* instance_j,
+                             const double* motion, double robust_multiplier, int observed_scale,
+                             const double* scale_matrix);
 /* The scaled residuals (before the loss) of one constraint between shots
  * and their Jacobian.  kind 0 relative rotation (params: rotation[3], then
  * the row-major scale matrix [9]), 1 common position (params: margin,
  * std_deviation), 2 linear motion (params: alpha, position std, orientation
- * std), 3 gauge scale (params: the distance; rig camera poses unused).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
+ * std), 3 gauge scale (params: the distance; rig camera poses unused), 5
+ * relative motion (params: motion[7], observed-scale flag, scale matrix
+ * [49], scale_i, scale_j; rig camera poses unused; the scales' columns are
+ * 24 and 25).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
  * cameras) for the n = 2 (3 for linear motion) shots, [rx ry rz tx ty tz]
  * with t the position.  Writes m = 3 (6 for linear motion, 1 for the gauge
- * scale) residuals, J[m][36]
+ * scale, 7 for a relative motion) residuals, J[m][36]
  * (12 columns per shot: instance rotation, instance position, rig camera
  * rotation, rig camera position) and m to *n_residuals.  Host arithmetic
  * only. */

@@ -293,6 +293,12 @@ void BundleAdjuster::Run() {
   opts_.compute_covariances = compute_covariances_;
   auto solver = make_solver(opts_.precision);
   summary_ = solver->solve(problem_, opts_);
+  // the solved reconstruction scales, then the rig cameras without the
+  // scale blocks again
+  for (const ScaleBlock& b : scale_blocks_)
+    reconstructions_.at(b.reconstruction).scales[b.instance] = problem_.rig_cameras[b.block].value[0];
+  problem_.rig_cameras.resize(n_rig_cameras_);
+  scale_blocks_.clear();
   if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
   else {
     errors_.clear();
@@ -431,7 +437,58 @@ void BundleAdjuster::AddAbsolutePositionHeatmap(const std::string& shot, const s
   heatmap_terms_.push_back({shot, it->second, x_offset, y_offset, std_deviation});
 }
 
+void BundleAdjuster::AddReconstruction(const std::string& id, bool constant) {
+  ReconstructionScales r;
+  r.constant = constant;
+  r.shared = true;
+  reconstructions_[id] = r;
+}
+
+void BundleAdjuster::AddReconstructionInstance(const std::string& reconstruction_id, double scale,
+                                               const std::string& instance_id) {
+  const auto it = reconstructions_.find(reconstruction_id);
+  if (it == reconstructions_.end()) return;
+  it->second.scales[instance_id] = scale;
+  reconstruction_of_[instance_id] = reconstruction_id;
+}
+
+void BundleAdjuster::SetScaleSharing(const std::string& id, bool share) {
+  const auto it = reconstructions_.find(id);
+  if (it != reconstructions_.end()) it->second.shared = share;
+}
+
+double BundleAdjuster::GetReconstructionScale(const std::string& reconstruction_id,
+                                              const std::string& instance_id) const {
+  const auto it = reconstructions_.find(reconstruction_id);
+  if (it == reconstructions_.end())
+    throw std::runtime_error("Reconstruction " + reconstruction_id + " doesn't exist.");
+  const ReconstructionScales& r = it->second;
+  if (r.shared) {
+    if (r.scales.empty()) throw std::out_of_range("Reconstruction " + reconstruction_id + " has no instance.");
+    return r.scales.begin()->second;
+  }
+  return r.scales.at(instance_id);
+}
+
+void BundleAdjuster::AddRelativeMotion(const std::string& instance_i, const std::string& instance_j,
+                                       const double* motion, double robust_multiplier, bool observed_scale,
+                                       const double* scale_matrix) {
+  PendingMotion m{};
+  m.instances[0] = instance_i;
+  m.instances[1] = instance_j;
+  for (int k = 0; k < 7; ++k) m.motion[k] = motion[k];
+  for (int k = 0; k < 49; ++k) m.scale_matrix[k] = scale_matrix ? scale_matrix[k] : (k % 8 == 0 ? 1.0 : 0.0);
+  m.robust_multiplier = robust_multiplier;
+  m.observed_scale = observed_scale;
+  motions_.push_back(m);
+}
+
 void BundleAdjuster::PrepareRun() {
+  // scale blocks of an earlier run that did not finish
+  if (!scale_blocks_.empty()) {
+    problem_.rig_cameras.resize(n_rig_cameras_);
+    scale_blocks_.clear();
+  }
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
   bool known = false;
@@ -539,6 +596,46 @@ void BundleAdjuster::PrepareRun() {
     const double* b = problem_.instances[t.instance[1]].value + 3;
     t.distance = std::sqrt((a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) + (a[2] - b[2]) * (a[2] - b[2]));
     problem_.relative_terms.push_back(t);
+  }
+  // relative motions: the reconstruction scales become one-coordinate
+  // blocks after the rig cameras (a shared scale is the reconstruction's
+  // first entry, as Reconstruction::GetScalePtr picks it)
+  n_rig_cameras_ = problem_.rig_cameras.size();
+  if (!motions_.empty()) {
+    auto block_of = [&](const std::string& instance) {
+      const std::string& rec_id = reconstruction_of_.at(instance);
+      ReconstructionScales& rec = reconstructions_.at(rec_id);
+      const std::string key = rec.shared ? rec.scales.begin()->first : instance;
+      for (const ScaleBlock& b : scale_blocks_)
+        if (b.reconstruction == rec_id && b.instance == key) return b.block;
+      PoseBlock pb;
+      pb.value[0] = rec.scales.at(key);
+      pb.free_mask[0] = rec.constant ? 0 : 1;
+      pb.has_prior = false;
+      pb.used = true;
+      pb.scale_block = true;
+      const int block = int(problem_.rig_cameras.size());
+      problem_.rig_cameras.push_back(pb);
+      scale_blocks_.push_back({rec_id, key, block});
+      return block;
+    };
+    for (const PendingMotion& m : motions_) {
+      RelativeTerm t;
+      t.kind = RelativeTerm::kRelativeMotion;
+      t.n_shots = 2;
+      for (int k = 0; k < 2; ++k) {
+        const auto it = instance_index_.find(m.instances[k]);
+        if (it == instance_index_.end()) throw std::out_of_range("Rig instance " + m.instances[k] + " doesn't exist.");
+        t.instance[k] = it->second;
+        t.scale_block[k] = block_of(m.instances[k]);
+      }
+      for (int k = 0; k < 7; ++k) t.motion[k] = m.motion[k];
+      for (int k = 0; k < 49; ++k) t.motion_matrix[k] = m.scale_matrix[k];
+      t.observed_scale = m.observed_scale;
+      t.loss_scale = relative_loss_threshold_ * m.robust_multiplier;
+      any_rotation = true;  // the relative-motion loss is needed
+      problem_.relative_terms.push_back(t);
+    }
   }
   if (any_rotation) {
     // CreateLossFunction (bundle_adjuster.cc:485-499)

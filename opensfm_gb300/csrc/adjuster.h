@@ -51,6 +51,21 @@ class BundleAdjuster {
   // two shots' rig instance positions, d their distance at the start of the
   // run (:1140-1157).
   void SetGaugeFixShots(const std::string& shot_origin, const std::string& shot_scale);
+  // Reconstructions and their scales (bundle_adjuster.cc:219-244): a
+  // reconstruction holds one scale per instance, or one shared by all of
+  // them; constant or optimised (the lower bound 0 of the reference is not
+  // enforced).  Unknown reconstruction ids are ignored, as in the reference.
+  void AddReconstruction(const std::string& id, bool constant);
+  void AddReconstructionInstance(const std::string& reconstruction_id, double scale, const std::string& instance_id);
+  void SetScaleSharing(const std::string& id, bool share);
+  // Reconstruction::GetScale: the shared scale, or the instance's
+  double GetReconstructionScale(const std::string& reconstruction_id, const std::string& instance_id) const;
+  bool HasReconstruction(const std::string& id) const { return reconstructions_.count(id) != 0; }
+  // AddRelativeMotion (bundle_adjuster.cc:303-305, added at :872-910):
+  // motion = [rx ry rz tx ty tz scale], scale_matrix 7 x 7 row-major (null:
+  // identity)
+  void AddRelativeMotion(const std::string& instance_i, const std::string& instance_j, const double* motion,
+                         double robust_multiplier, bool observed_scale, const double* scale_matrix);
   // AddHeatmap / AddAbsolutePositionHeatmap (bundle_adjuster.cc:331-350):
   // a cost grid (row-major, `width` columns, `resolution` metres per cell)
   // and a shot's position looked up in it, centred at (x_offset, y_offset).
@@ -159,6 +174,28 @@ class BundleAdjuster {
   };
   std::vector<PendingRelative> relatives_;
   std::string relative_loss_name_ = "CauchyLoss";
+  struct ReconstructionScales {
+    std::map<std::string, double> scales;  // instance id -> scale (std::map: the first is the shared one)
+    bool constant = false;
+    bool shared = true;
+  };
+  std::map<std::string, ReconstructionScales> reconstructions_;
+  std::unordered_map<std::string, std::string> reconstruction_of_;  // instance id -> reconstruction id
+  struct PendingMotion {
+    std::string instances[2];
+    double motion[7];
+    double scale_matrix[49];
+    double robust_multiplier;
+    bool observed_scale;
+  };
+  std::vector<PendingMotion> motions_;
+  // the scale blocks of the last run: (reconstruction, instance key, rig-camera block)
+  struct ScaleBlock {
+    std::string reconstruction, instance;
+    int block;
+  };
+  std::vector<ScaleBlock> scale_blocks_;
+  size_t n_rig_cameras_ = 0;  // rig cameras before the scale blocks
   std::unordered_map<std::string, int> heatmap_index_;
   struct PendingHeatmap {
     std::string shot;

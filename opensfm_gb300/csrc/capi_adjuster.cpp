@@ -220,17 +220,54 @@ int gbba_heatmap_residual(const double* grid, int64_t n, int64_t width, double r
     t.scale = 1.0 / std_deviation;
     const double* pi[3] = {instance_pose, nullptr, nullptr};
     const double* pc[3] = {rig_camera_pose, nullptr, nullptr};
-    gbba::orient::Dual<12> r[6];
+    gbba::orient::Dual<12> r[7];
     gbba::orient::relative_residuals<12>(t, pi, pc, r);
     residual[0] = r[0].v;
     for (int k = 0; k < 12; ++k) jacobian[k] = r[0].d[k];
   });
 }
 
+int gbba_add_reconstruction(gbba_adjuster_t* h, const char* id, int constant) {
+  return guarded([&] { ba_of(h).AddReconstruction(str(id), constant != 0); });
+}
+
+int gbba_add_reconstruction_instance(gbba_adjuster_t* h, const char* reconstruction_id, double scale,
+                                     const char* instance_id) {
+  return guarded([&] { ba_of(h).AddReconstructionInstance(str(reconstruction_id), scale, str(instance_id)); });
+}
+
+int gbba_set_scale_sharing(gbba_adjuster_t* h, const char* id, int share) {
+  return guarded([&] { ba_of(h).SetScaleSharing(str(id), share != 0); });
+}
+
+int gbba_get_reconstruction_scale(const gbba_adjuster_t* h, const char* reconstruction_id, const char* instance_id,
+                                  double* scale) {
+  return guarded([&] {
+    need(scale, "scale");
+    *scale = ba_of(h).GetReconstructionScale(str(reconstruction_id), str(instance_id));
+  });
+}
+
+int gbba_has_reconstruction(const gbba_adjuster_t* h, const char* reconstruction_id) {
+  int has = 0;
+  const int st = guarded([&] { has = ba_of(h).HasReconstruction(str(reconstruction_id)) ? 1 : 0; });
+  return st == GBBA_OK ? has : -1;
+}
+
+int gbba_add_relative_motion(gbba_adjuster_t* h, const char* instance_i, const char* instance_j,
+                             const double* motion, double robust_multiplier, int observed_scale,
+                             const double* scale_matrix) {
+  return guarded([&] {
+    need(motion, "motion");
+    ba_of(h).AddRelativeMotion(str(instance_i), str(instance_j), motion, robust_multiplier, observed_scale != 0,
+                               scale_matrix);
+  });
+}
+
 int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                            const double* params, double* residuals, double* jacobian, int* n_residuals) {
   return guarded([&] {
-    if (kind < 0 || kind > 3 || !instance_poses || !params || !residuals || !jacobian || !n_residuals)
+    if (kind < 0 || kind > 5 || kind == 4 || !instance_poses || !params || !residuals || !jacobian || !n_residuals)
       throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_relative_residual: invalid argument");
     gbba::RelativeTerm t;
     t.kind = kind;
@@ -243,6 +280,10 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
       t.scale = 1.0 / params[1];
     } else if (kind == gbba::RelativeTerm::kGaugeScale) {
       t.distance = params[0];
+    } else if (kind == gbba::RelativeTerm::kRelativeMotion) {
+      for (int k = 0; k < 7; ++k) t.motion[k] = params[k];
+      t.observed_scale = params[7] != 0.0;
+      for (int k = 0; k < 49; ++k) t.motion_matrix[k] = params[8 + k];
     } else {
       t.alpha = params[0];
       t.position_scale = 1.0 / params[1];
@@ -254,8 +295,10 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
       pi[k] = instance_poses + 6 * k;
       pc[k] = rig_camera_poses ? rig_camera_poses + 6 * k : nullptr;
     }
-    gbba::orient::Dual<36> r[6];
-    const int m = gbba::orient::relative_residuals<36>(t, pi, pc, r);
+    gbba::orient::Dual<36> r[7];
+    const double scales[2] = {kind == gbba::RelativeTerm::kRelativeMotion ? params[57] : 1.0,
+                              kind == gbba::RelativeTerm::kRelativeMotion ? params[58] : 1.0};
+    const int m = gbba::orient::relative_residuals<36>(t, pi, pc, r, scales);
     for (int q = 0; q < m; ++q) {
       residuals[q] = r[q].v;
       for (int k = 0; k < 36; ++k) jacobian[36 * q + k] = r[q].d[k];

@@ -23,6 +23,11 @@
 //                         128-173): a bicubic lookup of a cost grid at the
 //                         shot's horizontal position, no loss
 //                         (bundle_adjuster.cc:1000-1009).
+//   relative motion       RelativeMotionError (relative_motion_errors.h:
+//                         13-64) between two rig instances and their
+//                         reconstruction scales, under the relative-motion
+//                         loss scaled by the term's robust multiplier
+//                         (bundle_adjuster.cc:872-910).
 //
 // Shot rotation and position compose the rig instance with the rig camera
 // as ShotRotationFunctor / ShotPositionFunctor do (position_functors.h:
@@ -56,7 +61,14 @@ struct HeatmapGrid {
 // derivative slots: instance rotation (0..2), instance position (3..5), rig
 // camera rotation (6..8), rig camera position (9..11).
 struct RelativeTerm {
-  enum Kind { kRelativeRotation = 0, kCommonPosition = 1, kLinearMotion = 2, kGaugeScale = 3, kHeatmap = 4 };
+  enum Kind {
+    kRelativeRotation = 0,
+    kCommonPosition = 1,
+    kLinearMotion = 2,
+    kGaugeScale = 3,
+    kHeatmap = 4,
+    kRelativeMotion = 5
+  };
   int kind = kRelativeRotation;
   int n_shots = 2;
   int instance[3] = {0, 0, 0};
@@ -68,6 +80,14 @@ struct RelativeTerm {
   double distance = 1.0;  // gauge scale: the instances' distance at the start of the run
   HeatmapGrid grid;       // heatmap: the grid, the offsets of its centre, scale = 1 / std
   double x_offset = 0.0, y_offset = 0.0;
+  // relative motion: observed rotation, translation and scale, the 7 x 7
+  // scale matrix (row-major), whether the scale is observed, the loss
+  // scale, and the scale blocks of the two instances (slots 24 and 25)
+  double motion[7] = {0, 0, 0, 0, 0, 0, 1};
+  double motion_matrix[49] = {};
+  bool observed_scale = false;
+  double loss_scale = 1.0;
+  int scale_block[2] = {-1, -1};
 };
 
 namespace orient {
@@ -339,14 +359,41 @@ inline double bicubic(const HeatmapGrid& g, double r, double c, double* dfdr, do
   return v;
 }
 
-// Scaled residuals (3 or 6) of a relative term from the shots' instance
-// and rig camera poses (pc[k] null: no rig camera); returns the count.
+// Scaled residuals (at most 7) of a relative term from the shots' instance
+// and rig camera poses (pc[k] null: no rig camera) and, for a relative
+// motion, the two reconstruction scales (slots 24 and 25); returns the
+// count.
 template <int N>
-inline int relative_residuals(const RelativeTerm& t, const double* const* pi, const double* const* pc,
-                              Dual<N>* r) {
+inline int relative_residuals(const RelativeTerm& t, const double* const* pi, const double* const* pc, Dual<N>* r,
+                              const double* scales = nullptr) {
   ShotPose<N> s[3];
-  for (int k = 0; k < t.n_shots; ++k) s[k] = shot_pose<N>(k, pi[k], pc[k]);
+  for (int k = 0; k < t.n_shots; ++k) s[k] = shot_pose<N>(k, pi[k], t.kind == RelativeTerm::kRelativeMotion ? nullptr : pc[k]);
   switch (t.kind) {
+    case RelativeTerm::kRelativeMotion: {
+      // rotation log(R_ij R_i^T R_j); translation t_ij - s_j R_j^T (t_i -
+      // t_j); scale S_ij - s_j / s_i when observed; times the scale matrix.
+      // A zero scale makes the residual undefined (the functor fails).
+      const Dual<N> si = var<N>(scales[0], 24), sj = var<N>(scales[1], 25);
+      Dual<N> e[7], rij[3], neg_i[3], neg_j[3], tmp[3], d[3], rd[3];
+      for (int i = 0; i < 3; ++i) {
+        rij[i] = Dual<N>(t.motion[i]);
+        neg_i[i] = -s[0].rotation[i];
+        neg_j[i] = -s[1].rotation[i];
+        d[i] = s[0].position[i] - s[1].position[i];
+      }
+      compose(rij, neg_i, tmp);
+      compose(tmp, s[1].rotation, e);
+      rotate(neg_j, d, rd);
+      for (int i = 0; i < 3; ++i) e[3 + i] = Dual<N>(t.motion[3 + i]) - sj * rd[i];
+      e[6] = t.observed_scale ? Dual<N>(t.motion[6]) - sj / si : Dual<N>(0.0);
+      const bool undefined = scales[0] == 0.0 || scales[1] == 0.0;
+      for (int i = 0; i < 7; ++i) {
+        Dual<N> acc(0.0);
+        for (int j = 0; j < 7; ++j) acc = acc + Dual<N>(t.motion_matrix[7 * i + j]) * e[j];
+        r[i] = undefined ? Dual<N>(std::numeric_limits<double>::quiet_NaN()) : acc;
+      }
+      return 7;
+    }
     case RelativeTerm::kRelativeRotation: {
       // log(R_ij R_i^T R_j), then the scale matrix
       Dual<N> rij[3], neg[3], tmp[3], e[3];

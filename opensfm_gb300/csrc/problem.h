@@ -47,6 +47,9 @@ struct PoseBlock {
   int scale_group = -1;
   int bias_camera = -1;       // camera whose bias transforms the GPS prior
   bool used = true;           // rig cameras: false when identity and fixed
+  // a reconstruction scale (value[0]) held in a rig-camera block that no
+  // shot references: camera-side unknowns for the relative motions
+  bool scale_block = false;
 };
 
 struct PointBlock {
@@ -120,8 +123,8 @@ struct Problem {
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
   double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
-  // UP PAN TILT ROLL ROT POS MOTION GAUGE HEATMAP
-  double ratio_host[9] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};
+  // UP PAN TILT ROLL ROT POS MOTION GAUGE HEATMAP REL
+  double ratio_host[10] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};
   // AddHeatmap grids (the relative terms of kind kHeatmap point into them)
   struct Heatmap {
     std::vector<double> data;

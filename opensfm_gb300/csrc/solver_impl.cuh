@@ -538,7 +538,7 @@ void mixture_params(const std::vector<double>& cov_in, int k, double density_rat
 // loss-free residuals the IRLS mixture reads, the free camera-side
 // coordinate of every slot (-1: fixed), and w rho(|r|^2).
 struct HostTermLin {
-  static constexpr int kMaxRows = 6, kMaxSlots = 36;
+  static constexpr int kMaxRows = 7, kMaxSlots = 36;
   int m = 0, ns = 0;
   double r[kMaxRows] = {}, raw[kMaxRows] = {};
   double J[kMaxRows][kMaxSlots] = {};
@@ -547,10 +547,10 @@ struct HostTermLin {
 };
 
 // IRLS groups of the host constraint terms: UP, PAN, TILT, ROLL (by
-// orientation kind), ROT, POS, MOTION, GAUGE, HEATMAP (by relative kind)
-constexpr int kHostGroups = 9;
-const char* const kHostGroupNames[kHostGroups] = {"UP",  "PAN",    "TILT",  "ROLL",   "ROT",
-                                                  "POS", "MOTION", "GAUGE", "HEATMAP"};
+// orientation kind), ROT, POS, MOTION, GAUGE, HEATMAP, REL (by relative kind)
+constexpr int kHostGroups = 10;
+const char* const kHostGroupNames[kHostGroups] = {"UP",     "PAN",   "TILT",    "ROLL", "ROT",
+                                                  "POS",    "MOTION", "GAUGE", "HEATMAP", "REL"};
 
 MixtureResult mixture_group(const std::vector<std::vector<double>>& res, std::vector<double>& weights,
                             double density_ratio) {
@@ -855,7 +855,8 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   for (int r = 0; r < n_rig_; ++r)
     for (int k = 0; k < 6; ++k) {
       xc_[cl_.rig_base + 8 * r + k] = P.rig_cameras[r].value[k];
-      cmask_[cl_.rig_base + 8 * r + k] = (P.rig_cameras[r].used && kc_.rig) ? P.rig_cameras[r].free_mask[k] : 0;
+      cmask_[cl_.rig_base + 8 * r + k] =
+          (P.rig_cameras[r].used && (kc_.rig || P.rig_cameras[r].scale_block)) ? P.rig_cameras[r].free_mask[k] : 0;
     }
   for (int c = 0; c < n_cam_; ++c)
     for (int k = 0; k < P.cameras[c].n; ++k) {
@@ -1502,14 +1503,28 @@ void DeviceSolver<R>::host_term(int q, const std::vector<double>& x, HostTermLin
       for (int a = 0; a < 6; ++a) L.coord[12 * k + 6 + a] = coord_of(rb + a);
     }
   }
-  orient::Dual<N> r[6];
-  L.m = orient::relative_residuals<N>(t, pi, pc, r);
+  double scales[2] = {1.0, 1.0};
+  if (t.kind == RelativeTerm::kRelativeMotion) {
+    // the reconstruction scales: value[0] of their blocks, slots 24 and 25
+    for (int k = 0; k < 2; ++k) {
+      const int sb = cl_.rig_base + 8 * t.scale_block[k];
+      scales[k] = x[sb];
+      L.coord[24 + k] = coord_of(sb);
+    }
+  }
+  orient::Dual<N> r[7];
+  L.m = orient::relative_residuals<N>(t, pi, pc, r, scales);
   L.ns = N;
   for (int i = 0; i < L.m; ++i) L.raw[i] = r[i].v;
-  // relative rotation: the relative-motion loss; Tukey(1); Cauchy(1); none; none
-  static const int kLoss[5] = {-1, 5, 3, 0, 0};
-  const int loss = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss : kLoss[t.kind];
-  const double a = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss_threshold : 1.0;
+  // relative rotation and motion: the relative-motion loss (for a motion
+  // at its threshold times the term's robust multiplier); common position
+  // Tukey(1); linear motion Cauchy(1); gauge and heatmap none
+  static const int kLoss[6] = {-1, 5, 3, 0, 0, -1};
+  const bool rel_loss = t.kind == RelativeTerm::kRelativeRotation || t.kind == RelativeTerm::kRelativeMotion;
+  const int loss = rel_loss ? P.relative_loss : kLoss[t.kind];
+  const double a = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss_threshold
+                   : t.kind == RelativeTerm::kRelativeMotion ? t.loss_scale
+                                                             : 1.0;
   L.rho = orient::loss_correct<N>(loss, a, L.m, r, w);
   for (int i = 0; i < L.m; ++i) {
     L.r[i] = r[i].v;

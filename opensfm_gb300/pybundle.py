@@ -63,6 +63,12 @@ def _declare(L) -> None:
         "gbba_set_relative_motion_loss_function": ([_H, S, C.c_double], C.c_int),
         "gbba_relative_residual": ([C.c_int, _D, _D, _D, _D, _D, C.POINTER(C.c_int)], C.c_int),
         "gbba_set_gauge_fix_shots": ([_H, S, S], C.c_int),
+        "gbba_add_reconstruction": ([_H, S, C.c_int], C.c_int),
+        "gbba_add_reconstruction_instance": ([_H, S, C.c_double, S], C.c_int),
+        "gbba_set_scale_sharing": ([_H, S, C.c_int], C.c_int),
+        "gbba_get_reconstruction_scale": ([_H, S, S, _D], C.c_int),
+        "gbba_has_reconstruction": ([_H, S], C.c_int),
+        "gbba_add_relative_motion": ([_H, S, S, _D, C.c_double, C.c_int, _D], C.c_int),
         "gbba_add_heatmap": ([_H, S, _D, C.c_int64, C.c_int64, C.c_double], C.c_int),
         "gbba_add_absolute_position_heatmap": ([_H, S, S, C.c_double, C.c_double, C.c_double], C.c_int),
         "gbba_heatmap_residual": ([_D, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double, _D, _D,
@@ -130,6 +136,42 @@ def _vec(x, n: int) -> np.ndarray:
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(_D)
+
+
+class RelativeMotion:
+    """bundle::RelativeMotion (bundle_adjuster.h:75-104): the motion from
+    rig instance i to j -- rotation, translation, scale -- its robust
+    multiplier and whether the scale is observed; a 7 x 7 scale matrix."""
+
+    def __init__(self, rig_instance_i: str, rig_instance_j: str, rotation, translation, scale: float,
+                 robust_multiplier: float, observed_scale: bool) -> None:
+        self.rig_instance_i = rig_instance_i
+        self.rig_instance_j = rig_instance_j
+        self.rotation = np.asarray(rotation, dtype=np.float64).reshape(3).copy()
+        self.translation = np.asarray(translation, dtype=np.float64).reshape(3).copy()
+        self.scale = float(scale)
+        self.robust_multiplier = float(robust_multiplier)
+        self.observed_scale = bool(observed_scale)
+        self.scale_matrix = np.eye(7)
+
+    def set_scale_matrix(self, s) -> None:
+        self.scale_matrix = np.asarray(s, dtype=np.float64).reshape(7, 7).copy()
+
+
+class Reconstruction:
+    """bundle::Reconstruction as get_reconstruction returns it: get_scale
+    reads the adjuster's current scale of an instance (the shared one when
+    the reconstruction shares its scale)."""
+
+    def __init__(self, ba: "BundleAdjuster", reconstruction_id: str) -> None:
+        self._ba = ba
+        self.id = reconstruction_id
+
+    def get_scale(self, instance_id: str) -> float:
+        v = C.c_double(0.0)
+        self._ba._check(self._ba._L.gbba_get_reconstruction_scale(self._ba._h, _b(self.id), _b(instance_id),
+                                                                   C.byref(v)))
+        return v.value
 
 
 class RelativeRotation:
@@ -361,6 +403,29 @@ class BundleAdjuster:
                                                                float(x_offset), float(y_offset),
                                                                float(std_deviation)))
 
+    def add_reconstruction(self, reconstruction_id: str, constant: bool) -> None:
+        self._check(self._L.gbba_add_reconstruction(self._h, _b(reconstruction_id), int(bool(constant))))
+
+    def add_reconstruction_instance(self, reconstruction_id: str, scale: float, instance_id: str) -> None:
+        self._check(self._L.gbba_add_reconstruction_instance(self._h, _b(reconstruction_id), float(scale),
+                                                             _b(instance_id)))
+
+    def set_scale_sharing(self, reconstruction_id: str, share: bool) -> None:
+        self._check(self._L.gbba_set_scale_sharing(self._h, _b(reconstruction_id), int(bool(share))))
+
+    def get_reconstruction(self, reconstruction_id: str) -> "Reconstruction":
+        # the reference raises for an unknown id (bundle_adjuster.cc:1344-1350)
+        if not self._L.gbba_has_reconstruction(self._h, _b(reconstruction_id)):
+            raise RuntimeError(f"Reconstruction {reconstruction_id} doesn't exist.")
+        return Reconstruction(self, reconstruction_id)
+
+    def add_relative_motion(self, rm: "RelativeMotion") -> None:
+        motion = np.ascontiguousarray(np.r_[rm.rotation, rm.translation, rm.scale], dtype=np.float64)
+        sm = np.ascontiguousarray(rm.scale_matrix, dtype=np.float64).reshape(49)
+        self._check(self._L.gbba_add_relative_motion(self._h, _b(rm.rig_instance_i), _b(rm.rig_instance_j),
+                                                     _dp(motion), float(rm.robust_multiplier),
+                                                     int(bool(rm.observed_scale)), _dp(sm)))
+
     def set_gauge_fix_shots(self, shot_origin: str, shot_scale: str) -> None:
         self._check(self._L.gbba_set_gauge_fix_shots(self._h, _b(shot_origin), _b(shot_scale)))
 
@@ -486,11 +551,6 @@ class BundleAdjuster:
     def _unsupported(self, *args, **kwargs):
         raise NotImplementedError("this constraint type is not implemented by the GPU bundle adjuster")
 
-    add_relative_motion = _unsupported
-    add_reconstruction = _unsupported
-    add_reconstruction_instance = _unsupported
-    set_scale_sharing = _unsupported
-    get_reconstruction = _unsupported
     set_adjust_absolute_position_std = _unsupported
 
 
@@ -579,7 +639,8 @@ def orientation_residual(kind: str, target, std_deviation: float, instance_rotat
     return r[: m.value].copy(), J[: 6 * m.value].reshape(m.value, 6)
 
 
-RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3}
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3,
+                  "relative_motion": 5}
 
 
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
@@ -593,7 +654,7 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
     pi = np.ascontiguousarray(instance_poses, dtype=np.float64)
     pc = None if rig_camera_poses is None else np.ascontiguousarray(rig_camera_poses, dtype=np.float64)
     prm = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
-    r, J = np.zeros(6), np.zeros(6 * 36)
+    r, J = np.zeros(7), np.zeros(7 * 36)
     m = C.c_int(0)
     _lib.check(L.gbba_relative_residual(RELATIVE_KINDS[kind], _dp(pi), _dp(pc) if pc is not None else None,
                                         _dp(prm), _dp(r), _dp(J), C.byref(m)))
@@ -654,5 +715,6 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
     return ba
 
 
-__all__ = ["BundleAdjuster", "BundleBatch", "Point", "RelativeRotation", "adjuster_from_scene",
+__all__ = ["BundleAdjuster", "BundleBatch", "Point", "Reconstruction", "RelativeMotion", "RelativeRotation",
+           "adjuster_from_scene",
            "heatmap_residual", "orientation_residual", "relative_residual"]

@@ -150,7 +150,7 @@ class _Problem(C.Structure):
         ("n_orient", C.c_int32), ("orient_kind", I32), ("orient_shot", I32), ("orient_target", D), ("orient_std", D),
         ("n_rel", C.c_int32), ("rel_kind", I32), ("rel_shots", I32), ("rel_params", D), ("rel_loss", C.c_int32),
         ("rel_loss_threshold", C.c_double), ("heat_grid", D), ("heat_n", C.c_int64), ("heat_width", C.c_int32),
-        ("heat_resolution", C.c_double),
+        ("heat_resolution", C.c_double), ("n_scales", C.c_int32), ("scales", D), ("scale_free", U8),
     ]
 
 
@@ -161,7 +161,7 @@ class _Options(C.Structure):
 
 
 class _Result(C.Structure):
-    _fields_ = [("camera_values", D), ("instance_poses", D), ("rig_poses", D), ("points", D),
+    _fields_ = [("camera_values", D), ("instance_poses", D), ("rig_poses", D), ("points", D), ("scales", D),
                 ("obs_weights", D), ("obs_errors", D), ("trace_cost", D), ("trace_capacity", C.c_int32),
                 ("trace_n", C.c_int32), ("initial_cost", C.c_double), ("final_cost", C.c_double),
                 ("iterations", C.c_int32), ("successful", C.c_int32), ("termination", C.c_int32)]
@@ -199,7 +199,9 @@ def orientation_residual(kind: str, target, std: float, instance_rotation, camer
     return r[:m].copy(), J[: 6 * m].reshape(m, 6)
 
 
-RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3, "heatmap": 4}
+RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3, "heatmap": 4,
+                  "relative_motion": 5}
+REL_PARAMS = 64
 
 
 def heatmap_residual(grid, width, resolution, x_offset, y_offset, std, instance_pose, rig_camera_pose=None):
@@ -217,26 +219,28 @@ def heatmap_residual(grid, width, resolution, x_offset, y_offset, std, instance_
     return r, J
 
 
-def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
+def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None, scales=None):
     """Scaled residuals and Jacobian [m][36] of one constraint between shots
-    (oracle/solver.cpp restatement)."""
+    (oracle/solver.cpp restatement); ``scales`` the two reconstruction
+    scales of a relative motion (columns 24 and 25)."""
     L = lib()
     f = L.oracle_relative_residual
-    f.argtypes = [C.c_int, D, D, D, D, D]
+    f.argtypes = [C.c_int, D, D, D, D, D, D]
     f.restype = C.c_int
     pi = np.ascontiguousarray(instance_poses, np.float64)
     pc = None if rig_camera_poses is None else np.ascontiguousarray(rig_camera_poses, np.float64)
-    prm = np.zeros(12)
+    prm = np.zeros(REL_PARAMS)
     v = np.asarray(params, np.float64).reshape(-1)
     prm[: len(v)] = v
-    r, J = np.zeros(6), np.zeros(6 * 36)
-    m = f(RELATIVE_KINDS[kind], _p(pi), _p(pc), _p(prm), _p(r), _p(J))
+    sc = np.ones(2) if scales is None else np.ascontiguousarray(scales, np.float64)
+    r, J = np.zeros(7), np.zeros(7 * 36)
+    m = f(RELATIVE_KINDS[kind], _p(pi), _p(pc), _p(prm), _p(sc), _p(r), _p(J))
     return r[:m].copy(), J[: 36 * m].reshape(m, 36)
 
 
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
           density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
-          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None):
+          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None, scales=()):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
@@ -248,8 +252,11 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     (origin shot, scale shot) as set_gauge_fix_shots takes them.
     ``heatmap``: (grid, width, resolution), the grid of the ``relative``
     entries of kind "heatmap" (shots (s,), params (x_offset, y_offset,
-    std)).  Returns a dict with the final parameters, costs and the cost
-    trace."""
+    std)).  ``scales``: reconstruction scales (value, free) -- the unknowns
+    of "relative_motion" entries, whose params are motion[7], the
+    observed-scale flag, the 7 x 7 scale matrix, the robust multiplier and
+    the two scale indices.  Returns a dict with the final parameters,
+    scales, costs and the cost trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
     L.oracle_solve.restype = C.c_int
@@ -310,7 +317,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     nr = len(relative)
     r_kind = np.array([RELATIVE_KINDS[c[0]] for c in relative], np.int32).reshape(nr)
     r_shots = np.zeros((max(nr, 1), 3), np.int32)
-    r_params = np.zeros((max(nr, 1), 12))
+    r_params = np.zeros((max(nr, 1), REL_PARAMS))
     for q, c in enumerate(relative):
         r_shots[q, : len(c[1])] = c[1]
         v = np.asarray(c[2], np.float64).reshape(-1)
@@ -324,6 +331,10 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     else:
         h_grid, h_width, h_res = np.zeros(1), 1, 1.0
     keep.append(h_grid)
+    ns = len(scales)
+    s_val = np.array([float(v) for v, _ in scales] or [1.0], np.float64)
+    s_free = np.array([1 if f else 0 for _, f in scales] or [0], np.uint8)
+    keep += [s_val, s_free]
     u8 = lambda a: a.ctypes.data_as(U8)  # noqa: E731
     i32 = lambda a: a.ctypes.data_as(I32)  # noqa: E731
     P = _Problem(nc, i32(scene.camera_projection), _p(cam_values), _p(cam_values.copy() if False else cam_values),
@@ -335,7 +346,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
                  scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
                  _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std),
                  nr, i32(r_kind), i32(r_shots), _p(r_params), LOSSES[relative_loss[0]], float(relative_loss[1]),
-                 _p(h_grid), h_grid.size, h_width, h_res)
+                 _p(h_grid), h_grid.size, h_width, h_res, ns, _p(s_val), u8(s_free))
     loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
     O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
                  int(skip_initial_reweighting), threads or os.cpu_count() or 1)
@@ -346,11 +357,13 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     out_w = np.zeros(scene.n_observations)
     out_err = np.zeros((scene.n_observations, 3))
     trace = np.zeros(max_iterations + 2)
-    R = _Result(_p(out_cam), _p(out_inst), _p(out_rig), _p(out_pts), _p(out_w), _p(out_err), _p(trace),
+    out_scl = s_val.copy()
+    R = _Result(_p(out_cam), _p(out_inst), _p(out_rig), _p(out_pts), _p(out_scl), _p(out_w), _p(out_err), _p(trace),
                 len(trace), 0, 0.0, 0.0, 0, 0, 0)
     L.oracle_solve(C.byref(P), C.byref(O), C.byref(R))
     del keep
-    return dict(cameras=out_cam, instances=out_inst, points=out_pts, weights=out_w, errors=out_err,
+    return dict(cameras=out_cam, instances=out_inst, points=out_pts, scales=out_scl[:ns].copy(), weights=out_w,
+                errors=out_err,
                 trace=trace[: R.trace_n].copy(), initial_cost=R.initial_cost, final_cost=R.final_cost,
                 iterations=R.iterations, successful=R.successful, termination=R.termination)
 

@@ -83,9 +83,13 @@ struct OracleProblem {
   const double* orient_std;
   // constraints between shots
   int32_t n_rel;
-  const int32_t* rel_kind;     // 0 relative rotation, 1 common position, 2 linear motion
+  const int32_t* rel_kind;     // 0 relative rotation, 1 common position, 2 linear motion, 3 gauge, 4 heatmap,
+                               // 5 relative motion
   const int32_t* rel_shots;    // [n][3]
-  const double* rel_params;    // [n][12]: rotation[3] + scale matrix[9]; margin, std; alpha, position std, orientation std
+  // [n][64]: rotation[3] + scale matrix[9]; margin, std; alpha, position
+  // std, orientation std; distance; x offset, y offset, std; motion[7],
+  // observed flag, scale matrix[49], robust multiplier, scale indices i, j
+  const double* rel_params;
   int32_t rel_loss;            // loss of the relative rotations (projection loss kinds)
   double rel_loss_threshold;
   // the heatmap of the kind-4 constraints (params: x offset, y offset, std)
@@ -93,6 +97,10 @@ struct OracleProblem {
   int64_t heat_n;
   int32_t heat_width;
   double heat_resolution;
+  // reconstruction scales (the unknowns of the relative motions)
+  int32_t n_scales;
+  const double* scales;
+  const uint8_t* scale_free;
 };
 
 struct OracleOptions {
@@ -110,6 +118,7 @@ struct OracleResult {
   double* instance_poses;  // [n][6]
   double* rig_poses;       // [n][6]
   double* points;          // [n][3]
+  double* scales;          // [n_scales]
   double* obs_weights;     // [n_obs]
   double* obs_errors;      // [n_obs][3] unscaled residuals
   double* trace_cost;      // [capacity]
@@ -128,13 +137,16 @@ namespace {
 
 struct State {
   std::vector<double> cam, inst, rig, pts;  // cam [n][16], inst/rig [n][6], pts [n][3]
+  std::vector<double> scl;                  // reconstruction scales
 };
 
 // Compact indices of the optimised camera-side coordinates.
 struct Index {
-  std::vector<int> inst, rig, cam;  // -1 for fixed coordinates
+  std::vector<int> inst, rig, cam, scl;  // -1 for fixed coordinates
   int n = 0;
 };
+
+constexpr int kRelParams = 64;
 
 struct Mixture {
   double ll = 0.0;
@@ -345,7 +357,34 @@ double heat_value(const HeatGrid& g, double r, double c, double* fr, double* fc)
 }
 
 int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r,
-                      const HeatGrid* grid = nullptr) {
+                      const HeatGrid* grid = nullptr, const double* scales = nullptr) {
+  if (kind == 5) {
+    // RelativeMotionError (relative_motion_errors.h:13-64) on the instance
+    // poses alone: rotation log(R_ij R_i^T R_j), translation t_ij - s_j
+    // R_j^T (t_i - t_j), scale S_ij - s_j / s_i when observed; then the 7 x
+    // 7 matrix.  Scales in slots 24, 25.
+    const ShotFrame fi = shot_frame(0, pi[0], nullptr), fj = shot_frame(1, pi[1], nullptr);
+    const D36 si = D36::var(scales[0], 24), sj = D36::var(scales[1], 25);
+    D36 rij[3], Rij[9], T1[9], T2[9], e[7];
+    for (int i = 0; i < 3; ++i) rij[i] = D36(prm[i]);
+    rotation_matrix(rij, Rij);
+    matmul3(Rij, fi.R, T1, true);
+    matmul3(T1, fj.R, T2);
+    log_rotation(T2, e);
+    for (int i = 0; i < 3; ++i) {
+      D36 v(0.0);
+      for (int k = 0; k < 3; ++k) v = v + fj.R[3 * k + i] * (fi.p[k] - fj.p[k]);  // (R_j^T d)_i
+      e[3 + i] = prm[3 + i] - sj * v;
+    }
+    e[6] = prm[7] != 0.0 ? prm[6] - sj / si : D36(0.0);
+    const bool undefined = scales[0] == 0.0 || scales[1] == 0.0;
+    for (int i = 0; i < 7; ++i) {
+      D36 acc(0.0);
+      for (int k = 0; k < 7; ++k) acc = acc + e[k] * prm[8 + 7 * i + k];
+      r[i] = undefined ? D36(std::numeric_limits<double>::quiet_NaN()) : acc;
+    }
+    return 7;
+  }
   if (kind == 4) {
     const ShotFrame f = shot_frame(0, pi[0], pc[0]);
     const int height = int(grid->n / grid->width);
@@ -455,6 +494,9 @@ struct Solver {
       for (int k = 0; k < C; ++k)
         if (P.camera_free[16 * c + k]) idx.cam[16 * c + k] = idx.n++;
     }
+    idx.scl.assign(std::max(0, P.n_scales), -1);
+    for (int k = 0; k < P.n_scales; ++k)
+      if (P.scale_free[k]) idx.scl[k] = idx.n++;
     w_obs.assign(P.n_obs, 1.0);
     w_cam.assign(P.n_cameras, 1.0);
     w_rig.assign(P.n_rig_cameras, 1.0);
@@ -474,6 +516,7 @@ struct Solver {
   // raw residuals through raw.
   int relative_term(const State& s, int q, D36* r, int* col, double* rho, double* raw = nullptr) const {
     const int kind = P.rel_kind[q], n = kind == 2 ? 3 : (kind == 4 ? 1 : 2);
+    const double* prm = P.rel_params + kRelParams * q;
     const double* pi[3] = {nullptr, nullptr, nullptr};
     const double* pc[3] = {nullptr, nullptr, nullptr};
     for (int a = 0; a < 36; ++a) col[a] = -1;
@@ -482,22 +525,32 @@ struct Solver {
       const int inst = P.shot_instance[sh], rc = P.shot_rig[sh];
       pi[k] = &s.inst[6 * inst];
       for (int a = 0; a < 6; ++a) col[12 * k + a] = idx.inst[6 * inst + a];
-      // the heatmap functor always composes the rig camera
-      if (rc >= 0 && (P.rig_used[rc] || kind == 4)) {
+      // the heatmap functor always composes the rig camera; the relative
+      // motion none
+      if (rc >= 0 && (P.rig_used[rc] || kind == 4) && kind != 5) {
         pc[k] = &s.rig[6 * rc];
         for (int a = 0; a < 6; ++a) col[12 * k + 6 + a] = idx.rig[6 * rc + a];
       }
     }
     const HeatGrid grid{P.heat_grid, P.heat_n, P.heat_width, P.heat_resolution};
-    const int m = relative_residual(kind, pi, pc, P.rel_params + 12 * q, r, &grid);
+    double scales[2] = {1.0, 1.0};
+    if (kind == 5)
+      for (int k = 0; k < 2; ++k) {
+        const int si = int(prm[58 + k]);
+        scales[k] = s.scl[si];
+        col[24 + k] = idx.scl[si];
+      }
+    const int m = relative_residual(kind, pi, pc, prm, r, &grid, scales);
     double sq = 0.0;
     for (int a = 0; a < m; ++a) {
       sq += r[a].v * r[a].v;
       if (raw) raw[a] = r[a].v;
     }
-    static const int kLoss[5] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL};  // Tukey(1), Cauchy(1), none
-    const int loss = kind == 0 ? P.rel_loss : kLoss[kind];
-    const double la = kind == 0 ? P.rel_loss_threshold : 1.0;
+    // relative rotation and motion: the relative-motion loss (a motion's at
+    // threshold x robust multiplier); Tukey(1); Cauchy(1); none; none
+    static const int kLoss[6] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL, -1};
+    const int loss = (kind == 0 || kind == 5) ? P.rel_loss : kLoss[kind];
+    const double la = kind == 0 ? P.rel_loss_threshold : kind == 5 ? P.rel_loss_threshold * prm[57] : 1.0;
     double rh[3];
     loss_rho5(loss, la, sq, rh);
     for (double& v : rh) v *= w_rel[q];
@@ -613,7 +666,7 @@ struct Solver {
   double prior_cost(const State& s) const {
     double c = 0.0;
     for (int q = 0; q < P.n_rel; ++q) {
-      D36 r[6];
+      D36 r[7];
       int col[36];
       double rho;
       relative_term(s, q, r, col, &rho);
@@ -803,7 +856,7 @@ struct Solver {
       }
     }
     for (int q = 0; q < P.n_rel; ++q) {
-      D36 rr[6];
+      D36 rr[7];
       int col[36];
       double rho;
       const int m = relative_term(s, q, rr, col, &rho);
@@ -1024,7 +1077,7 @@ struct Solver {
       }
     }
     for (int q = 0; q < P.n_rel; ++q) {
-      D36 rr[6];
+      D36 rr[7];
       int col[36];
       double rho;
       const int m = relative_term(s, q, rr, col, &rho);
@@ -1052,6 +1105,8 @@ struct Solver {
     for (int64_t p = 0; p < P.n_points; ++p)
       if (P.point_free[p])
         for (int k = 0; k < 3; ++k) t.pts[3 * p + k] += dp[3 * p + k];
+    for (int k = 0; k < P.n_scales; ++k)
+      if (idx.scl[k] >= 0) t.scl[k] += dc[idx.scl[k]];
     return t;
   }
 
@@ -1213,14 +1268,14 @@ struct Solver {
       }
       total += mixture(res, w, O.density_ratio);
     }
-    for (int kind = 0; kind < 5; ++kind) {  // groups ROT, POS, MOTION, GAUGE, HEATMAP
+    for (int kind = 0; kind < 6; ++kind) {  // groups ROT, POS, MOTION, GAUGE, HEATMAP, REL
       std::vector<std::vector<double>> res;
       std::vector<double*> w;
       for (int q = 0; q < P.n_rel; ++q) {
         if (P.rel_kind[q] != kind) continue;
-        D36 rr[6];
+        D36 rr[7];
         int col[36];
-        double rho, raw[6];
+        double rho, raw[7];
         const int m = relative_term(s, q, rr, col, &rho, raw);
         res.emplace_back(raw, raw + m);
         w.push_back(&w_rel[q]);
@@ -1265,7 +1320,7 @@ extern "C" int oracle_orientation_residual(int kind, const double* target, doubl
 // (kind and params as OracleProblem holds them; rig camera poses may be
 // null); returns m.
 extern "C" int oracle_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
-                                        const double* params, double* r, double* J) {
+                                        const double* params, const double* scales, double* r, double* J) {
   const int n = kind == 2 ? 3 : 2;
   const double* pi[3] = {nullptr, nullptr, nullptr};
   const double* pc[3] = {nullptr, nullptr, nullptr};
@@ -1273,8 +1328,8 @@ extern "C" int oracle_relative_residual(int kind, const double* instance_poses, 
     pi[k] = instance_poses + 6 * k;
     pc[k] = rig_camera_poses ? rig_camera_poses + 6 * k : nullptr;
   }
-  D36 d[6];
-  const int m = relative_residual(kind, pi, pc, params, d);
+  D36 d[7];
+  const int m = relative_residual(kind, pi, pc, params, d, nullptr, scales);
   for (int q = 0; q < m; ++q) {
     r[q] = d[q].v;
     for (int k = 0; k < 36; ++k) J[36 * q + k] = d[q].d[k];
@@ -1290,7 +1345,7 @@ extern "C" double oracle_heatmap_residual(const double* grid, int64_t n, int wid
   const HeatGrid g{grid, n, width, resolution};
   const double* pi[3] = {instance_pose, nullptr, nullptr};
   const double* pc[3] = {rig_camera_pose, nullptr, nullptr};
-  D36 r[6];
+  D36 r[7];
   relative_residual(4, pi, pc, params, r, &g);
   for (int k = 0; k < 12; ++k) J[k] = r[0].d[k];
   return r[0].v;
@@ -1305,6 +1360,7 @@ extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, Or
   x.inst.assign(P.instance_poses, P.instance_poses + 6 * P.n_instances);
   x.rig.assign(P.rig_poses, P.rig_poses + 6 * std::max(0, P.n_rig_cameras));
   x.pts.assign(P.points, P.points + 3 * P.n_points);
+  x.scl.assign(P.scales, P.scales + std::max(0, P.n_scales));
   S.cur = &x;
   double ll = -std::numeric_limits<double>::infinity();
   const bool irls = O.irls == 1;
@@ -1398,6 +1454,7 @@ extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, Or
         for (double v : x.inst) xn += v * v;
         for (double v : x.rig) xn += v * v;
         for (double v : x.pts) xn += v * v;
+        for (double v : x.scl) xn += v * v;
         if (std::sqrt(step2) <= 1e-8 * (std::sqrt(xn) + 1e-8)) inner = true;
       }
     }
@@ -1435,6 +1492,7 @@ extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, Or
   std::memcpy(out->instance_poses, x.inst.data(), sizeof(double) * x.inst.size());
   if (P.n_rig_cameras) std::memcpy(out->rig_poses, x.rig.data(), sizeof(double) * x.rig.size());
   std::memcpy(out->points, x.pts.data(), sizeof(double) * x.pts.size());
+  if (out->scales && P.n_scales > 0) std::memcpy(out->scales, x.scl.data(), sizeof(double) * x.scl.size());
   std::vector<double> resid(3 * P.n_obs);
   S.cost(x, &resid);
   for (int64_t i = 0; i < P.n_obs; ++i) {

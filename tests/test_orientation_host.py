@@ -215,3 +215,49 @@ def test_heatmap_interpolates_grid_nodes():
             y = (2.5 - i) * res
             r, _ = pybundle.heatmap_residual(grid, 7, res, 0.0, 0.0, 1.0, np.r_[0, 0, 0, x, y, 0])
             assert abs(r - grid[i, j]) < 1e-12
+
+
+def test_relative_motion_matches_oracle_and_finite_differences():
+    # RelativeMotionError (relative_motion_errors.h:13-64): instance poses
+    # only (rig cameras unused), the two scales in columns 24 and 25
+    rng = np.random.default_rng(12)
+    for i in range(30):
+        poses = np.concatenate([rng.normal(size=(2, 3)) * 0.7, rng.normal(size=(2, 3)) * 3], axis=1)
+        motion = np.r_[rng.normal(size=3) * 0.4, rng.normal(size=3), rng.uniform(0.5, 2)]
+        observed = float(i % 2)
+        M = np.eye(7) + 0.1 * rng.normal(size=(7, 7))
+        sc = rng.uniform(0.3, 3.0, 2)
+        prm = np.r_[motion, observed, M.ravel(), sc]
+        r, J = pybundle.relative_residual("relative_motion", poses, prm)
+        ro, Jo = oracle.relative_residual("relative_motion", poses, np.r_[motion, observed, M.ravel()], scales=sc)
+        np.testing.assert_allclose(r, ro, rtol=1e-9, atol=1e-9)
+        np.testing.assert_allclose(J, Jo, rtol=1e-7, atol=1e-7)
+        assert np.all(J[:, 6:12] == 0) and np.all(J[:, 18:24] == 0) and np.all(J[:, 26:] == 0)
+        h = 1e-6
+        for col in list(range(6)) + list(range(12, 18)) + [24, 25]:
+            dp, ds = poses.copy(), sc.copy()
+            if col < 24:
+                dp[col // 12, col % 12] += h
+            else:
+                ds[col - 24] += h
+            rp, _ = pybundle.relative_residual("relative_motion", dp, np.r_[motion, observed, M.ravel(), ds])
+            dp, ds = poses.copy(), sc.copy()
+            if col < 24:
+                dp[col // 12, col % 12] -= h
+            else:
+                ds[col - 24] -= h
+            rm, _ = pybundle.relative_residual("relative_motion", dp, np.r_[motion, observed, M.ravel(), ds])
+            np.testing.assert_allclose((rp - rm) / (2 * h), J[:, col], rtol=1e-5, atol=2e-5)
+    # a zero scale leaves the residual undefined, as the functor fails
+    r, _ = pybundle.relative_residual("relative_motion", np.zeros((2, 6)), np.r_[np.zeros(7), 0, np.eye(7).ravel(),
+                                                                                 0.0, 1.0])
+    assert np.all(np.isnan(r))
+
+
+def test_relative_motion_known_value():
+    # test_bundle.py:167-194: instances at (0,0,0) and (2,0,0), identity
+    # rotations, t_ij = (-1, 0, 0): zero residual at s_j = 0.5
+    poses = np.array([[0, 0, 0, 0, 0, 0], [0, 0, 0, 2, 0, 0]], np.float64)
+    prm = np.r_[0, 0, 0, -1, 0, 0, 1, 0, np.eye(7).ravel(), 4.0, 0.5]
+    r, _ = pybundle.relative_residual("relative_motion", poses, prm)
+    np.testing.assert_allclose(r, 0, atol=1e-15)

@@ -99,12 +99,32 @@ def test_density_ratio_settings(ba):
 
 def test_unsupported_constraints_raise(ba):
     with pytest.raises(NotImplementedError):
-        ba.add_relative_motion(None)
-    with pytest.raises(NotImplementedError):
-        ba.add_reconstruction("r", False)
+        ba.set_adjust_absolute_position_std(True)
     # the gauge fix looks the origin shot up at once (bundle_adjuster.cc:391)
     with pytest.raises(IndexError):
         ba.set_gauge_fix_shots("a", "b")
+
+
+def test_reconstruction_bookkeeping(ba):
+    # bundle_adjuster.cc:219-244, 1344-1350: unknown reconstruction ids are
+    # ignored by the adders and raise in get_reconstruction
+    ba.add_rig_instance("1", pygeometry.Pose(), {"s1": "cam1"}, {"s1": "rig_cam1"}, False)
+    ba.add_rig_instance("2", pygeometry.Pose(), {"s2": "cam1"}, {"s2": "rig_cam1"}, False)
+    ba.add_reconstruction("12", False)
+    ba.add_reconstruction_instance("12", 4.0, "2")
+    ba.add_reconstruction_instance("12", 3.0, "1")
+    ba.add_reconstruction_instance("nope", 1.0, "1")
+    ba.set_scale_sharing("nope", False)
+    r = ba.get_reconstruction("12")
+    # shared (the default): the first instance in id order
+    assert r.get_scale("2") == 3.0 and r.get_scale("1") == 3.0
+    ba.set_scale_sharing("12", False)
+    assert r.get_scale("2") == 4.0 and r.get_scale("1") == 3.0
+    with pytest.raises(RuntimeError):
+        ba.get_reconstruction("nope")
+    with pytest.raises(IndexError):
+        r.get_scale("3")
+    ba.add_relative_motion(pybundle.RelativeMotion("1", "2", [0, 0, 0], [-1, 0, 0], 1, 1, False))
 
 
 def test_relative_constraints_on_unknown_shots_are_index_errors(ba):
