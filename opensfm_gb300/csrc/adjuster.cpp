@@ -534,8 +534,8 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
-  static const char* kHostGroups[9] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE", "HEATMAP"};
-  for (int k = 0; k < 9; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
+  static const char* kHostGroups[10] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE", "HEATMAP", "REL"};
+  for (int k = 0; k < 10; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
   // constraints between shots, composed with the rig cameras that are
   // optimised or not the identity (IsRigCameraUseful), as Run passes them
   // (bundle_adjuster.cc:912-1138)
