@@ -291,14 +291,19 @@ double BundleAdjuster::GetGroupDensityRatio(const std::string& g) const {
 void BundleAdjuster::Run() {
   PrepareRun();
   opts_.compute_covariances = compute_covariances_;
-  auto solver = make_solver(opts_.precision);
-  summary_ = solver->solve(problem_, opts_);
+  std::unique_ptr<SolverBase> solver;
+  try {
+    solver = make_solver(opts_.precision);
+    summary_ = solver->solve(problem_, opts_);
+  } catch (...) {
+    DropScaleBlocks();
+    throw;
+  }
   // the solved reconstruction scales, then the rig cameras without the
   // scale blocks again
   for (const ScaleBlock& b : scale_blocks_)
     reconstructions_.at(b.reconstruction).scales[b.instance] = problem_.rig_cameras[b.block].value[0];
-  problem_.rig_cameras.resize(n_rig_cameras_);
-  scale_blocks_.clear();
+  DropScaleBlocks();
   if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
   else {
     errors_.clear();
@@ -483,12 +488,14 @@ void BundleAdjuster::AddRelativeMotion(const std::string& instance_i, const std:
   motions_.push_back(m);
 }
 
+void BundleAdjuster::DropScaleBlocks() {
+  if (scale_blocks_.empty()) return;
+  problem_.rig_cameras.resize(n_rig_cameras_);
+  scale_blocks_.clear();
+}
+
 void BundleAdjuster::PrepareRun() {
-  // scale blocks of an earlier run that did not finish
-  if (!scale_blocks_.empty()) {
-    problem_.rig_cameras.resize(n_rig_cameras_);
-    scale_blocks_.clear();
-  }
+  DropScaleBlocks();
   static const char* kSolvers[] = {"DENSE_NORMAL_CHOLESKY", "DENSE_QR", "SPARSE_NORMAL_CHOLESKY", "DENSE_SCHUR",
                                    "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"};
   bool known = false;
@@ -619,23 +626,29 @@ void BundleAdjuster::PrepareRun() {
       scale_blocks_.push_back({rec_id, key, block});
       return block;
     };
-    for (const PendingMotion& m : motions_) {
-      RelativeTerm t;
-      t.kind = RelativeTerm::kRelativeMotion;
-      t.n_shots = 2;
-      for (int k = 0; k < 2; ++k) {
-        const auto it = instance_index_.find(m.instances[k]);
-        if (it == instance_index_.end()) throw std::out_of_range("Rig instance " + m.instances[k] + " doesn't exist.");
-        t.instance[k] = it->second;
-        t.scale_block[k] = block_of(m.instances[k]);
+    try {
+      for (const PendingMotion& m : motions_) {
+        RelativeTerm t;
+        t.kind = RelativeTerm::kRelativeMotion;
+        t.n_shots = 2;
+        for (int k = 0; k < 2; ++k) {
+          const auto it = instance_index_.find(m.instances[k]);
+          if (it == instance_index_.end())
+            throw std::out_of_range("Rig instance " + m.instances[k] + " doesn't exist.");
+          t.instance[k] = it->second;
+          t.scale_block[k] = block_of(m.instances[k]);
+        }
+        for (int k = 0; k < 7; ++k) t.motion[k] = m.motion[k];
+        for (int k = 0; k < 49; ++k) t.motion_matrix[k] = m.scale_matrix[k];
+        t.observed_scale = m.observed_scale;
+        t.loss_scale = relative_loss_threshold_ * m.robust_multiplier;
+        problem_.relative_terms.push_back(t);
       }
-      for (int k = 0; k < 7; ++k) t.motion[k] = m.motion[k];
-      for (int k = 0; k < 49; ++k) t.motion_matrix[k] = m.scale_matrix[k];
-      t.observed_scale = m.observed_scale;
-      t.loss_scale = relative_loss_threshold_ * m.robust_multiplier;
-      any_rotation = true;  // the relative-motion loss is needed
-      problem_.relative_terms.push_back(t);
+    } catch (...) {
+      DropScaleBlocks();
+      throw;
     }
+    any_rotation = true;  // the relative-motion loss is needed
   }
   if (any_rotation) {
     // CreateLossFunction (bundle_adjuster.cc:485-499)
@@ -646,7 +659,10 @@ void BundleAdjuster::PrepareRun() {
     else if (n == "SoftLOneLoss") loss = kLossSoftLOne;
     else if (n == "CauchyLoss") loss = kLossCauchy;
     else if (n == "ArctanLoss") loss = kLossArctan;
-    else throw std::runtime_error("ceres::LossFunction with name " + n + " not found.");
+    else {
+      DropScaleBlocks();
+      throw std::runtime_error("ceres::LossFunction with name " + n + " not found.");
+    }
     problem_.relative_loss = loss;
     problem_.relative_loss_threshold = relative_loss_threshold_;
   }

@@ -109,6 +109,8 @@ class BundleAdjuster {
   // solve, the problem and options the batch solves, and the result of the
   // batch for this problem.
   void PrepareRun();
+  // the rig cameras without the scale blocks a run set-up added
+  void DropScaleBlocks();
   Problem& MutableProblem() { return problem_; }
   const SolverOptions& Options() const { return opts_; }
   void SetBatchResult(const SolveSummary& s, std::vector<double> errors);

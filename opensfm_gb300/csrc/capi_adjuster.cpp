@@ -689,24 +689,35 @@ int gbba_batch_run(gbba_batch_t* b) {
     if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
     if (b->items.empty()) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch is empty");
     std::vector<gbba::Problem*> problems;
-    for (size_t i = 0; i < b->items.size(); ++i) {
-      gbba::BundleAdjuster& ba = ba_of(b->items[i]);
-      ba.PrepareRun();
-      const gbba::SolverOptions& o = ba.Options();
-      if (i == 0) {
-        b->opts.loss = o.loss;
-        b->opts.loss_threshold = o.loss_threshold;
-      } else if (o.loss != b->opts.loss || o.loss_threshold != b->opts.loss_threshold) {
-        throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "every adjuster of a batch needs the same loss function");
-      }
-      problems.push_back(&ba.MutableProblem());
-    }
-    auto solver = gbba::make_batch_solver(b->precision);
+    // the scale blocks a run set-up adds (relative motions, which batches
+    // reject) leave the adjusters on every failure
+    auto drop = [&] {
+      for (gbba_adjuster_t* item : b->items) ba_of(item).DropScaleBlocks();
+    };
     try {
-      b->summary = solver->solve_batch(problems, b->opts);
-    } catch (const std::invalid_argument& e) {
-      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+      for (size_t i = 0; i < b->items.size(); ++i) {
+        gbba::BundleAdjuster& ba = ba_of(b->items[i]);
+        ba.PrepareRun();
+        const gbba::SolverOptions& o = ba.Options();
+        if (i == 0) {
+          b->opts.loss = o.loss;
+          b->opts.loss_threshold = o.loss_threshold;
+        } else if (o.loss != b->opts.loss || o.loss_threshold != b->opts.loss_threshold) {
+          throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "every adjuster of a batch needs the same loss function");
+        }
+        problems.push_back(&ba.MutableProblem());
+      }
+      auto solver = gbba::make_batch_solver(b->precision);
+      try {
+        b->summary = solver->solve_batch(problems, b->opts);
+      } catch (const std::invalid_argument& e) {
+        throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+      }
+    } catch (...) {
+      drop();
+      throw;
     }
+    drop();
     for (size_t i = 0; i < b->items.size(); ++i) {
       gbba::BatchProblemSummary& p = b->summary.problems[i];
       gbba::SolveSummary s;

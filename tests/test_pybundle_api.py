@@ -175,3 +175,21 @@ def test_pose_data_round_trip():
     np.testing.assert_allclose(q.rotation, p.rotation, atol=1e-14)
     np.testing.assert_allclose(q.translation, p.translation, atol=1e-14)
     np.testing.assert_allclose(p.transform_inverse(p.transform([1, 2, 3])), [1, 2, 3], atol=1e-12)
+
+
+def test_run_checks_relative_constraints_before_the_solve(ba):
+    # both failures come from the run's set-up, before any device work: a
+    # relative motion needs its instances in a reconstruction
+    # (reconstructions_assignments_.at, bundle_adjuster.cc:892-897), and the
+    # relative-motion loss name must exist (CreateLossFunction, :485-499)
+    ba.add_rig_instance("1", pygeometry.Pose(), {"s1": "cam1"}, {"s1": "rig_cam1"}, False)
+    ba.add_rig_instance("2", pygeometry.Pose(), {"s2": "cam1"}, {"s2": "rig_cam1"}, False)
+    ba.add_relative_motion(pybundle.RelativeMotion("1", "2", [0, 0, 0], [-1, 0, 0], 1, 1, False))
+    with pytest.raises(IndexError):
+        ba.run()
+    ba.add_reconstruction("12", False)
+    ba.add_reconstruction_instance("12", 1.0, "1")
+    ba.add_reconstruction_instance("12", 1.0, "2")
+    ba.set_relative_motion_loss_function("NoSuchLoss", 1.0)
+    with pytest.raises(RuntimeError, match="NoSuchLoss"):
+        ba.run()
