@@ -1,0 +1,213 @@
+"""Local bundle adjustment around shots: the neighbourhood selection and
+the problem set-up of ``sfm::BAHelpers::BundleLocal``
+(opensfm/src/lib/sfm/src/ba_helpers.cc:64-440), on the flat scene arrays
+of :mod:`opensfm_gb300.scene`, driving the GPU adjuster.
+
+* :func:`shot_neighborhood` -- ``ShotNeighborhood`` / ``DirectShotNeighbors``
+  (ba_helpers.cc:64-136): the interior grows from the central shots (and
+  their rig-instance siblings) by ``radius - 1`` hops over shots sharing at
+  least ``min_common_points`` points, most shared points first, up to
+  ``max_interior_size`` shots; the boundary is every other shot that sees a
+  point of the interior.  Ties in the shared-point count are broken by shot
+  index (the reference's ``std::sort`` leaves their order unspecified).
+* :func:`local_problem` -- the set-up of ``BundleLocal`` (ba_helpers.cc:
+  176-330): cameras and rig cameras fixed; the rig instances of interior and
+  boundary shots, fixed when one of their shots is on the boundary; the
+  averaged GPS of an instance's interior shots as its position prior;
+  every point seen from the interior (the reference's grid selection of
+  tracks, ``local_bundle_grid``, is not applied) with all its observations.
+* :func:`bundle_local` -- one local bundle solved and written back.
+* :func:`bundle_local_batch` -- many local bundles at once: the problems
+  the batched solver takes (no position priors) go through one
+  :class:`~opensfm_gb300.pybundle.BundleBatch` solve (one captured LM
+  iteration for all of them), the others run one at a time.  Results are
+  written back in the order of ``central_shots`` (a shot in several
+  interiors keeps the last one's pose).
+
+Defaults are the reference's configuration values (opensfm/config.py:
+``local_bundle_radius`` 3, ``local_bundle_min_common_points`` 20,
+``local_bundle_max_shots`` 30).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Set, Tuple
+
+import numpy as np
+
+from . import pybundle
+from .pygeometry import Camera, Pose
+from .scene import NUM_PARAMS, SceneArrays
+
+
+@dataclass
+class Covisibility:
+    """Shot <-> point incidence of a scene (each pair once)."""
+    shot_points: List[np.ndarray]
+    point_shots: List[np.ndarray]
+    instance_shots: Dict[int, List[int]]
+    shot_instance: np.ndarray
+
+    @classmethod
+    def of(cls, scene: SceneArrays) -> "Covisibility":
+        n_shots = len(scene.shot_camera)
+        n_points = len(scene.points)
+        pairs = np.unique(np.stack([np.asarray(scene.obs_shot, np.int64), np.asarray(scene.obs_point, np.int64)], 1),
+                          axis=0)
+        by_shot = np.argsort(pairs[:, 0], kind="stable")
+        sp = np.split(pairs[by_shot, 1], np.searchsorted(pairs[by_shot, 0], np.arange(1, n_shots)))
+        by_point = np.lexsort((pairs[:, 0], pairs[:, 1]))
+        ps = np.split(pairs[by_point, 0], np.searchsorted(pairs[by_point, 1], np.arange(1, n_points)))
+        inst = np.asarray(scene.shot_rig_instance, np.int64)
+        instance_shots: Dict[int, List[int]] = {}
+        for s in range(n_shots):
+            instance_shots.setdefault(int(inst[s]), []).append(s)
+        return cls(sp, ps, instance_shots, inst)
+
+
+def direct_shot_neighbors(cov: Covisibility, shots: Set[int], min_common_points: int,
+                          max_neighbors: int) -> Set[int]:
+    """DirectShotNeighbors (ba_helpers.cc:95-136): shots outside ``shots``
+    that see at least ``min_common_points`` of their points, most first, at
+    most ``max_neighbors`` of them, each with its rig-instance siblings."""
+    points = set()
+    for s in shots:
+        points.update(cov.shot_points[s].tolist())
+    common: Dict[int, int] = {}
+    for p in points:
+        for s in cov.point_shots[p].tolist():
+            if s not in shots:
+                common[s] = common.get(s, 0) + 1
+    pairs = sorted(common.items(), key=lambda kv: (-kv[1], kv[0]))
+    max_n = min(max_neighbors, len(pairs))
+    neighbors: Set[int] = set()
+    for idx, (s, n) in enumerate(pairs):
+        if n >= min_common_points and idx < max_n:
+            neighbors.update(cov.instance_shots[int(cov.shot_instance[s])])
+        else:
+            break
+    return neighbors
+
+
+def shot_neighborhood(cov: Covisibility, central_shots: Sequence[int], radius: int = 3,
+                      min_common_points: int = 20, max_interior_size: int = 30) -> Tuple[Set[int], Set[int]]:
+    """ShotNeighborhood (ba_helpers.cc:64-93): (interior, boundary)."""
+    interior: Set[int] = set()
+    for c in central_shots:
+        interior.update(cov.instance_shots[int(cov.shot_instance[c])])
+        interior.add(int(c))
+    distance = 1
+    while distance < radius and len(interior) < max_interior_size:
+        interior |= direct_shot_neighbors(cov, interior, min_common_points, max_interior_size - len(interior))
+        distance += 1
+    boundary = direct_shot_neighbors(cov, interior, 1, 1_000_000)
+    return interior, boundary
+
+
+@dataclass
+class LocalProblem:
+    """A local bundle set up on a scene."""
+    adjuster: pybundle.BundleAdjuster
+    interior: Set[int]
+    boundary: Set[int]
+    point_ids: np.ndarray                  # scene point indices in the problem
+    free_instances: List[int] = field(default_factory=list)
+    has_position_priors: bool = False
+
+
+def local_problem(scene: SceneArrays, central_shots: Sequence[int], cov: Optional[Covisibility] = None,
+                  radius: int = 3, min_common_points: int = 20, max_shots: int = 30, use_gps: bool = True,
+                  precision: str = "mixed", loss: Optional[tuple] = None, max_iterations: int = 10,
+                  linear_solver: Optional[str] = None) -> LocalProblem:
+    """The local bundle of ``BundleLocal`` around ``central_shots``."""
+    cov = cov or Covisibility.of(scene)
+    interior, boundary = shot_neighborhood(cov, central_shots, radius, min_common_points, max_shots)
+    shots = sorted(interior | boundary)
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    ba.set_max_num_iterations(max_iterations)
+    if linear_solver is not None:
+        ba.set_linear_solver_type(linear_solver)
+    if loss is not None:
+        ba.set_point_projection_loss_function(*loss)
+    used_cameras = sorted({int(scene.shot_camera[s]) for s in shots})
+    for c in used_cameras:
+        m = int(scene.camera_projection[c])
+        cam = Camera(m, scene.camera_values[c, : NUM_PARAMS[m]])
+        ba.add_camera(str(c), cam, cam, True)
+    ba.add_rig_camera("rig", Pose(), Pose(), True)
+    gps = scene.extras.get("gps") if use_gps else None
+    gps_std = scene.extras.get("gps_std") if use_gps else None
+    free_instances, has_priors = [], False
+    for inst in sorted({int(cov.shot_instance[s]) for s in shots}):
+        members = cov.instance_shots[inst]
+        fixed = any(s in boundary for s in members)
+        pose = Pose.from_ba_data(scene.rig_instance_poses[inst])
+        ba.add_rig_instance(str(inst), pose, {str(s): str(int(scene.shot_camera[s])) for s in members},
+                            {str(s): "rig" for s in members}, fixed)
+        if not fixed:
+            free_instances.append(inst)
+            if gps is not None:
+                inner = [s for s in members if s in interior]
+                if inner:
+                    ba.add_rig_instance_position_prior(str(inst), np.mean([gps[s] for s in inner], axis=0),
+                                                       np.mean([gps_std[s] for s in inner], axis=0), "")
+                    has_priors = True
+    point_ids = np.unique(np.concatenate([cov.shot_points[s] for s in sorted(interior)]) if interior
+                          else np.zeros(0, np.int64))
+    # every observation of these points (their shots are all in interior or boundary)
+    keep = np.isin(np.asarray(scene.obs_point), point_ids)
+    local_index = -np.ones(len(scene.points), np.int64)
+    local_index[point_ids] = np.arange(len(point_ids))
+    ba.add_points(scene.points[point_ids])
+    shot_index = {s: ba._L.gbba_shot_index(ba._h, str(s).encode()) for s in shots}
+    obs_shot = np.array([shot_index[int(s)] for s in np.asarray(scene.obs_shot)[keep]], np.int32)
+    ba.add_point_projection_observations(obs_shot, local_index[np.asarray(scene.obs_point)[keep]].astype(np.int32),
+                                         np.asarray(scene.obs_xy)[keep], np.asarray(scene.obs_std)[keep])
+    return LocalProblem(ba, interior, boundary, point_ids, free_instances, has_priors)
+
+
+def _write_back(scene: SceneArrays, lp: LocalProblem, poses: np.ndarray, points: np.ndarray) -> None:
+    for inst in lp.free_instances:
+        poses[inst] = lp.adjuster.get_rig_instance_pose(str(inst)).ba_data()
+    points[lp.point_ids] = lp.adjuster.get_points()
+
+
+def bundle_local(scene: SceneArrays, central_shot: int, **kw) -> Tuple[np.ndarray, np.ndarray, LocalProblem]:
+    """One local bundle around ``central_shot`` on the GPU; returns the
+    scene's rig-instance poses and points with the local solution written
+    in, and the problem (its adjuster holds the summary)."""
+    lp = local_problem(scene, [central_shot], **kw)
+    lp.adjuster.run()
+    poses, points = np.array(scene.rig_instance_poses, copy=True), np.array(scene.points, copy=True)
+    _write_back(scene, lp, poses, points)
+    return poses, points, lp
+
+
+def bundle_local_batch(scene: SceneArrays, central_shots: Sequence[int], batch_precision: str = "mixed",
+                       batch_pcg_iterations: int = 50, batch_pcg_tolerance: float = 1e-3,
+                       **kw) -> Tuple[np.ndarray, np.ndarray, List[LocalProblem]]:
+    """Local bundles around each of ``central_shots``: those without
+    position priors solved together as one batched GPU solve, the rest one
+    at a time.  Returns the updated poses and points and the problems."""
+    cov = Covisibility.of(scene)
+    problems = [local_problem(scene, [c], cov=cov, **kw) for c in central_shots]
+    batched = [lp for lp in problems if not lp.has_position_priors]
+    if batched:
+        batch = pybundle.BundleBatch()
+        batch.set_options(precision=batch_precision, max_iterations=kw.get("max_iterations", 10),
+                          pcg_iterations=batch_pcg_iterations, pcg_tolerance=batch_pcg_tolerance)
+        for lp in batched:
+            batch.add(lp.adjuster)
+        batch.run()
+    for lp in problems:
+        if lp.has_position_priors:
+            lp.adjuster.run()
+    poses, points = np.array(scene.rig_instance_poses, copy=True), np.array(scene.points, copy=True)
+    for lp in problems:
+        _write_back(scene, lp, poses, points)
+    return poses, points, problems
+
+
+__all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "direct_shot_neighbors",
+           "local_problem", "shot_neighborhood"]
