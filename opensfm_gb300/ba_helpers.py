@@ -160,7 +160,7 @@ def local_problem(scene: SceneArrays, central_shots: Sequence[int], cov: Optiona
     local_index = -np.ones(len(scene.points), np.int64)
     local_index[point_ids] = np.arange(len(point_ids))
     ba.add_points(scene.points[point_ids])
-    shot_index = {s: ba._L.gbba_shot_index(ba._h, str(s).encode()) for s in shots}
+    shot_index = {s: ba.shot_index(str(s)) for s in shots}
     obs_shot = np.array([shot_index[int(s)] for s in np.asarray(scene.obs_shot)[keep]], np.int32)
     ba.add_point_projection_observations(obs_shot, local_index[np.asarray(scene.obs_point)[keep]].astype(np.int32),
                                          np.asarray(scene.obs_xy)[keep], np.asarray(scene.obs_std)[keep])
