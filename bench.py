@@ -375,7 +375,8 @@ def dense_benchmark(sizes=(1024, 2048, 4096), street_shots: int = 500, street_po
             "time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None,
             "iterations": s["iterations"], "final_cost": s["final_cost"], "solve_s": s["seconds"],
             "linear_solver_s": s["linear_solver_seconds"], "linear_iterations": int(tr[:, 4].sum()),
-            "setup_s": s["setup_seconds"]}
+            "setup_s": s["setup_seconds"], "dense_failures": int(s["linear_solver_failures"]),
+            "unsuccessful_steps": int(s["unsuccessful_steps"])}
     return out
 
 

@@ -456,6 +456,7 @@ typedef struct gbba_summary {
   int usable;
   int64_t kernel_launches;
   double setup_seconds; /* problem setup inside run(): sorts, uploads */
+  int64_t linear_solver_failures; /* dense factorizations of a damped system that was not positive definite */
 } gbba_summary_t;
 int gbba_get_summary(const gbba_adjuster_t* h, gbba_summary_t* out);
 /* Iteration trace of the last run: records of 8 doubles

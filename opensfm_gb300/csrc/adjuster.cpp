@@ -745,6 +745,8 @@ std::string BundleAdjuster::FullReport() const {
      << summary_.setup_seconds << "\n";
   ss << "  Kernel launches      " << summary_.kernel_launches << "\n";
   ss << "  PCG refinements      " << summary_.pcg_refinements << " (FP64 residuals of the mixed-precision solve)\n";
+  ss << "  Dense failures       " << summary_.linear_solver_failures
+     << " (factorizations of a damped system that was not positive definite)\n";
   ss << "  Jacobians            " << (summary_.matrix_free ? "matrix-free (evaluated in every pass)" : "stored")
      << "\n";
   ss << "  Termination          " << summary_.termination << "\n";

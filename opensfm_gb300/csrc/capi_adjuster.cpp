@@ -601,6 +601,7 @@ int gbba_get_summary(const gbba_adjuster_t* h, gbba_summary_t* out) {
     out->unsuccessful_steps = s.unsuccessful_steps;
     out->kernel_launches = s.kernel_launches;
     out->setup_seconds = s.setup_seconds;
+    out->linear_solver_failures = s.linear_solver_failures;
     out->usable = s.usable ? 1 : 0;
   });
 }

@@ -163,6 +163,7 @@ struct SolveSummary {
   double setup_seconds = 0;  // slot sorts, uploads, device buffers
   int64_t kernel_launches = 0;
   int64_t pcg_refinements = 0;  // FP64 residual evaluations (mixed-precision iterative refinement)
+  int64_t linear_solver_failures = 0;  // dense factorizations that found the damped system not positive definite
   bool matrix_free = false;      // the record passes evaluated the Jacobians instead of reading them
   std::string linear_solver;
   std::vector<IterationRecord> trace;

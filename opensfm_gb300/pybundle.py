@@ -35,7 +35,7 @@ class Summary(C.Structure):
                 ("linear_solver_seconds", C.c_double), ("jacobian_seconds", C.c_double),
                 ("residual_seconds", C.c_double), ("iterations", C.c_int), ("successful_steps", C.c_int),
                 ("unsuccessful_steps", C.c_int), ("usable", C.c_int), ("kernel_launches", C.c_int64),
-                ("setup_seconds", C.c_double)]
+                ("setup_seconds", C.c_double), ("linear_solver_failures", C.c_int64)]
 
 
 def _declare(L) -> None:
