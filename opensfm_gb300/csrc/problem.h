@@ -13,7 +13,7 @@
 // below hold one flag per parameter (1 = optimised).
 #pragma once
 
-#include "orientation_terms.h"
+#include "host_terms.h"
 
 #include <cstdint>
 #include <string>
