@@ -193,3 +193,25 @@ def test_run_checks_relative_constraints_before_the_solve(ba):
     ba.set_relative_motion_loss_function("NoSuchLoss", 1.0)
     with pytest.raises(RuntimeError, match="NoSuchLoss"):
         ba.run()
+
+
+def test_heatmap_and_residual_argument_checks(ba):
+    ba.add_rig_instance("1", pygeometry.Pose(), {"s1": "cam1"}, {"s1": "rig_cam1"}, False)
+    # a grid must hold a positive multiple of its width
+    with pytest.raises(pybundle._lib.GbbaError):
+        ba.add_heatmap("h", [0.0] * 5, 2, 1.0)
+    with pytest.raises(pybundle._lib.GbbaError):
+        ba.add_heatmap("h", [0.0] * 4, 0, 1.0)
+    ba.add_heatmap("h", [0.0] * 4, 2, 1.0)
+    with pytest.raises(IndexError):
+        ba.add_absolute_position_heatmap("s1", "missing", 0.0, 0.0, 1.0)
+    with pytest.raises(IndexError):
+        ba.add_absolute_position_heatmap("s2", "h", 0.0, 0.0, 1.0)
+    ba.add_absolute_position_heatmap("s1", "h", 0.0, 0.0, 1.0)
+    # residual helpers: unknown kinds and non-positive deviations
+    with pytest.raises(KeyError):
+        pybundle.relative_residual("heatmap", np.zeros((2, 6)), [0.0])
+    with pytest.raises(pybundle._lib.GbbaError):
+        pybundle.heatmap_residual(np.zeros(6), 4, 1.0, 0.0, 0.0, 1.0, np.zeros(6))
+    r, J = pybundle.heatmap_residual(np.ones(6), 3, 1.0, 0.0, 0.0, 0.5, np.zeros(6))
+    assert r == pytest.approx(2.0) and np.all(J == 0.0)  # a constant grid: value / std, no slope
