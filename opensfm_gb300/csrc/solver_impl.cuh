@@ -704,6 +704,9 @@ class DeviceSolver : public SolverBase {
   std::vector<double> hdiag_;
   int n_hblocks_ = 0;
   std::vector<double> host_weight_;  // IRLS weight of every host constraint term
+  // the host terms linearized at the current state (the linear-model
+  // decrease of a step reads them instead of evaluating the terms again)
+  std::vector<HostTermLin> host_lin_;
   std::vector<int> group_count_, group_dim_;
   std::vector<double> group_ratio_;
   std::vector<double> prior_weight_cam_, prior_weight_rig_, prior_weight_gps_;
@@ -1428,8 +1431,10 @@ double DeviceSolver<R>::prior_terms(const std::vector<double>& x, bool want_deri
   }
   // host constraint terms: J^T r and J^T J over their free coordinates,
   // as 8 x 8 blocks of the coordinate groups they couple
+  if (want_derivs) host_lin_.assign(size_t(n_host_terms()), HostTermLin());
   for (int q = 0; q < n_host_terms(); ++q) {
-    HostTermLin L;
+    HostTermLin tmp;
+    HostTermLin& L = want_derivs ? host_lin_[size_t(q)] : tmp;
     host_term(q, x, L);
     cost += 0.5 * L.rho;
     if (!want_derivs) continue;
@@ -1578,9 +1583,12 @@ double DeviceSolver<R>::prior_model_change(const std::vector<double>& x, const s
       total += term(prior_weight_gps_[g], scale * (x[j] - prior[k]), scale, dx[j]);
     }
   }
+  // x is the state the solver linearized at: the cached linearization
+  const bool cached = &x == &xc_ && host_lin_.size() == size_t(n_host_terms());
   for (int q = 0; q < n_host_terms(); ++q) {
-    HostTermLin L;
-    host_term(q, x, L);
+    HostTermLin tmp;
+    if (!cached) host_term(q, x, tmp);
+    const HostTermLin& L = cached ? host_lin_[size_t(q)] : tmp;
     for (int i = 0; i < L.m; ++i) {
       double jd = 0.0;
       for (int a = 0; a < L.ns; ++a)
