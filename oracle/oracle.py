@@ -240,7 +240,7 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None, 
 
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
           density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
-          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None, scales=()):
+          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None, scales=(), fixed_instances=()):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
@@ -250,6 +250,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     linear motion) shot indices and params as gbba_relative_residual takes
     them; ``relative_loss`` the loss of the relative rotations.  ``gauge``:
     (origin shot, scale shot) as set_gauge_fix_shots takes them.
+    ``fixed_instances``: rig instances held constant.
     ``heatmap``: (grid, width, resolution), the grid of the ``relative``
     entries of kind "heatmap" (shots (s,), params (x_offset, y_offset,
     std)).  ``scales``: reconstruction scales (value, free) -- the unknowns
@@ -275,6 +276,8 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     ni = len(scene.rig_instance_poses)
     inst = np.ascontiguousarray(scene.rig_instance_poses)
     inst_free = np.ones((ni, 6), np.uint8)
+    for i in fixed_instances:
+        inst_free[int(i)] = 0
     has_gps = np.zeros(ni, np.uint8)
     gps_pos = np.zeros((ni, 3))
     gps_std = np.ones((ni, 3))

@@ -220,3 +220,38 @@ def test_ring_heatmap_matches_oracle(precision, solver):
     s = ba.summary()
     assert s["usable"]
     assert abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"] < 1e-6, (s["final_cost"], ref["final_cost"])
+
+
+def _three(precision, fixed=(False, False, False), rotations=((0, 0, 0),) * 3):
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    ba.set_skip_initial_reweighting(True)
+    cam = pygeometry.Camera.create_perspective(1.0, 0.0, 0.0)
+    ba.add_camera("cam1", cam, cam, True)
+    ba.add_rig_camera("rig_cam1", pygeometry.Pose(), pygeometry.Pose(), True)
+    for i in range(3):
+        iid = str(i + 1)
+        ba.add_rig_instance(iid, pygeometry.Pose(np.array(rotations[i], np.float64), np.zeros(3)), {iid: "cam1"},
+                            {iid: "rig_cam1"}, fixed[i])
+    return ba
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_linear_motion_prior_position(precision):
+    # test_bundle.py:529-552
+    ba = _three(precision)
+    ba.add_rig_instance_position_prior("1", np.zeros(3), np.ones(3), "")
+    ba.add_rig_instance_position_prior("3", np.array([2.0, 0, 0]), np.ones(3), "")
+    ba.add_linear_motion("1", "2", "3", 0.5, 0.1, 0.1)
+    ba.run()
+    for i, t in zip("123", ([0, 0, 0], [-1, 0, 0], [-2, 0, 0])):
+        assert np.allclose(ba.get_rig_instance_pose(i).translation, t, atol=1e-6), (i, t)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_linear_motion_prior_rotation(precision):
+    # test_bundle.py:555-590
+    ba = _three(precision, fixed=(True, False, True), rotations=((0, 0, 0), (0, 0, 0), (0, 1, 0)))
+    ba.add_linear_motion("1", "2", "3", 0.3, 0.1, 0.1)
+    ba.run()
+    assert np.allclose(ba.get_rig_instance_pose("2").rotation, [0, 0.3, 0], atol=1e-6)

@@ -153,3 +153,30 @@ def test_ring_relative_motions_match_oracle(precision, solver):
     assert abs(s["final_cost"] - ref["final_cost"]) / ref["final_cost"] < 1e-6, (s["final_cost"], ref["final_cost"])
     got = [ba.get_reconstruction("A").get_scale("0"), ba.get_reconstruction("B").get_scale("10")]
     np.testing.assert_allclose(got, ref["scales"], atol=1e-5 if precision == "fp64" else 1e-4)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_four_cams_one_fixed(precision):
+    # test_bundle.py:455-526
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    ba.set_skip_initial_reweighting(True)
+    cam = pygeometry.Camera.create_perspective(1.0, 0.0, 0.0)
+    ba.add_camera("cam1", cam, cam, True)
+    ba.add_rig_camera("rig_cam1", pygeometry.Pose(), pygeometry.Pose(), True)
+    for i in range(4):
+        iid = str(i + 1)
+        ba.add_rig_instance(iid, pygeometry.Pose(np.zeros(3), np.zeros(3)), {iid: "cam1"}, {iid: "rig_cam1"}, i == 0)
+    ba.add_reconstruction("1234", False)
+    for i in "1234":
+        ba.add_reconstruction_instance("1234", 1, i)
+    ba.set_scale_sharing("1234", True)
+    ba.add_relative_motion(_motion("1", "2", [-1, 0, 0]))
+    ba.add_relative_motion(_motion("1", "3", [0, -1, 0]))
+    ba.add_relative_motion(_motion("1", "4", [0, 0, -1]))
+    ba.add_rig_instance_position_prior("1", np.array([100.0, 0, 0]), np.ones(3), "")
+    ba.add_rig_instance_position_prior("2", np.array([2.0, 0, 0]), np.ones(3), "")
+    ba.add_rig_instance_position_prior("3", np.array([0, 2.0, 0]), np.ones(3), "")
+    ba.run()
+    for i, t in zip("1234", ([0, 0, 0], [-2, 0, 0], [0, -2, 0], [0, 0, -2])):
+        assert np.allclose(ba.get_rig_instance_pose(i).translation, t, atol=1e-6), (i, t)

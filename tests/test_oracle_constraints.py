@@ -104,3 +104,30 @@ def test_heatmap_singletons():
     _, poses = _solve(s, relative=rel, heatmap=(grid, size, res))
     for p, (xo, yo) in zip(poses, offsets):
         np.testing.assert_allclose(-p.translation, [xo + hx, yo + hy, 0], atol=res)
+
+
+def test_four_cams_one_fixed():
+    # test_bundle.py:455-526: the fixed instance ignores its own GPS prior
+    s = _scene([pygeometry.Pose()] * 4, gps=[([100, 0, 0], [1, 1, 1]), ([2, 0, 0], [1, 1, 1]),
+                                             ([0, 2, 0], [1, 1, 1]), ([0, 0, 0], [1e9, 1e9, 1e9])])
+    rel = [_motion(0, 1, [-1, 0, 0], 0, 0), _motion(0, 2, [0, -1, 0], 0, 0), _motion(0, 3, [0, 0, -1], 0, 0)]
+    _, poses = _solve(s, relative=rel, scales=[(1.0, True)], fixed_instances=[0])
+    for p, t in zip(poses, ([0, 0, 0], [-2, 0, 0], [0, -2, 0], [0, 0, -2])):
+        np.testing.assert_allclose(p.translation, t, atol=1e-6)
+
+
+def test_linear_motion_prior_position():
+    # test_bundle.py:529-552: the middle instance has no GPS
+    s = _scene([pygeometry.Pose()] * 3, gps=[([0, 0, 0], [1, 1, 1]), ([0, 0, 0], [1e9, 1e9, 1e9]),
+                                             ([2, 0, 0], [1, 1, 1])])
+    _, poses = _solve(s, relative=[("linear_motion", (0, 1, 2), [0.5, 0.1, 0.1])])
+    for p, t in zip(poses, ([0, 0, 0], [-1, 0, 0], [-2, 0, 0])):
+        np.testing.assert_allclose(p.translation, t, atol=1e-6)
+
+
+def test_linear_motion_prior_rotation():
+    # test_bundle.py:555-590: the end instances held, the middle rotation
+    # interpolated at alpha = 0.3
+    s = _scene([pygeometry.Pose(), pygeometry.Pose(), pygeometry.Pose(np.array([0, 1.0, 0]), np.zeros(3))])
+    _, poses = _solve(s, relative=[("linear_motion", (0, 1, 2), [0.3, 0.1, 0.1])], fixed_instances=[0, 2])
+    np.testing.assert_allclose(poses[1].rotation, [0, 0.3, 0], atol=1e-6)
