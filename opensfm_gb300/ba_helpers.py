@@ -10,12 +10,19 @@ of :mod:`opensfm_gb300.scene`, driving the GPU adjuster.
   ``max_interior_size`` shots; the boundary is every other shot that sees a
   point of the interior.  Ties in the shared-point count are broken by shot
   index (the reference's ``std::sort`` leaves their order unspecified).
+* :func:`select_tracks_grid` -- ``SelectTracksGrid`` (ba_helpers.cc:
+  938-1004): in every interior shot's image, a grid_size x grid_size grid
+  keeps the longest track (most observations) per cell that no earlier shot
+  selected; the other tracks seen from the interior are returned for
+  retriangulation.  Shots are visited in index order and observations in
+  scene order (the reference iterates a hash set).
 * :func:`local_problem` -- the set-up of ``BundleLocal`` (ba_helpers.cc:
   176-330): cameras and rig cameras fixed; the rig instances of interior and
   boundary shots, fixed when one of their shots is on the boundary; the
-  averaged GPS of an instance's interior shots as its position prior;
-  every point seen from the interior (the reference's grid selection of
-  tracks, ``local_bundle_grid``, is not applied) with all its observations.
+  averaged GPS of an instance's interior shots as its position prior; the
+  grid-selected tracks (``local_bundle_grid``, default 12) with all their
+  observations.  Without image sizes, or with grid_size <= 1, every track
+  seen from the interior is taken (the reference would take none).
 * :func:`bundle_local` -- one local bundle solved and written back.
 * :func:`bundle_local_batch` -- many local bundles at once: the problems
   the batched solver takes (no position priors) go through one
@@ -104,6 +111,38 @@ def shot_neighborhood(cov: Covisibility, central_shots: Sequence[int], radius: i
     return interior, boundary
 
 
+def select_tracks_grid(scene: SceneArrays, cov: Covisibility, shots: Set[int], grid_size: int, width: int,
+                       height: int) -> Tuple[np.ndarray, np.ndarray]:
+    """SelectTracksGrid (ba_helpers.cc:938-1004): (selected tracks, other
+    tracks seen from ``shots``), as sorted point indices."""
+    if not shots or grid_size <= 1 or width <= 0 or height <= 0:
+        return np.zeros(0, np.int64), np.zeros(0, np.int64)
+    obs_shot = np.asarray(scene.obs_shot)
+    obs_point = np.asarray(scene.obs_point)
+    xy = np.asarray(scene.obs_xy)
+    track_len = np.array([len(ps) for ps in cov.point_shots], np.int64)
+    normalize = max(width, height)
+    order = np.argsort(obs_shot, kind="stable")
+    starts = np.searchsorted(obs_shot[order], np.arange(len(scene.shot_camera) + 1))
+    selected: Set[int] = set()
+    seen: Set[int] = set()
+    for s in sorted(shots):
+        cells: Dict[int, Tuple[int, int]] = {}
+        for o in order[starts[s]:starts[s + 1]]:
+            p = int(obs_point[o])
+            seen.add(p)
+            x = min(1.0, max(0.0, (xy[o, 0] * normalize + width * 0.5) / width))
+            y = min(1.0, max(0.0, (xy[o, 1] * normalize + height * 0.5) / height))
+            gx = min(int(x * grid_size), grid_size - 1)
+            gy = min(int(y * grid_size), grid_size - 1)
+            cell = gx + gy * grid_size
+            best = cells.get(cell, (-1, 0))
+            if track_len[p] > best[1] and p not in selected:
+                cells[cell] = (p, int(track_len[p]))
+        selected.update(p for p, _ in cells.values())
+    return (np.array(sorted(selected), np.int64), np.array(sorted(seen - selected), np.int64))
+
+
 @dataclass
 class LocalProblem:
     """A local bundle set up on a scene."""
@@ -113,13 +152,17 @@ class LocalProblem:
     point_ids: np.ndarray                  # scene point indices in the problem
     free_instances: List[int] = field(default_factory=list)
     has_position_priors: bool = False
+    other_tracks: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int64))  # to retriangulate
 
 
 def local_problem(scene: SceneArrays, central_shots: Sequence[int], cov: Optional[Covisibility] = None,
                   radius: int = 3, min_common_points: int = 20, max_shots: int = 30, use_gps: bool = True,
                   precision: str = "mixed", loss: Optional[tuple] = None, max_iterations: int = 10,
-                  linear_solver: Optional[str] = None) -> LocalProblem:
-    """The local bundle of ``BundleLocal`` around ``central_shots``."""
+                  linear_solver: Optional[str] = None, grid_size: int = 12, image_size: Optional[Tuple[int, int]] = None
+                  ) -> LocalProblem:
+    """The local bundle of ``BundleLocal`` around ``central_shots``.
+    ``image_size`` (width, height) for the track grid; by default the
+    scene's ``extras`` width and height when present."""
     cov = cov or Covisibility.of(scene)
     interior, boundary = shot_neighborhood(cov, central_shots, radius, min_common_points, max_shots)
     shots = sorted(interior | boundary)
@@ -153,8 +196,14 @@ def local_problem(scene: SceneArrays, central_shots: Sequence[int], cov: Optiona
                     ba.add_rig_instance_position_prior(str(inst), np.mean([gps[s] for s in inner], axis=0),
                                                        np.mean([gps_std[s] for s in inner], axis=0), "")
                     has_priors = True
-    point_ids = np.unique(np.concatenate([cov.shot_points[s] for s in sorted(interior)]) if interior
-                          else np.zeros(0, np.int64))
+    if image_size is None and "width" in scene.extras and "height" in scene.extras:
+        image_size = (int(scene.extras["width"]), int(scene.extras["height"]))
+    other_tracks = np.zeros(0, np.int64)
+    if image_size is not None and grid_size > 1:
+        point_ids, other_tracks = select_tracks_grid(scene, cov, interior, grid_size, *image_size)
+    else:
+        point_ids = np.unique(np.concatenate([cov.shot_points[s] for s in sorted(interior)]) if interior
+                              else np.zeros(0, np.int64))
     # every observation of these points (their shots are all in interior or boundary)
     keep = np.isin(np.asarray(scene.obs_point), point_ids)
     local_index = -np.ones(len(scene.points), np.int64)
@@ -164,7 +213,7 @@ def local_problem(scene: SceneArrays, central_shots: Sequence[int], cov: Optiona
     obs_shot = np.array([shot_index[int(s)] for s in np.asarray(scene.obs_shot)[keep]], np.int32)
     ba.add_point_projection_observations(obs_shot, local_index[np.asarray(scene.obs_point)[keep]].astype(np.int32),
                                          np.asarray(scene.obs_xy)[keep], np.asarray(scene.obs_std)[keep])
-    return LocalProblem(ba, interior, boundary, point_ids, free_instances, has_priors)
+    return LocalProblem(ba, interior, boundary, point_ids, free_instances, has_priors, other_tracks)
 
 
 def _write_back(scene: SceneArrays, lp: LocalProblem, poses: np.ndarray, points: np.ndarray) -> None:
@@ -210,4 +259,4 @@ def bundle_local_batch(scene: SceneArrays, central_shots: Sequence[int], batch_p
 
 
 __all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "direct_shot_neighbors",
-           "local_problem", "shot_neighborhood"]
+           "local_problem", "select_tracks_grid", "shot_neighborhood"]

@@ -74,3 +74,31 @@ def test_local_problem_set_up():
     keep = np.isin(scene.obs_point, np.arange(10, 55))
     assert int(L.gbba_num_projections(h)) == int(keep.sum())
     assert sorted(lp.free_instances) == [1, 2, 3] and not lp.has_position_priors
+
+
+def test_select_tracks_grid_keeps_the_longest_track_per_cell():
+    # SelectTracksGrid (ba_helpers.cc:938-1004) on a 2 x 2 grid of a 100 x 100
+    # image.  Track lengths: p1 3, p2 2, p5 2, the others 1.  Shot 0 keeps
+    # p1 (over p0) in cell 0, p2 in cell 1 and p3 in cell 3; shot 1 skips
+    # the already selected p1 and keeps p4 (cell 2) and p5 (cell 0, out of
+    # the image: clamped)
+    obs = [(0, 0, (-0.3, -0.3)), (0, 1, (-0.2, -0.2)), (0, 2, (0.3, -0.3)), (0, 3, (0.3, 0.3)),
+           (1, 1, (-0.3, 0.3)), (1, 4, (-0.2, 0.2)), (1, 5, (-0.9, -0.9)),
+           (2, 1, (0.0, 0.0)), (2, 2, (0.0, 0.0)), (2, 5, (0.0, 0.0))]
+    scene = sc.SceneArrays(
+        camera_projection=[sc.PERSPECTIVE], camera_values=np.array([[0.0, 0.0, 1.0]]),
+        rig_instance_poses=np.zeros((3, 6)), shot_rig_instance=np.arange(3), shot_camera=np.zeros(3),
+        points=np.zeros((6, 3)), obs_shot=np.array([o[0] for o in obs], np.int32),
+        obs_point=np.array([o[1] for o in obs], np.int32), obs_xy=np.array([o[2] for o in obs], np.float64),
+        obs_std=np.full(len(obs), 1e-3))
+    cov = ba_helpers.Covisibility.of(scene)
+    selected, other = ba_helpers.select_tracks_grid(scene, cov, {0, 1}, 2, 100, 100)
+    assert selected.tolist() == [1, 2, 3, 4, 5] and other.tolist() == [0]
+    # one cell per image: the longest track of each shot
+    selected, other = ba_helpers.select_tracks_grid(scene, cov, {0, 1}, 1, 100, 100)
+    assert selected.size == 0 and other.size == 0  # grid_size <= 1 selects nothing
+    selected, _ = ba_helpers.select_tracks_grid(scene, cov, {0}, 2, 100, 100)
+    assert selected.tolist() == [1, 2, 3]
+    # the local problem takes the grid selection when the image size is known
+    lp = ba_helpers.local_problem(scene, [0], radius=1, min_common_points=1, grid_size=2, image_size=(100, 100))
+    assert lp.point_ids.tolist() == [1, 2, 3] and lp.other_tracks.tolist() == [0]
