@@ -31,12 +31,25 @@ of :mod:`opensfm_gb300.scene`, driving the GPU adjuster.
   written back in the order of ``central_shots`` (a shot in several
   interiors keeps the last one's pose).
 
+* :func:`bundle_stochastic` -- ``BundleStochastic`` (ba_helpers.cc:
+  1231-1370): K = min(ceil(3 S / N), max_rounds) rounds, each a local
+  bundle around ``random_shots`` seeds drawn by a partial Fisher-Yates
+  shuffle of the shots, with the stochastic radius and an interior budget
+  of N shots; every round starts from the previous round's result.  The
+  seeds come from numpy's generator (the reference's ``std::mt19937(42)``
+  draws differ); GCP-anchored seeds and the GPS-bias compensation of
+  ``BundleLocalStochastic`` are not applied.
+
 Defaults are the reference's configuration values (opensfm/config.py:
 ``local_bundle_radius`` 3, ``local_bundle_min_common_points`` 20,
-``local_bundle_max_shots`` 30).
+``local_bundle_max_shots`` 30, ``stochastic_bundle_max_shots`` 500,
+``stochastic_bundle_random_shots`` 20, ``stochastic_bundle_radius`` 100,
+``stochastic_bundle_max_rounds`` 100).
 """
 from __future__ import annotations
 
+import copy
+import math
 from dataclasses import dataclass, field
 from typing import Dict, List, Optional, Sequence, Set, Tuple
 
@@ -258,5 +271,51 @@ def bundle_local_batch(scene: SceneArrays, central_shots: Sequence[int], batch_p
     return poses, points, problems
 
 
-__all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "direct_shot_neighbors",
-           "local_problem", "select_tracks_grid", "shot_neighborhood"]
+def stochastic_rounds(num_shots: int, max_shots: int = 500, max_rounds: int = 100) -> Tuple[int, int]:
+    """(rounds, interior budget) of BundleStochastic (ba_helpers.cc:
+    1246-1266): P(a shot is adjusted at least once) ~ 1 - exp(-K N / S),
+    K = ceil(3 S / N) for about 95% coverage, capped at ``max_rounds``."""
+    n = max(1, min(max_shots, num_shots))
+    k = int(math.ceil(3.0 * num_shots / n))
+    return max(1, min(k, max_rounds)), n
+
+
+def stochastic_seeds(rng: np.random.Generator, shot_ids: List[int], random_shots: int) -> List[int]:
+    """The round's seeds: a partial Fisher-Yates shuffle of ``shot_ids``
+    (in place, carried over rounds), its first ``random_shots`` entries."""
+    k = max(1, min(random_shots, len(shot_ids)))
+    seeds = []
+    for i in range(k):
+        j = int(rng.integers(i, len(shot_ids)))
+        shot_ids[i], shot_ids[j] = shot_ids[j], shot_ids[i]
+        seeds.append(shot_ids[i])
+    return seeds
+
+
+def bundle_stochastic(scene: SceneArrays, max_shots: int = 500, random_shots: int = 20, radius: int = 100,
+                      max_rounds: int = 100, seed: int = 42, **kw) -> Tuple[np.ndarray, np.ndarray, dict]:
+    """BundleStochastic: rounds of local bundles around random seeds, each
+    starting from the previous round's poses and points.  Returns the final
+    poses and points and a report (rounds, seeds and summaries)."""
+    n_shots = len(scene.shot_camera)
+    rounds, budget = stochastic_rounds(n_shots, max_shots, max_rounds)
+    rng = np.random.default_rng(seed)
+    ids = list(range(n_shots))
+    work = copy.copy(scene)
+    work.rig_instance_poses = np.array(scene.rig_instance_poses, copy=True)
+    work.points = np.array(scene.points, copy=True)
+    cov = Covisibility.of(scene)
+    report = {"num_rounds": rounds, "interior_budget": budget, "rounds": []}
+    for _ in range(rounds):
+        seeds = stochastic_seeds(rng, ids, random_shots)
+        lp = local_problem(work, seeds, cov=cov, radius=radius, max_shots=budget, **kw)
+        lp.adjuster.run()
+        _write_back(work, lp, work.rig_instance_poses, work.points)
+        report["rounds"].append({"seeds": seeds, "interior": len(lp.interior), "points": int(len(lp.point_ids)),
+                                 "summary": lp.adjuster.summary()})
+    return work.rig_instance_poses, work.points, report
+
+
+__all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "bundle_stochastic",
+           "direct_shot_neighbors", "local_problem", "select_tracks_grid", "shot_neighborhood", "stochastic_rounds",
+           "stochastic_seeds"]

@@ -102,3 +102,20 @@ def test_select_tracks_grid_keeps_the_longest_track_per_cell():
     # the local problem takes the grid selection when the image size is known
     lp = ba_helpers.local_problem(scene, [0], radius=1, min_common_points=1, grid_size=2, image_size=(100, 100))
     assert lp.point_ids.tolist() == [1, 2, 3] and lp.other_tracks.tolist() == [0]
+
+
+def test_stochastic_rounds_and_seeds():
+    # BundleStochastic (ba_helpers.cc:1246-1266): K = ceil(3 S / N) rounds,
+    # capped, N = min(max shots, S)
+    assert ba_helpers.stochastic_rounds(4000, 500, 100) == (24, 500)
+    assert ba_helpers.stochastic_rounds(4000, 50, 100) == (100, 50)
+    assert ba_helpers.stochastic_rounds(10, 500, 100) == (3, 10)
+    assert ba_helpers.stochastic_rounds(0, 500, 100) == (1, 1)
+    # seeds: distinct within a round, drawn by a partial shuffle carried
+    # over rounds
+    rng = np.random.default_rng(42)
+    ids = list(range(30))
+    first = ba_helpers.stochastic_seeds(rng, ids, 20)
+    assert len(set(first)) == 20 and sorted(ids) == list(range(30))
+    assert ids[:20] == first
+    assert len(ba_helpers.stochastic_seeds(rng, ids, 100)) == 30

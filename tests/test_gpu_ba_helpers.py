@@ -39,3 +39,17 @@ def test_bundle_local_batch_solves_every_problem():
         s = lp.adjuster.summary()
         assert s["usable"] and s["final_cost"] <= s["initial_cost"], s
     assert np.isfinite(poses).all() and np.isfinite(points).all()
+
+
+def test_bundle_stochastic_rounds_lower_the_cost():
+    # BundleStochastic (ba_helpers.cc:1231-1370): three rounds of local
+    # bundles around random seeds, each from the previous round's result
+    scene = _scene()
+    poses, points, report = ba_helpers.bundle_stochastic(scene, max_shots=10, random_shots=3, max_rounds=3,
+                                                         use_gps=False, loss=("SoftLOneLoss", 1.0))
+    assert report["num_rounds"] == 3 and len(report["rounds"]) == 3
+    for r in report["rounds"]:
+        s = r["summary"]
+        assert s["usable"] and s["final_cost"] <= s["initial_cost"], s
+        assert 3 <= r["interior"] <= 12
+    assert np.isfinite(poses).all() and np.isfinite(points).all()
