@@ -31,6 +31,12 @@ of :mod:`opensfm_gb300.scene`, driving the GPU adjuster.
   written back in the order of ``central_shots`` (a shot in several
   interiors keeps the last one's pose).
 
+* :func:`shot_poses_problem` / :func:`bundle_shot_poses` --
+  ``BundleShotPoses`` (ba_helpers.cc): the poses of the given shots alone --
+  cameras, rig cameras and every point they see held constant, an instance
+  fixed when one of its shots is not among them, averaged GPS on the free
+  instances, the given shots' observations, 10 iterations with exact
+  (``DENSE_QR``) steps.
 * :func:`bundle_stochastic` -- ``BundleStochastic`` (ba_helpers.cc:
   1231-1370): K = min(ceil(3 S / N), max_rounds) rounds, each a local
   bundle around ``random_shots`` seeds drawn by a partial Fisher-Yates
@@ -271,6 +277,67 @@ def bundle_local_batch(scene: SceneArrays, central_shots: Sequence[int], batch_p
     return poses, points, problems
 
 
+def shot_poses_problem(scene: SceneArrays, shot_ids: Sequence[int], cov: Optional[Covisibility] = None,
+                       use_gps: bool = True, precision: str = "mixed", loss: Optional[tuple] = None,
+                       max_iterations: int = 10) -> LocalProblem:
+    """The problem of BundleShotPoses for ``shot_ids`` (its ``interior``;
+    the boundary is empty: every point is held)."""
+    cov = cov or Covisibility.of(scene)
+    chosen = {int(s) for s in shot_ids}
+    instances = sorted({int(cov.shot_instance[s]) for s in chosen})
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    ba.set_max_num_iterations(max_iterations)
+    ba.set_linear_solver_type("DENSE_QR")
+    if loss is not None:
+        ba.set_point_projection_loss_function(*loss)
+    members_of = {i: cov.instance_shots[i] for i in instances}
+    shots = sorted({s for i in instances for s in members_of[i]})
+    for c in sorted({int(scene.shot_camera[s]) for s in shots}):
+        m = int(scene.camera_projection[c])
+        cam = Camera(m, scene.camera_values[c, : NUM_PARAMS[m]])
+        ba.add_camera(str(c), cam, cam, True)
+    ba.add_rig_camera("rig", Pose(), Pose(), True)
+    gps = scene.extras.get("gps") if use_gps else None
+    gps_std = scene.extras.get("gps_std") if use_gps else None
+    free_instances, has_priors = [], False
+    for inst in instances:
+        members = members_of[inst]
+        fixed = any(s not in chosen for s in members)
+        ba.add_rig_instance(str(inst), Pose.from_ba_data(scene.rig_instance_poses[inst]),
+                            {str(s): str(int(scene.shot_camera[s])) for s in members},
+                            {str(s): "rig" for s in members}, fixed)
+        if not fixed:
+            free_instances.append(inst)
+            if gps is not None:
+                ba.add_rig_instance_position_prior(str(inst), np.mean([gps[s] for s in members], axis=0),
+                                                   np.mean([gps_std[s] for s in members], axis=0), "")
+                has_priors = True
+    point_ids = np.unique(np.concatenate([cov.shot_points[s] for s in sorted(chosen)]) if chosen
+                          else np.zeros(0, np.int64))
+    local_index = -np.ones(len(scene.points), np.int64)
+    local_index[point_ids] = np.arange(len(point_ids))
+    ba.add_points(scene.points[point_ids], np.ones(len(point_ids), np.uint8))
+    keep = np.isin(np.asarray(scene.obs_shot), sorted(chosen))
+    shot_index = {s: ba.shot_index(str(s)) for s in shots}
+    obs_shot = np.array([shot_index[int(s)] for s in np.asarray(scene.obs_shot)[keep]], np.int32)
+    ba.add_point_projection_observations(obs_shot, local_index[np.asarray(scene.obs_point)[keep]].astype(np.int32),
+                                         np.asarray(scene.obs_xy)[keep], np.asarray(scene.obs_std)[keep])
+    return LocalProblem(ba, chosen, set(), point_ids, free_instances, has_priors)
+
+
+def bundle_shot_poses(scene: SceneArrays, shot_ids: Sequence[int], **kw) -> Tuple[np.ndarray, LocalProblem]:
+    """BundleShotPoses on the GPU: the given shots' rig-instance poses
+    refined against constant points; returns the scene's poses with them
+    written in, and the problem."""
+    lp = shot_poses_problem(scene, shot_ids, **kw)
+    lp.adjuster.run()
+    poses = np.array(scene.rig_instance_poses, copy=True)
+    for inst in lp.free_instances:
+        poses[inst] = lp.adjuster.get_rig_instance_pose(str(inst)).ba_data()
+    return poses, lp
+
+
 def stochastic_rounds(num_shots: int, max_shots: int = 500, max_rounds: int = 100) -> Tuple[int, int]:
     """(rounds, interior budget) of BundleStochastic (ba_helpers.cc:
     1246-1266): P(a shot is adjusted at least once) ~ 1 - exp(-K N / S),
@@ -316,6 +383,6 @@ def bundle_stochastic(scene: SceneArrays, max_shots: int = 500, random_shots: in
     return work.rig_instance_poses, work.points, report
 
 
-__all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "bundle_stochastic",
-           "direct_shot_neighbors", "local_problem", "select_tracks_grid", "shot_neighborhood", "stochastic_rounds",
-           "stochastic_seeds"]
+__all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "bundle_shot_poses",
+           "bundle_stochastic", "direct_shot_neighbors", "local_problem", "select_tracks_grid", "shot_neighborhood",
+           "shot_poses_problem", "stochastic_rounds", "stochastic_seeds"]

@@ -119,3 +119,17 @@ def test_stochastic_rounds_and_seeds():
     assert len(set(first)) == 20 and sorted(ids) == list(range(30))
     assert ids[:20] == first
     assert len(ba_helpers.stochastic_seeds(rng, ids, 100)) == 30
+
+
+def test_shot_poses_problem_set_up():
+    # BundleShotPoses: the given shots' observations only, every point they
+    # see held constant; shot 3 shares its rig instance with shot 2, which
+    # is not among them, so that instance stays fixed
+    scene = _chain(instances=[0, 1, 2, 2, 3, 4])
+    lp = ba_helpers.shot_poses_problem(scene, [1, 3])
+    assert lp.interior == {1, 3} and lp.boundary == set()
+    assert lp.free_instances == [1]
+    # shot 1 sees points 10..34, shot 3 points 30..54
+    np.testing.assert_array_equal(lp.point_ids, np.arange(10, 55))
+    L, h = lp.adjuster._L, lp.adjuster._h
+    assert int(L.gbba_num_projections(h)) == 50

@@ -53,3 +53,17 @@ def test_bundle_stochastic_rounds_lower_the_cost():
         assert s["usable"] and s["final_cost"] <= s["initial_cost"], s
         assert 3 <= r["interior"] <= 12
     assert np.isfinite(poses).all() and np.isfinite(points).all()
+
+
+def test_bundle_shot_poses_refines_the_given_shots():
+    # BundleShotPoses: two shots moved off, refined against constant points
+    scene = _scene()
+    moved = np.array(scene.rig_instance_poses, copy=True)
+    moved[[5, 6], 3:] += 0.3
+    scene.rig_instance_poses = moved
+    poses, lp = ba_helpers.bundle_shot_poses(scene, [5, 6], use_gps=False, loss=("SoftLOneLoss", 1.0))
+    s = lp.adjuster.summary()
+    assert s["usable"] and s["final_cost"] < 0.5 * s["initial_cost"], s
+    others = np.setdiff1d(np.arange(len(poses)), [5, 6])
+    np.testing.assert_array_equal(poses[others], moved[others])
+    assert np.abs(poses[[5, 6]] - moved[[5, 6]]).max() > 0.01
