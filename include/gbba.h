@@ -310,6 +310,11 @@ int gbba_add_heatmap(gbba_adjuster_t* h, const char* heatmap_id, const double* d
                      double resolution);
 int gbba_add_absolute_position_heatmap(gbba_adjuster_t* h, const char* shot_id, const char* heatmap_id,
                                        double x_offset, double y_offset, double std_deviation);
+/* rho(s), rho'(s), rho''(s) of the host constraint losses: kind 0 trivial,
+ * 1 Huber, 2 soft-L1, 3 Cauchy, 4 arctan (the names of
+ * set_relative_motion_loss_function), 5 Tukey, at scale a.  Host arithmetic
+ * only. */
+int gbba_host_loss(int kind, double a, double s, double* rho);
 /* The heatmap residual at instance pose [6] and rig camera pose [6] (NULL:
  * none) and its Jacobian [12] (instance rotation, instance position, rig
  * camera rotation, rig camera position).  Host arithmetic only. */

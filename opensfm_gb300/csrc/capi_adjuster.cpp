@@ -202,6 +202,14 @@ int gbba_add_absolute_position_heatmap(gbba_adjuster_t* h, const char* shot_id, 
   });
 }
 
+int gbba_host_loss(int kind, double a, double s, double* rho) {
+  return guarded([&] {
+    if (kind < 0 || kind > 5 || !rho || !(a > 0.0))
+      throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_host_loss: invalid argument");
+    gbba::orient::loss_rho(kind, a, s, rho);
+  });
+}
+
 int gbba_heatmap_residual(const double* grid, int64_t n, int64_t width, double resolution, double x_offset,
                           double y_offset, double std_deviation, const double* instance_pose,
                           const double* rig_camera_pose, double* residual, double* jacobian) {

@@ -261,3 +261,31 @@ def test_relative_motion_known_value():
     prm = np.r_[0, 0, 0, -1, 0, 0, 1, 0, np.eye(7).ravel(), 4.0, 0.5]
     r, _ = pybundle.relative_residual("relative_motion", poses, prm)
     np.testing.assert_allclose(r, 0, atol=1e-15)
+
+
+def test_host_losses_match_the_oracle():
+    # the losses of the relative rotations and motions (host FP64) against
+    # the oracle's projection losses (Ceres' documented forms), and Tukey's
+    # closed form (the common-position loss)
+    import ctypes as C
+    from opensfm_gb300 import _lib
+    L = _lib.lib()
+    f = L.gbba_host_loss
+    f.argtypes = [C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double)]
+    f.restype = C.c_int
+
+    def host(kind, a, s):
+        rho = (C.c_double * 3)()
+        assert f(kind, a, s, rho) == 0
+        return np.array(rho[:])
+
+    for kind in range(5):
+        for a in (0.5, 1.0, 2.0):
+            for s in (0.0, 0.1, 0.9, 1.0, 3.0, 40.0):
+                np.testing.assert_allclose(host(kind, a, s), oracle.loss(kind, a, s), rtol=1e-12, atol=1e-300)
+    for a in (0.5, 1.0, 2.0):
+        for s in (0.0, 0.1, 0.9, 3.0, 40.0):
+            b = a * a
+            v = 1 - s / b
+            want = [b / 3 * (1 - v ** 3), v * v, -2 * v / b] if s <= b else [b / 3, 0.0, 0.0]
+            np.testing.assert_allclose(host(5, a, s), want, rtol=1e-12, atol=1e-300)
