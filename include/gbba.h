@@ -344,6 +344,12 @@ int gbba_has_reconstruction(const gbba_adjuster_t* h, const char* reconstruction
 int gbba_add_relative_motion(gbba_adjuster_t* h, const char* instance_i, const char* instance_j,
                              const double* motion, double robust_multiplier, int observed_scale,
                              const double* scale_matrix);
+/* SetAdjustAbsolutePositionStd (bundle_adjuster.cc:402-404, used at
+ * :772-838): with adjust != 0 a run divides the GPS priors of each scale
+ * group by a std multiplier it optimises (from 1), regularised by
+ * log(1 / sqrt(2 pi m^2)) (StdDeviationConstraint); IRLS groups GPS and
+ * STDDEV.  Batched solves reject it. */
+int gbba_set_adjust_absolute_position_std(gbba_adjuster_t* h, int adjust);
 /* The scaled residuals (before the loss) of one constraint between shots
  * and their Jacobian.  kind 0 relative rotation (params: rotation[3], then
  * the row-major scale matrix [9]), 1 common position (params: margin,
@@ -351,10 +357,12 @@ int gbba_add_relative_motion(gbba_adjuster_t* h, const char* instance_i, const c
  * std), 3 gauge scale (params: the distance; rig camera poses unused), 5
  * relative motion (params: motion[7], observed-scale flag, scale matrix
  * [49], scale_i, scale_j; rig camera poses unused; the scales' columns are
- * 24 and 25).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
+ * 24 and 25), 6 adjusted GPS prior (params: prior[3], std[3], multiplier;
+ * one instance pose; the multiplier's column is 24), 7 std-multiplier
+ * regulariser (params: multiplier; no pose; column 24).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
  * cameras) for the n = 2 (3 for linear motion) shots, [rx ry rz tx ty tz]
  * with t the position.  Writes m = 3 (6 for linear motion, 1 for the gauge
- * scale, 7 for a relative motion) residuals, J[m][36]
+ * scale and the regulariser, 7 for a relative motion) residuals, J[m][36]
  * (12 columns per shot: instance rotation, instance position, rig camera
  * rotation, rig camera position) and m to *n_residuals.  Host arithmetic
  * only. */

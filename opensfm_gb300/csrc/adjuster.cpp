@@ -2,6 +2,8 @@
 
 #include <cmath>
 #include <cstdio>
+#include <limits>
+#include <map>
 #include <sstream>
 #include <stdexcept>
 
@@ -302,7 +304,8 @@ void BundleAdjuster::Run() {
   // the solved reconstruction scales, then the rig cameras without the
   // scale blocks again
   for (const ScaleBlock& b : scale_blocks_)
-    reconstructions_.at(b.reconstruction).scales[b.instance] = problem_.rig_cameras[b.block].value[0];
+    if (b.reconstruction_scale)
+      reconstructions_.at(b.reconstruction).scales[b.instance] = problem_.rig_cameras[b.block].value[0];
   DropScaleBlocks();
   if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
   else {
@@ -489,6 +492,8 @@ void BundleAdjuster::AddRelativeMotion(const std::string& instance_i, const std:
 }
 
 void BundleAdjuster::DropScaleBlocks() {
+  for (int i : moved_priors_) problem_.instances[i].has_position_prior = true;
+  moved_priors_.clear();
   if (scale_blocks_.empty()) return;
   problem_.rig_cameras.resize(n_rig_cameras_);
   scale_blocks_.clear();
@@ -541,8 +546,9 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
-  static const char* kHostGroups[10] = {"UP", "PAN", "TILT", "ROLL", "ROT", "POS", "MOTION", "GAUGE", "HEATMAP", "REL"};
-  for (int k = 0; k < 10; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
+  static const char* kHostGroups[12] = {"UP",     "PAN",   "TILT",    "ROLL", "ROT", "POS",
+                                        "MOTION", "GAUGE", "HEATMAP", "REL",  "GPS", "STDDEV"};
+  for (int k = 0; k < 12; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);
   // constraints between shots, composed with the rig cameras that are
   // optimised or not the identity (IsRigCameraUseful), as Run passes them
   // (bundle_adjuster.cc:912-1138)
@@ -614,7 +620,7 @@ void BundleAdjuster::PrepareRun() {
       ReconstructionScales& rec = reconstructions_.at(rec_id);
       const std::string key = rec.shared ? rec.scales.begin()->first : instance;
       for (const ScaleBlock& b : scale_blocks_)
-        if (b.reconstruction == rec_id && b.instance == key) return b.block;
+        if (b.reconstruction_scale && b.reconstruction == rec_id && b.instance == key) return b.block;
       PoseBlock pb;
       pb.value[0] = rec.scales.at(key);
       pb.free_mask[0] = rec.constant ? 0 : 1;
@@ -623,7 +629,7 @@ void BundleAdjuster::PrepareRun() {
       pb.scale_block = true;
       const int block = int(problem_.rig_cameras.size());
       problem_.rig_cameras.push_back(pb);
-      scale_blocks_.push_back({rec_id, key, block});
+      scale_blocks_.push_back({rec_id, key, block, true});
       return block;
     };
     try {
@@ -649,6 +655,49 @@ void BundleAdjuster::PrepareRun() {
       throw;
     }
     any_rotation = true;  // the relative-motion loss is needed
+  }
+  if (adjust_position_std_) {
+    // one std multiplier per scale group of the GPS priors, starting at 1;
+    // the priors become host terms divided by it, and each multiplier gets
+    // StdDeviationConstraint (bundle_adjuster.cc:772-838)
+    std::map<int, int> group_block;
+    for (size_t i = 0; i < problem_.instances.size(); ++i) {
+      PoseBlock& b = problem_.instances[i];
+      if (!b.has_position_prior) continue;
+      auto g = group_block.find(b.scale_group);
+      if (g == group_block.end()) {
+        PoseBlock pb;
+        pb.value[0] = 1.0;
+        pb.free_mask[0] = 1;
+        pb.has_prior = false;
+        pb.used = true;
+        pb.scale_block = true;
+        const int block = int(problem_.rig_cameras.size());
+        problem_.rig_cameras.push_back(pb);
+        scale_blocks_.push_back({"", "", block, false});
+        g = group_block.emplace(b.scale_group, block).first;
+      }
+      RelativeTerm t;
+      t.kind = RelativeTerm::kGpsStd;
+      t.n_shots = 1;
+      t.instance[0] = int(i);
+      for (int k = 0; k < 3; ++k) {
+        t.prior[k] = b.position_prior[k];
+        t.prior_scale[k] = 1.0 / std::max(b.position_sigma[k], std::numeric_limits<double>::epsilon());
+      }
+      t.bias_camera = b.bias_camera;
+      t.scale_block[0] = g->second;
+      problem_.relative_terms.push_back(t);
+      b.has_position_prior = false;  // the diagonal GPS prior is replaced
+      moved_priors_.push_back(int(i));
+    }
+    for (const auto& gb : group_block) {
+      RelativeTerm t;
+      t.kind = RelativeTerm::kStdDeviation;
+      t.n_shots = 0;
+      t.scale_block[0] = gb.second;
+      problem_.relative_terms.push_back(t);
+    }
   }
   if (any_rotation) {
     // CreateLossFunction (bundle_adjuster.cc:485-499)

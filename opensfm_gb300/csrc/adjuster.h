@@ -66,6 +66,10 @@ class BundleAdjuster {
   // identity)
   void AddRelativeMotion(const std::string& instance_i, const std::string& instance_j, const double* motion,
                          double robust_multiplier, bool observed_scale, const double* scale_matrix);
+  // SetAdjustAbsolutePositionStd (bundle_adjuster.cc:402-404): the GPS
+  // priors of each scale group are divided by a std multiplier that the run
+  // optimises, regularised by StdDeviationConstraint (:772-838)
+  void SetAdjustAbsolutePositionStd(bool adjust) { adjust_position_std_ = adjust; }
   // AddHeatmap / AddAbsolutePositionHeatmap (bundle_adjuster.cc:331-350):
   // a cost grid (row-major, `width` columns, `resolution` metres per cell)
   // and a shot's position looked up in it, centred at (x_offset, y_offset).
@@ -193,10 +197,13 @@ class BundleAdjuster {
   std::vector<PendingMotion> motions_;
   // the scale blocks of the last run: (reconstruction, instance key, rig-camera block)
   struct ScaleBlock {
-    std::string reconstruction, instance;
+    std::string reconstruction, instance;  // empty for a GPS std multiplier
     int block;
+    bool reconstruction_scale = true;
   };
   std::vector<ScaleBlock> scale_blocks_;
+  bool adjust_position_std_ = false;
+  std::vector<int> moved_priors_;  // instances whose GPS prior a run turned into a host term
   size_t n_rig_cameras_ = 0;  // rig cameras before the scale blocks
   std::unordered_map<std::string, int> heatmap_index_;
   struct PendingHeatmap {

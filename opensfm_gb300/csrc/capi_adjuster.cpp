@@ -256,6 +256,10 @@ int gbba_get_reconstruction_scale(const gbba_adjuster_t* h, const char* reconstr
   });
 }
 
+int gbba_set_adjust_absolute_position_std(gbba_adjuster_t* h, int adjust) {
+  return guarded([&] { ba_of(h).SetAdjustAbsolutePositionStd(adjust != 0); });
+}
+
 int gbba_has_reconstruction(const gbba_adjuster_t* h, const char* reconstruction_id) {
   int has = 0;
   const int st = guarded([&] { has = ba_of(h).HasReconstruction(str(reconstruction_id)) ? 1 : 0; });
@@ -275,11 +279,16 @@ int gbba_add_relative_motion(gbba_adjuster_t* h, const char* instance_i, const c
 int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                            const double* params, double* residuals, double* jacobian, int* n_residuals) {
   return guarded([&] {
-    if (kind < 0 || kind > 5 || kind == 4 || !instance_poses || !params || !residuals || !jacobian || !n_residuals)
+    if (kind < 0 || kind > 7 || kind == 4 || !params || !residuals || !jacobian || !n_residuals ||
+        (kind != 7 && !instance_poses))
       throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_relative_residual: invalid argument");
     gbba::RelativeTerm t;
     t.kind = kind;
-    t.n_shots = kind == gbba::RelativeTerm::kLinearMotion ? 3 : 2;
+    t.n_shots = kind == gbba::RelativeTerm::kLinearMotion ? 3
+                : kind == gbba::RelativeTerm::kGpsStd          ? 1
+                : kind == gbba::RelativeTerm::kStdDeviation    ? 0
+                                                               : 2;
+    double scales[2] = {1.0, 1.0};
     if (kind == gbba::RelativeTerm::kRelativeRotation) {
       for (int k = 0; k < 3; ++k) t.rotation[k] = params[k];
       for (int k = 0; k < 9; ++k) t.scale_matrix[k] = params[3 + k];
@@ -292,6 +301,16 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
       for (int k = 0; k < 7; ++k) t.motion[k] = params[k];
       t.observed_scale = params[7] != 0.0;
       for (int k = 0; k < 49; ++k) t.motion_matrix[k] = params[8 + k];
+      scales[0] = params[57];
+      scales[1] = params[58];
+    } else if (kind == gbba::RelativeTerm::kGpsStd) {
+      for (int k = 0; k < 3; ++k) {
+        t.prior[k] = params[k];
+        t.prior_scale[k] = 1.0 / params[3 + k];
+      }
+      scales[0] = params[6];
+    } else if (kind == gbba::RelativeTerm::kStdDeviation) {
+      scales[0] = params[0];
     } else {
       t.alpha = params[0];
       t.position_scale = 1.0 / params[1];
@@ -304,8 +323,6 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
       pc[k] = rig_camera_poses ? rig_camera_poses + 6 * k : nullptr;
     }
     gbba::orient::Dual<36> r[7];
-    const double scales[2] = {kind == gbba::RelativeTerm::kRelativeMotion ? params[57] : 1.0,
-                              kind == gbba::RelativeTerm::kRelativeMotion ? params[58] : 1.0};
     const int m = gbba::orient::relative_residuals<36>(t, pi, pc, r, scales);
     for (int q = 0; q < m; ++q) {
       residuals[q] = r[q].v;

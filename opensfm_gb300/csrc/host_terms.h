@@ -28,6 +28,12 @@
 //                         reconstruction scales, under the relative-motion
 //                         loss scaled by the term's robust multiplier
 //                         (bundle_adjuster.cc:872-910).
+//   adjusted GPS          with SetAdjustAbsolutePositionStd: the position
+//                         prior divided by its scale group's std multiplier
+//                         (DataPriorError with adjust_scales, prior_error.h:
+//                         54-93), and StdDeviationConstraint
+//                         (parameters_errors.h:7-16) on each multiplier, no
+//                         loss (bundle_adjuster.cc:772-838).
 //
 // Shot rotation and position compose the rig instance with the rig camera
 // as ShotRotationFunctor / ShotPositionFunctor do (position_functors.h:
@@ -67,7 +73,9 @@ struct RelativeTerm {
     kLinearMotion = 2,
     kGaugeScale = 3,
     kHeatmap = 4,
-    kRelativeMotion = 5
+    kRelativeMotion = 5,
+    kGpsStd = 6,
+    kStdDeviation = 7
   };
   int kind = kRelativeRotation;
   int n_shots = 2;
@@ -88,6 +96,10 @@ struct RelativeTerm {
   bool observed_scale = false;
   double loss_scale = 1.0;
   int scale_block[2] = {-1, -1};
+  // adjusted GPS: the position prior (bias applied) and 1 / std per axis;
+  // the group's std multiplier is slot 24
+  double prior[3] = {0, 0, 0}, prior_scale[3] = {1, 1, 1};
+  int bias_camera = -1;
 };
 
 namespace orient {
@@ -369,6 +381,20 @@ inline int relative_residuals(const RelativeTerm& t, const double* const* pi, co
   ShotPose<N> s[3];
   for (int k = 0; k < t.n_shots; ++k) s[k] = shot_pose<N>(k, pi[k], t.kind == RelativeTerm::kRelativeMotion ? nullptr : pc[k]);
   switch (t.kind) {
+    case RelativeTerm::kGpsStd: {
+      // (t_k - prior_k) / (std_k m) on the instance position
+      const Dual<N> m = var<N>(scales[0], 24);
+      for (int k = 0; k < 3; ++k)
+        r[k] = Dual<N>(t.prior_scale[k]) * (s[0].position[k] - Dual<N>(t.prior[k])) / m;
+      return 3;
+    }
+    case RelativeTerm::kStdDeviation: {
+      // log(1 / sqrt(2 pi m^2))
+      const double m = scales[0];
+      r[0] = Dual<N>(std::log(1.0 / std::sqrt(2.0 * M_PI * m * m)));
+      r[0].d[24] = -1.0 / m;
+      return 1;
+    }
     case RelativeTerm::kRelativeMotion: {
       // rotation log(R_ij R_i^T R_j); translation t_ij - s_j R_j^T (t_i -
       // t_j); scale S_ij - s_j / s_i when observed; times the scale matrix.

@@ -123,8 +123,8 @@ struct Problem {
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
   double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
-  // UP PAN TILT ROLL ROT POS MOTION GAUGE HEATMAP REL
-  double ratio_host[10] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};
+  // UP PAN TILT ROLL ROT POS MOTION GAUGE HEATMAP REL GPS STDDEV
+  double ratio_host[12] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};
   // AddHeatmap grids (the relative terms of kind kHeatmap point into them)
   struct Heatmap {
     std::vector<double> data;

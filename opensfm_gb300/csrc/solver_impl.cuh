@@ -547,10 +547,11 @@ struct HostTermLin {
 };
 
 // IRLS groups of the host constraint terms: UP, PAN, TILT, ROLL (by
-// orientation kind), ROT, POS, MOTION, GAUGE, HEATMAP, REL (by relative kind)
-constexpr int kHostGroups = 10;
-const char* const kHostGroupNames[kHostGroups] = {"UP",     "PAN",   "TILT",    "ROLL", "ROT",
-                                                  "POS",    "MOTION", "GAUGE", "HEATMAP", "REL"};
+// orientation kind), ROT, POS, MOTION, GAUGE, HEATMAP, REL, GPS, STDDEV (by
+// relative kind)
+constexpr int kHostGroups = 12;
+const char* const kHostGroupNames[kHostGroups] = {"UP",     "PAN",    "TILT",    "ROLL", "ROT", "POS",
+                                                  "MOTION", "GAUGE", "HEATMAP", "REL",  "GPS", "STDDEV"};
 
 MixtureResult mixture_group(const std::vector<std::vector<double>>& res, std::vector<double>& weights,
                             double density_ratio) {
@@ -1508,23 +1509,35 @@ void DeviceSolver<R>::host_term(int q, const std::vector<double>& x, HostTermLin
       for (int a = 0; a < 6; ++a) L.coord[12 * k + 6 + a] = coord_of(rb + a);
     }
   }
+  // the reconstruction scales or the GPS std multiplier: value[0] of their
+  // blocks, slots 24 and 25
   double scales[2] = {1.0, 1.0};
-  if (t.kind == RelativeTerm::kRelativeMotion) {
-    // the reconstruction scales: value[0] of their blocks, slots 24 and 25
-    for (int k = 0; k < 2; ++k) {
-      const int sb = cl_.rig_base + 8 * t.scale_block[k];
-      scales[k] = x[sb];
-      L.coord[24 + k] = coord_of(sb);
-    }
+  const int n_scales = t.kind == RelativeTerm::kRelativeMotion ? 2
+                       : (t.kind == RelativeTerm::kGpsStd || t.kind == RelativeTerm::kStdDeviation) ? 1
+                                                                                                     : 0;
+  for (int k = 0; k < n_scales; ++k) {
+    const int sb = cl_.rig_base + 8 * t.scale_block[k];
+    scales[k] = x[sb];
+    L.coord[24 + k] = coord_of(sb);
   }
   orient::Dual<N> r[7];
-  L.m = orient::relative_residuals<N>(t, pi, pc, r, scales);
+  if (t.kind == RelativeTerm::kGpsStd && t.bias_camera >= 0) {
+    // the prior through the camera bias, as the diagonal GPS prior takes it
+    RelativeTerm tb = t;
+    const Bias& bs = P.biases[t.bias_camera];
+    double rp[3];
+    rotate_aa(bs.r, t.prior, rp);
+    for (int k = 0; k < 3; ++k) tb.prior[k] = bs.s * rp[k] + bs.t[k];
+    L.m = orient::relative_residuals<N>(tb, pi, pc, r, scales);
+  } else {
+    L.m = orient::relative_residuals<N>(t, pi, pc, r, scales);
+  }
   L.ns = N;
   for (int i = 0; i < L.m; ++i) L.raw[i] = r[i].v;
   // relative rotation and motion: the relative-motion loss (for a motion
   // at its threshold times the term's robust multiplier); common position
-  // Tukey(1); linear motion Cauchy(1); gauge and heatmap none
-  static const int kLoss[6] = {-1, 5, 3, 0, 0, -1};
+  // Tukey(1); linear motion Cauchy(1); gauge, heatmap and adjusted GPS none
+  static const int kLoss[8] = {-1, 5, 3, 0, 0, -1, 0, 0};
   const bool rel_loss = t.kind == RelativeTerm::kRelativeRotation || t.kind == RelativeTerm::kRelativeMotion;
   const int loss = rel_loss ? P.relative_loss : kLoss[t.kind];
   const double a = t.kind == RelativeTerm::kRelativeRotation ? P.relative_loss_threshold

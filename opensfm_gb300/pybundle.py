@@ -9,9 +9,8 @@ shot or point in ``add_point_projection_observation`` raises ``IndexError``
 
 Beyond the reference's methods it exposes bulk (numpy) adders for large
 problems, the precision / IRLS switches of the GPU solver and the iteration
-trace.  Constraint types that the GPU solver does not implement (relative
-motions, absolute up-vector / pan / tilt / roll, linear motion, heatmaps,
-common positions, reconstruction scales, gauge fixing) raise
+trace.  The two features that the GPU solver does not implement (depth
+priors on observations, optimised camera biases) raise
 ``NotImplementedError`` instead of being silently ignored.
 """
 from __future__ import annotations
@@ -68,6 +67,7 @@ def _declare(L) -> None:
         "gbba_set_scale_sharing": ([_H, S, C.c_int], C.c_int),
         "gbba_get_reconstruction_scale": ([_H, S, S, _D], C.c_int),
         "gbba_has_reconstruction": ([_H, S], C.c_int),
+        "gbba_set_adjust_absolute_position_std": ([_H, C.c_int], C.c_int),
         "gbba_add_relative_motion": ([_H, S, S, _D, C.c_double, C.c_int, _D], C.c_int),
         "gbba_add_heatmap": ([_H, S, _D, C.c_int64, C.c_int64, C.c_double], C.c_int),
         "gbba_add_absolute_position_heatmap": ([_H, S, S, C.c_double, C.c_double, C.c_double], C.c_int),
@@ -426,6 +426,9 @@ class BundleAdjuster:
                                                      _dp(motion), float(rm.robust_multiplier),
                                                      int(bool(rm.observed_scale)), _dp(sm)))
 
+    def set_adjust_absolute_position_std(self, adjust: bool) -> None:
+        self._check(self._L.gbba_set_adjust_absolute_position_std(self._h, int(bool(adjust))))
+
     def set_gauge_fix_shots(self, shot_origin: str, shot_scale: str) -> None:
         self._check(self._L.gbba_set_gauge_fix_shots(self._h, _b(shot_origin), _b(shot_scale)))
 
@@ -547,12 +550,6 @@ class BundleAdjuster:
         self._check(self._L.gbba_get_trace(self._h, n.value, _dp(out), C.byref(n)))
         return out
 
-    # -- constraint types outside the GPU solver ---------------------------
-    def _unsupported(self, *args, **kwargs):
-        raise NotImplementedError("this constraint type is not implemented by the GPU bundle adjuster")
-
-    set_adjust_absolute_position_std = _unsupported
-
 
 class BatchSummary(C.Structure):
     _fields_ = [("seconds", C.c_double), ("setup_seconds", C.c_double), ("solve_seconds", C.c_double),
@@ -640,23 +637,27 @@ def orientation_residual(kind: str, target, std_deviation: float, instance_rotat
 
 
 RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3,
-                  "relative_motion": 5}
+                  "relative_motion": 5, "gps_std": 6, "std_deviation": 7}
 
 
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
-    """Scaled residuals (before the loss) and Jacobian [m][36] of one
-    constraint between shots -- RelativeRotationError, CommonPositionError
-    (relative_motion_errors.h:66-126) or LinearMotionError
-    (motion_prior_errors.h:12-74).  Poses [n][6] as [rx ry rz tx ty tz] with
-    t the position; params as gbba_relative_residual takes them."""
+    """Scaled residuals (before the loss) and Jacobian [m][36] of one host
+    constraint -- RelativeRotationError, CommonPositionError
+    (relative_motion_errors.h:66-126), LinearMotionError
+    (motion_prior_errors.h:12-74), the gauge scale, RelativeMotionError, the
+    std-adjusted GPS prior (prior_error.h:54-93) or StdDeviationConstraint
+    (parameters_errors.h:7-16).  Poses [n][6] as [rx ry rz tx ty tz] with t
+    the position (None for the std regulariser); params as
+    gbba_relative_residual takes them."""
     L = _lib.lib()
     _declare(L)
-    pi = np.ascontiguousarray(instance_poses, dtype=np.float64)
+    pi = None if instance_poses is None else np.ascontiguousarray(instance_poses, dtype=np.float64)
     pc = None if rig_camera_poses is None else np.ascontiguousarray(rig_camera_poses, dtype=np.float64)
     prm = np.ascontiguousarray(params, dtype=np.float64).reshape(-1)
     r, J = np.zeros(7), np.zeros(7 * 36)
     m = C.c_int(0)
-    _lib.check(L.gbba_relative_residual(RELATIVE_KINDS[kind], _dp(pi), _dp(pc) if pc is not None else None,
+    _lib.check(L.gbba_relative_residual(RELATIVE_KINDS[kind], _dp(pi) if pi is not None else None,
+                                        _dp(pc) if pc is not None else None,
                                         _dp(prm), _dp(r), _dp(J), C.byref(m)))
     return r[: m.value].copy(), J[: 36 * m.value].reshape(m.value, 36)
 

@@ -200,7 +200,7 @@ def orientation_residual(kind: str, target, std: float, instance_rotation, camer
 
 
 RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3, "heatmap": 4,
-                  "relative_motion": 5}
+                  "relative_motion": 5, "gps_std": 6, "std_deviation": 7}
 REL_PARAMS = 64
 
 

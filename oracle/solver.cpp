@@ -358,6 +358,19 @@ double heat_value(const HeatGrid& g, double r, double c, double* fr, double* fc)
 
 int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r,
                       const HeatGrid* grid = nullptr, const double* scales = nullptr) {
+  if (kind == 6) {
+    // DataPriorError with adjust_scales (prior_error.h:54-93): (t - prior) /
+    // (std m) on the instance position, m in slot 24
+    const D36 m = D36::var(scales[0], 24);
+    for (int k = 0; k < 3; ++k) r[k] = (D36::var(pi[0][3 + k], 3 + k) - prm[k]) / (m * prm[3 + k]);
+    return 3;
+  }
+  if (kind == 7) {
+    // StdDeviationConstraint (parameters_errors.h:7-16)
+    const D36 m = D36::var(scales[0], 24);
+    r[0] = log(1.0 / sqrt(m * m * (2.0 * M_PI)));
+    return 1;
+  }
   if (kind == 5) {
     // RelativeMotionError (relative_motion_errors.h:13-64) on the instance
     // poses alone: rotation log(R_ij R_i^T R_j), translation t_ij - s_j
@@ -515,7 +528,7 @@ struct Solver {
   // weight, the compact columns of the 36 slots, w rho through *rho and the
   // raw residuals through raw.
   int relative_term(const State& s, int q, D36* r, int* col, double* rho, double* raw = nullptr) const {
-    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : (kind == 4 ? 1 : 2);
+    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : (kind == 4 || kind == 6) ? 1 : kind == 7 ? 0 : 2;
     const double* prm = P.rel_params + kRelParams * q;
     const double* pi[3] = {nullptr, nullptr, nullptr};
     const double* pc[3] = {nullptr, nullptr, nullptr};
@@ -526,8 +539,8 @@ struct Solver {
       pi[k] = &s.inst[6 * inst];
       for (int a = 0; a < 6; ++a) col[12 * k + a] = idx.inst[6 * inst + a];
       // the heatmap functor always composes the rig camera; the relative
-      // motion none
-      if (rc >= 0 && (P.rig_used[rc] || kind == 4) && kind != 5) {
+      // motion and the GPS prior none
+      if (rc >= 0 && (P.rig_used[rc] || kind == 4) && kind != 5 && kind != 6) {
         pc[k] = &s.rig[6 * rc];
         for (int a = 0; a < 6; ++a) col[12 * k + 6 + a] = idx.rig[6 * rc + a];
       }
@@ -540,6 +553,12 @@ struct Solver {
         scales[k] = s.scl[si];
         col[24 + k] = idx.scl[si];
       }
+    if (kind == 6 || kind == 7) {
+      // the std multiplier: params[6] (GPS prior) or params[0] (regulariser)
+      const int si = int(prm[kind == 6 ? 6 : 0]);
+      scales[0] = s.scl[si];
+      col[24] = idx.scl[si];
+    }
     const int m = relative_residual(kind, pi, pc, prm, r, &grid, scales);
     double sq = 0.0;
     for (int a = 0; a < m; ++a) {
@@ -548,7 +567,7 @@ struct Solver {
     }
     // relative rotation and motion: the relative-motion loss (a motion's at
     // threshold x robust multiplier); Tukey(1); Cauchy(1); none; none
-    static const int kLoss[6] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL, -1};
+    static const int kLoss[8] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL, -1, LOSS_TRIVIAL, LOSS_TRIVIAL};
     const int loss = (kind == 0 || kind == 5) ? P.rel_loss : kLoss[kind];
     const double la = kind == 0 ? P.rel_loss_threshold : kind == 5 ? P.rel_loss_threshold * prm[57] : 1.0;
     double rh[3];
@@ -1268,7 +1287,7 @@ struct Solver {
       }
       total += mixture(res, w, O.density_ratio);
     }
-    for (int kind = 0; kind < 6; ++kind) {  // groups ROT, POS, MOTION, GAUGE, HEATMAP, REL
+    for (int kind = 0; kind < 8; ++kind) {  // groups ROT, POS, MOTION, GAUGE, HEATMAP, REL, GPS, STDDEV
       std::vector<std::vector<double>> res;
       std::vector<double*> w;
       for (int q = 0; q < P.n_rel; ++q) {
@@ -1321,7 +1340,7 @@ extern "C" int oracle_orientation_residual(int kind, const double* target, doubl
 // null); returns m.
 extern "C" int oracle_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                                         const double* params, const double* scales, double* r, double* J) {
-  const int n = kind == 2 ? 3 : 2;
+  const int n = kind == 2 ? 3 : kind == 6 ? 1 : kind == 7 ? 0 : 2;
   const double* pi[3] = {nullptr, nullptr, nullptr};
   const double* pc[3] = {nullptr, nullptr, nullptr};
   for (int k = 0; k < n; ++k) {
