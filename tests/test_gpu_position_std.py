@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle
-from opensfm_gb300 import pygeometry
+from opensfm_gb300 import pybundle, pygeometry
 from opensfm_gb300 import synthetic as syn
 from opensfm_gb300.pybundle import adjuster_from_scene
 
@@ -63,3 +63,22 @@ def test_adjusting_lowers_the_cost_of_noisy_gps(precision):
     adj.run()
     rel = abs(adj.summary()["final_cost"] - plain.summary()["final_cost"]) / plain.summary()["final_cost"]
     assert rel < 1e-3
+
+
+def test_batch_rejects_adjusted_gps_and_restores_the_priors():
+    # the batch set-up fails on the multiplier (a free camera-side block)
+    # and leaves the adjuster as it was: a plain run afterwards still sees
+    # its GPS priors
+    scene = _scene(0.3)
+    ba = adjuster_from_scene(scene, precision="mixed", irls="none", constant_cameras=True)
+    ba.set_adjust_absolute_position_std(True)
+    batch = pybundle.BundleBatch()
+    batch.add(ba)
+    with pytest.raises(Exception, match="batched solves"):
+        batch.run()
+    ba.set_adjust_absolute_position_std(False)
+    ba.run()
+    ref = adjuster_from_scene(scene, precision="mixed", irls="none", constant_cameras=True)
+    ref.run()
+    rel = abs(ba.summary()["final_cost"] - ref.summary()["final_cost"]) / ref.summary()["final_cost"]
+    assert rel < 1e-5

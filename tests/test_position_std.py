@@ -78,3 +78,24 @@ def test_oracle_multiplier_is_optimal():
 
     assert 0 <= f(m) - f(m_star) < 1e-6 * ref["final_cost"]
     np.testing.assert_allclose(m, m_star, rtol=1e-2)
+
+
+def test_batch_set_up_drops_the_multiplier_and_restores_the_priors():
+    # a batch rejects the multiplier (a free camera-side block) on the host,
+    # before any device work; the failed set-up leaves the adjuster as it
+    # was, so the next set-up without adjusting meets the GPS priors again
+    scene = syn.ring_scene(n_points=100, seed=5)
+    n = len(scene.shot_camera)
+    scene.extras["gps"] = np.ascontiguousarray(scene.extras["true_poses"][:, 3:])
+    scene.extras["gps_std"] = np.full((n, 3), 0.1)
+    ba = pybundle.adjuster_from_scene(scene, precision="mixed", irls="none", constant_cameras=True)
+    ba.set_adjust_absolute_position_std(True)
+    batch = pybundle.BundleBatch()
+    batch.add(ba)
+    with pytest.raises(Exception, match="fixed rig cameras"):
+        batch.run()
+    with pytest.raises(Exception, match="fixed rig cameras"):
+        batch.run()
+    ba.set_adjust_absolute_position_std(False)
+    with pytest.raises(Exception, match="no position priors"):
+        batch.run()
