@@ -35,7 +35,24 @@ def _has_gpu() -> bool:
         return False
 
 
+# Dependency order of the GPU files: the solver and its kernels first, then
+# the constraint terms built on the solver, then the callers built on both
+# (local bundles).  Under -x a failure in a caller then cannot hide the
+# result of the layer it stands on.  Files not listed keep their place
+# after these.
+_GPU_ORDER = ("test_gpu_evaluate.py", "test_gpu_solver.py", "test_gpu_dense.py", "test_gpu_matrix_free.py",
+              "test_gpu_batch.py", "test_gpu_autograd.py", "test_gpu_outliers.py", "test_gpu_covariance.py",
+              "test_gpu_orientation.py", "test_gpu_relative.py", "test_gpu_relative_motion.py",
+              "test_gpu_position_std.py", "test_gpu_ba_helpers.py")
+
+
+def _file_rank(item) -> int:
+    name = Path(str(item.fspath)).name
+    return _GPU_ORDER.index(name) if name in _GPU_ORDER else len(_GPU_ORDER)
+
+
 def pytest_collection_modifyitems(config, items):
+    items.sort(key=_file_rank)  # stable: the order within a file stays
     if _has_gpu():
         return
     skip = pytest.mark.skip(reason="no CUDA device")
