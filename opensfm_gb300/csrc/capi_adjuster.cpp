@@ -1,6 +1,8 @@
 // extern "C" entry points of the bundle adjuster (include/gbba.h).
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <string>
 #include <vector>
@@ -306,7 +308,8 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
     } else if (kind == gbba::RelativeTerm::kGpsStd) {
       for (int k = 0; k < 3; ++k) {
         t.prior[k] = params[k];
-        t.prior_scale[k] = 1.0 / params[3 + k];
+        // DataPriorError's 1 / max(sigma, epsilon) (prior_error.h:27-36)
+        t.prior_scale[k] = 1.0 / std::max(params[3 + k], std::numeric_limits<double>::epsilon());
       }
       scales[0] = params[6];
     } else if (kind == gbba::RelativeTerm::kStdDeviation) {
