@@ -334,7 +334,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     else:
         h_grid, h_width, h_res = np.zeros(1), 1, 1.0
     keep.append(h_grid)
-    ns = len(scales)
+    n_scl = len(scales)
     s_val = np.array([float(v) for v, _ in scales] or [1.0], np.float64)
     s_free = np.array([1 if f else 0 for _, f in scales] or [0], np.uint8)
     keep += [s_val, s_free]
@@ -349,7 +349,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
                  scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
                  _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std),
                  nr, i32(r_kind), i32(r_shots), _p(r_params), LOSSES[relative_loss[0]], float(relative_loss[1]),
-                 _p(h_grid), h_grid.size, h_width, h_res, ns, _p(s_val), u8(s_free))
+                 _p(h_grid), h_grid.size, h_width, h_res, n_scl, _p(s_val), u8(s_free))
     loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
     O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
                  int(skip_initial_reweighting), threads or os.cpu_count() or 1)
@@ -363,9 +363,10 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     out_scl = s_val.copy()
     R = _Result(_p(out_cam), _p(out_inst), _p(out_rig), _p(out_pts), _p(out_scl), _p(out_w), _p(out_err), _p(trace),
                 len(trace), 0, 0.0, 0.0, 0, 0, 0)
-    L.oracle_solve(C.byref(P), C.byref(O), C.byref(R))
+    if L.oracle_solve(C.byref(P), C.byref(O), C.byref(R)) != 0:
+        raise ValueError("oracle_solve: an index array disagrees with the problem's counts")
     del keep
-    return dict(cameras=out_cam, instances=out_inst, points=out_pts, scales=out_scl[:ns].copy(), weights=out_w,
+    return dict(cameras=out_cam, instances=out_inst, points=out_pts, scales=out_scl[:n_scl].copy(), weights=out_w,
                 errors=out_err,
                 trace=trace[: R.trace_n].copy(), initial_cost=R.initial_cost, final_cost=R.final_cost,
                 iterations=R.iterations, successful=R.successful, termination=R.termination)

@@ -1373,6 +1373,15 @@ extern "C" double oracle_heatmap_residual(const double* grid, int64_t n, int wid
 extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, OracleResult* out) {
   const OracleProblem& P = *Pp;
   const OracleOptions& O = *Op;
+  // Index checks: a problem whose counts disagree with its index arrays is
+  // refused (-1) before anything is read out of range.
+  for (int s = 0; s < P.n_shots; ++s)
+    if (P.shot_instance[s] < 0 || P.shot_instance[s] >= P.n_instances || P.shot_camera[s] < 0 ||
+        P.shot_camera[s] >= P.n_cameras || P.shot_rig[s] < -1 || P.shot_rig[s] >= std::max(1, P.n_rig_cameras))
+      return -1;
+  for (int64_t i = 0; i < P.n_obs; ++i)
+    if (P.obs_shot[i] < 0 || P.obs_shot[i] >= P.n_shots || P.obs_point[i] < 0 || P.obs_point[i] >= P.n_points)
+      return -1;
   Solver S(P, O);
   State x;
   x.cam.assign(P.camera_values, P.camera_values + 16 * P.n_cameras);
