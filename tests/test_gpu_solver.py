@@ -148,6 +148,14 @@ def test_solution_written_back_and_reports():
     assert "Final cost" in ba.full_report()
     tr = ba.trace()
     assert tr.shape[1] == 8 and tr[0, 0] == 0
-    assert np.all(np.diff(tr[tr[:, 3] > 0, 1]) <= 1e-9 * tr[0, 1]) or True
+    # Ceres' non-monotonic steps may accept a cost above the previous one, so
+    # the trace is checked against the acceptance rule instead: an accepted
+    # step passed the gain-ratio test, a rejected one left the cost as it was,
+    # and the run ends below where it started.
+    succ = tr[1:, 3] > 0
+    assert succ.any()
+    assert np.all(tr[1:, 6][succ] > 1e-3)
+    assert np.all(tr[1:, 1][~succ] == tr[:-1, 1][~succ])
+    assert tr[-1, 1] < tr[0, 1]
     p = ba.get_point("0")
     assert p.p.shape == (3,)
