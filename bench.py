@@ -173,6 +173,150 @@ def cpu_baseline(scene, target_s: float = 10.0) -> dict:
                       f"{threads} threads, {dt:.1f} s"}
 
 
+def fp64_eval_rate(scene, steps: int, warmup: int, stream) -> dict:
+    """Device residual+Jacobian throughput with FP64 records (FP64
+    arithmetic throughout), timed like the mixed passes: CUDA events on the
+    launching stream around `steps` passes after `warmup` untimed ones."""
+    import torch
+    from opensfm_gb300 import _lib
+    from opensfm_gb300.scene import Evaluator
+    ev = Evaluator(scene, _lib.PRECISION_FP64)
+    sh = stream.cuda_stream
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            ev.run(sh)
+        torch.cuda.synchronize()
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(steps):
+            ev.run(sh)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    dt = t0.elapsed_time(t1) / 1e3
+    ev.close()
+    return {"value": scene.n_observations * steps / dt / 1e6, "unit": UNIT, "ms_per_step": dt / steps * 1e3,
+            "dtype": "f64", "record_bytes_per_obs": None}
+
+
+def headline(result: dict) -> dict:
+    """Compact summary of both halves of the metric, printed as the last key
+    of the line (so that a reader of the line's tail sees it): device and
+    end-to-end evaluation rates, and the time-to-converge comparisons."""
+    def r3(x):
+        return None if x is None else float(f"{x:.4g}")
+    h = {"eval_mixed_mobs": r3(result["value"]), "eval_fp64_mobs": r3(result["value_fp64"]["value"]),
+         "e2e_mobs": r3(result["e2e"]["value"]), "roofline_frac": r3(result["roofline"]["frac"]),
+         "cpu_port_mobs": r3(result.get("cpu_baseline", {}).get("value"))}
+    c = result.get("converge")
+    if c:
+        h["c3_converge"] = {
+            "mixed_s": r3(c["mixed"]["time_to_target_s"]), "fp64_s": r3(c["fp64"]["time_to_target_s"]),
+            "speedup": r3(c["speedup_mixed_vs_fp64"]),
+            "iters_mixed_fp64": [c["mixed"]["iterations_to_target"], c["fp64"]["iterations_to_target"]],
+            "final_rel_mixed_vs_fp64": r3(c["mixed_final_rel_to_fp64"]),
+            "point_rms_mm": r3(1e3 * c["mixed_vs_fp64_solution"]["point_rms_m"]),
+            "centre_rms_mm": r3(1e3 * c["mixed_vs_fp64_solution"]["centre_rms_m"]),
+            "rotation_rms_urad": r3(1e6 * c["mixed_vs_fp64_solution"]["rotation_rms_rad"])}
+    st = result.get("street")
+    if st:
+        h["c2_street"] = {"mixed_s": r3(st["mixed_s"]), "fp64_s": r3(st["fp64_s"]),
+                          "speedup": r3(st["speedup_mixed_vs_fp64"]),
+                          "iters_mixed_fp64": [st["mixed"]["iterations"], st["fp64"]["iterations"]],
+                          "final_rel_mixed_vs_fp64": r3(st["final_rel_mixed_vs_fp64"]),
+                          "inlier_rms_px_fp64": r3(st["fp64"]["inlier_rms_px"])}
+        if "oracle_rel" in st:
+            h["c2_street"]["oracle_rel_fp64_mixed"] = [r3(st["oracle_rel"]["fp64"]), r3(st["oracle_rel"]["mixed"])]
+    b = result.get("batched_local_ba")
+    if b:
+        h["c4_batch"] = {"batch_s": r3(b.get("batch_s")), "one_at_a_time_s": r3(b.get("one_at_a_time_s")),
+                         "speedup": r3(b.get("speedup"))}
+    d = result.get("dense_rcs")
+    if d and d.get("spd"):
+        big = d["spd"][-1]
+        h["dense_factor"] = {"n": big["n"], "ms": r3(big["factor_ms"]), "tflops": r3(big["factor_tflops"])}
+    return h
+
+
+def street_benchmark(n_shots: int = 500, n_points: int = 200_000, seed: int = 7, max_iterations: int = 200,
+                     outlier_ratio: float = 0.02, oracle: bool = True, oracle_shots: int = 50,
+                     oracle_points: int = 20_000, oracle_iterations: int = 60) -> dict:
+    """The medium terrestrial workload as specified: 500 Brown cameras
+    sharing 4 camera models along a random-walk street, 200k points, ~1.4M
+    observations, 2% outliers uniform over the image, soft-L1 loss (1 px).
+    FP64 and mixed GPU solves with the linear solver the reference picks for
+    this size (SPARSE_SCHUR above 200 shots, ba_helpers.cc:42-49), and the
+    time each takes to reach the FP64 final cost x (1 + 1e-6).
+
+    Error against the FP64 CPU oracle: the oracle's LM (an unblocked
+    single-threaded Cholesky of the reduced system) needs minutes for the
+    full problem, so it solves a bounded street problem of the same kind
+    (oracle_shots shots, oracle_points points, the same outlier ratio and
+    loss), which the GPU solves in both precisions too; their final costs
+    and RMS reprojection errors are compared with the oracle's."""
+    from opensfm_gb300 import synthetic as syn
+    from opensfm_gb300.pybundle import adjuster_from_scene
+    loss = ("SoftLOneLoss", 1.0)
+    kw = dict(loss=loss, irls="none", gps=False, linear_solver="SPARSE_SCHUR")
+
+    def rms_px(e, inliers):
+        # RMS reprojection error of the inliers (the 2% outliers, uniform over
+        # the image, would dominate an RMS over every observation)
+        e = e[inliers]
+        return float(np.sqrt(np.mean(np.sum(e[:, :2] ** 2, axis=1))) * 1000.0)
+
+    def solve_both(scene, iterations):
+        runs = {}
+        for precision in ("fp64", "mixed"):
+            ba = adjuster_from_scene(scene, precision=precision, max_iterations=iterations, **kw)
+            ba.run()
+            errs, _, _ = ba.projection_results()
+            runs[precision] = (ba.summary(), ba.trace(), errs)
+            del ba
+        return runs
+
+    scene = syn.street_scene(n_shots=n_shots, n_points=n_points, seed=seed, outlier_ratio=outlier_ratio)
+    out = {"n_shots": n_shots, "n_points": int(len(scene.points)), "n_observations": int(scene.n_observations),
+           "outlier_ratio": outlier_ratio, "loss": list(loss), "linear_solver": "SPARSE_SCHUR",
+           "max_iterations": max_iterations}
+    inl = ~scene.extras["outliers"]
+    runs = solve_both(scene, max_iterations)
+    c64 = runs["fp64"][0]["final_cost"]
+    target = c64 * (1.0 + 1e-6)
+    for precision, (s, tr, errs) in runs.items():
+        hit = np.nonzero(tr[:, 1] <= target)[0]
+        out[precision] = {"time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None,
+                          "iterations": s["iterations"], "converged": s["iterations"] < max_iterations,
+                          "final_cost": s["final_cost"], "solve_s": s["seconds"],
+                          "unsuccessful_steps": int(s["unsuccessful_steps"]),
+                          "dense_failures": int(s["linear_solver_failures"]), "inlier_rms_px": rms_px(errs, inl)}
+    out["target_cost"] = target
+    out["mixed_s"], out["fp64_s"] = out["mixed"]["time_to_target_s"], out["fp64"]["time_to_target_s"]
+    out["speedup_mixed_vs_fp64"] = (out["fp64_s"] / out["mixed_s"]) if (out["mixed_s"] and out["fp64_s"]) else None
+    out["final_rel_mixed_vs_fp64"] = abs(runs["mixed"][0]["final_cost"] - c64) / c64
+    out["rms_px_mixed_vs_fp64"] = abs(out["mixed"]["inlier_rms_px"] - out["fp64"]["inlier_rms_px"])
+    if oracle:
+        from oracle import oracle as orc
+        small = syn.street_scene(n_shots=oracle_shots, n_points=oracle_points, seed=seed + 1,
+                                 outlier_ratio=outlier_ratio)
+        sinl = ~small.extras["outliers"]
+        t0 = time.perf_counter()
+        ref = orc.solve(small, loss=loss, irls="none", max_iterations=oracle_iterations, gps=False)
+        cpu_s = time.perf_counter() - t0
+        sruns = solve_both(small, oracle_iterations)
+        out["oracle_check"] = {
+            "n_shots": oracle_shots, "n_observations": int(small.n_observations),
+            "iterations": oracle_iterations, "oracle_final_cost": ref["final_cost"],
+            "oracle_iterations": ref["iterations"], "oracle_seconds": cpu_s,
+            "oracle_inlier_rms_px": rms_px(ref["errors"], sinl),
+            **{f"{p}_rel_cost": abs(sruns[p][0]["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+               for p in ("fp64", "mixed")},
+            **{f"{p}_inlier_rms_px_diff": abs(rms_px(sruns[p][2], sinl) - rms_px(ref["errors"], sinl))
+               for p in ("fp64", "mixed")}}
+        out["oracle_rel"] = {p: out["oracle_check"][f"{p}_rel_cost"] for p in ("fp64", "mixed")}
+    return out
+
+
 def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_tolerance: float = 1e-3) -> dict:
     """Time to converge: FP64 and mixed-precision GPU solves of the same
     scene with a fixed objective (robust loss, IRLS off).  The FP64 solve's
@@ -606,6 +750,11 @@ def run_ours(args) -> None:
         elapsed = float(t.item())
     rec_ms = float(np.mean([ev_mid[k].elapsed_time(ev_end[k]) for k in range(args.steps)]))
     value = n_obs * args.steps * world / elapsed / 1e6
+    # the same passes with FP64 records: the device rate at the arithmetic
+    # width of the CPU reference arm
+    ev.close()
+    value_fp64 = fp64_eval_rate(scene, args.steps, args.warmup, stream)
+    ev = Evaluator(scene, _lib.PRECISION_MIXED)
 
     # e2e: the one-shot host-buffer call
     nr, cmax = scene.layout()
@@ -658,6 +807,7 @@ def run_ours(args) -> None:
             "clocks": dict(clocks.summary(), window=f"timed region plus an untimed continuation of the same "
                                                     f"kernel loop, {CLOCK_WINDOW_S:.1f} s in all"),
             "gpu_launches": args.steps * ev.launches_per_run,
+            "value_fp64": value_fp64,
         }
         if not args.no_cpu_baseline:
             result["cpu_baseline"] = cpu_baseline(scene)
@@ -682,6 +832,11 @@ def run_ours(args) -> None:
         if not args.no_covariance:
             ev.close()
             result["covariances"] = covariance_benchmark(street_shots=args.covariance_shots)
+        if not args.no_street:
+            ev.close()
+            result["street"] = street_benchmark(n_shots=args.street_shots, n_points=args.street_points,
+                                                oracle=not args.no_street_oracle)
+        result["headline"] = headline(result)
         print(json.dumps(result), flush=True)
     ev.close()
     if dist:
@@ -708,6 +863,10 @@ def main() -> None:
     ap.add_argument("--no-outliers", action="store_true")
     ap.add_argument("--outlier-observations", type=int, default=0, help="0: the workload's observation count")
     ap.add_argument("--no-covariance", action="store_true")
+    ap.add_argument("--no-street", action="store_true", help="skip the street (500 Brown cameras) solves")
+    ap.add_argument("--no-street-oracle", action="store_true", help="skip the street solve of the FP64 CPU oracle")
+    ap.add_argument("--street-shots", type=int, default=500)
+    ap.add_argument("--street-points", type=int, default=200_000)
     ap.add_argument("--covariance-shots", type=int, default=500)
     ap.add_argument("--dense-sizes", type=int, nargs="*", default=[1024, 2048, 4096])
     ap.add_argument("--dense-street-shots", type=int, default=500, help="0: skip the street solves")

@@ -432,6 +432,38 @@ int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance);
  * path always stores them. */
 int gbba_set_matrix_free(gbba_adjuster_t* h, int mode);
 
+/* ---- Point-partitioned (sharded) solve over several GPUs
+ *
+ * No counterpart in the reference, which scales out by rounds of local
+ * bundles (sfm::BAHelpers::BundleStochastic, ba_helpers.cc:1231-1370).
+ * One adjuster per rank (one process or thread per GPU), each given the
+ * whole problem.  A rank solves with the points gbba_get_shard_points
+ * assigns it and all of their observations; cameras, rig cameras and rig
+ * instances are held by every rank.  The ranks exchange, through the
+ * caller's all-reduce: the camera-side gradient and column norms of each
+ * linearization, the Schur right-hand side and preconditioner blocks of
+ * each step, the Schur product of each PCG iteration (one camera-sized
+ * vector), rank 0's PCG scalars and camera step, and the scalar sums (cost,
+ * model decrease, step norm, IRLS group statistics).  The steps come from
+ * PCG (the dense path and the covariances are single-rank).  After gbba_run
+ * every rank holds the same camera side and the solved values of its own
+ * points; another rank's points keep their values from before the run, and
+ * their reprojection errors and weights read back as NaN.
+ *
+ * allreduce(ctx, data, count, op) reduces `count` doubles in host memory in
+ * place over the ranks (op GBBA_REDUCE_SUM or GBBA_REDUCE_MAX) and returns
+ * 0, or nonzero on failure (gbba_run then fails with GBBA_ERR_RUNTIME).
+ * Every rank makes the same sequence of calls.  world_size 1 (the default)
+ * is the ordinary single-GPU solve. */
+#define GBBA_REDUCE_SUM 0
+#define GBBA_REDUCE_MAX 1
+typedef int (*gbba_allreduce_fn)(void* ctx, double* data, int64_t count, int op);
+int gbba_set_shard(gbba_adjuster_t* h, int rank, int world_size, gbba_allreduce_fn allreduce, void* ctx);
+/* Points [*first, *last) (insertion order) that `rank` solves with under
+ * the adjuster's world size: contiguous ranges with nearly equal numbers of
+ * observations. */
+int gbba_get_shard_points(const gbba_adjuster_t* h, int rank, int64_t* first, int64_t* last);
+
 /* BundleAdjuster::Run (bundle_adjuster.cc:670-1203). */
 int gbba_run(gbba_adjuster_t* h);
 

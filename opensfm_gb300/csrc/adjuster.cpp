@@ -1,11 +1,13 @@
 #include "adjuster.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <limits>
 #include <map>
 #include <sstream>
 #include <stdexcept>
+#include <tuple>
 
 #include "camera_models.cuh"
 #include "solver.h"
@@ -290,16 +292,89 @@ double BundleAdjuster::GetGroupDensityRatio(const std::string& g) const {
   return it == group_ratio_.end() ? opts_.default_density_ratio : it->second;
 }
 
+void BundleAdjuster::SetShard(int rank, int world, int (*allreduce)(void*, double*, int64_t, int), void* ctx) {
+  if (world < 1 || rank < 0 || rank >= world)
+    throw std::invalid_argument("shard: rank must be in [0, world_size) and world_size >= 1");
+  if (world > 1 && !allreduce) throw std::invalid_argument("shard: a world_size above 1 needs an all-reduce");
+  opts_.shard.rank = rank;
+  opts_.shard.world = world;
+  opts_.shard.allreduce = world > 1 ? allreduce : nullptr;
+  opts_.shard.ctx = world > 1 ? ctx : nullptr;
+}
+
+std::pair<int64_t, int64_t> BundleAdjuster::ShardRange(int rank) const {
+  const int64_t np = int64_t(problem_.points.size());
+  const int world = std::max(1, opts_.shard.world);
+  if (world == 1) return {0, np};
+  if (rank < 0 || rank >= world) throw std::invalid_argument("shard: rank out of range");
+  // rank r starts at the first point before which at least r/world of the
+  // observations lie
+  std::vector<int64_t> cum(size_t(np) + 1, 0);
+  for (const Observation& o : problem_.observations) ++cum[size_t(o.point) + 1];
+  for (int64_t p = 0; p < np; ++p) cum[size_t(p) + 1] += cum[size_t(p)];
+  const int64_t total = cum[size_t(np)];
+  auto start = [&](int r) -> int64_t {
+    if (r <= 0) return 0;
+    if (r >= world) return np;
+    const int64_t want = (total * r + world - 1) / world;  // ceil(total r / world)
+    return int64_t(std::lower_bound(cum.begin(), cum.end(), want) - cum.begin());
+  };
+  const int64_t a = std::min(start(rank), np), b = std::min(std::max(start(rank + 1), a), np);
+  return {a, b};
+}
+
 void BundleAdjuster::Run() {
   PrepareRun();
   opts_.compute_covariances = compute_covariances_;
+  const bool shard = opts_.shard.active();
+  // Sharded: the problem without points and observations, then this
+  // rank's points and the observations of them (point indices relative to
+  // the range's first point).
+  Problem sub;
+  std::vector<int64_t> sub_obs;  // index in problem_.observations of each of sub's observations
+  int64_t p0 = 0, p1 = 0;
+  if (shard) {
+    std::tie(p0, p1) = ShardRange(opts_.shard.rank);
+    std::vector<PointBlock> pts;
+    std::vector<Observation> obs;
+    pts.swap(problem_.points);
+    obs.swap(problem_.observations);
+    sub = problem_;
+    pts.swap(problem_.points);
+    obs.swap(problem_.observations);
+    sub.points.assign(problem_.points.begin() + p0, problem_.points.begin() + p1);
+    for (size_t i = 0; i < problem_.observations.size(); ++i) {
+      const Observation& o = problem_.observations[i];
+      if (o.point < p0 || o.point >= p1) continue;
+      Observation q = o;
+      q.point = int(o.point - p0);
+      sub.observations.push_back(q);
+      sub_obs.push_back(int64_t(i));
+    }
+    opts_.compute_covariances = false;
+  }
+  // Mixed precision is for the iterative path.  Exact dense steps solve the
+  // explicit reduced camera system, whose assembly is FP64 in both
+  // precisions; FP32 Jacobians there only perturb the gauge directions of
+  // S (nearly singular without a gauge prior), which the exact solve then
+  // amplifies into rejected steps.  Such runs take FP64 records.
+  const bool exact = exact_dense_steps(shard ? sub : problem_, opts_);
+  const int precision = exact ? 0 : opts_.precision;
   std::unique_ptr<SolverBase> solver;
   try {
-    solver = make_solver(opts_.precision);
-    summary_ = solver->solve(problem_, opts_);
+    solver = make_solver(precision);
+    summary_ = solver->solve(shard ? sub : problem_, opts_);
+    if (exact && opts_.precision != 0) summary_.linear_solver += "; FP64 records (exact steps)";
   } catch (...) {
     DropScaleBlocks();
     throw;
+  }
+  if (shard) {
+    // the camera side (identical on every rank) and this rank's points
+    for (size_t c = 0; c < sub.cameras.size(); ++c) problem_.cameras[c] = sub.cameras[c];
+    for (size_t r = 0; r < sub.rig_cameras.size(); ++r) problem_.rig_cameras[r] = sub.rig_cameras[r];
+    for (size_t i = 0; i < sub.instances.size(); ++i) problem_.instances[i] = sub.instances[i];
+    for (int64_t p = p0; p < p1; ++p) problem_.points[size_t(p)] = sub.points[size_t(p - p0)];
   }
   // the solved reconstruction scales, then the rig cameras without the
   // scale blocks again
@@ -307,8 +382,20 @@ void BundleAdjuster::Run() {
     if (b.reconstruction_scale)
       reconstructions_.at(b.reconstruction).scales[b.instance] = problem_.rig_cameras[b.block].value[0];
   DropScaleBlocks();
-  if (opts_.compute_reprojection_errors) solver->reprojection(errors_, weights_);
-  else {
+  if (opts_.compute_reprojection_errors && shard) {
+    // this rank's observations; the others' are NaN here
+    std::vector<double> e, w;
+    solver->reprojection(e, w);
+    errors_.assign(3 * problem_.observations.size(), std::numeric_limits<double>::quiet_NaN());
+    weights_.assign(problem_.observations.size(), std::numeric_limits<double>::quiet_NaN());
+    for (size_t k = 0; k < sub_obs.size(); ++k) {
+      const size_t i = size_t(sub_obs[k]);
+      for (int a = 0; a < 3; ++a) errors_[3 * i + a] = e[3 * k + a];
+      weights_[i] = w[k];
+    }
+  } else if (opts_.compute_reprojection_errors) {
+    solver->reprojection(errors_, weights_);
+  } else {
     errors_.clear();
     weights_.clear();
   }

@@ -106,6 +106,19 @@ class BundleAdjuster {
   double GetGroupDensityRatio(const std::string& g) const;
   void SetPcgTolerance(double t) { opts_.pcg_tolerance = t; }
   void SetMatrixFree(int mode) { opts_.matrix_free = mode; }
+  // Point-partitioned solve over `world` ranks (one per GPU): every rank
+  // holds the whole problem, and this one solves with the points of
+  // ShardRange(rank) and all of their observations, exchanging the
+  // camera-side sums through `allreduce` (ShardComm, problem.h).  After the
+  // run every rank holds the same cameras, rig cameras and instances, and
+  // the solved values of its own points; the other points keep their values
+  // from before the run.
+  void SetShard(int rank, int world, int (*allreduce)(void*, double*, int64_t, int), void* ctx);
+  // Points [first, last) of a rank: contiguous ranges of point indices with
+  // nearly equal numbers of observations (a function of the problem only, so
+  // every rank computes the same partition).
+  std::pair<int64_t, int64_t> ShardRange(int rank) const;
+  const ShardComm& Shard() const { return opts_.shard; }
 
   void Run();
 

@@ -512,6 +512,28 @@ int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance) {
   });
 }
 
+int gbba_set_shard(gbba_adjuster_t* h, int rank, int world_size, gbba_allreduce_fn allreduce, void* ctx) {
+  return guarded([&] {
+    try {
+      ba_of(h).SetShard(rank, world_size, allreduce, ctx);
+    } catch (const std::invalid_argument& e) {
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
+    }
+  });
+}
+
+int gbba_get_shard_points(const gbba_adjuster_t* h, int rank, int64_t* first, int64_t* last) {
+  return guarded([&] {
+    need(first, "first");
+    need(last, "last");
+    const gbba::BundleAdjuster& ba = ba_of(h);
+    if (rank < 0 || rank >= ba.Shard().world) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "rank out of range");
+    const auto r = ba.ShardRange(rank);
+    *first = r.first;
+    *last = r.second;
+  });
+}
+
 int gbba_run(gbba_adjuster_t* h) {
   return guarded([&] { ba_of(h).Run(); });
 }
@@ -681,7 +703,8 @@ void gbba_batch_destroy(gbba_batch_t* b) { delete b; }
 int gbba_batch_add(gbba_batch_t* b, gbba_adjuster_t* h) {
   return guarded([&] {
     if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
-    ba_of(h);
+    if (ba_of(h).Shard().world > 1)
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "a sharded adjuster cannot join a batch (the batch is single-rank)");
     b->items.push_back(h);
   });
 }

@@ -83,6 +83,23 @@ struct Observation {
   bool is_gcp = false;
 };
 
+// Point-partitioned solve over several ranks (one process or thread per
+// GPU).  Every rank holds all cameras, rig cameras and instances and a share
+// of the points with all of their observations; the camera-side sums of the
+// observations (gradient, Schur right-hand side, preconditioner blocks, the
+// Schur product of every PCG iteration) and the scalar sums (cost, model
+// decrease, IRLS statistics) are combined by `allreduce`.  The callback
+// reduces `count` doubles in place across the ranks (op 0: sum, 1: max) and
+// returns 0, or nonzero on failure; every rank calls it the same number of
+// times with the same counts.
+struct ShardComm {
+  int rank = 0;
+  int world = 1;
+  int (*allreduce)(void* ctx, double* data, int64_t count, int op) = nullptr;
+  void* ctx = nullptr;
+  bool active() const { return world > 1 && allreduce != nullptr; }
+};
+
 struct SolverOptions {
   int max_iterations = 500;
   int loss = kLossTrivial;
@@ -104,6 +121,7 @@ struct SolverOptions {
   int pcg_max_iterations = 500;
   bool compute_reprojection_errors = true;
   bool record_trace = true;
+  ShardComm shard;  // world > 1: this rank's share of a point-partitioned solve
 };
 
 struct Problem {

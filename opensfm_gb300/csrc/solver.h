@@ -79,6 +79,37 @@ std::unique_ptr<BatchSolverBase> make_batch_solver(int precision);
 std::unique_ptr<BatchSolverBase> make_batch_solver_fp64();
 std::unique_ptr<BatchSolverBase> make_batch_solver_mixed();
 
+// Optimised camera-side coordinates of a problem: the free coordinates of
+// the rig instances, of the rig cameras that some shot applies with a free
+// coordinate (and of the scale blocks), and of the cameras.  The solver's
+// explicit reduced camera system has this size.
+inline int camera_side_unknowns(const Problem& P) {
+  bool any_rig_free = false;
+  for (const Shot& s : P.shots)
+    if (s.rig_camera >= 0 && P.rig_cameras[s.rig_camera].used)
+      for (int k = 0; k < 6; ++k) any_rig_free |= P.rig_cameras[s.rig_camera].free_mask[k] != 0;
+  int n = 0;
+  for (const PoseBlock& b : P.instances)
+    for (int k = 0; k < 6; ++k) n += b.free_mask[k] != 0;
+  for (const PoseBlock& b : P.rig_cameras)
+    if (b.used && (any_rig_free || b.scale_block))
+      for (int k = 0; k < 6; ++k) n += b.free_mask[k] != 0;
+  for (const CameraBlock& c : P.cameras)
+    for (int k = 0; k < c.n; ++k) n += c.free_mask[k] != 0;
+  return n;
+}
+
+// Whether a solve takes exact steps from the explicit reduced camera system
+// (dense mode): an exact linear solver type, a single rank, and at most
+// opts.dense_max_unknowns camera-side unknowns.
+inline bool exact_dense_steps(const Problem& P, const SolverOptions& opts) {
+  const std::string& ls = opts.linear_solver;
+  const bool exact = ls == "DENSE_SCHUR" || ls == "DENSE_QR" || ls == "DENSE_NORMAL_CHOLESKY" ||
+                     ls == "SPARSE_SCHUR" || ls == "SPARSE_NORMAL_CHOLESKY";
+  const int n = camera_side_unknowns(P);
+  return exact && !opts.shard.active() && n > 0 && n <= opts.dense_max_unknowns;
+}
+
 // precision 0: FP64; otherwise mixed FP32/FP64.
 std::unique_ptr<SolverBase> make_solver(int precision);
 std::unique_ptr<SolverBase> make_solver_fp64();

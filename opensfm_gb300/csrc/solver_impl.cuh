@@ -685,6 +685,17 @@ class DeviceSolver : public SolverBase {
                          std::vector<std::pair<std::string, std::pair<int, int>>>& other);
   // ---- results
   void finish(Problem& P);
+  // ---- sharded solve (opts_.shard): collectives over the ranks, no-ops on
+  // a single rank.  Observation sums are reduced right after the record
+  // pass that forms them, before any prior or host term (replicated on
+  // every rank) is added.  Decisions taken on values that every rank
+  // computes for itself (PCG scalars, the camera step) use rank 0's values,
+  // so that all ranks take the same branches and issue the same collectives.
+  bool sharded() const { return opts_.shard.active(); }
+  void shard_reduce(double* h, int64_t n, int op);
+  void shard_bcast(double* h, int64_t n);
+  template <typename T>
+  void shard_reduce_device(T* d, int64_t n);
 
   Problem* prob_ = nullptr;
   SolverOptions opts_;
@@ -713,6 +724,7 @@ class DeviceSolver : public SolverBase {
   std::vector<double> prior_weight_cam_, prior_weight_rig_, prior_weight_gps_;
   std::vector<int> gps_inst_;
   std::vector<PointPriorDev> point_priors_;
+  int64_t pp_offset_ = 0, n_pp_total_ = 0;  // this rank's first point prior in the GCP3D group, the group size
   std::vector<double> point_prior_w_;
   double ratio_cam_ = 1e-3, ratio_rig_ = 1e-3, ratio_gps_ = 1e-3, ratio_gcp3d_ = 1e-3;
   int64_t launches_ = 0;
@@ -945,8 +957,14 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     n_dense_ = 0;
     for (int j = 0; j < cl_.n; ++j)
       if (cmask_[j]) dmap[j] = n_dense_++;
-    dense_ = exact && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
-    dense_ready_ = (dense_ || opts.compute_covariances) && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
+    // a sharded solve takes its steps from PCG on the implicit Schur product
+    // (one camera-side all-reduce per iteration); the explicit system and
+    // the covariances are single-rank features
+    dense_ = !sharded() && exact && n_dense_ > 0 && n_dense_ <= opts.dense_max_unknowns;
+    if (dense_ != exact_dense_steps(P, opts) || (exact && n_dense_ != camera_side_unknowns(P)))
+      throw std::logic_error("dense mode: camera-side unknown count disagrees with camera_side_unknowns()");
+    dense_ready_ = !sharded() && (dense_ || opts.compute_covariances) && n_dense_ > 0 &&
+                   n_dense_ <= opts.dense_max_unknowns;
     dmap_host_ = dmap;
     if (dense_ready_) {
       // pairs (o1 >= o2) of the observations of every point, as point-major
@@ -1114,6 +1132,16 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   group_dim_.assign(n_shots_ + 1, 2);
   for (int s = 0; s < n_shots_; ++s) group_dim_[s] = P.cameras[P.shots[s].camera].model == kSpherical ? 3 : 2;
   if (gcp_shot >= 0) group_dim_[n_shots_] = group_dim_[gcp_shot];
+  if (sharded()) {
+    // group sizes over every rank's observations (the small-group rule reads
+    // them); the GCP2D group takes the larger residual size found on any rank
+    std::vector<double> cnt(group_count_.begin(), group_count_.end());
+    shard_reduce(cnt.data(), int64_t(cnt.size()), 0);
+    for (size_t g = 0; g < cnt.size(); ++g) group_count_[g] = int(cnt[g] + 0.5);
+    double gd = gcp_shot >= 0 ? double(group_dim_[n_shots_]) : 0.0;
+    shard_reduce(&gd, 1, 1);
+    if (gd > 0.0) group_dim_[n_shots_] = int(gd);
+  }
   group_ratio_ = P.group_density_ratio;
   if (group_ratio_.size() != size_t(n_shots_ + 1)) group_ratio_.assign(n_shots_ + 1, opts.default_density_ratio);
   d_group_dim_.upload(group_dim_);
@@ -1143,6 +1171,20 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     point_priors_.push_back(d);
   }
   point_prior_w_.assign(point_priors_.size(), 1.0);
+  // the GCP3D reweighting group spans the point priors of every rank, in
+  // rank order
+  pp_offset_ = 0;
+  n_pp_total_ = int64_t(point_priors_.size());
+  if (sharded()) {
+    std::vector<double> cnt(size_t(opts.shard.world), 0.0);
+    cnt[size_t(opts.shard.rank)] = double(point_priors_.size());
+    shard_reduce(cnt.data(), int64_t(cnt.size()), 0);
+    n_pp_total_ = 0;
+    for (int r = 0; r < opts.shard.world; ++r) {
+      if (r == opts.shard.rank) pp_offset_ = n_pp_total_;
+      n_pp_total_ += int64_t(cnt[size_t(r)] + 0.5);
+    }
+  }
   if (!point_priors_.empty()) {
     d_pp_.upload(point_priors_);
     d_pp_w_.upload(point_prior_w_);
@@ -1277,6 +1319,34 @@ struct CostLaunch {
   }
 };
 
+template <typename R>
+void DeviceSolver<R>::shard_reduce(double* h, int64_t n, int op) {
+  if (!sharded() || n <= 0) return;
+  if (opts_.shard.allreduce(opts_.shard.ctx, h, n, op) != 0)
+    throw std::runtime_error("sharded solve: the all-reduce failed on rank " + std::to_string(opts_.shard.rank));
+}
+
+// rank 0's values on every rank (a sum to which the other ranks add zeros)
+template <typename R>
+void DeviceSolver<R>::shard_bcast(double* h, int64_t n) {
+  if (!sharded() || n <= 0) return;
+  if (opts_.shard.rank != 0) std::fill(h, h + n, 0.0);
+  shard_reduce(h, n, 0);
+}
+
+// Sums a device buffer over the ranks (through host memory, in FP64).
+template <typename R>
+template <typename T>
+void DeviceSolver<R>::shard_reduce_device(T* d, int64_t n) {
+  if (!sharded() || n <= 0) return;
+  std::vector<T> t(static_cast<size_t>(n));
+  GB_CUDA(cudaMemcpy(t.data(), d, sizeof(T) * size_t(n), cudaMemcpyDeviceToHost));
+  std::vector<double> h(t.begin(), t.end());
+  shard_reduce(h.data(), n, 0);
+  for (int64_t i = 0; i < n; ++i) t[size_t(i)] = T(h[size_t(i)]);
+  GB_CUDA(cudaMemcpy(d, t.data(), sizeof(T) * size_t(n), cudaMemcpyHostToDevice));
+}
+
 // FP64 cost of the current (or candidate) state; projection part on the
 // device, priors on the host.  In mixed mode a candidate's residuals are
 // always kept (d_resid_cand_): the next linearization uses them if the
@@ -1300,6 +1370,7 @@ double DeviceSolver<R>::cost_pass(bool candidate, bool store_residuals) {
   GB_CUDA(cudaGetLastError());
   double c[2];
   GB_CUDA(cudaMemcpy(c, d_scal_.get() + 6, sizeof(c), cudaMemcpyDeviceToHost));
+  shard_reduce(c, 2, 0);  // observations and point priors of every rank
   return c[0] + c[1] + prior_terms(candidate ? xc_cand_ : xc_, false);
 }
 
@@ -1327,6 +1398,8 @@ void DeviceSolver<R>::linearize() {
   p.plane_mask = matrix_free_ ? uint64_t(0) : plane_mask_;
   record_pass(p);
   launches_ += 2;
+  shard_reduce_device(d_gc_.get(), int64_t(d_gc_.size()));
+  shard_reduce_device(d_dc_.get(), int64_t(d_dc_.size()));
   if (!point_priors_.empty()) {
     point_prior_linearize_kernel<R><<<elem_grid(int64_t(point_priors_.size())), 256>>>(
         int(point_priors_.size()), d_pp_.get(), d_pp_w_.get(), d_X_.get(), d_point_free_.get(), d_Vp_.get(),

@@ -27,6 +27,8 @@ _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
 _U8 = C.POINTER(C.c_uint8)
 _H = C.c_void_p
+# int allreduce(void* ctx, double* data, int64_t count, int op)
+ALLREDUCE_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.c_int)
 
 
 class Summary(C.Structure):
@@ -98,6 +100,8 @@ def _declare(L) -> None:
         "gbba_get_group_density_ratio": ([_H, S], C.c_double),
         "gbba_set_pcg_tolerance": ([_H, C.c_double], C.c_int),
         "gbba_set_matrix_free": ([_H, C.c_int], C.c_int),
+        "gbba_set_shard": ([_H, C.c_int, C.c_int, ALLREDUCE_FN, C.c_void_p], C.c_int),
+        "gbba_get_shard_points": ([_H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
         "gbba_run": ([_H], C.c_int),
         "gbba_get_camera": ([_H, S, C.POINTER(C.c_int), _D, C.c_int, C.POINTER(C.c_int)], C.c_int),
         "gbba_get_rig_instance_pose": ([_H, S, _D], C.c_int),
@@ -119,6 +123,30 @@ def _declare(L) -> None:
         f.argtypes = args
         f.restype = res
     L._gbba_adjuster_declared = True
+
+
+REDUCE_SUM = 0
+REDUCE_MAX = 1
+
+
+def torch_allreduce(group=None):
+    """An all-reduce for BundleAdjuster.set_shard over a torch.distributed
+    process group: gloo reduces the host array directly; NCCL through a copy
+    on the current CUDA device."""
+    import torch
+    import torch.distributed as dist
+    nccl = dist.get_backend(group) == "nccl"
+
+    def f(a: np.ndarray, op: int) -> None:
+        t = torch.from_numpy(a)
+        rop = dist.ReduceOp.SUM if op == REDUCE_SUM else dist.ReduceOp.MAX
+        if nccl:
+            d = t.to("cuda")
+            dist.all_reduce(d, op=rop, group=group)
+            t.copy_(d.cpu())
+        else:
+            dist.all_reduce(t, op=rop, group=group)
+    return f
 
 
 def _b(s) -> bytes:
@@ -463,6 +491,35 @@ class BundleAdjuster:
         """0: store the Jacobian records when they fit in device memory (the
         default), 1: evaluate them in every pass, -1: always store them."""
         self._check(self._L.gbba_set_matrix_free(self._h, int(mode)))
+
+    def set_shard(self, rank: int, world_size: int, allreduce=None) -> None:
+        """Makes this adjuster rank `rank` of a point-partitioned solve over
+        `world_size` GPUs (include/gbba.h, gbba_set_shard).  `allreduce(data,
+        op)` reduces the float64 numpy array `data` in place over the ranks
+        (op REDUCE_SUM or REDUCE_MAX); torch_allreduce() makes one from a
+        torch.distributed process group.  world_size 1 restores the
+        single-GPU solve."""
+        if world_size > 1 and allreduce is None:
+            raise ValueError("a sharded solve needs an all-reduce")
+        if world_size > 1:
+            def _cb(ctx, data, count, op):
+                try:
+                    allreduce(np.ctypeslib.as_array(data, shape=(int(count),)), int(op))
+                    return 0
+                except Exception:  # reported to the solver as a failed collective
+                    import traceback
+                    traceback.print_exc()
+                    return 1
+            self._allreduce_cb = ALLREDUCE_FN(_cb)
+        else:
+            self._allreduce_cb = ALLREDUCE_FN()
+        self._check(self._L.gbba_set_shard(self._h, int(rank), int(world_size), self._allreduce_cb, None))
+
+    def shard_points(self, rank: int) -> tuple[int, int]:
+        """Points [first, last) (insertion order) that `rank` solves with."""
+        a, b = C.c_int64(0), C.c_int64(0)
+        self._check(self._L.gbba_get_shard_points(self._h, int(rank), C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def set_max_num_iterations(self, n: int) -> None:
         self._check(self._L.gbba_set_max_num_iterations(self._h, int(n)))

@@ -155,6 +155,8 @@ def test_sparse_schur_picks_dense_for_small_systems():
                              gps=False)
     ba.run()
     assert _linear_solver(ba).startswith("DENSE_SCHUR")
+    # mixed precision is for the iterative path: exact steps take FP64 records
+    assert "FP64 records" in _linear_solver(ba)
     ba2 = adjuster_from_scene(scene, precision="mixed", loss=("HuberLoss", 1.0), irls="none", max_iterations=5,
                               gps=False, linear_solver="ITERATIVE_SCHUR")
     ba2.run()

@@ -1,0 +1,121 @@
+"""Point-partitioned (sharded) solve on the GPU: two ranks against one.
+
+Two spawned processes, each an adjuster with the whole problem and half of
+the points, exchange their camera-side sums through gloo (host memory).  On
+this machine both ranks use the same GPU: their kernels never wait on one
+another, the exchange happens on the host between launches.  The sharded
+solve must follow the single-rank solve's trajectory: the same LM decisions
+(every iteration's success flag) and per-iteration costs within 1e-10
+relative in FP64 (the sums are the same, added in another order), and the
+same final camera side.  Mixed precision, and IRLS mixture reweighting
+(group statistics reduced over the ranks), end at the single-rank final cost
+within the solver tests' bars.
+"""
+import multiprocessing as mp
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from opensfm_gb300 import pybundle
+from opensfm_gb300 import synthetic as syn
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "street_fp64": dict(scene=lambda: syn.street_scene(n_shots=60, n_points=8000, seed=11, outlier_ratio=0.0),
+                        kw=dict(precision="fp64", loss=("SoftLOneLoss", 1.0), irls="none", gps=False,
+                                max_iterations=15, pcg_tolerance=1e-10, linear_solver="ITERATIVE_SCHUR")),
+    "aerial_gps_mixed": dict(scene=lambda: syn.aerial_scene(seed=2, nx=8, ny=8, n_points=6000),
+                             kw=dict(precision="mixed", loss=("HuberLoss", 2.0), irls="none", gps=True,
+                                     max_iterations=20, pcg_tolerance=1e-4, linear_solver="ITERATIVE_SCHUR")),
+    "ring_irls_fp64": dict(scene=lambda: syn.ring_scene(n_points=2000, outlier_ratio=0.03, seed=5),
+                           kw=dict(precision="fp64", irls="mixture", gps=False, max_iterations=40,
+                                   pcg_tolerance=1e-10, linear_solver="ITERATIVE_SCHUR")),
+}
+
+
+def _solve(case, rank=0, world=1, allreduce=None):
+    c = CASES[case]
+    scene = c["scene"]()
+    ba = pybundle.adjuster_from_scene(scene, **c["kw"])
+    if world > 1:
+        ba.set_shard(rank, world, allreduce)
+    ba.run()
+    n_inst = len(scene.rig_instance_poses)
+    poses = np.array([ba.get_rig_instance_pose(str(i)).ba_data() for i in range(n_inst)])
+    a, b = ba.shard_points(rank) if world > 1 else (0, len(scene.points))
+    pts = ba.get_points()[a:b]
+    return {"trace": ba.trace(), "summary": ba.summary(), "poses": poses, "points": pts, "range": (a, b)}
+
+
+def _rank_main(case, rank, world, port, q):
+    try:
+        from datetime import timedelta
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(0)
+        os.environ["MASTER_ADDR"] = "127.0.0.1"
+        os.environ["MASTER_PORT"] = str(port)
+        dist.init_process_group("gloo", rank=rank, world_size=world, timeout=timedelta(seconds=120))
+        out = _solve(case, rank, world, pybundle.torch_allreduce())
+        dist.destroy_process_group()
+        q.put((rank, out))
+    except Exception as e:  # pragma: no cover - reported to the parent
+        import traceback
+        q.put((rank, traceback.format_exc() + repr(e)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _sharded(case, world=2):
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(case, r, world, port, q)) for r in range(world)]
+    for p in procs:
+        p.start()
+    out = {}
+    try:
+        for _ in range(world):
+            rank, res = q.get(timeout=600)
+            assert not isinstance(res, str), res
+            out[rank] = res
+    finally:
+        for p in procs:
+            p.join(timeout=60)
+            if p.is_alive():
+                p.terminate()
+    return out
+
+
+def test_fp64_sharded_solve_follows_single_rank_trajectory():
+    single = _solve("street_fp64")
+    shard = _sharded("street_fp64")
+    t1, t2 = single["trace"], shard[0]["trace"]
+    assert t1.shape == t2.shape, (t1.shape, t2.shape)
+    np.testing.assert_array_equal(t1[:, 3], t2[:, 3])  # the same accepted / rejected steps
+    np.testing.assert_allclose(t2[:, 1], t1[:, 1], rtol=1e-10, atol=0)
+    np.testing.assert_array_equal(shard[0]["trace"][:, 1], shard[1]["trace"][:, 1])  # ranks agree exactly
+    np.testing.assert_array_equal(shard[0]["poses"], shard[1]["poses"])
+    np.testing.assert_allclose(shard[0]["poses"], single["poses"], rtol=0, atol=1e-8)
+    # each rank's own points against the single-rank solve's
+    for r in (0, 1):
+        a, b = shard[r]["range"]
+        np.testing.assert_allclose(shard[r]["points"], single["points"][a:b], rtol=0, atol=1e-8)
+    assert shard[0]["range"][1] == shard[1]["range"][0]
+
+
+@pytest.mark.parametrize("case,bar", [("aerial_gps_mixed", 1e-6), ("ring_irls_fp64", 1e-6)])
+def test_sharded_final_cost_matches_single_rank(case, bar):
+    single = _solve(case)
+    shard = _sharded(case)
+    c1, c2 = single["summary"]["final_cost"], shard[0]["summary"]["final_cost"]
+    assert abs(c2 - c1) / c1 < bar, (c1, c2)
+    assert shard[0]["summary"]["final_cost"] == shard[1]["summary"]["final_cost"]
+    np.testing.assert_array_equal(shard[0]["poses"], shard[1]["poses"])

@@ -1,16 +1,19 @@
-"""gbba_evaluate_projections_noalloc against gbba_evaluate_projections.
+"""gbba_evaluate_projections_noalloc against gbba_evaluate_projections and
+the FP64 oracle.
 
 The no-allocation entry point evaluates a scene held in caller-owned device
 memory into caller-owned device outputs.  Two calls in a row must both agree
-with the host-buffer entry point (FP64) on the same scene; bad inputs must
-come back as the same status codes.  This file is collected last so that it
-also runs after every other test in one process.
+with the host-buffer entry point (FP64) on the same scene, and with the FP64
+oracle within the FP64 evaluation bar (1e-10 of each block's magnitude); bad
+inputs must come back as the same status codes.  This file is collected last
+so that it also runs after every other test in one process.
 """
 import ctypes as C
 
 import numpy as np
 import pytest
 
+from oracle import oracle
 from opensfm_gb300 import _lib
 from opensfm_gb300 import synthetic as syn
 from opensfm_gb300.scene import BROWN, FISHEYE, FISHEYE624, PERSPECTIVE, SPHERICAL, evaluate_projections
@@ -107,6 +110,7 @@ def test_noalloc_matches_evaluate_projections_twice(name, make):
     scene = make()
     nr, cmax = scene.layout()
     ref = evaluate_projections(scene, _lib.PRECISION_FP64)
+    orc = oracle.evaluate_scene(scene)
     dscene = DeviceScene(scene)
     got = []
     for _ in range(2):
@@ -124,6 +128,11 @@ def test_noalloc_matches_evaluate_projections_twice(name, make):
             # same FP64 arithmetic; the single-model specialisation of the
             # host-buffer path may contract a few operations differently
             assert err <= 1e-12 * scale, f"{name} {nm}: {err:g} (scale {scale:g})"
+            # and the oracle (same bar as the FP64 evaluation tests)
+            o = orc[k]
+            oscale = max(1.0, float(np.abs(o).max()))
+            oerr = float(np.abs(g - o).max())
+            assert oerr <= 1e-10 * oscale, f"{name} {nm} vs oracle: {oerr:g} (scale {oscale:g})"
     for k in range(5):
         np.testing.assert_array_equal(got[0][k], got[1][k])
 
@@ -159,9 +168,40 @@ def test_noalloc_rejects_bad_inputs():
     d.s.n_shots = 8193
     assert _call(d, nr, cmax, outs) == _lib.GBBA_ERR_INVALID_ARGUMENT
     assert b"at most 8192" in _lib.lib().gbba_last_error()
+    # a shot whose camera does not exist: found by the shot kernel, reported
+    # with the shot's index
+    bad = syn.random_scene(3, [PERSPECTIVE], n_shots=10, n_points=300)
+    bad.shot_camera[4] = 5
+    d = DeviceScene(bad)
+    assert _call(d, nr, cmax, outs) == _lib.GBBA_ERR_OUT_OF_RANGE
+    assert b"shot 4" in _lib.lib().gbba_last_error()
+    # an unknown projection type
+    bad = syn.random_scene(3, [PERSPECTIVE], n_shots=10, n_points=300)
+    bad.camera_projection[0] = 42
+    d = DeviceScene(bad)
+    assert _call(d, nr, cmax, outs) == _lib.GBBA_ERR_RUNTIME
+    assert b"ProjectionType" in _lib.lib().gbba_last_error()
     # a good call afterwards still matches
     good = DeviceScene(scene)
     outs = DeviceOutputs(n, nr, cmax)
     _lib.check(_call(good, nr, cmax, outs))
     ref = evaluate_projections(scene, _lib.PRECISION_FP64)
     np.testing.assert_allclose(outs.host()[0], ref.residuals, rtol=0, atol=1e-12 * max(1, np.abs(ref.residuals).max()))
+
+
+def test_noalloc_null_outputs_are_skipped():
+    """Outputs passed as NULL are not written; the others match the full call."""
+    scene = syn.random_scene(5, [BROWN, FISHEYE, SPHERICAL, FISHEYE624], n_shots=12, n_points=150, rig=True)
+    nr, cmax = scene.layout()
+    d = DeviceScene(scene)
+    full = DeviceOutputs(scene.n_observations, nr, cmax)
+    _lib.check(_call(d, nr, cmax, full))
+    part = DeviceOutputs(scene.n_observations, nr, cmax)
+    part.o.jac_camera = C.POINTER(C.c_double)()
+    part.o.jac_rig_camera = C.POINTER(C.c_double)()
+    _lib.check(_call(d, nr, cmax, part))
+    a, b = full.host(), part.host()
+    for k in (0, 2, 4):
+        np.testing.assert_array_equal(a[k], b[k])
+    for k in (1, 3):
+        assert np.isnan(b[k]).all()
