@@ -137,13 +137,18 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "source": "fallback"}
 
 
-def traffic_per_obs(kernel: str, precision: str):
-    """DRAM bytes per observation of a kernel from a committed ncu summary."""
-    p = ROOT / "profiles" / "ncu_traffic.json"
+def traffic_per_obs(kernel: str, workload: str = "aerial_small"):
+    """DRAM bytes (read + write) per observation of a kernel, from the
+    committed ncu summary of one launch (profiles/<kernel>_<workload>.md,
+    line "DRAM bytes per observation (...): B").  Traffic grows with the
+    observations processed, so the per-launch figure of the bench is this
+    times its observation count."""
+    import re
+    p = ROOT / "profiles" / f"{kernel}_{workload}.md"
     if not p.exists():
         return None
-    d = json.loads(p.read_text())
-    return d.get(f"{kernel}:{precision}")
+    m = re.search(r"^DRAM bytes per observation[^:]*:\s*([0-9.]+)", p.read_text(), re.M)
+    return float(m.group(1)) if m else None
 
 
 def cpu_baseline(scene, target_s: float = 10.0) -> dict:
@@ -782,7 +787,7 @@ def run_ours(args) -> None:
 
     peaks = measured_peaks()
     achieved = (in_bytes + rec_bytes) / (rec_ms / 1e3) / 1e9
-    tpo = traffic_per_obs("eval_records_kernel", "mixed")
+    tpo = traffic_per_obs("eval_records_kernel")
     result = None
     if rank == 0:
         result = {
