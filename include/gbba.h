@@ -387,6 +387,19 @@ int gbba_add_points_bulk(gbba_adjuster_t* h, int64_t n, const double* xyz, const
 int gbba_add_point_projection_observations_bulk(gbba_adjuster_t* h, int64_t n, const int32_t* shot_index,
                                                 const int32_t* point_index, const double* xy,
                                                 const double* std_dev, const uint8_t* is_gcp);
+/* The depth_prior argument of AddPointProjectionObservation
+ * (bundle_adjuster.cc:274-301, pybind.cc:94-100): map::Depth {value,
+ * is_radial, std_deviation} (map/observation.h:10-18) attached to n
+ * observations given by their insertion index (0-based, over every
+ * observation added so far, string or bulk).  At Run each becomes a
+ * RelativeDepthError residual (bundle_adjuster.cc:572-604,
+ * bundle/error/relative_depth_error.h) in the IRLS group "DEPTH", under the
+ * point-projection loss; value and std are stored as floats, as map::Depth
+ * holds them.  is_radial may be NULL (radial).  A std that is not positive
+ * is GBBA_ERR_INVALID_ARGUMENT; a non-finite value fails at gbba_run with
+ * GBBA_ERR_RUNTIME ("<shot> has non-finite depth prior", :582-586). */
+int gbba_set_observation_depth_priors(gbba_adjuster_t* h, int64_t n, const int64_t* observation_index,
+                                      const double* value, const double* std_dev, const uint8_t* is_radial);
 
 /* Settings (bundle_adjuster.cc:400-483).  The point-projection loss
  * (pybundle.pyi:131) takes the names of CreateLossFunction

@@ -209,6 +209,17 @@ void BundleAdjuster::AddPointProjectionObservation(const std::string& shot, cons
   problem_.observations.push_back(o);
 }
 
+void BundleAdjuster::SetObservationDepthPrior(int64_t index, double value, double std_dev, bool is_radial) {
+  if (index < 0 || index >= int64_t(problem_.observations.size()))
+    throw std::out_of_range("depth prior references an unknown observation");
+  if (!(std_dev > 0.0)) throw std::invalid_argument("depth prior std deviation must be positive");
+  Observation& o = problem_.observations[size_t(index)];
+  o.has_depth = true;
+  o.depth_radial = is_radial;
+  o.depth = float(value);
+  o.depth_std = float(std_dev);
+}
+
 int64_t BundleAdjuster::ShotIndex(const std::string& shot) const {
   auto s = shot_index_.find(shot);
   return s == shot_index_.end() ? -1 : s->second;
@@ -633,6 +644,11 @@ void BundleAdjuster::PrepareRun() {
   problem_.ratio_rig = GetGroupDensityRatio("RCAM");
   problem_.ratio_gps = GetGroupDensityRatio("GPS");
   problem_.ratio_gcp3d = GetGroupDensityRatio("GCP3D");
+  problem_.ratio_depth = GetGroupDensityRatio("DEPTH");
+  // AddRelativeDepthError refuses a non-finite depth (bundle_adjuster.cc:582-586)
+  for (const Observation& o : problem_.observations)
+    if (o.has_depth && !std::isfinite(o.depth))
+      throw std::runtime_error(shot_ids_[size_t(o.shot)] + " has non-finite depth prior");
   static const char* kHostGroups[12] = {"UP",     "PAN",   "TILT",    "ROLL", "ROT", "POS",
                                         "MOTION", "GAUGE", "HEATMAP", "REL",  "GPS", "STDDEV"};
   for (int k = 0; k < 12; ++k) problem_.ratio_host[k] = GetGroupDensityRatio(kHostGroups[k]);

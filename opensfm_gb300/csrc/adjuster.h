@@ -78,6 +78,12 @@ class BundleAdjuster {
                                   double y_offset, double std_deviation);
   void AddPointProjectionObservation(const std::string& shot, const std::string& point, const double* obs,
                                      double std_dev, bool is_gcp);
+  // The depth_prior argument of AddPointProjectionObservation
+  // (bundle_adjuster.cc:274-301; added as a RelativeDepthError block at Run,
+  // :572-604): attaches map::Depth {value, is_radial, std_deviation} to the
+  // observation added `index`-th (0-based).  The value and std are stored as
+  // floats, as map::Depth holds them; a non-finite value makes Run throw.
+  void SetObservationDepthPrior(int64_t index, double value, double std_dev, bool is_radial);
   // index-based adders (the raw-pointer path of AddPointProjectionObservationRaw)
   int64_t ShotIndex(const std::string& shot) const;
   int64_t PointIndex(const std::string& point) const;

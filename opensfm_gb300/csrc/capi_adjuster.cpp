@@ -365,6 +365,27 @@ int gbba_add_point_projection_observation(gbba_adjuster_t* h, const char* shot, 
   });
 }
 
+int gbba_set_observation_depth_priors(gbba_adjuster_t* h, int64_t n, const int64_t* observation_index,
+                                      const double* value, const double* std_dev, const uint8_t* is_radial) {
+  return guarded([&] {
+    if (n < 0) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative depth prior count");
+    if (n == 0) return;
+    need(observation_index, "observation_index");
+    need(value, "value");
+    need(std_dev, "std_dev");
+    auto& ba = ba_of(h);
+    // check every entry before attaching any
+    for (int64_t i = 0; i < n; ++i) {
+      if (observation_index[i] < 0 || observation_index[i] >= ba.NumObservations())
+        throw std::out_of_range("depth prior " + std::to_string(i) + " references an unknown observation");
+      if (!(std_dev[i] > 0.0))
+        throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "depth prior " + std::to_string(i) + ": std deviation must be positive");
+    }
+    for (int64_t i = 0; i < n; ++i)
+      ba.SetObservationDepthPrior(observation_index[i], value[i], std_dev[i], is_radial ? is_radial[i] != 0 : true);
+  });
+}
+
 int64_t gbba_shot_index(const gbba_adjuster_t* h, const char* shot) {
   int64_t r = -1;
   guarded([&] { r = ba_of(h).ShotIndex(str(shot)); });

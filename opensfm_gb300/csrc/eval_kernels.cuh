@@ -51,9 +51,16 @@ constexpr int planes_of(int width) {
 }
 
 // Observation record: observed coordinates, 1/std and the shot index
-// (16 B in FP32, 32 B in FP64), read with vector loads.
+// (16 B in FP32, 32 B in FP64), read with vector loads.  A depth prior of
+// the solver (RelativeDepthError) rides on a slot of its own with
+// x = the prior depth, y = 1 when the depth is radial (0: the camera-frame
+// z) and w = -1/std: a negative weight marks it.
 template <typename R>
 struct ObsPack;
+
+// What a solver slot holds: a projection, a ground-control projection
+// (IRLS group GCP2D) or a depth prior (group DEPTH).
+enum SlotKind : uint8_t { kSlotProjection = 0, kSlotGcp = 1, kSlotDepth = 2 };
 template <>
 struct alignas(16) ObsPack<float> {
   float x, y, w;

@@ -236,8 +236,13 @@ struct ObsInputs {
 // Evaluates the scaled residual and (if JAC) its Jacobian into rec[] using
 // RecordLayout<NR, CMAX, RIG>.  Follows ReprojectionError2DAnalytic<C>::
 // Evaluate (projection_errors.h:67-207) and ReprojectionError3DAnalytic
-// (:255-374) for spherical cameras.
-template <typename R, int M, int NR, int CMAX, bool RIG, bool JAC>
+// (:255-374) for spherical cameras.  A depth prior (negative weight, see
+// ObsPack) follows RelativeDepthError (bundle/error/relative_depth_error.h):
+// one residual (depth(p) - value) / std, depth(p) = |p| when radial, else
+// p.z, on the same camera-frame point p (so the same pose chain rule), with
+// no camera columns.  Only the solver's slots hold depth priors: kernels of
+// other callers instantiate DEPTH = false and carry no depth branch.
+template <typename R, int M, int NR, int CMAX, bool RIG, bool JAC, bool DEPTH = false>
 __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec) {
   using L = RecordLayout<NR, CMAX, RIG>;
   const R v0 = in.v[0], v1 = in.v[1], v2 = in.v[2];
@@ -246,8 +251,32 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
 #pragma unroll
   for (int i = 0; i < 3; ++i) p[i] = g.rot[i * 3 + 0] * v0 + g.rot[i * 3 + 1] * v1 + g.rot[i * 3 + 2] * v2 + g.tc[i];
 
+  const bool depth = DEPTH && in.w < R(0);
+  const R w = depth ? -in.w : in.w;
   R Jq[NR * 3];  // d(residual)/d(p) before scaling
-  if (NR == 3 && in.model == kSpherical) {
+  if (depth) {
+    R d;
+    if (in.oy > R(0.5)) {
+      d = sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+      const R id = R(1) / d;
+      Jq[0] = p[0] * id;
+      Jq[1] = p[1] * id;
+      Jq[2] = p[2] * id;
+    } else {
+      d = p[2];
+      Jq[0] = Jq[1] = R(0);
+      Jq[2] = R(1);
+    }
+    rec[L::kR + 0] = w * (d - in.ox);
+#pragma unroll
+    for (int i = 1; i < NR; ++i) rec[L::kR + i] = R(0);
+    if (JAC) {
+#pragma unroll
+      for (int i = 3; i < NR * 3; ++i) Jq[i] = R(0);
+#pragma unroll
+      for (int i = 0; i < NR * CMAX; ++i) rec[L::kCam + i] = R(0);
+    }
+  } else if (NR == 3 && in.model == kSpherical) {
     // bearing residual: normalize(p) - b(obs), obs = (lon, lat) / 2pi
     R o[3];
     normalize_stage<R>(p, o, Jq);
@@ -255,7 +284,7 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
     const R cl = cos(lat);
     const R b[3] = {cl * sin(lon), -sin(lat), cl * cos(lon)};
 #pragma unroll
-    for (int i = 0; i < NR; ++i) rec[L::kR + i] = in.w * (o[i] - b[i]);
+    for (int i = 0; i < NR; ++i) rec[L::kR + i] = w * (o[i] - b[i]);
     if (JAC) {
 #pragma unroll
       for (int i = 0; i < NR * CMAX; ++i) rec[L::kCam + i] = R(0);
@@ -263,8 +292,8 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
   } else {
     R uv[2], Jc[2 * CMAX], Jp2[6];
     project_dispatch<M, CMAX, R>(in.model, p, in.cam, uv, Jp2, Jc);
-    rec[L::kR + 0] = in.w * (uv[0] - in.ox);
-    rec[L::kR + 1] = in.w * (uv[1] - in.oy);
+    rec[L::kR + 0] = w * (uv[0] - in.ox);
+    rec[L::kR + 1] = w * (uv[1] - in.oy);
     if (NR == 3) rec[L::kR + 2] = R(0);
     if (JAC) {
 #pragma unroll
@@ -275,7 +304,7 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
 #pragma unroll
       for (int i = 0; i < 2; ++i)
 #pragma unroll
-        for (int j = 0; j < CMAX; ++j) rec[L::kCam + i * CMAX + j] = in.w * Jc[i * CMAX + j];
+        for (int j = 0; j < CMAX; ++j) rec[L::kCam + i * CMAX + j] = w * Jc[i * CMAX + j];
       if (NR == 3) {
 #pragma unroll
         for (int j = 0; j < CMAX; ++j) rec[L::kCam + 2 * CMAX + j] = R(0);
@@ -285,7 +314,7 @@ __device__ __forceinline__ void eval_observation(const ObsInputs<R>& in, R* rec)
   if constexpr (JAC) {
 #pragma unroll
   for (int i = 0; i < NR; ++i) {
-    const R a0 = in.w * Jq[i * 3 + 0], a1 = in.w * Jq[i * 3 + 1], a2 = in.w * Jq[i * 3 + 2];
+    const R a0 = w * Jq[i * 3 + 0], a1 = w * Jq[i * 3 + 1], a2 = w * Jq[i * 3 + 2];
     R jp[3];
 #pragma unroll
     for (int j = 0; j < 3; ++j) {

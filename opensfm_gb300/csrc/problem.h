@@ -81,6 +81,15 @@ struct Observation {
   double x = 0, y = 0;
   double std_dev = 1.0;
   bool is_gcp = false;
+  // optional depth prior of the observation (map::Depth: value, is_radial,
+  // std_deviation, stored as floats; map/observation.h:10-18): a second
+  // residual, std^-1 (depth of the point in the camera - value), the depth
+  // being the camera-frame z or, when radial, the distance to the camera
+  // (RelativeDepthError, bundle/error/relative_depth_error.h)
+  bool has_depth = false;
+  bool depth_radial = true;
+  float depth = 0.0f;
+  float depth_std = 1.0f;
 };
 
 // Point-partitioned solve over several ranks (one process or thread per
@@ -140,7 +149,7 @@ struct Problem {
   // IRLS density ratios: one per projection group (shot groups "PROJ_<shot>"
   // then "GCP2D"), and the prior groups.
   std::vector<double> group_density_ratio;
-  double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3;
+  double ratio_cam = 1e-3, ratio_rig = 1e-3, ratio_gps = 1e-3, ratio_gcp3d = 1e-3, ratio_depth = 1e-3;
   // UP PAN TILT ROLL ROT POS MOTION GAUGE HEATMAP REL GPS STDDEV
   double ratio_host[12] = {1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3, 1e-3};
   // AddHeatmap grids (the relative terms of kind kHeatmap point into them)

@@ -57,7 +57,7 @@ struct EvaluatedRecords {
     ldg_copy(s.obs + i, ob);
     ObsInputs<R> in;
     load_inputs<R, M>(s, ob, s.obs_point[i], s.cam_params, s.cam_model, in);
-    eval_observation<R, M, NR, CMAX, RIG, true>(in, rec);
+    eval_observation<R, M, NR, CMAX, RIG, true, true>(in, rec);
     if (v.resid64) {
 #pragma unroll
       for (int q = 0; q < NR; ++q) rec[L::kR + q] = R(v.resid64[4 * i + q]);

@@ -78,29 +78,42 @@ struct RecordPassLaunch : RecordPassArgs<R> {
 // by `order`): observation packs, point index, GCP flag and unit IRLS
 // weights; padding slots get point -1.
 template <typename R>
-__global__ void build_slots_kernel(int64_t n_obs, int64_t n_slots, const Observation* __restrict__ raw,
-                                   const int32_t* __restrict__ order, ObsPack<R>* __restrict__ ob,
-                                   ObsPack<double>* __restrict__ ob64, int* __restrict__ opt,
-                                   uint8_t* __restrict__ gcp, R* __restrict__ weight) {
+__global__ void build_slots_kernel(int64_t n_terms, int64_t n_proj, int64_t n_slots,
+                                   const Observation* __restrict__ raw, const int32_t* __restrict__ order,
+                                   ObsPack<R>* __restrict__ ob, ObsPack<double>* __restrict__ ob64,
+                                   int* __restrict__ opt, uint8_t* __restrict__ gcp, R* __restrict__ weight) {
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   for (int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; s < n_slots; s += stride) {
     ObsPack<R> o{};
     ObsPack<double> o64{};
     int pt = -1;
     uint8_t g = 0;
-    if (s < n_obs) {
-      const Observation q = raw[order[s]];
-      const double w = 1.0 / q.std_dev;
-      o.x = R(q.x);
-      o.y = R(q.y);
-      o.w = R(w);
+    if (s < n_terms) {
+      const int32_t t = order[s];
+      const Observation q = raw[t];
+      if (t < n_proj) {
+        const double w = 1.0 / q.std_dev;
+        o.x = R(q.x);
+        o.y = R(q.y);
+        o.w = R(w);
+        o64.x = q.x;
+        o64.y = q.y;
+        o64.w = w;
+        g = q.is_gcp ? kSlotGcp : kSlotProjection;
+      } else {
+        // a depth prior (ObsPack doc: negative weight, value, radial flag)
+        const double w = 1.0 / double(q.depth_std);
+        o.x = R(q.depth);
+        o.y = R(q.depth_radial ? 1 : 0);
+        o.w = R(-w);
+        o64.x = double(q.depth);
+        o64.y = q.depth_radial ? 1.0 : 0.0;
+        o64.w = -w;
+        g = kSlotDepth;
+      }
       o.shot = q.shot;
-      o64.x = q.x;
-      o64.y = q.y;
-      o64.w = w;
       o64.shot = q.shot;
       pt = q.point;
-      g = q.is_gcp ? 1 : 0;
     }
     ob[s] = o;
     if (ob64) ob64[s] = o64;
@@ -702,7 +715,8 @@ class DeviceSolver : public SolverBase {
   KernelConfig kc_{};
   CamLayout cl_{};
   int n_inst_ = 0, n_rig_ = 0, n_cam_ = 0, n_shots_ = 0;
-  int64_t n_pt_ = 0, n_obs_ = 0, n_slots_ = 0;
+  int64_t n_pt_ = 0, n_obs_ = 0, n_terms_ = 0, n_slots_ = 0;
+  std::vector<int64_t> depth_obs_;  // the observations with a depth prior, in observation order
   int n_planes_ = 0;
   uint64_t plane_mask_ = 0;
   int cam_tri_stride_ = 0;
@@ -811,6 +825,13 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   n_shots_ = int(P.shots.size());
   n_pt_ = int64_t(P.points.size());
   n_obs_ = int64_t(P.observations.size());
+  // residual terms on slots: every observation, then its depth prior if it
+  // has one (RelativeDepthError, added beside the projection error at
+  // bundle_adjuster.cc:861-869)
+  depth_obs_.clear();
+  for (int64_t o = 0; o < n_obs_; ++o)
+    if (P.observations[size_t(o)].has_depth) depth_obs_.push_back(o);
+  n_terms_ = n_obs_ + int64_t(depth_obs_.size());
 
   // kernel configuration
   bool any_sph = false, single = true, any_rig_free = false, any_rig_used = false;
@@ -887,9 +908,13 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   // makes three sequential passes over the observations (counts, point
   // scatter, shot scatter); the per-slot arrays are built on the device from
   // the uploaded observations.
-  if (n_obs_ > int64_t(std::numeric_limits<int32_t>::max()) - 32)
+  if (n_terms_ > int64_t(std::numeric_limits<int32_t>::max()) - 32)
     throw std::invalid_argument("more observations than a 32-bit slot index can address");
-  n_slots_ = std::max<int64_t>(32, (n_obs_ + 31) / 32 * 32);
+  n_slots_ = std::max<int64_t>(32, (n_terms_ + 31) / 32 * 32);
+  // observation of term t (a depth prior's is the observation it belongs to)
+  auto term = [&](int64_t t) -> const Observation& {
+    return P.observations[size_t(t < n_obs_ ? t : depth_obs_[size_t(t - n_obs_)])];
+  };
   std::vector<int> rank(n_shots_);
   {
     std::vector<int> shots(n_shots_);
@@ -899,26 +924,35 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     for (int r = 0; r < n_shots_; ++r) rank[shots[r]] = r;
   }
   std::vector<int64_t> pstart(n_pt_ + 1, 0), sstart(n_shots_ + 1, 0);
-  group_count_.assign(n_shots_ + 1, 0);
+  // IRLS groups of the slots: one per shot, GCP2D, DEPTH
+  group_count_.assign(n_shots_ + 2, 0);
   int gcp_shot = -1;
-  for (const Observation& q : P.observations) {
+  for (int64_t t = 0; t < n_terms_; ++t) {
+    const Observation& q = term(t);
     ++pstart[q.point + 1];
     ++sstart[rank[q.shot] + 1];
-    ++group_count_[q.is_gcp ? n_shots_ : q.shot];
-    if (q.is_gcp && gcp_shot < 0) gcp_shot = q.shot;
+    ++group_count_[t >= n_obs_ ? n_shots_ + 1 : q.is_gcp ? n_shots_ : q.shot];
+    if (t < n_obs_ && q.is_gcp && gcp_shot < 0) gcp_shot = q.shot;
   }
   for (int64_t p = 0; p < n_pt_; ++p) pstart[p + 1] += pstart[p];
   for (int r = 0; r < n_shots_; ++r) sstart[r + 1] += sstart[r];
-  std::vector<int32_t> order(n_obs_);
-  for (int64_t o = 0; o < n_obs_; ++o) order[pstart[P.observations[o].point]++] = int32_t(o);
+  std::vector<int32_t> order(n_terms_);
+  for (int64_t o = 0; o < n_terms_; ++o) order[pstart[term(o).point]++] = int32_t(o);
   std::vector<int32_t> src(n_slots_, -1);
-  for (int64_t s = 0; s < n_obs_; ++s) src[sstart[rank[P.observations[order[s]].shot]]++] = int32_t(s);
-  slot_obs_.assign(n_slots_, -1);
-  for (int64_t s = 0; s < n_obs_; ++s) slot_obs_[s] = order[s];
+  for (int64_t s = 0; s < n_terms_; ++s) src[sstart[rank[term(order[s]).shot]]++] = int32_t(s);
+  slot_obs_.assign(n_slots_, -1);  // the observation of a projection slot; -1: depth prior or padding
+  for (int64_t s = 0; s < n_terms_; ++s) slot_obs_[s] = order[s] < n_obs_ ? order[s] : -1;
   {
-    DeviceArray<Observation> raw;
+    DeviceArray<Observation> raw(size_t(std::max<int64_t>(1, n_terms_)));
     DeviceArray<int32_t> d_order;
-    raw.upload(P.observations);
+    if (n_obs_)
+      GB_CUDA(cudaMemcpyAsync(raw.get(), P.observations.data(), size_t(n_obs_) * sizeof(Observation),
+                              cudaMemcpyHostToDevice));
+    if (!depth_obs_.empty()) {
+      std::vector<Observation> dt(depth_obs_.size());
+      for (size_t k = 0; k < dt.size(); ++k) dt[k] = P.observations[size_t(depth_obs_[k])];
+      GB_CUDA(cudaMemcpy(raw.get() + n_obs_, dt.data(), dt.size() * sizeof(Observation), cudaMemcpyHostToDevice));
+    }
     d_order.upload(order);
     d_sm_src_.upload(src);
     d_obs_.resize(n_slots_);
@@ -928,7 +962,8 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
     d_weight_.resize(n_slots_);
     d_sm_point_.resize(n_slots_);
     d_sm_shot_.resize(n_slots_);
-    build_slots_kernel<R><<<elem_grid(n_slots_), 256>>>(n_obs_, n_slots_, raw.get(), d_order.get(), d_obs_.get(),
+    build_slots_kernel<R><<<elem_grid(n_slots_), 256>>>(n_terms_, n_obs_, n_slots_, raw.get(), d_order.get(),
+                                                         d_obs_.get(),
                                                          kMixed ? d_obs64_.get() : nullptr, d_obs_point_.get(),
                                                          d_gcp_.get(), d_weight_.get());
     build_shot_major_kernel<R><<<elem_grid(n_slots_), 256>>>(n_slots_, d_sm_src_.get(), d_obs_point_.get(),
@@ -977,14 +1012,14 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
       std::vector<int> raw_keys;
       {
         int64_t s0 = 0;
-        while (s0 < n_obs_) {
-          const int p = P.observations[order[s0]].point;
+        while (s0 < n_terms_) {
+          const int p = term(order[s0]).point;
           int64_t s1 = s0 + 1;
-          while (s1 < n_obs_ && P.observations[order[s1]].point == p) ++s1;
+          while (s1 < n_terms_ && term(order[s1]).point == p) ++s1;
           for (int64_t a = s0; a < s1; ++a) {
-            const int64_t sa = P.observations[order[a]].shot;
+            const int64_t sa = term(order[a]).shot;
             for (int64_t b = s0; b <= a; ++b) {
-              const int64_t sb = P.observations[order[b]].shot;
+              const int64_t sb = term(order[b]).shot;
               raw_pairs.push_back(make_int2(int(a), int(b)));
               raw_keys.push_back(int((sa * n_shots_ + sb) * 2 + (a == b ? 1 : 0)));
             }
@@ -1128,10 +1163,12 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   d_scal_.resize(8);
   d_bad_.resize(2);
 
-  // IRLS projection groups: one per shot, plus GCP2D (counted with the slots)
-  group_dim_.assign(n_shots_ + 1, 2);
+  // IRLS slot groups: one per shot, GCP2D, and DEPTH (one residual each),
+  // counted with the slots
+  group_dim_.assign(n_shots_ + 2, 2);
   for (int s = 0; s < n_shots_; ++s) group_dim_[s] = P.cameras[P.shots[s].camera].model == kSpherical ? 3 : 2;
   if (gcp_shot >= 0) group_dim_[n_shots_] = group_dim_[gcp_shot];
+  group_dim_[n_shots_ + 1] = 1;
   if (sharded()) {
     // group sizes over every rank's observations (the small-group rule reads
     // them); the GCP2D group takes the larger residual size found on any rank
@@ -1144,10 +1181,11 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
   }
   group_ratio_ = P.group_density_ratio;
   if (group_ratio_.size() != size_t(n_shots_ + 1)) group_ratio_.assign(n_shots_ + 1, opts.default_density_ratio);
+  group_ratio_.push_back(P.ratio_depth);
   d_group_dim_.upload(group_dim_);
-  d_irls_stats_.resize(8 * (n_shots_ + 1));
-  d_irls_ll_.resize(2 * (n_shots_ + 1));
-  d_irls_params_.resize(n_shots_ + 1);
+  d_irls_stats_.resize(8 * (n_shots_ + 2));
+  d_irls_ll_.resize(2 * (n_shots_ + 2));
+  d_irls_params_.resize(n_shots_ + 2);
 
   // priors
   prior_weight_cam_.assign(n_cam_, 1.0);

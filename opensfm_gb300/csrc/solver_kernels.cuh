@@ -325,7 +325,7 @@ __global__ void __launch_bounds__(256) linearize_kernel(SolveView<R> v, uint64_t
       ldg_copy(s.obs + i, ob);
       ObsInputs<R> in;
       load_inputs<R, M>(s, ob, pt, cams, models, in);
-      eval_observation<R, M, NR, CMAX, RIG, true>(in, rec);
+      eval_observation<R, M, NR, CMAX, RIG, true, true>(in, rec);
       if (v.resid64) {
         // mixed precision: the residual itself comes from the FP64 cost pass
         // of the same state (the FP32 one carries ~1e-4 sigma of rounding
@@ -654,7 +654,7 @@ __global__ void __launch_bounds__(256) cost_kernel(SceneView<double> s, const fl
     ObsInputs<double> in;
     load_inputs<double, M>(s, ob, pt, cams, models, in);
     double rec[L::kWidth];
-    eval_observation<double, M, NR, CMAX, RIG, false>(in, rec);
+    eval_observation<double, M, NR, CMAX, RIG, false, true>(in, rec);
     double sq = 0.0;
 #pragma unroll
     for (int q = 0; q < NR; ++q) sq += rec[q] * rec[q];
@@ -690,14 +690,14 @@ static __global__ void point_store_kernel(int64_t n, const Point4* __restrict__ 
 
 // ---------------------------------------------------------------------------
 // IRLS mixture statistics per error group (one group per shot plus GCP2D,
-// bundle_adjuster.cc:559-562; mixture_reweighting.cc:10-109,
-// irls_helpers.cc:220-277).
+// bundle_adjuster.cc:559-562, and DEPTH, :599-602; mixture_reweighting.cc:
+// 10-109, irls_helpers.cc:220-277).
 //   stats pass:   S_g += w r r^T (upper triangle), W_g += w, N_g += 1
 //   weight pass:  p_in = exp(-r^T Sigma^-1 r / 2) / sqrt((2 pi)^k det),
 //                 w = clamp(p_in / (p_in + K), 1e-10, 1),
 //                 LL_g += log(p_in + K), out_g += (w < 0.5)
 struct IrlsGroupParams {
-  double inv[6];     // Sigma^-1 upper triangle (k = 2 uses 0, 1, 3)
+  double inv[6];     // Sigma^-1 upper triangle (k = 2 uses 0, 1, 3; k = 1 uses 0)
   double norm;       // 1 / sqrt((2 pi)^k det)
   double K;
   int active;        // group is being reweighted in this EM iteration
@@ -705,7 +705,8 @@ struct IrlsGroupParams {
 };
 
 __device__ __forceinline__ int irls_group(const SceneView<double>& s, int64_t i, const uint8_t* gcp, int n_shots) {
-  return gcp[i] ? n_shots : s.obs[i].shot;
+  // groups: shots, then GCP2D (n_shots), then DEPTH (n_shots + 1)
+  return gcp[i] == kSlotProjection ? s.obs[i].shot : n_shots + int(gcp[i]) - 1;
 }
 
 static __global__ void irls_stats_kernel(SceneView<double> s, const uint8_t* __restrict__ gcp, int n_shots,
@@ -747,6 +748,8 @@ static __global__ void irls_weight_kernel(SceneView<double> s, const uint8_t* __
     if (P.dim == 3) {
       m = P.inv[0] * r0 * r0 + P.inv[3] * r1 * r1 + P.inv[5] * r2 * r2 +
           2.0 * (P.inv[1] * r0 * r1 + P.inv[2] * r0 * r2 + P.inv[4] * r1 * r2);
+    } else if (P.dim == 1) {
+      m = P.inv[0] * r0 * r0;
     } else {
       m = P.inv[0] * r0 * r0 + 2.0 * P.inv[1] * r0 * r1 + P.inv[3] * r1 * r1;
     }

@@ -9,9 +9,9 @@ shot or point in ``add_point_projection_observation`` raises ``IndexError``
 
 Beyond the reference's methods it exposes bulk (numpy) adders for large
 problems, the precision / IRLS switches of the GPU solver and the iteration
-trace.  The two features that the GPU solver does not implement (depth
-priors on observations, optimised camera biases) raise
-``NotImplementedError`` instead of being silently ignored.
+trace.  The one feature that the GPU solver does not implement (optimised
+camera biases) raises ``NotImplementedError`` instead of being silently
+ignored.
 """
 from __future__ import annotations
 
@@ -110,6 +110,7 @@ def _declare(L) -> None:
         "gbba_has_point": ([_H, S], C.c_int),
         "gbba_num_projections": ([_H], C.c_int64),
         "gbba_num_points": ([_H], C.c_int64),
+        "gbba_set_observation_depth_priors": ([_H, C.c_int64, C.POINTER(C.c_int64), _D, _D, _U8], C.c_int),
         "gbba_get_points_bulk": ([_H, C.c_int64, C.c_int64, _D], C.c_int),
         "gbba_get_projection_results": ([_H, C.c_int64, _D, _D, _I32], C.c_int),
         "gbba_brief_report": ([_H, C.c_char_p, C.c_size_t], C.c_int),
@@ -226,6 +227,18 @@ class Point:
         self.reprojection_weights: Dict[str, float] = {}
 
 
+class Depth:
+    """map::Depth (opensfm/src/lib/map/observation.h:10-18, bound as
+    ``pymap.Depth``): a depth prior of an observation.  value and
+    std_deviation are floats (float32) in the reference; the adjuster
+    rounds them the same way."""
+
+    def __init__(self, value: float = 0.0, is_radial: bool = True, std_deviation: float = 1.0) -> None:
+        self.value = value
+        self.is_radial = is_radial
+        self.std_deviation = std_deviation
+
+
 class BundleAdjuster:
     """GPU bundle adjuster with the reference's pybind surface."""
 
@@ -337,13 +350,31 @@ class BundleAdjuster:
         return pt
 
     def add_point_projection_observation(self, shot: str, point: str, observation, std_deviation: float,
-                                         is_gcp: bool = False, depth_prior=None) -> None:
-        if depth_prior is not None:
-            raise NotImplementedError("depth priors are not implemented by the GPU bundle adjuster")
+                                         is_gcp: bool = False, depth_prior: Optional[Depth] = None) -> None:
+        """AddPointProjectionObservation (bundle_adjuster.cc:274-287); a
+        ``depth_prior`` (``Depth``: value, is_radial, std_deviation) adds a
+        RelativeDepthError residual at run (:572-604); a non-finite value
+        makes ``run`` raise RuntimeError, as the reference's Run does."""
         o = _vec(observation, 2)
         self._check(self._L.gbba_add_point_projection_observation(self._h, _b(shot), _b(point), _dp(o),
                                                                   float(std_deviation), int(is_gcp)))
         self._obs_keys.append((shot, point))
+        if depth_prior is not None:
+            n = int(self._L.gbba_num_projections(self._h))
+            self.set_depth_priors([n - 1], [depth_prior.value], [depth_prior.std_deviation],
+                                  [bool(depth_prior.is_radial)])
+
+    def set_depth_priors(self, observation_index, value, std_deviation, is_radial=True) -> None:
+        """Bulk form of ``depth_prior``: attaches depth priors to the
+        observations of the given insertion indices (0-based, over every
+        observation added so far)."""
+        idx = np.ascontiguousarray(observation_index, np.int64).reshape(-1)
+        n = len(idx)
+        val = np.ascontiguousarray(np.broadcast_to(np.asarray(value, np.float64), (n,)))
+        sd = np.ascontiguousarray(np.broadcast_to(np.asarray(std_deviation, np.float64), (n,)))
+        rad = np.ascontiguousarray(np.broadcast_to(np.asarray(is_radial, np.uint8), (n,)))
+        self._check(self._L.gbba_set_observation_depth_priors(
+            self._h, n, idx.ctypes.data_as(C.POINTER(C.c_int64)), _dp(val), _dp(sd), rad.ctypes.data_as(_U8)))
 
     # -- bulk interface (raw-index path of BAHelpers) ----------------------
     def shot_index(self, shot: str) -> int:
@@ -738,8 +769,12 @@ def heatmap_residual(grid, width: int, resolution: float, x_offset: float, y_off
 def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] = None, irls: str = "mixture",
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
-                        matrix_free: Optional[int] = None, covariances: bool = False) -> BundleAdjuster:
-    """Builds a BundleAdjuster from a SceneArrays (bulk path)."""
+                        matrix_free: Optional[int] = None, covariances: bool = False, depth=None,
+                        rig_pose=None) -> BundleAdjuster:
+    """Builds a BundleAdjuster from a SceneArrays (bulk path).  ``depth``:
+    depth priors (observation indices, values, stds, radial flags);
+    ``rig_pose``: a fixed rig camera pose (angle-axis, centre) shared by every
+    shot (None: the identity)."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
     if matrix_free is not None:
@@ -759,7 +794,8 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
         from .scene import NUM_PARAMS
         cam = Camera(m, scene.camera_values[c, : NUM_PARAMS[m]])
         ba.add_camera(str(c), cam, cam, constant_cameras)
-    ba.add_rig_camera("rig", Pose(), Pose(), True)
+    rp = Pose() if rig_pose is None else Pose.from_ba_data(np.asarray(rig_pose, np.float64))
+    ba.add_rig_camera("rig", rp, rp, True)
     for s in range(len(scene.shot_camera)):
         inst = int(scene.shot_rig_instance[s])
         pose = Pose.from_ba_data(scene.rig_instance_poses[inst])
@@ -770,9 +806,11 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
                                                scene.extras["gps_std"][s], "")
     ba.add_points(scene.points)
     ba.add_point_projection_observations(scene.obs_shot, scene.obs_point, scene.obs_xy, scene.obs_std)
+    if depth is not None:
+        ba.set_depth_priors(*depth)
     return ba
 
 
-__all__ = ["BundleAdjuster", "BundleBatch", "Point", "Reconstruction", "RelativeMotion", "RelativeRotation",
+__all__ = ["BundleAdjuster", "BundleBatch", "Depth", "Point", "Reconstruction", "RelativeMotion", "RelativeRotation",
            "adjuster_from_scene",
            "heatmap_residual", "orientation_residual", "relative_residual"]

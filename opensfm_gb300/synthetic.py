@@ -233,6 +233,22 @@ def ring_scene(seed: int = 42, n_shots: int = 20, n_points: int = 2000, obs_per_
     return scene
 
 
+def depth_priors(scene: SceneArrays, fraction: float = 0.3, std: float = 0.05, radial: bool = True,
+                 noise: float = 0.02, seed: int = 0):
+    """Depth priors (map::Depth) on a seeded share of a scene's
+    observations: the true depth of the observed point in the camera (its
+    camera-frame z, or its distance when radial) plus Gaussian noise.
+    Returns (observation indices, values, stds, radial flags) as
+    BundleAdjuster.set_depth_priors takes them."""
+    rng = np.random.default_rng(seed)
+    idx = np.nonzero(rng.random(scene.n_observations) < fraction)[0].astype(np.int64)
+    poses = scene.extras["true_poses"][scene.shot_rig_instance[scene.obs_shot[idx]]]
+    pc = world_to_camera(poses, scene.extras["true_points"][scene.obs_point[idx]])
+    d = np.linalg.norm(pc, axis=-1) if radial else pc[:, 2]
+    value = d + rng.normal(0.0, noise, len(idx))
+    return idx, value, np.full(len(idx), std), np.full(len(idx), radial, np.uint8)
+
+
 def _geometric_lengths(rng, n, mean, lo, hi):
     # track lengths >= lo with geometric tail of the given mean
     p = 1.0 / max(mean - lo + 1, 1.0)

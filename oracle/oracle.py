@@ -151,6 +151,8 @@ class _Problem(C.Structure):
         ("n_rel", C.c_int32), ("rel_kind", I32), ("rel_shots", I32), ("rel_params", D), ("rel_loss", C.c_int32),
         ("rel_loss_threshold", C.c_double), ("heat_grid", D), ("heat_n", C.c_int64), ("heat_width", C.c_int32),
         ("heat_resolution", C.c_double), ("n_scales", C.c_int32), ("scales", D), ("scale_free", U8),
+        ("n_depth", C.c_int64), ("depth_obs", C.POINTER(C.c_int64)), ("depth_value", D), ("depth_std", D),
+        ("depth_radial", U8),
     ]
 
 
@@ -238,9 +240,26 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None, 
     return r[:m].copy(), J[: 36 * m].reshape(m, 36)
 
 
+def depth_residual(instance_pose, point, value, std, radial=True, rig_camera_pose=None):
+    """A depth prior's scaled residual and its Jacobian rows (d/d instance
+    pose [6], d/d rig camera pose [6], d/d point [3]) (oracle/residuals.h
+    restatement of RelativeDepthError).  value and std are used as given."""
+    L = lib()
+    f = L.oracle_depth_residual
+    f.argtypes = [D, D, D, C.c_double, C.c_double, C.c_int, D, D, D]
+    f.restype = C.c_double
+    pi = np.ascontiguousarray(instance_pose, np.float64)
+    pc = None if rig_camera_pose is None else np.ascontiguousarray(rig_camera_pose, np.float64)
+    X = np.ascontiguousarray(point, np.float64)
+    ji, jr, jp = np.zeros(6), np.zeros(6), np.zeros(3)
+    r = f(_p(pi), _p(pc), _p(X), float(value), float(std), 1 if radial else 0, _p(ji), _p(jr), _p(jp))
+    return r, ji, jr, jp
+
+
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
           density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
-          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None, scales=(), fixed_instances=()):
+          relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None, scales=(), fixed_instances=(),
+          depth=None, rig_pose=None):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
@@ -256,7 +275,11 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     std)).  ``scales``: reconstruction scales (value, free) -- the unknowns
     of "relative_motion" entries, whose params are motion[7], the
     observed-scale flag, the 7 x 7 scale matrix, the robust multiplier and
-    the two scale indices.  Returns a dict with the final parameters,
+    the two scale indices.  ``depth``: depth priors (observation indices,
+    values, stds, radial flags), values and stds rounded to float32 as
+    map::Depth stores them.  ``rig_pose``: one fixed rig camera pose
+    (angle-axis, centre) composed with every shot (None: the identity, not
+    composed).  Returns a dict with the final parameters,
     scales, costs and the cost trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
@@ -287,9 +310,9 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
             has_gps[i] = 1
             gps_pos[i] = scene.extras["gps"][s]
             gps_std[i] = scene.extras["gps_std"][s]
-    rig = np.zeros((1, 6))
+    rig = np.zeros((1, 6)) if rig_pose is None else np.asarray(rig_pose, np.float64).reshape(1, 6).copy()
     rig_free = np.zeros((1, 6), np.uint8)
-    rig_used = np.zeros(1, np.uint8)
+    rig_used = np.array([0 if rig_pose is None or not np.any(rig) else 1], np.uint8)
     rig_has_prior = np.ones(1, np.uint8)
     rig_prior = np.zeros((1, 6))
     rig_sigma = np.ones((1, 6))
@@ -338,6 +361,15 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     s_val = np.array([float(v) for v, _ in scales] or [1.0], np.float64)
     s_free = np.array([1 if f else 0 for _, f in scales] or [0], np.uint8)
     keep += [s_val, s_free]
+    if depth is not None:
+        d_obs = np.ascontiguousarray(depth[0], np.int64)
+        d_val = np.asarray(depth[1], np.float32).astype(np.float64)
+        d_std = np.asarray(depth[2], np.float32).astype(np.float64)
+        d_rad = np.ascontiguousarray(np.broadcast_to(np.asarray(depth[3], np.uint8), d_obs.shape))
+    else:
+        d_obs, d_val, d_std, d_rad = np.zeros(1, np.int64), np.zeros(1), np.ones(1), np.ones(1, np.uint8)
+    n_depth = 0 if depth is None else len(d_obs)
+    keep += [d_obs, d_val, d_std, d_rad]
     u8 = lambda a: a.ctypes.data_as(U8)  # noqa: E731
     i32 = lambda a: a.ctypes.data_as(I32)  # noqa: E731
     P = _Problem(nc, i32(scene.camera_projection), _p(cam_values), _p(cam_values.copy() if False else cam_values),
@@ -349,7 +381,8 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
                  scene.n_observations, i32(scene.obs_shot), i32(scene.obs_point), _p(scene.obs_xy),
                  _p(scene.obs_std), u8(gcp), no, i32(o_kind), i32(o_shot), _p(o_target), _p(o_std),
                  nr, i32(r_kind), i32(r_shots), _p(r_params), LOSSES[relative_loss[0]], float(relative_loss[1]),
-                 _p(h_grid), h_grid.size, h_width, h_res, n_scl, _p(s_val), u8(s_free))
+                 _p(h_grid), h_grid.size, h_width, h_res, n_scl, _p(s_val), u8(s_free),
+                 n_depth, d_obs.ctypes.data_as(C.POINTER(C.c_int64)), _p(d_val), _p(d_std), u8(d_rad))
     loss_kind, loss_a = (0, 1.0) if loss is None else (LOSSES[loss[0]], float(loss[1]))
     O = _Options(max_iterations, loss_kind, loss_a, 1 if irls == "mixture" else 0, density_ratio,
                  int(skip_initial_reweighting), threads or os.cpu_count() or 1)

@@ -135,6 +135,77 @@ inline void residual_jac(int model, const double* cam, const double* inst, const
 }
 
 // ---------------------------------------------------------------------------
+// Depth prior of an observation, restating RelativeDepthError
+// (opensfm/src/lib/bundle/error/relative_depth_error.h): the world point in
+// the camera frame (WorldToCameraCoordinatesRig with unit scale: the
+// instance pose, then the rig-camera pose when it is used), its depth z, or
+// its distance to the camera when radial, and the residual
+// (depth - value) / std.  value and std are floats in the reference
+// (map::Depth, map/observation.h:10-18); callers pass them rounded.
+template <class T>
+inline T depth_residual_generic(const T* inst, const T* rig, const T* X, double value, double std_dev,
+                                bool radial) {
+  using std::sqrt;
+  T p1[3], p2[3];
+  pose_forward_t<T>(X, inst, p1);
+  const T* pc = p1;
+  if (rig) {
+    pose_forward_t<T>(p1, rig, p2);
+    pc = p2;
+  }
+  const T d = radial ? sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]) : pc[2];
+  return (1.0 / std_dev) * (d - value);
+}
+
+// The same with its Jacobian rows: Jinst [6], Jrig [6] (zeros when
+// rig == null), Jpt [3]; chain rule through pose_jac as residual_jac.
+inline double depth_residual_jac(const double* inst, const double* rig, const double* X, double value,
+                                 double std_dev, bool radial, double* Jinst, double* Jrig, double* Jpt) {
+  const double scale = 1.0 / std_dev;
+  double p1[3], P1[27];
+  pose_jac(X, inst, p1, P1);
+  double pc[3], dX[9], dI[18], dR[18] = {0};
+  if (rig) {
+    double P2[27];
+    pose_jac(p1, rig, pc, P2);
+    for (int i = 0; i < 3; ++i) {
+      for (int j = 0; j < 3; ++j) {
+        double s = 0;
+        for (int k = 0; k < 3; ++k) s += P2[i * 9 + k] * P1[k * 9 + j];
+        dX[i * 3 + j] = s;
+      }
+      for (int j = 0; j < 6; ++j) {
+        double s = 0;
+        for (int k = 0; k < 3; ++k) s += P2[i * 9 + k] * P1[k * 9 + 3 + j];
+        dI[i * 6 + j] = s;
+        dR[i * 6 + j] = P2[i * 9 + 3 + j];
+      }
+    }
+  } else {
+    for (int i = 0; i < 3; ++i) {
+      pc[i] = p1[i];
+      for (int j = 0; j < 3; ++j) dX[i * 3 + j] = P1[i * 9 + j];
+      for (int j = 0; j < 6; ++j) dI[i * 6 + j] = P1[i * 9 + 3 + j];
+    }
+  }
+  double d, g[3];  // depth and d(depth)/d(pc)
+  if (radial) {
+    d = std::sqrt(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+    for (int k = 0; k < 3; ++k) g[k] = pc[k] / d;
+  } else {
+    d = pc[2];
+    g[0] = g[1] = 0.0;
+    g[2] = 1.0;
+  }
+  for (int j = 0; j < 3; ++j) Jpt[j] = scale * (g[0] * dX[j] + g[1] * dX[3 + j] + g[2] * dX[6 + j]);
+  for (int j = 0; j < 6; ++j) {
+    Jinst[j] = scale * (g[0] * dI[j] + g[1] * dI[6 + j] + g[2] * dI[12 + j]);
+    Jrig[j] = rig ? scale * (g[0] * dR[j] + g[1] * dR[6 + j] + g[2] * dR[12 + j]) : 0.0;
+  }
+  return scale * (d - value);
+}
+
+// ---------------------------------------------------------------------------
 // Robust losses rho(s), rho'(s), rho''(s) with s = |r|^2, following the
 // definitions in Ceres Solver's public documentation (LossFunction section):
 //   Trivial s; Huber(a): s <= a^2 ? s : 2a sqrt(s) - a^2;

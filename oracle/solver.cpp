@@ -101,6 +101,13 @@ struct OracleProblem {
   int32_t n_scales;
   const double* scales;
   const uint8_t* scale_free;
+  // depth priors of observations (RelativeDepthError, IRLS group DEPTH,
+  // under the projection loss): terms n_obs .. n_obs + n_depth - 1
+  int64_t n_depth;
+  const int64_t* depth_obs;     // [n] the observation it belongs to
+  const double* depth_value;    // [n]
+  const double* depth_std;      // [n]
+  const uint8_t* depth_radial;  // [n]
 };
 
 struct OracleOptions {
@@ -510,7 +517,7 @@ struct Solver {
     idx.scl.assign(std::max(0, P.n_scales), -1);
     for (int k = 0; k < P.n_scales; ++k)
       if (P.scale_free[k]) idx.scl[k] = idx.n++;
-    w_obs.assign(P.n_obs, 1.0);
+    w_obs.assign(n_terms(), 1.0);
     w_cam.assign(P.n_cameras, 1.0);
     w_rig.assign(P.n_rig_cameras, 1.0);
     for (int i = 0; i < P.n_instances; ++i)
@@ -634,8 +641,33 @@ struct Solver {
     for (auto& th : pool) th.join();
   }
 
-  // scaled residual of observation i at state s
+  // Residual terms: the observations, then the depth priors.
+  int64_t n_terms() const { return P.n_obs + std::max<int64_t>(0, P.n_depth); }
+  int64_t term_obs(int64_t i) const { return i < P.n_obs ? i : P.depth_obs[i - P.n_obs]; }
+  int term_point(int64_t i) const { return P.obs_point[term_obs(i)]; }
+
+  // depth prior k: the scaled residual and (when Ji) its Jacobian rows
+  double depth_term(const State& s, int64_t k, double* Ji = nullptr, double* Jr = nullptr, double* Jp = nullptr,
+                    bool* use_rig_out = nullptr) const {
+    const int64_t o = P.depth_obs[k];
+    const int sh = P.obs_shot[o];
+    const int rc = P.shot_rig[sh];
+    const bool use_rig = rc >= 0 && P.rig_used[rc];
+    if (use_rig_out) *use_rig_out = use_rig;
+    const double* inst = &s.inst[6 * P.shot_instance[sh]];
+    const double* rig = use_rig ? &s.rig[6 * rc] : nullptr;
+    const double* X = &s.pts[3 * P.obs_point[o]];
+    if (Ji) return depth_residual_jac(inst, rig, X, P.depth_value[k], P.depth_std[k], P.depth_radial[k] != 0, Ji, Jr, Jp);
+    return depth_residual_generic<double>(inst, rig, X, P.depth_value[k], P.depth_std[k], P.depth_radial[k] != 0);
+  }
+
+  // scaled residual of term i at state s
   int obs_residual(const State& s, int64_t i, double* r) const {
+    if (i >= P.n_obs) {
+      r[0] = depth_term(s, i - P.n_obs);
+      r[1] = r[2] = 0.0;
+      return 1;
+    }
     const int sh = P.obs_shot[i];
     const int cam = P.shot_camera[sh];
     const int model = P.camera_model[cam];
@@ -663,9 +695,11 @@ struct Solver {
     return C;
   }
 
+  // resid: [terms][3] when given (sized for every term or for the
+  // observations only)
   double cost(const State& s, std::vector<double>* resid) const {
     std::vector<double> part(threads, 0.0);
-    par(P.n_obs, [&](int64_t i, int t) {
+    par(n_terms(), [&](int64_t i, int t) {
       double r[3] = {0, 0, 0};
       const int nr = obs_residual(s, i, r);
       double sq = 0.0;
@@ -673,7 +707,7 @@ struct Solver {
       double rho[3];
       loss_eval(O.loss, O.loss_threshold, sq, rho);
       part[t] += 0.5 * w_obs[i] * rho[0];
-      if (resid)
+      if (resid && resid->size() >= size_t(3 * (i + 1)))
         for (int k = 0; k < 3; ++k) (*resid)[3 * i + k] = r[k];
     });
     double c = 0.0;
@@ -744,10 +778,12 @@ struct Solver {
 
   void linearize(const State& s) {
     const int n = idx.n;
-    lin.assign(P.n_obs, ObsLin());
-    par(P.n_obs, [&](int64_t i, int) {
+    lin.assign(n_terms(), ObsLin());
+    par(n_terms(), [&](int64_t i, int) {
       ObsLin& L = lin[i];
-      const int sh = P.obs_shot[i];
+      const int64_t o = term_obs(i);
+      const bool depth = i >= P.n_obs;
+      const int sh = P.obs_shot[o];
       const int cam = P.shot_camera[sh];
       const int model = P.camera_model[cam];
       const int C = model_desc(model).n_params;
@@ -755,9 +791,15 @@ struct Solver {
       const int rc = P.shot_rig[sh];
       const bool use_rig = rc >= 0 && P.rig_used[rc];
       double r[3] = {0, 0, 0}, Jc[48] = {0}, Ji[18] = {0}, Jr[18] = {0}, Jp[9] = {0};
-      residual_jac(model, &s.cam[16 * cam], &s.inst[6 * inst], use_rig ? &s.rig[6 * rc] : nullptr,
-                   &s.pts[3 * P.obs_point[i]], P.obs_xy + 2 * i, P.obs_std[i], r, Jc, Ji, Jr, Jp);
-      const int nr = residual_size(model);
+      int nr;
+      if (depth) {
+        r[0] = depth_term(s, i - P.n_obs, Ji, Jr, Jp);
+        nr = 1;
+      } else {
+        residual_jac(model, &s.cam[16 * cam], &s.inst[6 * inst], use_rig ? &s.rig[6 * rc] : nullptr,
+                     &s.pts[3 * P.obs_point[o]], P.obs_xy + 2 * o, P.obs_std[o], r, Jc, Ji, Jr, Jp);
+        nr = residual_size(model);
+      }
       L.nr = nr;
       // gather camera-side columns
       int m = 0;
@@ -771,7 +813,7 @@ struct Solver {
       for (int k = 0; k < 6; ++k) add_col(idx.inst[6 * inst + k], Ji, 6, k);
       if (use_rig)
         for (int k = 0; k < 6; ++k) add_col(idx.rig[6 * rc + k], Jr, 6, k);
-      if (model != SPHERICAL)
+      if (model != SPHERICAL && !depth)
         for (int k = 0; k < C; ++k) add_col(idx.cam[16 * cam + k], Jc, C, k);
       L.m = m;
       // robust correction
@@ -797,7 +839,7 @@ struct Solver {
       for (int k = 0; k < m; ++k) corr(&cols[0][k], 28);
       for (int a = 0; a < nr; ++a) {
         L.r[a] = rs * r[a];
-        for (int k = 0; k < 3; ++k) L.Jp[a * 3 + k] = P.point_free[P.obs_point[i]] ? Jp[a * 3 + k] : 0.0;
+        for (int k = 0; k < 3; ++k) L.Jp[a * 3 + k] = P.point_free[P.obs_point[o]] ? Jp[a * 3 + k] : 0.0;
         for (int k = 0; k < m; ++k) L.Jc[a * 28 + k] = cols[a][k];
       }
     });
@@ -805,9 +847,9 @@ struct Solver {
     g.assign(n, 0.0);
     V.assign(9 * P.n_points, 0.0);
     gp.assign(3 * P.n_points, 0.0);
-    for (int64_t i = 0; i < P.n_obs; ++i) {
+    for (int64_t i = 0; i < n_terms(); ++i) {
       const ObsLin& L = lin[i];
-      const int p = P.obs_point[i];
+      const int p = term_point(i);
       for (int a = 0; a < L.nr; ++a) {
         for (int k = 0; k < L.m; ++k) {
           g[L.col[k]] += L.Jc[a * 28 + k] * L.r[a];
@@ -933,15 +975,16 @@ struct Solver {
       I[8] = (A[0] * A[4] - A[1] * A[3]) / det;
     }
     // Schur complement, grouped by point
-    std::vector<int64_t> order(P.n_obs);
-    for (int64_t i = 0; i < P.n_obs; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t c) { return P.obs_point[a] < P.obs_point[c]; });
+    const int64_t nt = n_terms();
+    std::vector<int64_t> order(nt);
+    for (int64_t i = 0; i < nt; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t c) { return term_point(a) < term_point(c); });
     std::vector<int> wcol;
     std::vector<double> wval;  // [3] per entry: W = J_c^T J_p (entry per column)
-    for (int64_t a = 0; a < P.n_obs;) {
-      const int p = P.obs_point[order[a]];
+    for (int64_t a = 0; a < nt;) {
+      const int p = term_point(order[a]);
       int64_t e = a;
-      while (e < P.n_obs && P.obs_point[order[e]] == p) ++e;
+      while (e < nt && term_point(order[e]) == p) ++e;
       if (P.point_free[p]) {
         wcol.clear();
         wval.clear();
@@ -1007,9 +1050,9 @@ struct Solver {
     }
     // back-substitution
     std::vector<double> wd(3 * P.n_points, 0.0);
-    for (int64_t i = 0; i < P.n_obs; ++i) {
+    for (int64_t i = 0; i < nt; ++i) {
       const ObsLin& L = lin[i];
-      const int p = P.obs_point[i];
+      const int p = term_point(i);
       for (int r = 0; r < L.nr; ++r) {
         double t = 0.0;
         for (int k = 0; k < L.m; ++k) t += L.Jc[r * 28 + k] * dc[L.col[k]];
@@ -1026,9 +1069,9 @@ struct Solver {
     }
     // linear model decrease
     double mc = 0.0;
-    for (int64_t i = 0; i < P.n_obs; ++i) {
+    for (int64_t i = 0; i < nt; ++i) {
       const ObsLin& L = lin[i];
-      const int p = P.obs_point[i];
+      const int p = term_point(i);
       for (int r = 0; r < L.nr; ++r) {
         double t = 0.0;
         for (int k = 0; k < L.m; ++k) t += L.Jc[r * 28 + k] * dc[L.col[k]];
@@ -1205,18 +1248,20 @@ struct Solver {
   }
 
   double reweight(const State& s) {
-    std::vector<double> resid(3 * P.n_obs);
+    std::vector<double> resid(3 * n_terms());
     cost(s, &resid);
     double total = 0.0;
-    // projection groups: one per shot, plus GCP2D
-    std::vector<std::vector<int64_t>> groups(P.n_shots + 1);
+    // projection groups: one per shot, plus GCP2D; then DEPTH
+    // (bundle_adjuster.cc:559-562,599-602)
+    std::vector<std::vector<int64_t>> groups(P.n_shots + 2);
     for (int64_t i = 0; i < P.n_obs; ++i) groups[P.obs_gcp[i] ? P.n_shots : P.obs_shot[i]].push_back(i);
+    for (int64_t i = P.n_obs; i < n_terms(); ++i) groups[P.n_shots + 1].push_back(i);
     for (auto& grp : groups) {
       std::vector<std::vector<double>> res;
       std::vector<double*> w;
       for (int64_t i : grp) {
-        const int model = P.camera_model[P.shot_camera[P.obs_shot[i]]];
-        const int nr = residual_size(model);
+        const int model = P.camera_model[P.shot_camera[P.obs_shot[term_obs(i)]]];
+        const int nr = i >= P.n_obs ? 1 : residual_size(model);
         res.emplace_back(&resid[3 * i], &resid[3 * i] + nr);
         w.push_back(&w_obs[i]);
       }
@@ -1321,6 +1366,16 @@ extern "C" double oracle_mixture_group(int k, int64_t n, const double* residuals
   return Solver::mixture(res, w, density_ratio);
 }
 
+// One depth prior's scaled residual and its Jacobian rows: d/d instance
+// pose [6], d/d rig camera pose [6] (rig_camera_pose null: not composed,
+// zeros), d/d point [3].
+extern "C" double oracle_depth_residual(const double* instance_pose, const double* rig_camera_pose,
+                                        const double* point, double value, double std_dev, int radial,
+                                        double* jac_instance, double* jac_rig, double* jac_point) {
+  return depth_residual_jac(instance_pose, rig_camera_pose, point, value, std_dev, radial != 0, jac_instance, jac_rig,
+                            jac_point);
+}
+
 // One orientation constraint's scaled residuals and Jacobian [m][6]
 // (d/d instance rotation, d/d rig camera rotation); returns m.
 extern "C" int oracle_orientation_residual(int kind, const double* target, double std_dev, const double* ri,
@@ -1382,6 +1437,8 @@ extern "C" int oracle_solve(const OracleProblem* Pp, const OracleOptions* Op, Or
   for (int64_t i = 0; i < P.n_obs; ++i)
     if (P.obs_shot[i] < 0 || P.obs_shot[i] >= P.n_shots || P.obs_point[i] < 0 || P.obs_point[i] >= P.n_points)
       return -1;
+  for (int64_t k = 0; k < P.n_depth; ++k)
+    if (P.depth_obs[k] < 0 || P.depth_obs[k] >= P.n_obs || !(P.depth_std[k] > 0.0)) return -1;
   Solver S(P, O);
   State x;
   x.cam.assign(P.camera_values, P.camera_values + 16 * P.n_cameras);

@@ -34,13 +34,20 @@ CASES = {
     "ring_irls_fp64": dict(scene=lambda: syn.ring_scene(n_points=2000, outlier_ratio=0.03, seed=5),
                            kw=dict(precision="fp64", irls="mixture", gps=False, max_iterations=40,
                                    pcg_tolerance=1e-10, linear_solver="ITERATIVE_SCHUR")),
+    # depth priors ride with their points' observations on the rank that
+    # holds the point
+    "ring_depth_fp64": dict(scene=lambda: syn.ring_scene(n_points=2000, seed=9),
+                            depth=lambda s: syn.depth_priors(s, fraction=0.3, std=0.05, noise=0.02, seed=10),
+                            kw=dict(precision="fp64", loss=("HuberLoss", 1.0), irls="none", gps=False,
+                                    max_iterations=30, pcg_tolerance=1e-10, linear_solver="ITERATIVE_SCHUR")),
 }
 
 
 def _solve(case, rank=0, world=1, allreduce=None):
     c = CASES[case]
     scene = c["scene"]()
-    ba = pybundle.adjuster_from_scene(scene, **c["kw"])
+    depth = c["depth"](scene) if "depth" in c else None
+    ba = pybundle.adjuster_from_scene(scene, depth=depth, **c["kw"])
     if world > 1:
         ba.set_shard(rank, world, allreduce)
     ba.run()
@@ -123,7 +130,7 @@ def test_fp64_sharded_solve_follows_single_rank_trajectory():
     assert shard[0]["range"][1] == shard[1]["range"][0]
 
 
-@pytest.mark.parametrize("case,bar", [("aerial_gps_mixed", 1e-6), ("ring_irls_fp64", 1e-6)])
+@pytest.mark.parametrize("case,bar", [("aerial_gps_mixed", 1e-6), ("ring_irls_fp64", 1e-6), ("ring_depth_fp64", 1e-9)])
 def test_sharded_final_cost_matches_single_rank(case, bar):
     single = _solve(case)
     shard = _sharded(case)

@@ -100,8 +100,6 @@ def test_density_ratio_settings(ba):
 def test_unsupported_constraints_raise(ba):
     ba.add_rig_instance("1", pygeometry.Pose(), {"s1": "cam1"}, {"s1": "rig_cam1"}, False)
     ba.add_point("p", np.zeros(3), False)
-    with pytest.raises(NotImplementedError):
-        ba.add_point_projection_observation("s1", "p", np.zeros(2), 1.0, False, depth_prior=object())
     # the gauge fix looks the origin shot up at once (bundle_adjuster.cc:391)
     with pytest.raises(IndexError):
         ba.set_gauge_fix_shots("a", "b")
