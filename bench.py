@@ -322,7 +322,7 @@ def street_benchmark(n_shots: int = 500, n_points: int = 200_000, seed: int = 7,
                      "iterations": s["iterations"], "final_cost": s["final_cost"],
                      "final_rel_to_exact": (s["final_cost"] - c64) / c64, "solve_s": s["seconds"],
                      "run_wall_s": wall, "unsuccessful_steps": int(s["unsuccessful_steps"]),
-                     "dense_failures": int(s["linear_solver_failures"]), "linear_solver": s["linear_solver"],
+                     "dense_failures": int(s["linear_solver_failures"]),
                      "pcg_iterations": int(tr[:, 4].sum()), "inlier_rms_px": rms_px(errs, inl)}
     out["target_cost"] = target
     out["exact_run_to_run_rel"] = abs(runs["exact_fp64_repeat"][0]["final_cost"] - c64) / c64
