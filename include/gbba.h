@@ -226,9 +226,23 @@ void gbba_destroy(gbba_adjuster_t* h);
 int gbba_add_camera(gbba_adjuster_t* h, const char* id, int projection, const double* values,
                     const double* prior_values, int n_values, int constant);
 /* SetCameraBias (bundle_adjuster.cc:131-140): similarity applied to the GPS
- * priors of instances whose reference camera is camera_id (held fixed). */
+ * priors of instances whose reference camera is camera_id
+ * (SimilarityPriorTransform, bias.h:34-54: prior -> scale R(rotation) prior
+ * + translation).  Its parameters stay fixed unless
+ * gbba_set_camera_bias_parameters names some. */
 int gbba_set_camera_bias(gbba_adjuster_t* h, const char* camera_id, const double* rotation,
                          const double* translation, double scale);
+/* SetCameraBias's parameters_to_optimize (bundle_adjuster.cc:131-140,
+ * pybind.cc:68-70): indices of Similarity::Parameter (0-2 rotation, 3-5
+ * translation, 6 scale; bias.h:12), n = 0 to hold the bias fixed.  The GPS
+ * priors of the instances referencing the camera then optimise the bias
+ * with the poses (DataPriorError with SimilarityPriorTransform,
+ * bundle_adjuster.cc:806-838); gbba_get_bias reads the solved bias. */
+int gbba_set_camera_bias_parameters(gbba_adjuster_t* h, const char* camera_id, const int* indices, int n);
+/* GetBias (bundle_adjuster.cc:1317-1323): rotation[3] (angle-axis),
+ * translation[3], scale. */
+int gbba_get_bias(const gbba_adjuster_t* h, const char* camera_id, double* rotation, double* translation,
+                  double* scale);
 /* AddRigCamera (bundle_adjuster.cc:179-198). */
 int gbba_add_rig_camera(gbba_adjuster_t* h, const char* id, const double* pose, const double* pose_prior,
                         int fixed);
@@ -359,7 +373,11 @@ int gbba_set_adjust_absolute_position_std(gbba_adjuster_t* h, int adjust);
  * [49], scale_i, scale_j; rig camera poses unused; the scales' columns are
  * 24 and 25), 6 adjusted GPS prior (params: prior[3], std[3], multiplier;
  * one instance pose; the multiplier's column is 24), 7 std-multiplier
- * regulariser (params: multiplier; no pose; column 24).  instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
+ * regulariser (params: multiplier; no pose; column 24), 8 the GPS prior of
+ * kind 6 through an optimised camera bias (params: prior[3], std[3],
+ * multiplier, bias rotation[3], translation[3], scale; the bias rotation
+ * and translation's columns are 6..11, its scale's 25).
+ * instance_poses[n][6] and rig_camera_poses[n][6] (NULL: no rig
  * cameras) for the n = 2 (3 for linear motion) shots, [rx ry rz tx ty tz]
  * with t the position.  Writes m = 3 (6 for linear motion, 1 for the gauge
  * scale and the regulariser, 7 for a relative motion) residuals, J[m][36]

@@ -102,6 +102,29 @@ void BundleAdjuster::SetCameraBias(const std::string& camera, const double* rota
   b.s = scale;
 }
 
+void BundleAdjuster::SetCameraBiasParameters(const std::string& camera, const int* indices, int n) {
+  auto it = camera_index_.find(camera);
+  if (it == camera_index_.end()) throw std::runtime_error("Camera " + camera + " doesn't exist.");
+  uint8_t mask[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < n; ++i) {
+    if (indices[i] < 0 || indices[i] > 6) throw std::invalid_argument("bias parameter index out of range [0, 6]");
+    mask[indices[i]] = 1;
+  }
+  Bias& b = problem_.biases[it->second];
+  for (int k = 0; k < 7; ++k) b.free_mask[k] = mask[k];
+}
+
+void BundleAdjuster::GetBias(const std::string& camera, double* rotation, double* translation, double* scale) const {
+  auto it = camera_index_.find(camera);
+  if (it == camera_index_.end()) throw std::runtime_error("Camera " + camera + " doesn't exist.");
+  const Bias& b = problem_.biases[it->second];
+  for (int k = 0; k < 3; ++k) {
+    rotation[k] = b.r[k];
+    translation[k] = b.t[k];
+  }
+  *scale = b.s;
+}
+
 void BundleAdjuster::AddRigCamera(const std::string& id, const double* pose, const double* prior, bool fixed) {
   if (rig_camera_index_.count(id)) throw std::runtime_error("Rig model " + id + " already exist.");
   PoseBlock b;
@@ -387,11 +410,21 @@ void BundleAdjuster::Run() {
     for (size_t i = 0; i < sub.instances.size(); ++i) problem_.instances[i] = sub.instances[i];
     for (int64_t p = p0; p < p1; ++p) problem_.points[size_t(p)] = sub.points[size_t(p - p0)];
   }
-  // the solved reconstruction scales, then the rig cameras without the
-  // scale blocks again
-  for (const ScaleBlock& b : scale_blocks_)
+  // the solved reconstruction scales and camera biases, then the rig
+  // cameras without the scale blocks again
+  for (const ScaleBlock& b : scale_blocks_) {
     if (b.reconstruction_scale)
       reconstructions_.at(b.reconstruction).scales[b.instance] = problem_.rig_cameras[b.block].value[0];
+    if (b.bias_camera >= 0) {
+      Bias& bs = problem_.biases[size_t(b.bias_camera)];
+      const PoseBlock& pose = problem_.rig_cameras[size_t(b.block)];
+      for (int k = 0; k < 3; ++k) {
+        bs.r[k] = pose.value[k];
+        bs.t[k] = pose.value[3 + k];
+      }
+      bs.s = problem_.rig_cameras[size_t(b.block) + 1].value[0];
+    }
+  }
   DropScaleBlocks();
   if (opts_.compute_reprojection_errors && shard) {
     // this rank's observations; the others' are NaN here
@@ -759,14 +792,66 @@ void BundleAdjuster::PrepareRun() {
     }
     any_rotation = true;  // the relative-motion loss is needed
   }
-  if (adjust_position_std_) {
-    // one std multiplier per scale group of the GPS priors, starting at 1;
-    // the priors become host terms divided by it, and each multiplier gets
-    // StdDeviationConstraint (bundle_adjuster.cc:772-838)
-    std::map<int, int> group_block;
-    for (size_t i = 0; i < problem_.instances.size(); ++i) {
-      PoseBlock& b = problem_.instances[i];
-      if (!b.has_position_prior) continue;
+  // GPS priors as host terms: every prior when the std multipliers are
+  // adjusted (one per scale group, starting at 1, each with a
+  // StdDeviationConstraint, bundle_adjuster.cc:772-838), and the priors
+  // whose reference camera has an optimised bias (its rotation and
+  // translation a six-coordinate block, its scale a one-coordinate block,
+  // both after the rig cameras; SimilarityPriorTransform, bias.h:34-54).
+  std::map<int, int> group_block;
+  std::map<int, int> bias_block;
+  auto bias_block_of = [&](int cam) -> int {
+    auto it = bias_block.find(cam);
+    if (it != bias_block.end()) return it->second;
+    const Bias& bs = problem_.biases[size_t(cam)];
+    PoseBlock pose, scale;
+    for (int k = 0; k < 3; ++k) {
+      pose.value[k] = bs.r[k];
+      pose.value[3 + k] = bs.t[k];
+    }
+    for (int k = 0; k < 6; ++k) pose.free_mask[k] = bs.free_mask[k];
+    scale.value[0] = bs.s;
+    scale.free_mask[0] = bs.free_mask[6];
+    for (PoseBlock* b : {&pose, &scale}) {
+      b->has_prior = false;
+      b->used = true;
+      b->scale_block = true;
+    }
+    const int block = int(problem_.rig_cameras.size());
+    problem_.rig_cameras.push_back(pose);
+    problem_.rig_cameras.push_back(scale);
+    ScaleBlock sb;
+    sb.block = block;
+    sb.reconstruction_scale = false;
+    sb.bias_camera = cam;
+    scale_blocks_.push_back(sb);
+    bias_block.emplace(cam, block);
+    return block;
+  };
+  // (when some prior takes an optimised bias, every GPS prior becomes a host
+  // term, so that they stay one IRLS group "GPS" as in the reference)
+  bool any_biased = false;
+  for (const PoseBlock& b : problem_.instances)
+    any_biased |= b.has_position_prior && b.bias_camera >= 0 && problem_.biases[size_t(b.bias_camera)].optimised();
+  for (size_t i = 0; i < problem_.instances.size(); ++i) {
+    PoseBlock& b = problem_.instances[i];
+    if (!b.has_position_prior) continue;
+    const bool biased = b.bias_camera >= 0 && problem_.biases[size_t(b.bias_camera)].optimised();
+    if (!adjust_position_std_ && !any_biased) continue;
+    RelativeTerm t;
+    t.kind = RelativeTerm::kGpsStd;
+    t.n_shots = 1;
+    t.instance[0] = int(i);
+    for (int k = 0; k < 3; ++k) {
+      t.prior[k] = b.position_prior[k];
+      t.prior_scale[k] = 1.0 / std::max(b.position_sigma[k], std::numeric_limits<double>::epsilon());
+    }
+    t.bias_camera = b.bias_camera;
+    if (biased) {
+      t.bias_block[0] = bias_block_of(b.bias_camera);
+      t.bias_block[1] = t.bias_block[0] + 1;
+    }
+    if (adjust_position_std_) {
       auto g = group_block.find(b.scale_group);
       if (g == group_block.end()) {
         PoseBlock pb;
@@ -780,27 +865,18 @@ void BundleAdjuster::PrepareRun() {
         scale_blocks_.push_back({"", "", block, false});
         g = group_block.emplace(b.scale_group, block).first;
       }
-      RelativeTerm t;
-      t.kind = RelativeTerm::kGpsStd;
-      t.n_shots = 1;
-      t.instance[0] = int(i);
-      for (int k = 0; k < 3; ++k) {
-        t.prior[k] = b.position_prior[k];
-        t.prior_scale[k] = 1.0 / std::max(b.position_sigma[k], std::numeric_limits<double>::epsilon());
-      }
-      t.bias_camera = b.bias_camera;
       t.scale_block[0] = g->second;
-      problem_.relative_terms.push_back(t);
-      b.has_position_prior = false;  // the diagonal GPS prior is replaced
-      moved_priors_.push_back(int(i));
     }
-    for (const auto& gb : group_block) {
-      RelativeTerm t;
-      t.kind = RelativeTerm::kStdDeviation;
-      t.n_shots = 0;
-      t.scale_block[0] = gb.second;
-      problem_.relative_terms.push_back(t);
-    }
+    problem_.relative_terms.push_back(t);
+    b.has_position_prior = false;  // the diagonal GPS prior is replaced
+    moved_priors_.push_back(int(i));
+  }
+  for (const auto& gb : group_block) {
+    RelativeTerm t;
+    t.kind = RelativeTerm::kStdDeviation;
+    t.n_shots = 0;
+    t.scale_block[0] = gb.second;
+    problem_.relative_terms.push_back(t);
   }
   if (any_rotation) {
     // CreateLossFunction (bundle_adjuster.cc:485-499)

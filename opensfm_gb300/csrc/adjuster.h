@@ -91,6 +91,14 @@ class BundleAdjuster {
   void AddObservationsBulk(int64_t n, const int32_t* shot, const int32_t* point, const double* xy,
                            const double* std_dev, const uint8_t* is_gcp);
   void SetCameraBias(const std::string& camera, const double* rotation, const double* translation, double scale);
+  // SetCameraBias's parameters_to_optimize (bundle_adjuster.cc:131-140):
+  // indices of Similarity::Parameter (RX RY RZ TX TY TZ SCALE, bias.h:12);
+  // the GPS priors of the instances referencing the camera then take the
+  // bias as unknowns (DataPriorError with SimilarityPriorTransform,
+  // :806-838)
+  void SetCameraBiasParameters(const std::string& camera, const int* indices, int n);
+  // GetBias (bundle_adjuster.cc:1317-1323): rotation[3], translation[3], scale
+  void GetBias(const std::string& camera, double* rotation, double* translation, double* scale) const;
 
   // settings (bundle_adjuster.cc:400-483, pybundle.pyi:131)
   void SetPointProjectionLossFunction(const std::string& name, double threshold);
@@ -219,6 +227,7 @@ class BundleAdjuster {
     std::string reconstruction, instance;  // empty for a GPS std multiplier
     int block;
     bool reconstruction_scale = true;
+    int bias_camera = -1;  // >= 0: the camera's optimised bias (pose block; scale block = block + 1)
   };
   std::vector<ScaleBlock> scale_blocks_;
   bool adjust_position_std_ = false;

@@ -80,6 +80,24 @@ int gbba_set_camera_bias(gbba_adjuster_t* h, const char* camera_id, const double
   });
 }
 
+int gbba_set_camera_bias_parameters(gbba_adjuster_t* h, const char* camera_id, const int* indices, int n) {
+  return guarded([&] {
+    if (n < 0) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "negative bias parameter count");
+    if (n > 0) need(indices, "indices");
+    ba_of(h).SetCameraBiasParameters(str(camera_id), indices, n);
+  });
+}
+
+int gbba_get_bias(const gbba_adjuster_t* h, const char* camera_id, double* rotation, double* translation,
+                  double* scale) {
+  return guarded([&] {
+    need(rotation, "rotation");
+    need(translation, "translation");
+    need(scale, "scale");
+    ba_of(h).GetBias(str(camera_id), rotation, translation, scale);
+  });
+}
+
 int gbba_add_rig_camera(gbba_adjuster_t* h, const char* id, const double* pose, const double* pose_prior, int fixed) {
   return guarded([&] {
     need(pose, "pose");
@@ -281,9 +299,13 @@ int gbba_add_relative_motion(gbba_adjuster_t* h, const char* instance_i, const c
 int gbba_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                            const double* params, double* residuals, double* jacobian, int* n_residuals) {
   return guarded([&] {
-    if (kind < 0 || kind > 7 || kind == 4 || !params || !residuals || !jacobian || !n_residuals ||
+    if (kind < 0 || kind > 8 || kind == 4 || !params || !residuals || !jacobian || !n_residuals ||
         (kind != 7 && !instance_poses))
       throw gbba::ApiError(GBBA_ERR_INVALID_ARGUMENT, "gbba_relative_residual: invalid argument");
+    // kind 8: the GPS prior of kind 6 through an optimised camera bias
+    const bool biased = kind == 8;
+    if (biased) kind = gbba::RelativeTerm::kGpsStd;
+    double bias[7] = {0, 0, 0, 0, 0, 0, 1};
     gbba::RelativeTerm t;
     t.kind = kind;
     t.n_shots = kind == gbba::RelativeTerm::kLinearMotion ? 3
@@ -312,6 +334,8 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
         t.prior_scale[k] = 1.0 / std::max(params[3 + k], std::numeric_limits<double>::epsilon());
       }
       scales[0] = params[6];
+      if (biased)
+        for (int k = 0; k < 7; ++k) bias[k] = params[7 + k];
     } else if (kind == gbba::RelativeTerm::kStdDeviation) {
       scales[0] = params[0];
     } else {
@@ -326,7 +350,7 @@ int gbba_relative_residual(int kind, const double* instance_poses, const double*
       pc[k] = rig_camera_poses ? rig_camera_poses + 6 * k : nullptr;
     }
     gbba::orient::Dual<36> r[7];
-    const int m = gbba::orient::relative_residuals<36>(t, pi, pc, r, scales);
+    const int m = gbba::orient::relative_residuals<36>(t, pi, pc, r, scales, biased ? bias : nullptr);
     for (int q = 0; q < m; ++q) {
       residuals[q] = r[q].v;
       for (int k = 0; k < 36; ++k) jacobian[36 * q + k] = r[q].d[k];

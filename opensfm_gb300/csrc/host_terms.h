@@ -96,10 +96,15 @@ struct RelativeTerm {
   bool observed_scale = false;
   double loss_scale = 1.0;
   int scale_block[2] = {-1, -1};
-  // adjusted GPS: the position prior (bias applied) and 1 / std per axis;
-  // the group's std multiplier is slot 24
+  // GPS prior as a host term (the std multiplier of its scale group, or an
+  // optimised camera bias): the position prior and 1 / std per axis; the
+  // group's std multiplier is slot 24 (scale_block[0] < 0: none).  With a
+  // fixed bias the prior is taken through it as a constant; an optimised
+  // bias is read from bias_block[0] (rotation, translation: slots 6..11)
+  // and bias_block[1] (scale: slot 25).
   double prior[3] = {0, 0, 0}, prior_scale[3] = {1, 1, 1};
   int bias_camera = -1;
+  int bias_block[2] = {-1, -1};
 };
 
 namespace orient {
@@ -377,15 +382,29 @@ inline double bicubic(const HeatmapGrid& g, double r, double c, double* dfdr, do
 // count.
 template <int N>
 inline int relative_residuals(const RelativeTerm& t, const double* const* pi, const double* const* pc, Dual<N>* r,
-                              const double* scales = nullptr) {
+                              const double* scales = nullptr, const double* bias = nullptr) {
   ShotPose<N> s[3];
   for (int k = 0; k < t.n_shots; ++k) s[k] = shot_pose<N>(k, pi[k], t.kind == RelativeTerm::kRelativeMotion ? nullptr : pc[k]);
   switch (t.kind) {
     case RelativeTerm::kGpsStd: {
-      // (t_k - prior_k) / (std_k m) on the instance position
+      // (t_k - prior_k) / (std_k m) on the instance position; with an
+      // optimised bias (angle-axis w, translation b, scale c) the prior is
+      // c R(w) p + b (SimilarityPriorTransform, bias.h:34-54)
       const Dual<N> m = var<N>(scales[0], 24);
-      for (int k = 0; k < 3; ++k)
-        r[k] = Dual<N>(t.prior_scale[k]) * (s[0].position[k] - Dual<N>(t.prior[k])) / m;
+      Dual<N> prior[3];
+      if (bias) {
+        Dual<N> w[3], p[3], rp[3];
+        for (int k = 0; k < 3; ++k) {
+          w[k] = var<N>(bias[k], 6 + k);
+          p[k] = Dual<N>(t.prior[k]);
+        }
+        rotate(w, p, rp);
+        const Dual<N> c = var<N>(bias[6], 25);
+        for (int k = 0; k < 3; ++k) prior[k] = c * rp[k] + var<N>(bias[3 + k], 9 + k);
+      } else {
+        for (int k = 0; k < 3; ++k) prior[k] = Dual<N>(t.prior[k]);
+      }
+      for (int k = 0; k < 3; ++k) r[k] = Dual<N>(t.prior_scale[k]) * (s[0].position[k] - prior[k]) / m;
       return 3;
     }
     case RelativeTerm::kStdDeviation: {

@@ -67,6 +67,15 @@ struct Bias {
   double r[3] = {0, 0, 0};
   double t[3] = {0, 0, 0};
   double s = 1.0;
+  // the parameters the run optimises (SetCameraBias's
+  // parameters_to_optimize, Similarity::Parameter order RX RY RZ TX TY TZ
+  // SCALE); none by default (AddCamera, bundle_adjuster.cc:121-128)
+  uint8_t free_mask[7] = {0, 0, 0, 0, 0, 0, 0};
+  bool optimised() const {
+    for (uint8_t f : free_mask)
+      if (f) return true;
+    return false;
+  }
 };
 
 struct Shot {

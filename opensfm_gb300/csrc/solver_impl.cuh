@@ -1627,12 +1627,25 @@ void DeviceSolver<R>::host_term(int q, const std::vector<double>& x, HostTermLin
                        : (t.kind == RelativeTerm::kGpsStd || t.kind == RelativeTerm::kStdDeviation) ? 1
                                                                                                      : 0;
   for (int k = 0; k < n_scales; ++k) {
+    if (t.scale_block[k] < 0) continue;  // a GPS prior without a std multiplier: 1
     const int sb = cl_.rig_base + 8 * t.scale_block[k];
     scales[k] = x[sb];
     L.coord[24 + k] = coord_of(sb);
   }
   orient::Dual<N> r[7];
-  if (t.kind == RelativeTerm::kGpsStd && t.bias_camera >= 0) {
+  if (t.kind == RelativeTerm::kGpsStd && t.bias_block[0] >= 0) {
+    // optimised camera bias: rotation and translation in slots 6..11, the
+    // scale in slot 25
+    const int pb = cl_.rig_base + 8 * t.bias_block[0], sb = cl_.rig_base + 8 * t.bias_block[1];
+    double bias[7];
+    for (int k = 0; k < 6; ++k) {
+      bias[k] = x[pb + k];
+      L.coord[6 + k] = coord_of(pb + k);
+    }
+    bias[6] = x[sb];
+    L.coord[25] = coord_of(sb);
+    L.m = orient::relative_residuals<N>(t, pi, pc, r, scales, bias);
+  } else if (t.kind == RelativeTerm::kGpsStd && t.bias_camera >= 0) {
     // the prior through the camera bias, as the diagonal GPS prior takes it
     RelativeTerm tb = t;
     const Bias& bs = P.biases[t.bias_camera];

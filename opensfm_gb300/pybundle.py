@@ -21,7 +21,7 @@ from typing import Dict, Optional
 import numpy as np
 
 from . import _lib
-from .pygeometry import Camera, Pose
+from .pygeometry import Camera, Pose, Similarity
 
 _D = C.POINTER(C.c_double)
 _I32 = C.POINTER(C.c_int32)
@@ -48,6 +48,8 @@ def _declare(L) -> None:
         "gbba_destroy": ([_H], None),
         "gbba_add_camera": ([_H, S, C.c_int, _D, _D, C.c_int, C.c_int], C.c_int),
         "gbba_set_camera_bias": ([_H, S, _D, _D, C.c_double], C.c_int),
+        "gbba_set_camera_bias_parameters": ([_H, S, _I32, C.c_int], C.c_int),
+        "gbba_get_bias": ([_H, S, _D, _D, C.POINTER(C.c_double)], C.c_int),
         "gbba_add_rig_camera": ([_H, S, _D, _D, C.c_int], C.c_int),
         "gbba_add_rig_instance": ([_H, S, _D, C.c_int, C.POINTER(S), C.POINTER(S), C.POINTER(S), C.c_int], C.c_int),
         "gbba_add_rig_instance_position_prior": ([_H, S, _D, _D, S], C.c_int),
@@ -277,14 +279,20 @@ class BundleAdjuster:
         return cam
 
     def set_camera_bias(self, id: str, bias, parameters_to_optimize=()) -> None:
-        if parameters_to_optimize:
-            raise NotImplementedError("optimising camera biases is not implemented by the GPU bundle adjuster")
+        """SetCameraBias (bundle_adjuster.cc:131-140): the bias (a
+        ``pygeometry.Similarity``, or any object with rotation, translation
+        and scale) and the indices of the parameters the run optimises
+        (0-2 rotation, 3-5 translation, 6 scale)."""
         r = _vec(bias.rotation, 3)
         t = _vec(bias.translation, 3)
         self._check(self._L.gbba_set_camera_bias(self._h, _b(id), _dp(r), _dp(t), float(bias.scale)))
+        idx = np.ascontiguousarray([int(i) for i in parameters_to_optimize], np.int32)
+        self._check(self._L.gbba_set_camera_bias_parameters(self._h, _b(id), idx.ctypes.data_as(_I32), len(idx)))
 
-    def get_bias(self, id: str):
-        raise NotImplementedError("get_bias: camera biases are held fixed by the GPU bundle adjuster")
+    def get_bias(self, id: str) -> Similarity:
+        r, t, s = np.zeros(3), np.zeros(3), C.c_double(1.0)
+        self._check(self._L.gbba_get_bias(self._h, _b(id), _dp(r), _dp(t), C.byref(s)))
+        return Similarity(r, t, s.value)
 
     def add_rig_camera(self, id: str, pose: Pose, pose_prior: Pose, fixed: bool) -> None:
         a = np.ascontiguousarray(pose.ba_data())
@@ -725,7 +733,7 @@ def orientation_residual(kind: str, target, std_deviation: float, instance_rotat
 
 
 RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3,
-                  "relative_motion": 5, "gps_std": 6, "std_deviation": 7}
+                  "relative_motion": 5, "gps_std": 6, "std_deviation": 7, "gps_bias": 8}
 
 
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
@@ -736,7 +744,8 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None):
     std-adjusted GPS prior (prior_error.h:54-93) or StdDeviationConstraint
     (parameters_errors.h:7-16).  Poses [n][6] as [rx ry rz tx ty tz] with t
     the position (None for the std regulariser); params as
-    gbba_relative_residual takes them."""
+    gbba_relative_residual takes them ("gps_bias": the GPS prior through an
+    optimised camera bias, prior[3], std[3], multiplier, bias[7])."""
     L = _lib.lib()
     _declare(L)
     pi = None if instance_poses is None else np.ascontiguousarray(instance_poses, dtype=np.float64)
@@ -770,11 +779,13 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
                         matrix_free: Optional[int] = None, covariances: bool = False, depth=None,
-                        rig_pose=None) -> BundleAdjuster:
+                        rig_pose=None, bias=None, point_priors=None) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path).  ``depth``:
     depth priors (observation indices, values, stds, radial flags);
     ``rig_pose``: a fixed rig camera pose (angle-axis, centre) shared by every
-    shot (None: the identity)."""
+    shot (None: the identity); ``bias``: (rotation, translation, scale,
+    parameters to optimise) of every camera's bias; ``point_priors``: (point
+    indices, positions, stds) with altitude."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
     if matrix_free is not None:
@@ -804,7 +815,13 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
         for s in range(len(scene.shot_camera)):
             ba.add_rig_instance_position_prior(str(int(scene.shot_rig_instance[s])), scene.extras["gps"][s],
                                                scene.extras["gps_std"][s], "")
+    if bias is not None:
+        for c in range(len(scene.camera_projection)):
+            ba.set_camera_bias(str(c), Similarity(bias[0], bias[1], bias[2]), bias[3])
     ba.add_points(scene.points)
+    if point_priors is not None:
+        for k, pos, sd in zip(np.asarray(point_priors[0]), np.asarray(point_priors[1]), np.asarray(point_priors[2])):
+            ba.add_point_prior(str(int(k)), pos, sd, True)
     ba.add_point_projection_observations(scene.obs_shot, scene.obs_point, scene.obs_xy, scene.obs_std)
     if depth is not None:
         ba.set_depth_priors(*depth)

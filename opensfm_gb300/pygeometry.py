@@ -197,6 +197,27 @@ class Camera:
         return self.__copy__()
 
 
+class Similarity:
+    """geometry::Similarity (geometry/similarity.h): x -> scale R x +
+    translation, R given as an angle-axis ``rotation``; the camera bias of
+    the bundle adjuster (bundle/data/bias.h)."""
+
+    def __init__(self, rotation=None, translation=None, scale: float = 1.0):
+        self.rotation = np.zeros(3) if rotation is None else np.asarray(rotation, float).copy()
+        self.translation = np.zeros(3) if translation is None else np.asarray(translation, float).copy()
+        self.scale = float(scale)
+
+    def get_rotation_matrix(self) -> np.ndarray:
+        return _syn.rotation_matrix(self.rotation)
+
+    def transform(self, point) -> np.ndarray:
+        return self.scale * (self.get_rotation_matrix() @ np.asarray(point, float)) + self.translation
+
+    def is_valid(self) -> bool:
+        return bool(np.all(np.isfinite(self.rotation)) and np.all(np.isfinite(self.translation))
+                    and np.isfinite(self.scale))
+
+
 class Pose:
     """geometry::Pose: x_cam = R x_world + t, R given as an angle-axis.
 
@@ -274,5 +295,5 @@ class Pose:
         return f"Pose(rotation={self.rotation.tolist()}, translation={self.translation.tolist()})"
 
 
-__all__ = ["Camera", "CameraParameters", "Pose"]
+__all__ = ["Camera", "CameraParameters", "Pose", "Similarity"]
 _ = copy

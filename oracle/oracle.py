@@ -202,7 +202,7 @@ def orientation_residual(kind: str, target, std: float, instance_rotation, camer
 
 
 RELATIVE_KINDS = {"relative_rotation": 0, "common_position": 1, "linear_motion": 2, "gauge_scale": 3, "heatmap": 4,
-                  "relative_motion": 5, "gps_std": 6, "std_deviation": 7}
+                  "relative_motion": 5, "gps_std": 6, "std_deviation": 7, "gps_bias": 8}
 REL_PARAMS = 64
 
 
@@ -224,7 +224,9 @@ def heatmap_residual(grid, width, resolution, x_offset, y_offset, std, instance_
 def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None, scales=None):
     """Scaled residuals and Jacobian [m][36] of one constraint between shots
     (oracle/solver.cpp restatement); ``scales`` the two reconstruction
-    scales of a relative motion (columns 24 and 25)."""
+    scales of a relative motion (columns 24 and 25), or for "gps_bias" the
+    std multiplier (column 24) and the bias rotation, translation and scale
+    (columns 12..18)."""
     L = lib()
     f = L.oracle_relative_residual
     f.argtypes = [C.c_int, D, D, D, D, D, D]
@@ -234,7 +236,8 @@ def relative_residual(kind: str, instance_poses, params, rig_camera_poses=None, 
     prm = np.zeros(REL_PARAMS)
     v = np.asarray(params, np.float64).reshape(-1)
     prm[: len(v)] = v
-    sc = np.ones(2) if scales is None else np.ascontiguousarray(scales, np.float64)
+    sc = np.ones(8) if scales is None else np.ascontiguousarray(np.r_[scales, np.ones(8)][:max(8, len(scales))],
+                                                                 np.float64)
     r, J = np.zeros(7), np.zeros(7 * 36)
     m = f(RELATIVE_KINDS[kind], _p(pi), _p(pc), _p(prm), _p(sc), _p(r), _p(J))
     return r[:m].copy(), J[: 36 * m].reshape(m, 36)
@@ -259,7 +262,7 @@ def depth_residual(instance_pose, point, value, std, radial=True, rig_camera_pos
 def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, constant_cameras=False,
           density_ratio=1e-3, skip_initial_reweighting=False, threads=None, orientation=(), relative=(),
           relative_loss=("CauchyLoss", 1.0), gauge=None, heatmap=None, scales=(), fixed_instances=(),
-          depth=None, rig_pose=None):
+          depth=None, rig_pose=None, bias=None, point_priors=None):
     """Solves the bundle adjustment of a SceneArrays the way
     opensfm_gb300.pybundle.adjuster_from_scene configures the GPU solver.
     ``orientation``: absolute orientation constraints, tuples (kind, shot,
@@ -279,7 +282,11 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     values, stds, radial flags), values and stds rounded to float32 as
     map::Depth stores them.  ``rig_pose``: one fixed rig camera pose
     (angle-axis, centre) composed with every shot (None: the identity, not
-    composed).  Returns a dict with the final parameters,
+    composed).  ``bias``: (rotation, translation, scale, free parameter
+    indices) of the one camera's bias, through which every GPS prior is
+    taken (kind "gps_bias"; the solved bias is returned as "bias").
+    ``point_priors``: (point indices, positions [n][3], stds [n][3]) with
+    altitude (GCP3D).  Returns a dict with the final parameters,
     scales, costs and the cost trace."""
     L = lib()
     L.oracle_solve.argtypes = [C.POINTER(_Problem), C.POINTER(_Options), C.POINTER(_Result)]
@@ -304,12 +311,25 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     has_gps = np.zeros(ni, np.uint8)
     gps_pos = np.zeros((ni, 3))
     gps_std = np.ones((ni, 3))
+    bias_terms = []
     if gps and "gps" in scene.extras:
         for s in range(len(scene.shot_camera)):
             i = int(scene.shot_rig_instance[s])
+            if bias is not None:
+                # the GPS prior through the camera bias: scales 0..6 (after
+                # any reconstruction scales) hold the bias
+                bias_terms.append(("gps_bias", (s,), np.r_[scene.extras["gps"][s], scene.extras["gps_std"][s], -1.0,
+                                                           len(scales) + np.arange(7)]))
+                continue
             has_gps[i] = 1
             gps_pos[i] = scene.extras["gps"][s]
             gps_std[i] = scene.extras["gps_std"][s]
+    scales = list(scales)
+    if bias is not None:
+        free = set(int(k) for k in bias[3])
+        vals = np.r_[np.asarray(bias[0], np.float64), np.asarray(bias[1], np.float64), float(bias[2])]
+        n_before = len(scales)
+        scales += [(float(vals[k]), k in free) for k in range(7)]
     rig = np.zeros((1, 6)) if rig_pose is None else np.asarray(rig_pose, np.float64).reshape(1, 6).copy()
     rig_free = np.zeros((1, 6), np.uint8)
     rig_used = np.array([0 if rig_pose is None or not np.any(rig) else 1], np.uint8)
@@ -325,6 +345,11 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     pprior = np.zeros((npt, 3))
     psig = np.ones((npt, 3))
     palt = np.ones(npt, np.uint8)
+    if point_priors is not None:
+        pidx = np.asarray(point_priors[0], np.int64)
+        phas[pidx] = 1
+        pprior[pidx] = np.asarray(point_priors[1], np.float64)
+        psig[pidx] = np.asarray(point_priors[2], np.float64)
     gcp = np.zeros(scene.n_observations, np.uint8)
     no = len(orientation)
     o_kind = np.array([ORIENTATION_KINDS[o[0]] for o in orientation], np.int32).reshape(no)
@@ -334,7 +359,7 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
         v = np.atleast_1d(np.asarray(o[2], np.float64))
         o_target[q, : len(v)] = v
     o_std = np.array([float(o[3]) for o in orientation], np.float64).reshape(no)
-    relative = list(relative)
+    relative = list(relative) + bias_terms
     if gauge is not None:
         i0, i1 = (int(scene.shot_rig_instance[int(g)]) for g in gauge)
         inst_free[i0] = 0
@@ -399,7 +424,8 @@ def solve(scene, loss=None, irls="mixture", max_iterations=100, gps=True, consta
     if L.oracle_solve(C.byref(P), C.byref(O), C.byref(R)) != 0:
         raise ValueError("oracle_solve: an index array disagrees with the problem's counts")
     del keep
-    return dict(cameras=out_cam, instances=out_inst, points=out_pts, scales=out_scl[:n_scl].copy(), weights=out_w,
+    extra = {} if bias is None else {"bias": out_scl[n_before:n_before + 7].copy()}
+    return dict(**extra, cameras=out_cam, instances=out_inst, points=out_pts, scales=out_scl[:n_scl].copy(), weights=out_w,
                 errors=out_err,
                 trace=trace[: R.trace_n].copy(), initial_cost=R.initial_cost, final_cost=R.final_cost,
                 iterations=R.iterations, successful=R.successful, termination=R.termination)

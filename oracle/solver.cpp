@@ -365,6 +365,23 @@ double heat_value(const HeatGrid& g, double r, double c, double* fr, double* fc)
 
 int relative_residual(int kind, const double* const* pi, const double* const* pc, const double* prm, D36* r,
                       const HeatGrid* grid = nullptr, const double* scales = nullptr) {
+  if (kind == 8) {
+    // DataPriorError with SimilarityPriorTransform (prior_error.h:19-114,
+    // bias.h:34-54): (t - (c R(w) p + b)) / (std m) on the instance
+    // position t, the camera bias (w, b, c) in slots 12..18 (scales[1..7]),
+    // the std multiplier m in slot 24 (scales[0])
+    const D36 m = D36::var(scales[0], 24);
+    D36 w[3], Rw[9];
+    for (int k = 0; k < 3; ++k) w[k] = D36::var(scales[1 + k], 12 + k);
+    rotation_matrix(w, Rw);
+    const D36 c = D36::var(scales[7], 18);
+    for (int k = 0; k < 3; ++k) {
+      const D36 rp = Rw[3 * k] * prm[0] + Rw[3 * k + 1] * prm[1] + Rw[3 * k + 2] * prm[2];
+      const D36 prior = c * rp + D36::var(scales[4 + k], 15 + k);
+      r[k] = (D36::var(pi[0][3 + k], 3 + k) - prior) / (m * prm[3 + k]);
+    }
+    return 3;
+  }
   if (kind == 6) {
     // DataPriorError with adjust_scales (prior_error.h:54-93): (t - prior) /
     // (std m) on the instance position, m in slot 24
@@ -535,7 +552,7 @@ struct Solver {
   // weight, the compact columns of the 36 slots, w rho through *rho and the
   // raw residuals through raw.
   int relative_term(const State& s, int q, D36* r, int* col, double* rho, double* raw = nullptr) const {
-    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : (kind == 4 || kind == 6) ? 1 : kind == 7 ? 0 : 2;
+    const int kind = P.rel_kind[q], n = kind == 2 ? 3 : (kind == 4 || kind == 6 || kind == 8) ? 1 : kind == 7 ? 0 : 2;
     const double* prm = P.rel_params + kRelParams * q;
     const double* pi[3] = {nullptr, nullptr, nullptr};
     const double* pc[3] = {nullptr, nullptr, nullptr};
@@ -547,7 +564,7 @@ struct Solver {
       for (int a = 0; a < 6; ++a) col[12 * k + a] = idx.inst[6 * inst + a];
       // the heatmap functor always composes the rig camera; the relative
       // motion and the GPS prior none
-      if (rc >= 0 && (P.rig_used[rc] || kind == 4) && kind != 5 && kind != 6) {
+      if (rc >= 0 && (P.rig_used[rc] || kind == 4) && kind != 5 && kind != 6 && kind != 8) {
         pc[k] = &s.rig[6 * rc];
         for (int a = 0; a < 6; ++a) col[12 * k + 6 + a] = idx.rig[6 * rc + a];
       }
@@ -566,7 +583,21 @@ struct Solver {
       scales[0] = s.scl[si];
       col[24] = idx.scl[si];
     }
-    const int m = relative_residual(kind, pi, pc, prm, r, &grid, scales);
+    double biased[8] = {1, 0, 0, 0, 0, 0, 0, 1};
+    if (kind == 8) {
+      // the std multiplier (params[6], -1: none) and the seven bias
+      // unknowns (params[7..13])
+      if (prm[6] >= 0) {
+        biased[0] = s.scl[int(prm[6])];
+        col[24] = idx.scl[int(prm[6])];
+      }
+      for (int j = 0; j < 7; ++j) {
+        const int si = int(prm[7 + j]);
+        biased[1 + j] = s.scl[si];
+        col[12 + j] = idx.scl[si];
+      }
+    }
+    const int m = relative_residual(kind, pi, pc, prm, r, &grid, kind == 8 ? biased : scales);
     double sq = 0.0;
     for (int a = 0; a < m; ++a) {
       sq += r[a].v * r[a].v;
@@ -574,7 +605,8 @@ struct Solver {
     }
     // relative rotation and motion: the relative-motion loss (a motion's at
     // threshold x robust multiplier); Tukey(1); Cauchy(1); none; none
-    static const int kLoss[8] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL, -1, LOSS_TRIVIAL, LOSS_TRIVIAL};
+    static const int kLoss[9] = {-1, 5, LOSS_CAUCHY, LOSS_TRIVIAL, LOSS_TRIVIAL, -1, LOSS_TRIVIAL, LOSS_TRIVIAL,
+                                 LOSS_TRIVIAL};
     const int loss = (kind == 0 || kind == 5) ? P.rel_loss : kLoss[kind];
     const double la = kind == 0 ? P.rel_loss_threshold : kind == 5 ? P.rel_loss_threshold * prm[57] : 1.0;
     double rh[3];
@@ -1336,7 +1368,8 @@ struct Solver {
       std::vector<std::vector<double>> res;
       std::vector<double*> w;
       for (int q = 0; q < P.n_rel; ++q) {
-        if (P.rel_kind[q] != kind) continue;
+        // a GPS prior through an optimised bias (kind 8) is in group GPS
+        if (P.rel_kind[q] != kind && !(kind == 6 && P.rel_kind[q] == 8)) continue;
         D36 rr[7];
         int col[36];
         double rho, raw[7];
@@ -1395,7 +1428,7 @@ extern "C" int oracle_orientation_residual(int kind, const double* target, doubl
 // null); returns m.
 extern "C" int oracle_relative_residual(int kind, const double* instance_poses, const double* rig_camera_poses,
                                         const double* params, const double* scales, double* r, double* J) {
-  const int n = kind == 2 ? 3 : kind == 6 ? 1 : kind == 7 ? 0 : 2;
+  const int n = kind == 2 ? 3 : (kind == 6 || kind == 8) ? 1 : kind == 7 ? 0 : 2;
   const double* pi[3] = {nullptr, nullptr, nullptr};
   const double* pc[3] = {nullptr, nullptr, nullptr};
   for (int k = 0; k < n; ++k) {
