@@ -45,6 +45,22 @@ of :mod:`opensfm_gb300.scene`, driving the GPU adjuster.
   seeds come from numpy's generator (the reference's ``std::mt19937(42)``
   draws differ); GCP-anchored seeds and the GPS-bias compensation of
   ``BundleLocalStochastic`` are not applied.
+* :func:`bundle_full` -- ``BundleFull`` (ba_helpers.cc:1372-1671): the
+  whole scene with grid-selected tracks, optimised cameras, averaged GPS,
+  up-vector priors when the alignment is an orientation prior, ground
+  control points and the GPS-bias compensation, written back by
+  :func:`bundle_to_map` (``BundleToMap``, :1673-1736: NaN / Inf refused).
+* :func:`bundle_local_stochastic` -- ``BundleLocalStochastic``
+  (ba_helpers.cc:442-804): a local bundle with fixed cameras, the
+  GPS-bias compensation (every GPS-bearing instance as a fixed anchor) and
+  ground control points.
+* Ground control points: :class:`GroundControlPoint`,
+  :func:`triangulate_gcp` (``TriangulateGCP``), :func:`add_gcp_to_bundle`
+  (``AddGCPToBundle``), :func:`determine_gcp_bias_parameters`,
+  :func:`detect_alignment_constraints`.  Positions are in the scene's
+  (topocentric) frame; the reference converts latitude, longitude and
+  altitude first.  Retriangulation of the unselected tracks stays with the
+  caller (it is sfm::retriangulation, outside the adjuster).
 
 Defaults are the reference's configuration values (opensfm/config.py:
 ``local_bundle_radius`` 3, ``local_bundle_min_common_points`` 20,
@@ -62,7 +78,7 @@ from typing import Dict, List, Optional, Sequence, Set, Tuple
 import numpy as np
 
 from . import pybundle
-from .pygeometry import Camera, Pose
+from .pygeometry import Camera, Pose, Similarity
 from .scene import NUM_PARAMS, SceneArrays
 
 
@@ -383,6 +399,500 @@ def bundle_stochastic(scene: SceneArrays, max_shots: int = 500, random_shots: in
     return work.rig_instance_poses, work.points, report
 
 
-__all__ = ["Covisibility", "LocalProblem", "bundle_local", "bundle_local_batch", "bundle_shot_poses",
-           "bundle_stochastic", "direct_shot_neighbors", "local_problem", "select_tracks_grid", "shot_neighborhood",
-           "shot_poses_problem", "stochastic_rounds", "stochastic_seeds"]
+# ---------------------------------------------------------------------------
+# Full bundle, stochastic local bundles, ground control points, write-back
+# (BundleFull ba_helpers.cc:1372-1671, BundleLocalStochastic :442-804,
+# TriangulateGCP / AddGCPToBundle :822-936, AlignmentConstraints /
+# DetectAlignmentConstraints :1738-1802, DetermineGCPBiasParameters
+# :1804-1845, BundleToMap :1673-1736).
+
+# The configuration values the helpers read, with the reference's defaults
+# (opensfm/config.py).
+DEFAULT_CONFIG = {
+    "optimize_camera_parameters": True, "optimize_rig_parameters": False, "bundle_use_gps": True,
+    "bundle_use_gcp": True, "bundle_compensate_gps_bias": False, "gcp_reprojection_error_threshold": 0.05,
+    "gcp_global_weight": 0.04, "gcp_observation_sd": 0.001, "gcp_horizontal_sd": 0.01, "gcp_vertical_sd": 0.1,
+    "align_method": "auto", "align_orientation_prior": "horizontal", "exif_focal_sd": 0.01,
+    "aspect_ratio_sd": 0.01, "principal_point_sd": 0.01, "radial_distortion_k1_sd": 0.01,
+    "radial_distortion_k2_sd": 0.01, "tangential_distortion_p1_sd": 0.01, "tangential_distortion_p2_sd": 0.01,
+    "radial_distortion_k3_sd": 0.01, "radial_distortion_k4_sd": 0.01, "rig_translation_sd": 0.1,
+    "rig_rotation_sd": 0.1, "bundle_irls_density_ratio": 0.001, "bundle_irls_gcp_density_ratio": 0.00001,
+    "bundle_irls_gps_density_ratio": 0.00001, "bundle_max_iterations": 100, "local_bundle_radius": 3,
+    "local_bundle_min_common_points": 20, "local_bundle_max_shots": 30, "local_bundle_grid": 12,
+    "final_bundle_grid": 32,
+}
+
+
+def _config(config: Optional[dict]) -> dict:
+    c = dict(DEFAULT_CONFIG)
+    c.update(config or {})
+    return c
+
+
+@dataclass
+class GroundControlPoint:
+    """map::GroundControlPoint: observations (shot index, normalized image
+    point) and, unless only observed, the measured position in the scene's
+    (topocentric) frame -- the reference converts its latitude, longitude
+    and altitude with the map's topocentric converter first -- with an
+    optional standard deviation.  Check points take no part in the
+    adjustment."""
+    id: str
+    observations: List[Tuple[int, np.ndarray]]
+    position: Optional[np.ndarray] = None
+    std_dev: Optional[np.ndarray] = None
+    has_altitude: bool = True
+    role: str = "control"
+
+
+def determine_linear_solver(num_cameras: int) -> str:
+    """DetermineLinearSolver (ba_helpers.cc:42-49)."""
+    return "DENSE_SCHUR" if num_cameras <= 200 else "SPARSE_SCHUR"
+
+
+def are_points_collinear(X: np.ndarray) -> bool:
+    """ArePointsCollinear (ba_helpers.cc:26-40): two eigenvalues of the
+    scatter below 1e-10, or the largest over the middle above 5e3."""
+    X = np.asarray(X, float)
+    Z = X - X.mean(axis=0)
+    ev = np.linalg.eigvalsh(Z.T @ Z)
+    return int(np.sum(ev < 1e-10)) > 1 or abs(ev[2] / ev[1]) > 5e3
+
+
+def _shot_frame(scene: SceneArrays, shot: int) -> Tuple[np.ndarray, np.ndarray]:
+    """(camera-to-world rotation, camera centre) of a shot."""
+    pose = Pose.from_ba_data(scene.rig_instance_poses[int(scene.shot_rig_instance[shot])])
+    return pose.get_R_cam_to_world(), pose.get_origin()
+
+
+def _angle(a: np.ndarray, b: np.ndarray) -> float:
+    c = np.dot(a, b) / (np.linalg.norm(a) * np.linalg.norm(b))
+    return float(np.arccos(np.clip(c, -1.0, 1.0)))
+
+
+def triangulate_gcp(gcp: GroundControlPoint, scene: SceneArrays, threshold: float, min_ray_angle: float = 0.1 * math.pi / 180,
+                    min_depth: float = 1e-3, iterations: int = 10) -> Tuple[bool, np.ndarray, np.ndarray]:
+    """TriangulateGCP (ba_helpers.cc:822-857) with the steps of
+    TriangulateBearingsRobust (geometry/src/triangulation.cc:239-302): world
+    bearings of the observations from existing shots; some pair of rays
+    between min_ray_angle and pi - min_ray_angle; the midpoint solution
+    (least squares over the rays); inliers within `threshold` radians of
+    their ray, at least two; refinement of the bearing errors over the
+    inliers (Gauss-Newton, `iterations` steps); every inlier at least
+    min_depth in front.  The reference samples ray pairs by RANSAC; here
+    the inliers come from the all-ray solution, re-solved on them once, a
+    deterministic choice that agrees on outlier-free control points.
+    Returns (success, position, inlier flags)."""
+    n_shots = len(scene.shot_camera)
+    cams = [Camera(int(scene.camera_projection[c]), scene.camera_values[c, : NUM_PARAMS[int(scene.camera_projection[c])]])
+            for c in range(len(scene.camera_projection))]
+    centres, bearings = [], []
+    for shot, xy in gcp.observations:
+        if not 0 <= int(shot) < n_shots:
+            continue
+        R, c = _shot_frame(scene, int(shot))
+        centres.append(c)
+        bearings.append(R @ cams[int(scene.shot_camera[int(shot)])].bearing(xy))
+    n = len(centres)
+    if n < 2:
+        return False, np.zeros(3), np.zeros(n, bool)
+    C_, B_ = np.array(centres), np.array(bearings)
+    B_ = B_ / np.linalg.norm(B_, axis=1, keepdims=True)
+    if not any(min_ray_angle <= _angle(B_[i], B_[j]) <= math.pi - min_ray_angle
+               for i in range(n) for j in range(i)):
+        return False, np.zeros(3), np.zeros(n, bool)
+
+    def midpoint(idx):
+        A, b = np.zeros((3, 3)), np.zeros(3)
+        for i in idx:
+            P = np.eye(3) - np.outer(B_[i], B_[i])
+            A += P
+            b += P @ C_[i]
+        return np.linalg.lstsq(A, b, rcond=None)[0]
+
+    X = midpoint(range(n))
+    inl = np.array([_angle(X - C_[i], B_[i]) <= threshold for i in range(n)])
+    if inl.sum() < 2:
+        return False, np.zeros(3), inl
+    X = midpoint(np.nonzero(inl)[0])
+    idx = np.nonzero(inl)[0]
+    for _ in range(iterations):
+        # residual: the component of the normalized ray to X orthogonal to the bearing
+        J, r = [], []
+        for i in idx:
+            d = X - C_[i]
+            nd = np.linalg.norm(d)
+            u = d / nd
+            P = np.eye(3) - np.outer(B_[i], B_[i])
+            r.append(P @ u)
+            J.append(P @ (np.eye(3) - np.outer(u, u)) / nd)
+        J, r = np.concatenate(J), np.concatenate(r)
+        step = np.linalg.lstsq(J, -r, rcond=None)[0]
+        X = X + step
+        if np.linalg.norm(step) < 1e-12 * (1.0 + np.linalg.norm(X)):
+            break
+    for i in idx:
+        if np.dot(X - C_[i], B_[i]) < min_depth:
+            return False, np.zeros(3), inl
+    return True, X, inl
+
+
+def add_gcp_to_bundle(ba: pybundle.BundleAdjuster, scene: SceneArrays, gcps: Sequence[GroundControlPoint],
+                      config: dict, num_ba_points: int, num_ba_shots: int, ba_shots: Set[int]) -> int:
+    """AddGCPToBundle (ba_helpers.cc:860-936): each triangulated control
+    point seen from a shot of the problem becomes a point "gcp-<id>" with a
+    prior at its measured position (std / (gcp_global_weight * w)) and its
+    observations as GCP projections (std gcp_observation_sd / (weight *
+    w)), w = sqrt(max(1, points per shot)).  Returns the observations
+    added."""
+    c = _config(config)
+    weight = c["gcp_global_weight"] * math.sqrt(max(1.0, num_ba_points / max(1, num_ba_shots)))
+    added = 0
+    for g in gcps:
+        if g.role == "checkpoint":
+            continue
+        ok, X, _ = triangulate_gcp(g, scene, c["gcp_reprojection_error_threshold"])
+        if not ok or not any(int(s) in ba_shots for s, _ in g.observations):
+            continue
+        pid = "gcp-" + g.id
+        ba.add_point(pid, X, False)
+        if g.position is not None:
+            sd = (np.asarray(g.std_dev, float) if g.std_dev is not None else
+                  np.array([c["gcp_horizontal_sd"], c["gcp_horizontal_sd"], c["gcp_vertical_sd"]]))
+            ba.add_point_prior(pid, np.asarray(g.position, float), sd / weight, g.has_altitude)
+        for s, xy in g.observations:
+            if int(s) in ba_shots:
+                ba.add_point_projection_observation(str(int(s)), pid, np.asarray(xy, float),
+                                                    c["gcp_observation_sd"] / weight, True)
+                added += 1
+    return added
+
+
+def alignment_constraints(scene: SceneArrays, gcps: Sequence[GroundControlPoint], config: dict
+                          ) -> Tuple[np.ndarray, np.ndarray]:
+    """AlignmentConstraints (ba_helpers.cc:1738-1787): measured (Xp) and
+    reconstructed (X) positions of the triangulated control points and of
+    the shots with GPS."""
+    c = _config(config)
+    Xp, X = [], []
+    if c["bundle_use_gcp"]:
+        for g in gcps:
+            if g.position is None:
+                continue
+            ok, pos, _ = triangulate_gcp(g, scene, c["gcp_reprojection_error_threshold"])
+            if ok:
+                Xp.append(np.asarray(g.position, float))
+                X.append(pos)
+    if c["bundle_use_gps"] and "gps" in scene.extras:
+        for s in range(len(scene.shot_camera)):
+            Xp.append(np.asarray(scene.extras["gps"][s], float))
+            X.append(_shot_frame(scene, s)[1])
+    return np.array(Xp).reshape(-1, 3), np.array(X).reshape(-1, 3)
+
+
+def detect_alignment_constraints(scene: SceneArrays, gcps: Sequence[GroundControlPoint], config: dict) -> str:
+    """DetectAlignmentConstraints (ba_helpers.cc:1789-1802)."""
+    _, X = alignment_constraints(scene, gcps, config)
+    if len(X) < 3 or are_points_collinear(X):
+        return "orientation_prior"
+    return "naive"
+
+
+def determine_gcp_bias_parameters(scene: SceneArrays, gcps: Sequence[GroundControlPoint], config: dict) -> List[int]:
+    """DetermineGCPBiasParameters (ba_helpers.cc:1804-1845) as
+    SimilarityMaskToIndices gives it (bundle/data/parameter_mask.h:42-62):
+    every parameter without triangulated control points or with three or
+    more not collinear; the translation for one; translation and scale for
+    two or collinear ones."""
+    c = _config(config)
+    pts = []
+    for g in gcps:
+        ok, X, _ = triangulate_gcp(g, scene, c["gcp_reprojection_error_threshold"])
+        if ok:
+            pts.append(X)
+    if not pts:
+        return list(range(7))
+    if len(pts) == 1:
+        return [3, 4, 5]
+    if len(pts) == 2 or are_points_collinear(np.array(pts)):
+        return [3, 4, 5, 6]
+    return list(range(7))
+
+
+def _configure(ba: pybundle.BundleAdjuster, c: dict, n_shots: int) -> None:
+    ba.set_internal_parameters_prior_sd(c["exif_focal_sd"], c["aspect_ratio_sd"], c["principal_point_sd"],
+                                        c["radial_distortion_k1_sd"], c["radial_distortion_k2_sd"],
+                                        c["tangential_distortion_p1_sd"], c["tangential_distortion_p2_sd"],
+                                        c["radial_distortion_k3_sd"], c["radial_distortion_k4_sd"])
+    ba.set_rig_parameters_prior_sd(c["rig_translation_sd"], c["rig_rotation_sd"])
+    ba.set_default_density_ratio(c["bundle_irls_density_ratio"])
+    ba.set_group_density_ratio("GCP2D", c["bundle_irls_gcp_density_ratio"])
+    ba.set_group_density_ratio("GPS", c["bundle_irls_gps_density_ratio"])
+    ba.set_max_num_iterations(int(c["bundle_max_iterations"]))
+
+
+def _up_vector(scene: SceneArrays, gcps, c: dict) -> Optional[np.ndarray]:
+    method = c["align_method"]
+    if method == "auto":
+        method = detect_alignment_constraints(scene, gcps, c)
+    if method == "orientation_prior":
+        if c["align_orientation_prior"] == "vertical":
+            return np.array([0.0, 0.0, -1.0])
+        if c["align_orientation_prior"] == "horizontal":
+            return np.array([0.0, -1.0, 0.0])
+    return None
+
+
+def _instance_gps(scene: SceneArrays, members: Sequence[int]) -> Optional[Tuple[np.ndarray, np.ndarray]]:
+    """The averaged GPS position and accuracy of an instance's shots; an
+    accuracy component <= 0 is an error (ba_helpers.cc:1500-1510)."""
+    if "gps" not in scene.extras:
+        return None
+    pos, acc = [], []
+    for s in members:
+        a = np.asarray(scene.extras["gps_std"][s], float)
+        if np.any(a <= 0):
+            raise RuntimeError(f"Shot {s} has an accuracy component <= 0. Try modifying your input parser to "
+                               "filter such values.")
+        pos.append(np.asarray(scene.extras["gps"][s], float))
+        acc.append(a)
+    return np.mean(pos, axis=0), np.mean(acc, axis=0)
+
+
+def bundle_to_map(ba: pybundle.BundleAdjuster, scene: SceneArrays, update_cameras: bool,
+                  instances: Optional[Sequence[int]] = None, point_ids: Optional[np.ndarray] = None,
+                  biases: bool = True) -> Dict[str, np.ndarray]:
+    """BundleToMap (ba_helpers.cc:1673-1736) on the scene arrays: cameras
+    (when updated), biases and rig-instance poses, each refused with a
+    RuntimeError when it holds NaN or Inf; points written back, and a point
+    with a non-finite position gets unit reprojection errors and zero
+    weights.  Returns the reprojection errors and weights of the written
+    points' observations ("errors", "weights", per scene observation; NaN
+    where not written)."""
+    if update_cameras:
+        for c in range(len(scene.camera_projection)):
+            cam = ba.get_camera(str(c))
+            scene.camera_values[c, : len(cam.get_parameters_values())] = cam.get_parameters_values()
+    if biases:
+        out = scene.extras.setdefault("biases", {})
+        for c in range(len(scene.camera_projection)):
+            b = ba.get_bias(str(c))
+            if not b.is_valid():
+                raise RuntimeError(f"Bias {c} has either NaN or INF values.")
+            out[str(c)] = b
+    inst = range(len(scene.rig_instance_poses)) if instances is None else instances
+    for i in inst:
+        d = ba.get_rig_instance_pose(str(i)).ba_data()
+        if not np.all(np.isfinite(d)):
+            raise RuntimeError(f"Rig Instance {i} has either NaN or INF values.")
+        scene.rig_instance_poses[i] = d
+    ids = np.arange(len(scene.points)) if point_ids is None else np.asarray(point_ids)
+    pts = ba.get_points()[: len(ids)]
+    errors = np.full((scene.n_observations, 3), np.nan)
+    weights = np.full(scene.n_observations, np.nan)
+    try:
+        e, w, _ = ba.projection_results()
+    except Exception:  # reprojection errors not computed
+        e, w = None, None
+    if e is not None and len(e) >= 1:
+        # the adjuster's observations are the scene observations of these
+        # points, in scene order (the helpers add them so)
+        keep = np.nonzero(np.isin(np.asarray(scene.obs_point), ids))[0]
+        m = min(len(keep), len(e))
+        errors[keep[:m]] = e[:m]
+        weights[keep[:m]] = w[:m]
+    bad = ~np.all(np.isfinite(pts), axis=1)
+    if bad.any():
+        obs_bad = np.isin(np.asarray(scene.obs_point), ids[bad])
+        errors[obs_bad] = 1.0
+        weights[obs_bad] = 0.0
+    scene.points[ids] = pts
+    return {"errors": errors, "weights": weights}
+
+
+def _add_scene_shots(ba: pybundle.BundleAdjuster, scene: SceneArrays, cov: Covisibility, instances: Sequence[int],
+                     fixed: Set[int], use_gps: bool, gps_on_fixed: bool) -> List[int]:
+    moving = []
+    for inst in instances:
+        members = cov.instance_shots[inst]
+        f = inst in fixed
+        ba.add_rig_instance(str(inst), Pose.from_ba_data(scene.rig_instance_poses[inst]),
+                            {str(s): str(int(scene.shot_camera[s])) for s in members},
+                            {str(s): "rig" for s in members}, f)
+        if not f:
+            moving.append(inst)
+        if use_gps and (not f or gps_on_fixed):
+            g = _instance_gps(scene, members)
+            if g is not None:
+                ba.add_rig_instance_position_prior(str(inst), g[0], g[1], "dummy")
+    return moving
+
+
+def bundle_full(scene: SceneArrays, config: Optional[dict] = None, gcps: Sequence[GroundControlPoint] = (),
+                grid_size: Optional[int] = None, camera_priors: Optional[Sequence[Camera]] = None,
+                precision: str = "mixed") -> dict:
+    """BundleFull (ba_helpers.cc:1372-1671) on the GPU adjuster: the tracks
+    of SelectTracksGrid over every shot (grid_size <= 1 or no image size:
+    every point), cameras optimised unless optimize_camera_parameters is
+    off, rig instances with their averaged GPS, an up-vector prior per shot
+    when the alignment is an orientation prior, ground control points, the
+    GPS-bias compensation (every camera's bias with
+    determine_gcp_bias_parameters' parameters) when asked and control
+    points exist, the configuration's priors and IRLS density ratios, the
+    linear solver of determine_linear_solver; then the solution written
+    back (bundle_to_map).  Retriangulation of the other tracks is the
+    caller's.  Returns the report (brief, full and IRLS reports, wall
+    times, counts, the other tracks)."""
+    import time
+    c = _config(config)
+    t0 = time.perf_counter()
+    cov = Covisibility.of(scene)
+    n_shots = len(scene.shot_camera)
+    grid = c["final_bundle_grid"] if grid_size is None else grid_size
+    width, height = scene.extras.get("width"), scene.extras.get("height")
+    if width and height and grid > 1:
+        subset, other = select_tracks_grid(scene, cov, set(range(n_shots)), grid, int(width), int(height))
+    else:
+        subset, other = np.arange(len(scene.points)), np.zeros(0, np.int64)
+    t_grid = time.perf_counter()
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    fix_cameras = not c["optimize_camera_parameters"]
+    for k in range(len(scene.camera_projection)):
+        m = int(scene.camera_projection[k])
+        cam = Camera(m, scene.camera_values[k, : NUM_PARAMS[m]])
+        prior = camera_priors[k] if camera_priors is not None else cam
+        ba.add_camera(str(k), cam, prior, fix_cameras)
+    ba.add_points(scene.points[subset])
+    up = _up_vector(scene, gcps, c)
+    ba.add_rig_camera("rig", Pose(), Pose(), True)
+    _add_scene_shots(ba, scene, cov, sorted(cov.instance_shots), set(), bool(c["bundle_use_gps"]), False)
+    if up is not None:
+        for s in range(n_shots):
+            ba.add_absolute_up_vector(str(s), up, 1e-3)
+    keep = np.nonzero(np.isin(np.asarray(scene.obs_point), subset))[0]
+    local = -np.ones(len(scene.points), np.int64)
+    local[subset] = np.arange(len(subset))
+    shot_index = np.array([ba.shot_index(str(s)) for s in range(n_shots)], np.int32)
+    ba.add_point_projection_observations(shot_index[np.asarray(scene.obs_shot)[keep]],
+                                         local[np.asarray(scene.obs_point)[keep]].astype(np.int32),
+                                         np.asarray(scene.obs_xy)[keep], np.asarray(scene.obs_std)[keep])
+    if c["bundle_use_gcp"] and gcps:
+        add_gcp_to_bundle(ba, scene, gcps, c, len(subset), n_shots, set(range(n_shots)))
+    if c["bundle_compensate_gps_bias"] and gcps:
+        idx = determine_gcp_bias_parameters(scene, gcps, c)
+        biases = scene.extras.get("biases", {})
+        for k in range(len(scene.camera_projection)):
+            ba.set_camera_bias(str(k), biases.get(str(k), Similarity()), idx)
+    _configure(ba, c, n_shots)
+    ba.set_linear_solver_type(determine_linear_solver(n_shots))
+    t_setup = time.perf_counter()
+    ba.run()
+    t_run = time.perf_counter()
+    written = bundle_to_map(ba, scene, not fix_cameras, point_ids=subset)
+    t_down = time.perf_counter()
+    s = ba.summary()
+    return {"brief_report": ba.brief_report(), "irls_report": ba.irls_report(), "full_report": ba.full_report(),
+            "is_solution_usable": bool(s["usable"]), "summary": s,
+            "wall_times": {"grid": t_grid - t0, "setup": t_setup - t_grid, "run": t_run - t_setup,
+                           "teardown": t_down - t_run},
+            "num_images": n_shots, "num_points": int(len(subset)), "num_reprojections": int(len(keep)),
+            "other_tracks": other, "reprojection": written}
+
+
+def bundle_local_stochastic(scene: SceneArrays, central_shots: Sequence[int], config: Optional[dict] = None,
+                            gcps: Sequence[GroundControlPoint] = (), grid_size: Optional[int] = None,
+                            precision: str = "mixed") -> Tuple[np.ndarray, dict]:
+    """BundleLocalStochastic (ba_helpers.cc:442-804) on the GPU adjuster:
+    the neighbourhood of the central shots, the grid-selected tracks of its
+    interior, cameras and rig cameras fixed, an instance free only when all
+    its shots are interior; with GPS-bias compensation (when asked and
+    control points exist) every camera's bias is optimised, starting from
+    the scene's, and every other GPS-bearing instance joins as a fixed,
+    observation-free anchor with its prior; up-vector priors on the
+    interior; ground control points; then the moving instances, the points
+    and the biases written back.  Returns the point indices and the
+    report."""
+    import time
+    c = _config(config)
+    t0 = time.perf_counter()
+    cov = Covisibility.of(scene)
+    interior, boundary = shot_neighborhood(cov, central_shots, int(c["local_bundle_radius"]),
+                                           int(c["local_bundle_min_common_points"]), int(c["local_bundle_max_shots"]))
+    grid = c["local_bundle_grid"] if grid_size is None else grid_size
+    width, height = scene.extras.get("width"), scene.extras.get("height")
+    if width and height and grid > 1:
+        subset, other = select_tracks_grid(scene, cov, interior, grid, int(width), int(height))
+    else:
+        subset = np.unique(np.concatenate([cov.shot_points[s] for s in sorted(interior)])) if interior \
+            else np.zeros(0, np.int64)
+        other = np.zeros(0, np.int64)
+    ba = pybundle.BundleAdjuster()
+    ba.set_precision(precision)
+    for k in range(len(scene.camera_projection)):
+        m = int(scene.camera_projection[k])
+        cam = Camera(m, scene.camera_values[k, : NUM_PARAMS[m]])
+        ba.add_camera(str(k), cam, cam, True)
+    compensate = bool(c["bundle_compensate_gps_bias"]) and len(gcps) > 0
+    if compensate:
+        idx = determine_gcp_bias_parameters(scene, gcps, c)
+        biases = scene.extras.get("biases", {})
+        for k in range(len(scene.camera_projection)):
+            ba.set_camera_bias(str(k), biases.get(str(k), Similarity()), idx)
+    use_gps = bool(c["bundle_use_gps"])
+    shots = interior | boundary
+    instances = {int(cov.shot_instance[s]) for s in shots}
+    if compensate and use_gps and "gps" in scene.extras:
+        instances |= set(cov.instance_shots)  # every GPS-bearing instance, as a fixed anchor
+    fixed = {i for i in instances if any(s not in interior for s in cov.instance_shots[i])}
+    ba.add_rig_camera("rig", Pose(), Pose(), True)
+    moving = _add_scene_shots(ba, scene, cov, sorted(instances), fixed, use_gps, compensate)
+    up = _up_vector(scene, gcps, c)
+    if up is not None:
+        for s in sorted(interior):
+            ba.add_absolute_up_vector(str(s), up, 1e-3)
+    ba.add_points(scene.points[subset])
+    local = -np.ones(len(scene.points), np.int64)
+    local[subset] = np.arange(len(subset))
+    keep = np.nonzero(np.isin(np.asarray(scene.obs_point), subset) &
+                      np.isin(np.asarray(scene.obs_shot), sorted(shots)))[0]
+    shot_index = {s: ba.shot_index(str(s)) for s in shots}
+    ba.add_point_projection_observations(np.array([shot_index[int(s)] for s in np.asarray(scene.obs_shot)[keep]],
+                                                  np.int32),
+                                         local[np.asarray(scene.obs_point)[keep]].astype(np.int32),
+                                         np.asarray(scene.obs_xy)[keep], np.asarray(scene.obs_std)[keep])
+    if c["bundle_use_gcp"] and gcps:
+        add_gcp_to_bundle(ba, scene, gcps, c, len(subset), len(shots), shots)
+    _configure(ba, c, len(shots))
+    ba.set_linear_solver_type(determine_linear_solver(len(shots)))
+    t_setup = time.perf_counter()
+    ba.run()
+    t_run = time.perf_counter()
+    for i in moving:
+        scene.rig_instance_poses[i] = ba.get_rig_instance_pose(str(i)).ba_data()
+    pts = ba.get_points()[: len(subset)]
+    scene.points[subset] = pts
+    if compensate:
+        out = scene.extras.setdefault("biases", {})
+        for k in range(len(scene.camera_projection)):
+            b = ba.get_bias(str(k))
+            if not b.is_valid():
+                raise RuntimeError(f"Bias {k} has either NaN or INF values.")
+            out[str(k)] = b
+    s = ba.summary()
+    report = {"brief_report": ba.brief_report(), "full_report": ba.full_report(), "irls_report": ba.irls_report(),
+              "is_solution_usable": bool(s["usable"]), "summary": s,
+              "wall_times": {"setup": t_setup - t0, "run": t_run - t_setup},
+              "num_images": len(interior), "num_interior_images": len(interior),
+              "num_boundary_images": len(boundary),
+              "num_other_images": len(scene.shot_camera) - len(interior) - len(boundary),
+              "num_points": int(len(subset)), "num_reprojections": int(len(keep)), "other_tracks": other}
+    return subset, report
+
+
+__all__ = ["Covisibility", "DEFAULT_CONFIG", "GroundControlPoint", "LocalProblem", "add_gcp_to_bundle",
+           "alignment_constraints", "are_points_collinear", "bundle_full", "bundle_local", "bundle_local_batch",
+           "bundle_local_stochastic", "bundle_shot_poses", "bundle_stochastic", "bundle_to_map",
+           "detect_alignment_constraints", "determine_gcp_bias_parameters", "determine_linear_solver",
+           "direct_shot_neighbors", "local_problem", "select_tracks_grid", "shot_neighborhood", "shot_poses_problem",
+           "stochastic_rounds", "stochastic_seeds", "triangulate_gcp"]

@@ -188,6 +188,33 @@ class Camera:
         p = np.asarray(points, float)
         return _syn.project(self.model, np.broadcast_to(self._values, (len(p), self._values.size)), p)
 
+    def bearing(self, point, iterations: int = 20) -> np.ndarray:
+        """Camera::Bearing: the unit camera-frame direction that projects to
+        the normalized image point.  Spherical cameras invert their
+        longitude/latitude map directly; the other models solve project((x,
+        y, 1)) = point by Gauss-Newton with a central-difference Jacobian,
+        from the point itself divided by the focal length (the reference's
+        models invert their distortion by Newton steps too)."""
+        u = np.asarray(point, float)
+        if self.model == SPHERICAL:
+            lon, lat = 2 * np.pi * u[0], -2 * np.pi * u[1]
+            return np.array([np.cos(lat) * np.sin(lon), -np.sin(lat), np.cos(lat) * np.cos(lon)])
+        f = float(self._get(_P.focal)) if _P.focal in self.get_parameters_types() else 1.0
+        xy = u / (f if f else 1.0)
+        h = 1e-7
+        for _ in range(iterations):
+            r = self.project(np.r_[xy, 1.0]) - u
+            if np.abs(r).max() < 1e-14:
+                break
+            J = np.empty((2, 2))
+            for k in range(2):
+                d = np.zeros(2)
+                d[k] = h
+                J[:, k] = (self.project(np.r_[xy + d, 1.0]) - self.project(np.r_[xy - d, 1.0])) / (2 * h)
+            xy = xy - np.linalg.solve(J, r)
+        b = np.r_[xy, 1.0]
+        return b / np.linalg.norm(b)
+
     def __copy__(self):
         c = Camera(self.model, self._values)
         c.id, c.width, c.height = self.id, self.width, self.height

@@ -43,7 +43,7 @@ def _has_gpu() -> bool:
 _GPU_ORDER = ("test_gpu_evaluate.py", "test_gpu_solver.py", "test_gpu_dense.py", "test_gpu_matrix_free.py",
               "test_gpu_batch.py", "test_gpu_autograd.py", "test_gpu_outliers.py", "test_gpu_covariance.py",
               "test_gpu_orientation.py", "test_gpu_relative.py", "test_gpu_relative_motion.py",
-              "test_gpu_position_std.py", "test_gpu_depth.py", "test_gpu_bias.py", "test_gpu_ba_helpers.py")
+              "test_gpu_position_std.py", "test_gpu_depth.py", "test_gpu_bias.py", "test_gpu_ba_helpers.py", "test_gpu_ba_full.py")
 
 
 def _file_rank(item) -> int:
