@@ -247,7 +247,10 @@ def headline(result: dict) -> dict:
     b = result.get("batched_local_ba")
     if b:
         h["c4_batch"] = {"batch_s": r3(b.get("batch_s")), "one_at_a_time_s": r3(b.get("one_at_a_time_s")),
-                         "speedup": r3(b.get("speedup"))}
+                         "speedup": r3(b.get("speedup")), "lm_iterations": b.get("batch_lm_iterations"),
+                         "graph_launches": b.get("graph_launches"),
+                         "solve_s_device_loop_vs_per_iteration": [r3(b.get("batch_solve_s")),
+                                                                  r3(b.get("per_iteration_graph", {}).get("solve_s"))]}
     d = result.get("dense_rcs")
     if d and d.get("spd"):
         big = d["spd"][-1]
@@ -503,8 +506,21 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
     batch_conv = np.array([ba.summary()["iterations"] < max_iterations for ba in bas])
     out.update({"batch_s": batch_s, "batch_setup_s": s["setup_seconds"], "batch_solve_s": s["solve_seconds"],
                 "batch_lm_iterations": s["lm_iterations"], "graph_nodes": s["graph_nodes"],
+                "graph_launches": s["graph_launches"],
                 "autotuned_grid": s["grid"], "converged_batch": int(batch_conv.sum()),
                 "batch_mobs_per_s": out["n_observations"] / batch_s / 1e6})
+    # the same batch with one graph launch per LM iteration and a host check
+    # of the done count between them (the device-side loop removes those)
+    bas1 = adjusters()
+    b1 = BundleBatch()
+    for ba in bas1:
+        b1.add(ba)
+    b1.set_options(precision="mixed", max_iterations=max_iterations, pcg_iterations=100, pcg_tolerance=1e-3,
+                   use_graph=1)
+    b1.run()
+    s1 = b1.summary()
+    out["per_iteration_graph"] = {"solve_s": s1["solve_seconds"], "lm_iterations": s1["lm_iterations"],
+                                  "graph_launches": s1["graph_launches"]}
     if not one_at_a_time:
         return out
     # one at a time
@@ -520,6 +536,7 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
     out.update({
         "batch_s": batch_s, "batch_setup_s": s["setup_seconds"], "batch_solve_s": s["solve_seconds"],
         "batch_lm_iterations": s["lm_iterations"], "graph_nodes": s["graph_nodes"], "autotuned_grid": s["grid"],
+        "graph_launches": s["graph_launches"],
         "converged_batch": int(batch_conv.sum()), "converged_one_at_a_time": int(single_conv.sum()),
         "one_at_a_time_s": single_s, "speedup": single_s / batch_s,
         "batch_mobs_per_s": out["n_observations"] / batch_s / 1e6,

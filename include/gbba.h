@@ -557,8 +557,11 @@ void gbba_batch_destroy(gbba_batch_t* b);
 int gbba_batch_add(gbba_batch_t* b, gbba_adjuster_t* h);
 int gbba_batch_size(const gbba_batch_t* b);
 /* precision GBBA_PRECISION_*; LM iterations; PCG iterations per LM step;
- * PCG relative tolerance; record the iteration as a CUDA graph (1) or
- * launch it kernel by kernel (0); pick the slot-kernel grid by timing (1). */
+ * PCG relative tolerance; use_graph 2 (default in the bindings): the whole
+ * LM loop as one CUDA graph launch, a device-side while node that ends when
+ * every problem is done or max_iterations are taken; 1: one recorded LM
+ * iteration replayed per iteration with a host check between them; 0:
+ * kernel by kernel; pick the slot-kernel grid by timing (1). */
 int gbba_batch_set_options(gbba_batch_t* b, int precision, int max_iterations, int pcg_iterations,
                            double pcg_tolerance, int use_graph, int autotune);
 /* A problem has converged when an accepted step changes its cost by at
@@ -575,6 +578,7 @@ typedef struct gbba_batch_summary {
   int n_converged;
   int64_t graph_nodes;   /* nodes of the recorded LM iteration */
   int64_t kernel_launches;
+  int64_t graph_launches;  /* graph launches of the LM loop: 1 with the device-side loop */
 } gbba_batch_summary_t;
 int gbba_batch_get_summary(const gbba_batch_t* b, gbba_batch_summary_t* out);
 

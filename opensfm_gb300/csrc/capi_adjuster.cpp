@@ -768,7 +768,8 @@ int gbba_batch_set_options(gbba_batch_t* b, int precision, int max_iterations, i
     b->opts.max_iterations = max_iterations;
     b->opts.pcg_iterations = pcg_iterations;
     b->opts.pcg_tolerance = pcg_tolerance;
-    b->opts.use_graph = use_graph != 0;
+    if (use_graph < 0 || use_graph > 2) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "use_graph must be 0, 1 or 2");
+    b->opts.use_graph = use_graph;
     b->opts.autotune = autotune != 0;
   });
 }
@@ -849,6 +850,7 @@ int gbba_batch_get_summary(const gbba_batch_t* b, gbba_batch_summary_t* out) {
     out->n_converged = conv;
     out->graph_nodes = s.graph_nodes;
     out->kernel_launches = s.kernel_launches;
+    out->graph_launches = s.graph_launches;
   });
 }
 

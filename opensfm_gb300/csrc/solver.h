@@ -49,7 +49,9 @@ struct BatchOptions {
   int pcg_iterations = 50;           // per LM iteration (each problem stops at its tolerance)
   double pcg_tolerance = 1e-3;
   double function_tolerance = 1e-7;  // as the single-problem solver's inner convergence test
-  bool use_graph = true;             // record one LM iteration as a CUDA graph
+  // 2: the whole LM loop one CUDA graph launch (a device-side while node);
+  // 1: one recorded LM iteration replayed per iteration; 0: plain launches
+  int use_graph = 2;
   bool autotune = true;              // pick the slot-kernel grid by timing
 };
 
@@ -66,6 +68,7 @@ struct BatchSummary {
   int lm_iterations = 0;  // iterations of the batch (the slowest problem)
   int grid = 0;           // slot-kernel grid chosen by the autotuner
   int64_t graph_nodes = 0, kernel_launches = 0;
+  int64_t graph_launches = 0;  // graph launches of the LM loop (1 with the device-side loop)
 };
 
 class BatchSolverBase {

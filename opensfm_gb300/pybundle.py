@@ -650,7 +650,7 @@ class BundleAdjuster:
 class BatchSummary(C.Structure):
     _fields_ = [("seconds", C.c_double), ("setup_seconds", C.c_double), ("solve_seconds", C.c_double),
                 ("lm_iterations", C.c_int), ("grid", C.c_int), ("n_problems", C.c_int), ("n_converged", C.c_int),
-                ("graph_nodes", C.c_int64), ("kernel_launches", C.c_int64)]
+                ("graph_nodes", C.c_int64), ("kernel_launches", C.c_int64), ("graph_launches", C.c_int64)]
 
 
 class BundleBatch:
@@ -693,7 +693,10 @@ class BundleBatch:
         return int(self._L.gbba_batch_size(self._h))
 
     def set_options(self, precision: str = "mixed", max_iterations: int = 50, pcg_iterations: int = 50,
-                    pcg_tolerance: float = 1e-3, use_graph: bool = True, autotune: bool = True) -> None:
+                    pcg_tolerance: float = 1e-3, use_graph: int = 2, autotune: bool = True) -> None:
+        """use_graph 2: the whole LM loop one graph launch (device-side
+        termination); 1: one graph launch per LM iteration; 0: plain
+        launches."""
         p = {"fp64": _lib.PRECISION_FP64, "mixed": _lib.PRECISION_MIXED}[precision]
         _lib.check(self._L.gbba_batch_set_options(self._h, p, max_iterations, pcg_iterations, pcg_tolerance,
                                                   int(use_graph), int(autotune)))

@@ -52,19 +52,43 @@ def test_batch_matches_oracle(precision):
         assert abs(got_rms - ref_rms) < 1e-3 * max(ref_rms, 1e-12) + 1e-9
 
 
-def test_graph_and_plain_launches_agree():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_device_loop_graph_and_plain_launches_agree(precision):
+    # the whole LM loop as one graph launch (device-side while node), one
+    # graph launch per LM iteration, and plain launches: the same iterations
     scenes = _problems(4, seed=9)
-    costs = []
-    for use_graph in (True, False):
-        bas = _adjusters(scenes)
+    costs, iters = [], []
+    for use_graph in (2, 1, 0):
+        bas = _adjusters(scenes, precision)
         batch = BundleBatch()
         for ba in bas:
             batch.add(ba)
-        batch.set_options(max_iterations=60, use_graph=use_graph, autotune=False)
+        batch.set_options(precision=precision, max_iterations=60, use_graph=use_graph, autotune=False,
+                          pcg_tolerance=1e-10 if precision == "fp64" else 1e-3)
         batch.run()
+        s = batch.summary()
         costs.append([ba.summary()["final_cost"] for ba in bas])
-        assert (batch.summary()["graph_nodes"] > 0) == use_graph
-    np.testing.assert_allclose(costs[0], costs[1], rtol=1e-6)
+        iters.append(s["lm_iterations"])
+        assert (s["graph_nodes"] > 0) == (use_graph > 0)
+        assert s["graph_launches"] == {2: 1, 1: s["lm_iterations"], 0: 0}[use_graph]
+        assert s["n_converged"] == len(scenes)
+    np.testing.assert_allclose(costs[0], costs[1], rtol=1e-12 if precision == "fp64" else 1e-6)
+    np.testing.assert_allclose(costs[0], costs[2], rtol=1e-12 if precision == "fp64" else 1e-6)
+    assert iters[0] == iters[1] or precision == "mixed"
+
+
+def test_device_loop_stops_at_the_iteration_limit():
+    # a limit below what the problems need: the device-side loop ends there
+    scenes = _problems(3, seed=4)
+    bas = _adjusters(scenes, "fp64")
+    batch = BundleBatch()
+    for ba in bas:
+        batch.add(ba)
+    batch.set_options(precision="fp64", max_iterations=2, use_graph=2, autotune=False, pcg_tolerance=1e-10)
+    batch.run()
+    s = batch.summary()
+    assert s["lm_iterations"] == 2 and s["graph_launches"] == 1
+    assert all(ba.summary()["final_cost"] < ba.summary()["initial_cost"] for ba in bas)
 
 
 def test_batch_rejects_free_intrinsics():
