@@ -32,27 +32,29 @@ struct RecordPassArgs {
   const double* zbuf64 = nullptr;
   PrecondView<R> pc{};
   uint64_t plane_mask = 0;  // kPermute: shot-major planes to write
+  cudaStream_t stream = 0;  // the stream the pass is launched on
 
   template <int M, int NR, int CMAX, bool RIG, typename Src>
   void launch(const Src& recs) const {
     const int g = grid;
+    const cudaStream_t s = stream;
     switch (which) {
       case kSchurRhs:
-        schur_rhs_precond_sm_kernel<R, NR, CMAX, RIG, Src><<<g, 256>>>(v, sm, recs, dout, pc);
+        schur_rhs_precond_sm_kernel<R, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, sm, recs, dout, pc);
         break;
-      case kPointPass: schur_point_pass_kernel<R, R, NR, CMAX, RIG, Src><<<g, 256>>>(v, recs, x, out); break;
+      case kPointPass: schur_point_pass_kernel<R, R, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, recs, x, out); break;
       case kCameraPass:
-        schur_camera_pass_sm_kernel<R, R, NR, CMAX, RIG, Src><<<g, 256>>>(v, sm, recs, x, zbuf, out);
+        schur_camera_pass_sm_kernel<R, R, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, sm, recs, x, zbuf, out);
         break;
       case kPointPass64:
-        schur_point_pass_kernel<R, double, NR, CMAX, RIG, Src><<<g, 256>>>(v, recs, x64, dout);
+        schur_point_pass_kernel<R, double, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, recs, x64, dout);
         break;
       case kCameraPass64:
-        schur_camera_pass_sm_kernel<R, double, NR, CMAX, RIG, Src><<<g, 256>>>(v, sm, recs, x64, zbuf64, dout);
+        schur_camera_pass_sm_kernel<R, double, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, sm, recs, x64, zbuf64, dout);
         break;
-      case kModelChange: model_change_kernel<R, NR, CMAX, RIG, Src><<<g, 256>>>(v, recs, x, dp, dout); break;
+      case kModelChange: model_change_kernel<R, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, recs, x, dp, dout); break;
       case kPermute:
-        permute_records_kernel<R, NR, CMAX, RIG, Src><<<g, 256>>>(v, sm, recs, plane_mask);
+        permute_records_kernel<R, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, sm, recs, plane_mask);
         break;
     }
   }

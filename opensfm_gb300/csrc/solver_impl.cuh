@@ -378,6 +378,20 @@ static __global__ void pcg_rotate_kernel(double* s) {
   s[kRZN] = 0.0;
 }
 
+// The stopping test of one PCG iteration in the device-side loop (the host
+// loop's test after pcg_step_kernel): counts the iteration in ctl[0] and
+// ends the loop on a non-positive curvature p.Sp, a residual within
+// tolerance (*tol2 = tol^2 |b|^2), a non-finite residual, or ctl[1]
+// iterations -- the last bound ends the loop whatever the scalars are.
+static __global__ void pcg_control_kernel(const double* __restrict__ s, int* __restrict__ ctl,
+                                          const double* __restrict__ tol2, cudaGraphConditionalHandle cond) {
+  const int it = ctl[0] + 1;
+  ctl[0] = it;
+  const double pq = s[kPQ], rr = s[kRR];
+  const bool stop = !(pq > 0.0) || rr <= *tol2 || !isfinite(rr) || it >= ctl[1];
+  cudaGraphSetConditional(cond, stop ? 0u : 1u);
+}
+
 template <typename R>
 __global__ void copy_kernel(int n, const R* __restrict__ a, R* __restrict__ b) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
@@ -656,6 +670,7 @@ class DeviceSolver : public SolverBase {
     cov = cov_;
     return cov_valid_;
   }
+  ~DeviceSolver() override { release_pcg_graph(); }
 
  protected:
   // ---- setup
@@ -672,9 +687,10 @@ class DeviceSolver : public SolverBase {
   double prior_terms(const std::vector<double>& x, bool want_derivs);
   // y += H x for the host-computed Gauss-Newton blocks
   template <typename A>
-  void host_blocks_apply(const A* x, A* y) {
+  void host_blocks_apply(const A* x, A* y, cudaStream_t st = 0) {
     if (n_hblocks_ == 0) return;
-    host_block_spmv_kernel<A><<<(8 * n_hblocks_ + 255) / 256, 256>>>(n_hblocks_, d_hbase_.get(), d_hval_.get(), x, y);
+    host_block_spmv_kernel<A><<<(8 * n_hblocks_ + 255) / 256, 256, 0, st>>>(n_hblocks_, d_hbase_.get(),
+                                                                           d_hval_.get(), x, y);
     ++launches_;
   }
   double prior_model_change(const std::vector<double>& x, const std::vector<double>& dx);
@@ -685,6 +701,25 @@ class DeviceSolver : public SolverBase {
   // ---- linear solve
   int solve_step(double mu, bool first, double& model_change, std::vector<double>& dxc);
   int run_pcg(const R* rhs, double bb, double tol, int max_it);
+  // the PCG iterations as one CUDA graph launch: a while node whose body is
+  // one iteration and pcg_control_kernel (built on first use, again when
+  // the host-term blocks move); single-rank solves only
+  int run_pcg_device_loop(int max_it, double tol2);
+  void build_pcg_graph();
+  void release_pcg_graph();
+  cudaStream_t pcg_st_ = nullptr;
+  cudaGraph_t pcg_graph_ = nullptr;
+  cudaGraphExec_t pcg_exec_ = nullptr;
+  const void* pcg_graph_key_ = nullptr;  // the host-term block values the graph reads
+  int pcg_graph_blocks_ = -1;
+  // the views the recorded passes read (matrix-free passes evaluate the
+  // current state, whose buffers trade places with the candidate's on an
+  // accepted step): the graph is rebuilt when they change
+  SolveView<R> pcg_view_{};
+  ShotMajorView<R> pcg_sm_view_{};
+  int64_t pcg_body_nodes_ = 0;
+  DeviceArray<int> d_pcg_ctl_;      // [iterations done, iteration limit]
+  DeviceArray<double> d_pcg_tol2_;  // tol^2 |b|^2
   int solve_dense(double mu);
   void assemble_dense(double mu);
   bool compute_covariances();

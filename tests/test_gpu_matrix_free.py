@@ -47,7 +47,12 @@ def test_matrix_free_matches_stored(kind, precision):
     assert _storage(stored) == "stored"
     assert _storage(free).startswith("matrix-free")
     a, b = stored.summary()["final_cost"], free.summary()["final_cost"]
-    bar = 1e-10 if precision == "fp64" else (3e-5 if kind == "street" else 1e-6)
+    # Mixed precision on the street problem (four free Brown cameras shared
+    # by 40 shots, no gauge prior) ends at a cost that varies from run to
+    # run with the FP32 atomics' summation order: three stored-record runs
+    # ended at 9694.034, 9694.037 and 9695.19 (a spread of 1.2e-4), three
+    # matrix-free runs within 3e-7 of the lower two.
+    bar = 1e-10 if precision == "fp64" else (3e-4 if kind == "street" else 1e-6)
     assert abs(a - b) / a < bar, (a, b)
     if precision == "fp64":
         # the same trajectory: the same step sequence (FP64 atomics sum in
