@@ -11,10 +11,40 @@
 
 #include "kernel_config.cuh"
 #include "record_source.cuh"
+#include "record_stage.cuh"
 #include "solver_kernels.cuh"
 #include "solver_shot_major.cuh"
 
 namespace gbba {
+
+// Streaming multiprocessors of the current device (read once, before any
+// stream capture: solver setup calls it).
+inline int device_sm_count() {
+  static const int n = [] {
+    int dev = 0, v = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return 1;
+    return v > 0 ? v : 1;
+  }();
+  return n;
+}
+
+// Raises the dynamic shared-memory limit of the staged Schur-product
+// kernels of one configuration (once, at solver setup: outside any capture).
+template <typename R>
+struct StagedPrepare {
+  template <int M, int NR, int CMAX, bool RIG>
+  void run() {
+    if constexpr (staged_record_fits<R, NR, CMAX, RIG>()) {
+      constexpr int bytes = staged_smem_bytes<R, planes_of<R>(RecordLayout<NR, CMAX, RIG>::kWidth)>();
+      cudaFuncSetAttribute(staged_point_pass_kernel<R, R, NR, CMAX, RIG>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      cudaFuncSetAttribute(staged_camera_pass_kernel<R, R, NR, CMAX, RIG>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    }
+    device_sm_count();
+  }
+};
 
 template <typename R>
 struct RecordPassArgs {
@@ -38,6 +68,24 @@ struct RecordPassArgs {
   void launch(const Src& recs) const {
     const int g = grid;
     const cudaStream_t s = stream;
+    if constexpr (Src::kPrefetch && staged_record_fits<R, NR, CMAX, RIG>()) {
+      // a single problem's stored records: the PCG's Schur-product passes
+      // stage them through shared memory (record_stage.cuh), one grid of
+      // resident blocks (the FP64 products of iterative refinement keep the
+      // register pipeline)
+      constexpr int bytes = staged_smem_bytes<R, planes_of<R>(RecordLayout<NR, CMAX, RIG>::kWidth)>();
+      const int g1 = device_sm_count() * staged_min_blocks<R, R, NR, CMAX, RIG>();
+      if (which == kPointPass) {
+        staged_point_pass_kernel<R, R, NR, CMAX, RIG><<<g < g1 ? g : g1, kStagedBlock, bytes, s>>>(
+            v, recs.pm, recs.stride, x, out);
+        return;
+      }
+      if (which == kCameraPass) {
+        staged_camera_pass_kernel<R, R, NR, CMAX, RIG><<<g < g1 ? g : g1, kStagedBlock, bytes, s>>>(
+            v, sm, recs.stride, x, zbuf, out);
+        return;
+      }
+    }
     switch (which) {
       case kSchurRhs:
         schur_rhs_precond_sm_kernel<R, NR, CMAX, RIG, Src><<<g, 256, 0, s>>>(v, sm, recs, dout, pc);

@@ -1108,6 +1108,10 @@ void DeviceSolver<R>::setup(const Problem& P, const SolverOptions& opts) {
       d_rec_.zero();  // planes skipped by plane_mask_ must read as zero
       d_rec_sm_.resize(size_t(n_planes_) * n_slots_);
       d_rec_sm_.zero();
+      // the staged Schur-product passes' shared-memory limit, set before
+      // any pass is recorded into a graph
+      StagedPrepare<R> prep;
+      dispatch_config(kc_, prep);
     } else {
       d_rec_.release();
       d_rec_sm_.release();

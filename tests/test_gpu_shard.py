@@ -131,13 +131,15 @@ def test_fp64_sharded_solve_follows_single_rank_trajectory():
     np.testing.assert_array_equal(shard[0]["trace"][:, 1], shard[1]["trace"][:, 1])  # ranks agree exactly
     np.testing.assert_array_equal(shard[0]["poses"], shard[1]["poses"])
     # the final steps of a converged solve are tiny; one taken by only one of
-    # the two solves moves the poses by far less than 1e-6
+    # the two solves moves the poses by far less than 1e-6.  The positions
+    # are UTM-scale (y ~ 4e6 m, where one FP64 ulp is 5e-10 m): they are
+    # compared to a few ulps as well.
     tol = 1e-8 if len(t1) == len(t2) else 1e-6
-    np.testing.assert_allclose(shard[0]["poses"], single["poses"], rtol=0, atol=tol)
+    np.testing.assert_allclose(shard[0]["poses"], single["poses"], rtol=1e-14, atol=tol)
     # each rank's own points against the single-rank solve's
     for r in (0, 1):
         a, b = shard[r]["range"]
-        np.testing.assert_allclose(shard[r]["points"], single["points"][a:b], rtol=0, atol=tol)
+        np.testing.assert_allclose(shard[r]["points"], single["points"][a:b], rtol=1e-14, atol=tol)
     assert shard[0]["range"][1] == shard[1]["range"][0]
 
 
