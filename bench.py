@@ -932,6 +932,8 @@ def run_ours(args) -> None:
         if not args.no_street:
             ev.close()
             result["street"] = street_benchmark(n_shots=args.street_shots, n_points=args.street_points,
+                                                max_iterations=args.street_iterations,
+                                                pcg_iterations=max(1, args.street_iterations // 2),
                                                 oracle=not args.no_street_oracle)
         result["headline"] = headline(result)
         print(json.dumps(result), flush=True)
@@ -962,8 +964,13 @@ def main() -> None:
     ap.add_argument("--no-covariance", action="store_true")
     ap.add_argument("--no-street", action="store_true", help="skip the street (500 Brown cameras) solves")
     ap.add_argument("--no-cpu-converge", action="store_true", help="skip the ring solve on the host cores")
+    ap.add_argument("--pcg-host-loop", action="store_true",
+                    help="launch the PCG kernels one by one instead of as one graph per solve (profilers see "
+                         "kernels inside graphs with conditional nodes only as a whole)")
     ap.add_argument("--no-street-oracle", action="store_true", help="skip the street solve of the FP64 CPU oracle")
     ap.add_argument("--street-shots", type=int, default=500)
+    ap.add_argument("--street-iterations", type=int, default=200,
+                    help="LM iterations of the street solves (the PCG runs take half, at least 1)")
     ap.add_argument("--street-points", type=int, default=200_000)
     ap.add_argument("--covariance-shots", type=int, default=500)
     ap.add_argument("--dense-sizes", type=int, nargs="*", default=[1024, 2048, 4096])
@@ -977,6 +984,10 @@ def main() -> None:
     if args.impl == "reference":
         run_reference(args)
     else:
+        if args.pcg_host_loop:
+            import functools
+            from opensfm_gb300 import pybundle
+            pybundle.adjuster_from_scene = functools.partial(pybundle.adjuster_from_scene, pcg_graph=False)
         run_ours(args)
 
 

@@ -462,6 +462,13 @@ int gbba_set_pcg_tolerance(gbba_adjuster_t* h, double tolerance);
  * (matrix-free); 1: always matrix-free; -1: always stored.  The exact dense
  * path always stores them. */
 int gbba_set_matrix_free(gbba_adjuster_t* h, int mode);
+/* How the PCG iterations are launched.  1 (default): all of a linear
+ * solve's iterations as one CUDA graph launch, with the stopping test on the
+ * device; 0: kernel by kernel with the scalars read on the host every
+ * iteration (the same kernels and results; a profiler sees each launch --
+ * kernels inside a graph with a conditional node are not profiled one by
+ * one).  Sharded solves always launch kernel by kernel. */
+int gbba_set_pcg_graph(gbba_adjuster_t* h, int enable);
 
 /* ---- Point-partitioned (sharded) solve over several GPUs
  *

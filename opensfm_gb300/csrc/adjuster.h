@@ -120,6 +120,7 @@ class BundleAdjuster {
   double GetGroupDensityRatio(const std::string& g) const;
   void SetPcgTolerance(double t) { opts_.pcg_tolerance = t; }
   void SetMatrixFree(int mode) { opts_.matrix_free = mode; }
+  void SetPcgGraph(bool enable) { opts_.pcg_graph = enable; }
   // Point-partitioned solve over `world` ranks (one per GPU): every rank
   // holds the whole problem, and this one solves with the points of
   // ShardRange(rank) and all of their observations, exchanging the

@@ -543,6 +543,10 @@ double gbba_get_group_density_ratio(const gbba_adjuster_t* h, const char* group)
   return v;
 }
 
+int gbba_set_pcg_graph(gbba_adjuster_t* h, int enable) {
+  return guarded([&] { ba_of(h).SetPcgGraph(enable != 0); });
+}
+
 int gbba_set_matrix_free(gbba_adjuster_t* h, int mode) {
   return guarded([&] {
     if (mode < -1 || mode > 1) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "matrix-free mode must be -1, 0 or 1");

@@ -136,6 +136,7 @@ struct SolverOptions {
   // dense-sized (dense_max_unknowns)
   bool compute_covariances = false;
   double pcg_tolerance = 1e-3;    // relative residual of the reduced system
+  bool pcg_graph = true;          // PCG iterations as one graph launch (false: kernel by kernel)
   int pcg_max_iterations = 500;
   bool compute_reprojection_errors = true;
   bool record_trace = true;

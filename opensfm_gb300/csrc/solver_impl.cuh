@@ -717,6 +717,18 @@ class DeviceSolver : public SolverBase {
   // accepted step): the graph is rebuilt when they change
   SolveView<R> pcg_view_{};
   ShotMajorView<R> pcg_sm_view_{};
+  // The view as far as the recorded passes read it: passes over stored
+  // records read neither the points nor the FP64 residuals (whose buffers
+  // trade places with the candidate's on every accepted step), so those
+  // do not force a rebuild there.
+  SolveView<R> pcg_graph_view() {
+    SolveView<R> v = view();
+    if (!matrix_free_) {
+      v.scene.points = nullptr;
+      v.resid64 = nullptr;
+    }
+    return v;
+  }
   int64_t pcg_body_nodes_ = 0;
   DeviceArray<int> d_pcg_ctl_;      // [iterations done, iteration limit]
   DeviceArray<double> d_pcg_tol2_;  // tol^2 |b|^2

@@ -102,6 +102,7 @@ def _declare(L) -> None:
         "gbba_get_group_density_ratio": ([_H, S], C.c_double),
         "gbba_set_pcg_tolerance": ([_H, C.c_double], C.c_int),
         "gbba_set_matrix_free": ([_H, C.c_int], C.c_int),
+        "gbba_set_pcg_graph": ([_H, C.c_int], C.c_int),
         "gbba_set_shard": ([_H, C.c_int, C.c_int, ALLREDUCE_FN, C.c_void_p], C.c_int),
         "gbba_get_shard_points": ([_H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
         "gbba_run": ([_H], C.c_int),
@@ -531,6 +532,12 @@ class BundleAdjuster:
         default), 1: evaluate them in every pass, -1: always store them."""
         self._check(self._L.gbba_set_matrix_free(self._h, int(mode)))
 
+    def set_pcg_graph(self, enable: bool) -> None:
+        """True (default): a linear solve's PCG iterations run as one CUDA
+        graph launch; False: kernel by kernel (a profiler then sees every
+        launch)."""
+        self._check(self._L.gbba_set_pcg_graph(self._h, int(enable)))
+
     def set_shard(self, rank: int, world_size: int, allreduce=None) -> None:
         """Makes this adjuster rank `rank` of a point-partitioned solve over
         `world_size` GPUs (include/gbba.h, gbba_set_shard).  `allreduce(data,
@@ -782,7 +789,7 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
                         matrix_free: Optional[int] = None, covariances: bool = False, depth=None,
-                        rig_pose=None, bias=None, point_priors=None) -> BundleAdjuster:
+                        rig_pose=None, bias=None, point_priors=None, pcg_graph: bool = True) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path).  ``depth``:
     depth priors (observation indices, values, stds, radial flags);
     ``rig_pose``: a fixed rig camera pose (angle-axis, centre) shared by every
@@ -791,6 +798,8 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
     indices, positions, stds) with altitude."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
+    if not pcg_graph:
+        ba.set_pcg_graph(False)
     if matrix_free is not None:
         ba.set_matrix_free(matrix_free)
     if covariances:

@@ -159,3 +159,28 @@ def test_solution_written_back_and_reports():
     assert tr[-1, 1] < tr[0, 1]
     p = ba.get_point("0")
     assert p.p.shape == (3,)
+
+
+@pytest.mark.parametrize("precision", ["fp64"])
+def test_pcg_graph_and_host_loop_agree(precision):
+    # the PCG iterations as one graph launch (device-side stopping test) and
+    # kernel by kernel (scalars read on the host): the same kernels in the
+    # same order, so the same trajectory (FP64 atomics may sum in another
+    # order, hence the 1e-10).  In mixed precision the FP32 atomics alone
+    # move this street problem's trajectory by ~1e-7 per step from run to
+    # run (the matrix-free test records the spread), so only FP64 is compared.
+    scene = syn.street_scene(n_shots=40, n_points=3000, seed=11, outlier_ratio=0.0)
+    traces = []
+    for graph in (True, False):
+        ba = adjuster_from_scene(scene, precision=precision, loss=("SoftLOneLoss", 1.0), irls="none",
+                                 max_iterations=8, gps=False, linear_solver="ITERATIVE_SCHUR",
+                                 pcg_tolerance=1e-10 if precision == "fp64" else 1e-3, pcg_graph=graph)
+        ba.run()
+        traces.append(ba.trace())
+    a, b = traces
+    assert a.shape == b.shape
+    np.testing.assert_allclose(a[:, 1], b[:, 1], rtol=1e-10 if precision == "fp64" else 1e-6)
+    # the same accepted and rejected steps while the cost still moves; at the
+    # optimum the step-quality ratio of a step is rounding noise
+    moving = np.abs(np.diff(a[:, 1], prepend=a[0, 1])) > 1e-9 * a[:, 1]
+    np.testing.assert_array_equal(a[moving, 3], b[moving, 3])
