@@ -469,6 +469,26 @@ int gbba_set_matrix_free(gbba_adjuster_t* h, int mode);
  * kernels inside a graph with a conditional node are not profiled one by
  * one).  Sharded solves always launch kernel by kernel. */
 int gbba_set_pcg_graph(gbba_adjuster_t* h, int enable);
+/* Two-level PCG preconditioner for large blocks (an extension: Ceres'
+ * ITERATIVE_SCHUR, bundle_adjuster.cc:1159-1190, preconditions with the
+ * Schur-Jacobi blocks only).  leaf > 0 adds a coarse space: the rig
+ * instances are split into spatial clusters of at most `leaf` instances
+ * (more when the coarse system would pass 4096 unknowns), each with its
+ * seven similarity modes; the coarse matrix is probed with 7 Schur products
+ * per colour of a distance-2 colouring of the clusters once per
+ * linearization.  0 (default): block-Jacobi only.  PCG solves only (not the
+ * exact dense path, not sharded solves). */
+int gbba_set_coarse_preconditioner(gbba_adjuster_t* h, int leaf);
+/* The coarse space of the last run: clusters, colours, and the Schur
+ * products spent probing the coarse matrix (all 0 when it was not used). */
+int gbba_get_coarse_info(const gbba_adjuster_t* h, int* clusters, int* colours, int64_t* probes);
+/* The coarse space the current problem would get (host only, no solve):
+ * the cluster of every rig instance in insertion order (-1: no free
+ * coordinate; cluster_of_instance holds n_instances entries), the colour of
+ * every cluster (colour_of_cluster holds up to cluster_capacity entries),
+ * and the counts. */
+int gbba_coarse_space_layout(gbba_adjuster_t* h, int leaf, int* cluster_of_instance, int64_t n_instances,
+                             int* colour_of_cluster, int cluster_capacity, int* clusters, int* colours);
 
 /* ---- Point-partitioned (sharded) solve over several GPUs
  *

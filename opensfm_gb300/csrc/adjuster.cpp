@@ -357,6 +357,14 @@ std::pair<int64_t, int64_t> BundleAdjuster::ShardRange(int rank) const {
   return {a, b};
 }
 
+CoarseSpace BundleAdjuster::CoarseLayout(int leaf) {
+  PrepareRun();
+  std::vector<uint8_t> fm(problem_.instances.size() * 6);
+  for (size_t i = 0; i < problem_.instances.size(); ++i)
+    for (int k = 0; k < 6; ++k) fm[6 * i + k] = problem_.instances[i].free_mask[k];
+  return build_coarse_space(problem_, fm, leaf);
+}
+
 void BundleAdjuster::Run() {
   PrepareRun();
   opts_.compute_covariances = compute_covariances_;

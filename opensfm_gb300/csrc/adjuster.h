@@ -11,6 +11,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "coarse_space.h"
 #include "problem.h"
 
 namespace gbba {
@@ -121,6 +122,9 @@ class BundleAdjuster {
   void SetPcgTolerance(double t) { opts_.pcg_tolerance = t; }
   void SetMatrixFree(int mode) { opts_.matrix_free = mode; }
   void SetPcgGraph(bool enable) { opts_.pcg_graph = enable; }
+  void SetCoarsePreconditioner(int leaf) { opts_.coarse_leaf = leaf; }
+  // the coarse space a run would build (the run-time set-up, no solve)
+  CoarseSpace CoarseLayout(int leaf);
   // Point-partitioned solve over `world` ranks (one per GPU): every rank
   // holds the whole problem, and this one solves with the points of
   // ShardRange(rank) and all of their observations, exchanging the

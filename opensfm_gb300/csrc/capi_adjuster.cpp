@@ -547,6 +547,38 @@ int gbba_set_pcg_graph(gbba_adjuster_t* h, int enable) {
   return guarded([&] { ba_of(h).SetPcgGraph(enable != 0); });
 }
 
+int gbba_set_coarse_preconditioner(gbba_adjuster_t* h, int leaf) {
+  return guarded([&] {
+    if (leaf < 0) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "coarse cluster size must be >= 0");
+    ba_of(h).SetCoarsePreconditioner(leaf);
+  });
+}
+
+int gbba_get_coarse_info(const gbba_adjuster_t* h, int* clusters, int* colours, int64_t* probes) {
+  return guarded([&] {
+    const gbba::SolveSummary& s = ba_of(h).Summary();
+    if (clusters) *clusters = s.coarse_clusters;
+    if (colours) *colours = s.coarse_colours;
+    if (probes) *probes = s.coarse_probes;
+  });
+}
+
+int gbba_coarse_space_layout(gbba_adjuster_t* h, int leaf, int* cluster_of_instance, int64_t n_instances,
+                             int* colour_of_cluster, int cluster_capacity, int* clusters, int* colours) {
+  return guarded([&] {
+    if (leaf < 1) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "coarse cluster size must be >= 1");
+    const gbba::CoarseSpace cs = ba_of(h).CoarseLayout(leaf);
+    if (n_instances != int64_t(cs.cluster.size()))
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "cluster_of_instance must hold one entry per rig instance");
+    need(cluster_of_instance, "cluster_of_instance");
+    std::copy(cs.cluster.begin(), cs.cluster.end(), cluster_of_instance);
+    if (colour_of_cluster)
+      for (int c = 0; c < std::min(cluster_capacity, cs.n_clusters); ++c) colour_of_cluster[c] = cs.colour[c];
+    if (clusters) *clusters = cs.n_clusters;
+    if (colours) *colours = cs.n_colours;
+  });
+}
+
 int gbba_set_matrix_free(gbba_adjuster_t* h, int mode) {
   return guarded([&] {
     if (mode < -1 || mode > 1) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "matrix-free mode must be -1, 0 or 1");

@@ -716,11 +716,11 @@ __device__ __forceinline__ void load_tile(float* Ms, const float* __restrict__ m
   }
 }
 
-// Vs[j][c] = V[j * K + c] for c < K, else 0 (128 rows)
-__device__ __forceinline__ void load_rhs(float* Vs, const float* __restrict__ v, int K) {
+// Vs[j][c] = V[j * ldv + c] for c < K, else 0 (128 rows)
+__device__ __forceinline__ void load_rhs(float* Vs, const float* __restrict__ v, int K, int ldv) {
   for (int e = threadIdx.x; e < kTile * kRhs; e += kTsThreads) {
     const int j = e / kRhs, c = e % kRhs;
-    Vs[e] = c < K ? v[int64_t(j) * K + c] : 0.f;
+    Vs[e] = c < K ? v[int64_t(j) * ldv + c] : 0.f;
   }
 }
 
@@ -743,17 +743,22 @@ __device__ __forceinline__ void tile_product(const float* Ms, const float* Vs, f
 }
 
 // Forward step k: Y_k = Dinv_k B_k (CTA 0 stores it), B_i -= L_ik Y_k for
-// i = k + blockIdx.x > k.
+// i = k + blockIdx.x > k.  B and Y are [n_pad][ldb] row-major; CTA column
+// blockIdx.y takes the K columns from 32 blockIdx.y.
 __global__ void __launch_bounds__(kTsThreads) mfwd_step_kernel(const float* __restrict__ L, int ld,
                                                                const float* __restrict__ dinv, int k, int K,
-                                                               float* __restrict__ B, float* __restrict__ Y) {
+                                                               int ldb, float* __restrict__ B,
+                                                               float* __restrict__ Y) {
   extern __shared__ __align__(16) float msm[];
   float* Ms = msm;
   float* Vs = Ms + kTile * kMsLd;
   float* Os = Vs + kTile * kRhs;
   const int r0 = (threadIdx.x >> 3) * 4, c0 = (threadIdx.x & 7) * 4;
+  const int col = int(blockIdx.y) * kRhs;
+  B += col;
+  Y += col;
   load_tile(Ms, dinv + int64_t(k) * kTile * kTile, kTile, true);
-  load_rhs(Vs, B + int64_t(k) * kTile * K, K);
+  load_rhs(Vs, B + int64_t(k) * kTile * ldb, K, ldb);
   __syncthreads();
   float acc[4][4];
   tile_product(Ms, Vs, acc);
@@ -766,7 +771,7 @@ __global__ void __launch_bounds__(kTsThreads) mfwd_step_kernel(const float* __re
     for (int a = 0; a < 4; ++a)
 #pragma unroll
       for (int b = 0; b < 4; ++b)
-        if (c0 + b < K) Y[(int64_t(k) * kTile + r0 + a) * K + c0 + b] = acc[a][b];
+        if (c0 + b < K) Y[(int64_t(k) * kTile + r0 + a) * ldb + c0 + b] = acc[a][b];
     return;
   }
   const int i = k + int(blockIdx.x);
@@ -778,21 +783,25 @@ __global__ void __launch_bounds__(kTsThreads) mfwd_step_kernel(const float* __re
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b)
-      if (c0 + b < K) B[(int64_t(i) * kTile + r0 + a) * K + c0 + b] -= acc[a][b];
+      if (c0 + b < K) B[(int64_t(i) * kTile + r0 + a) * ldb + c0 + b] -= acc[a][b];
 }
 
 // Backward step k: X_k = Dinv_k^T Y_k (CTA k stores it), Y_i -= L_ki^T X_k
-// for i = blockIdx.x < k.
+// for i = blockIdx.x < k; columns as in the forward step.
 __global__ void __launch_bounds__(kTsThreads) mbwd_step_kernel(const float* __restrict__ L, int ld,
                                                                const float* __restrict__ dinv, int k, int K,
-                                                               float* __restrict__ Y, float* __restrict__ X) {
+                                                               int ldb, float* __restrict__ Y,
+                                                               float* __restrict__ X) {
   extern __shared__ __align__(16) float msm[];
   float* Ms = msm;
   float* Vs = Ms + kTile * kMsLd;
   float* Os = Vs + kTile * kRhs;
   const int r0 = (threadIdx.x >> 3) * 4, c0 = (threadIdx.x & 7) * 4;
+  const int col = int(blockIdx.y) * kRhs;
+  Y += col;
+  X += col;
   load_tile(Ms, dinv + int64_t(k) * kTile * kTile, kTile, false);
-  load_rhs(Vs, Y + int64_t(k) * kTile * K, K);
+  load_rhs(Vs, Y + int64_t(k) * kTile * ldb, K, ldb);
   __syncthreads();
   float acc[4][4];
   tile_product(Ms, Vs, acc);
@@ -806,7 +815,7 @@ __global__ void __launch_bounds__(kTsThreads) mbwd_step_kernel(const float* __re
     for (int a = 0; a < 4; ++a)
 #pragma unroll
       for (int b = 0; b < 4; ++b)
-        if (c0 + b < K) X[(int64_t(k) * kTile + r0 + a) * K + c0 + b] = acc[a][b];
+        if (c0 + b < K) X[(int64_t(k) * kTile + r0 + a) * ldb + c0 + b] = acc[a][b];
     return;
   }
   __syncthreads();
@@ -817,7 +826,7 @@ __global__ void __launch_bounds__(kTsThreads) mbwd_step_kernel(const float* __re
   for (int a = 0; a < 4; ++a)
 #pragma unroll
     for (int b = 0; b < 4; ++b)
-      if (c0 + b < K) Y[(int64_t(i) * kTile + r0 + a) * K + c0 + b] -= acc[a][b];
+      if (c0 + b < K) Y[(int64_t(i) * kTile + r0 + a) * ldb + c0 + b] -= acc[a][b];
 }
 
 // Z = D X (FP64, rows < n)
@@ -1122,6 +1131,64 @@ int DenseSpdSolver::solve(const double* b, double* x, double tol, int max_iterat
   return out.status;
 }
 
+// B = D (identity) on the first n columns of the [n_pad][ldb] matrix
+__global__ void unit_rhs_kernel(int n, int n_pad, int ldb, const double* __restrict__ d, float* __restrict__ B) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n_pad) * ldb) return;
+  const int row = int(t / ldb), c = int(t - int64_t(row) * ldb);
+  B[t] = (row == c && row < n) ? float(d[row]) : 0.f;
+}
+
+// inv[row][c] = d[row] X[row][c] for rows and columns < n
+__global__ void inverse_store_kernel(int n, int ldb, const double* __restrict__ d, const float* __restrict__ X,
+                                     float* __restrict__ inv, int ld) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n) * n) return;
+  const int row = int(t / n), c = int(t - int64_t(row) * n);
+  inv[int64_t(row) * ld + c] = float(d[row] * double(X[int64_t(row) * ldb + c]));
+}
+
+// inv = (inv + inv^T) / 2
+__global__ void symmetrize_kernel(int n, float* __restrict__ inv, int ld) {
+  const int64_t t = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (t >= int64_t(n) * n) return;
+  const int i = int(t / n), j = int(t - int64_t(i) * n);
+  if (j >= i) return;
+  const float a = inv[int64_t(i) * ld + j], b = inv[int64_t(j) * ld + i];
+  const float v = 0.5f * (a + b);
+  inv[int64_t(i) * ld + j] = v;
+  inv[int64_t(j) * ld + i] = v;
+}
+
+void DenseSpdSolver::explicit_inverse(float* inv, int ld) {
+  if (n_ <= 0) return;
+  const int n = n_;
+  const int ldb = (n + kRhs - 1) / kRhs * kRhs;
+  const int batches = ldb / kRhs;
+  const size_t vk = size_t(n_pad_) * ldb;
+  mts_.resize(3 * vk);
+  static bool configured = false;
+  if (!configured) {
+    set_smem(reinterpret_cast<const void*>(mfwd_step_kernel), kMsteps);
+    set_smem(reinterpret_cast<const void*>(mbwd_step_kernel), kMsteps);
+    configured = true;
+  }
+  float* TB = mts_.get();
+  float* TY = TB + vk;
+  float* TX = TY + vk;
+  unit_rhs_kernel<<<int((int64_t(vk) + 255) / 256), 256>>>(n, n_pad_, ldb, dscale_.get(), TB);
+  // every column batch in the same launch (blockIdx.y)
+  for (int k = 0; k < nt_; ++k)
+    mfwd_step_kernel<<<dim3(nt_ - k, batches), kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, kRhs, ldb,
+                                                                     TB, TY);
+  for (int k = nt_ - 1; k >= 0; --k)
+    mbwd_step_kernel<<<dim3(k + 1, batches), kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, kRhs, ldb, TY,
+                                                                   TX);
+  inverse_store_kernel<<<int((int64_t(n) * n + 255) / 256), 256>>>(n, ldb, dscale_.get(), TX, inv, ld);
+  symmetrize_kernel<<<int((int64_t(n) * n + 255) / 256), 256>>>(n, inv, ld);
+  GB_CUDA(cudaGetLastError());
+}
+
 int DenseSpdSolver::inverse_columns(const int* unit, int m, const int* gather, double* out, double tol,
                                     int max_iterations) {
   if (n_ <= 0 || m <= 0) return 0;
@@ -1163,9 +1230,9 @@ int DenseSpdSolver::inverse_columns(const int* unit, int m, const int* gather, d
     auto precondition = [&](double* Z) {
       GB_CUDA(cudaMemcpyAsync(TB, RS, vk * sizeof(float), cudaMemcpyDeviceToDevice));
       for (int k = 0; k < nt_; ++k)
-        mfwd_step_kernel<<<nt_ - k, kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, K, TB, TY);
+        mfwd_step_kernel<<<nt_ - k, kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, K, K, TB, TY);
       for (int k = nt_ - 1; k >= 0; --k)
-        mbwd_step_kernel<<<k + 1, kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, K, TY, TX);
+        mbwd_step_kernel<<<k + 1, kTsThreads, kMsteps>>>(L_.get(), n_pad_, dinv_.get(), k, K, K, TY, TX);
       mts_finish_kernel<<<gn, 256>>>(n, K, dscale_.get(), TX, Z);
     };
     mscal_.zero();

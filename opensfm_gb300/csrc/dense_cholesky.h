@@ -40,6 +40,12 @@ class DenseSpdSolver {
   // returns x at the dense indices gather[6 c .. 6 c + 5] (-1: 0) in
   // out[6 c .. 6 c + 5].  Host arrays of m columns.  Returns 0, or 1 when a
   // column met p.Ap <= 0 or did not converge within max_iterations.
+  // inv = D (L L^T)^-1 D, the inverse through the FP32 factor only (no
+  // refinement), as an n x n FP32 row-major matrix with leading dimension
+  // ld, symmetrized: the factor as a preconditioner, applied by one matrix
+  // product.  The multi-right-hand-side triangular steps solve all columns
+  // at once, 32 per CTA column of each step's grid.
+  void explicit_inverse(float* inv, int ld);
   static constexpr int kInverseBatch = 32;
   int inverse_columns(const int* unit, int m, const int* gather, double* out, double tol, int max_iterations);
   int n() const { return n_; }

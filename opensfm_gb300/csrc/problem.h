@@ -137,6 +137,10 @@ struct SolverOptions {
   bool compute_covariances = false;
   double pcg_tolerance = 1e-3;    // relative residual of the reduced system
   bool pcg_graph = true;          // PCG iterations as one graph launch (false: kernel by kernel)
+  // two-level PCG preconditioner: > 0 adds a coarse space of similarity
+  // modes over spatial clusters of at most this many rig instances
+  // (coarse_space.h); 0: block-Jacobi only
+  int coarse_leaf = 0;
   int pcg_max_iterations = 500;
   bool compute_reprojection_errors = true;
   bool record_trace = true;
@@ -202,6 +206,10 @@ struct SolveSummary {
   int64_t pcg_refinements = 0;  // FP64 residual evaluations (mixed-precision iterative refinement)
   int64_t linear_solver_failures = 0;  // dense factorizations that found the damped system not positive definite
   bool matrix_free = false;      // the record passes evaluated the Jacobians instead of reading them
+  // two-level preconditioner: clusters, colours of the probe set, and the
+  // Schur products spent on probing the coarse matrix
+  int coarse_clusters = 0, coarse_colours = 0;
+  int64_t coarse_probes = 0;
   std::string linear_solver;
   std::vector<IterationRecord> trace;
   std::vector<std::string> irls_lines;

@@ -13,6 +13,8 @@
 #include <sstream>
 #include <vector>
 
+#include "coarse_kernels.cuh"
+#include "coarse_space.h"
 #include "dense_cholesky.h"
 #include "dense_schur.cuh"
 #include "host_blocks.cuh"
@@ -729,6 +731,7 @@ class DeviceSolver : public SolverBase {
     }
     return v;
   }
+  bool pcg_graph_coarse_ = false;  // the graph applies the coarse correction
   int64_t pcg_body_nodes_ = 0;
   DeviceArray<int> d_pcg_ctl_;      // [iterations done, iteration limit]
   DeviceArray<double> d_pcg_tol2_;  // tol^2 |b|^2
@@ -805,6 +808,21 @@ class DeviceSolver : public SolverBase {
   int64_t n_pairs_ = 0;
   int64_t dense_failures_ = 0;  // factorizations that found the system not positive definite
   DenseSpdSolver dense_solver_;
+  // two-level preconditioner (coarse_space.h): built at the first PCG
+  // step; the Galerkin matrix is probed once per linearization and
+  // factored with the damping of every step
+  void coarse_prepare();
+  void coarse_apply(const R* r, R* z, double* rz, cudaStream_t st);
+  bool coarse_built_ = false, coarse_stale_ = true, coarse_active_ = false, coarse_have_e_ = false;
+  CoarseSpace cs_;
+  int64_t coarse_probes_ = 0;
+  int last_pcg_iterations_ = 0;  // of the previous linear solve
+  DeviceArray<double> d_cbasis_, d_cE_, d_cW_, d_cw_, d_cu_, d_cscal_;
+  DeviceArray<int> d_ccluster_, d_ccolour_, d_cpartner_, d_cmstart_, d_cmembers_;
+  DeviceArray<R> d_czero_, d_cprobe_;
+  DeviceArray<float> d_cinv_;  // E^-1 through the FP32 factor, [m][ld]
+  int coarse_ld_ = 0;
+  DenseSpdSolver coarse_solver_;
   std::vector<double> last_errors_, last_weights_;
 
   // device state
@@ -1475,6 +1493,7 @@ struct LinearizeLaunch {
 
 template <typename R>
 void DeviceSolver<R>::linearize() {
+  coarse_stale_ = true;
   d_Vp_.zero();
   d_gp_.zero();
   d_gc_.zero();

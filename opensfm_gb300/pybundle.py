@@ -103,6 +103,10 @@ def _declare(L) -> None:
         "gbba_set_pcg_tolerance": ([_H, C.c_double], C.c_int),
         "gbba_set_matrix_free": ([_H, C.c_int], C.c_int),
         "gbba_set_pcg_graph": ([_H, C.c_int], C.c_int),
+        "gbba_set_coarse_preconditioner": ([_H, C.c_int], C.c_int),
+        "gbba_get_coarse_info": ([_H, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int64)], C.c_int),
+        "gbba_coarse_space_layout": ([_H, C.c_int, C.POINTER(C.c_int), C.c_int64, C.POINTER(C.c_int), C.c_int,
+                                      C.POINTER(C.c_int), C.POINTER(C.c_int)], C.c_int),
         "gbba_set_shard": ([_H, C.c_int, C.c_int, ALLREDUCE_FN, C.c_void_p], C.c_int),
         "gbba_get_shard_points": ([_H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)], C.c_int),
         "gbba_run": ([_H], C.c_int),
@@ -538,6 +542,31 @@ class BundleAdjuster:
         launch)."""
         self._check(self._L.gbba_set_pcg_graph(self._h, int(enable)))
 
+    def set_coarse_preconditioner(self, leaf: int) -> None:
+        """leaf > 0: two-level PCG preconditioner, block-Jacobi plus a coarse
+        space of similarity modes over spatial clusters of at most `leaf` rig
+        instances (include/gbba.h, gbba_set_coarse_preconditioner); 0 (the
+        default): block-Jacobi only."""
+        self._check(self._L.gbba_set_coarse_preconditioner(self._h, int(leaf)))
+
+    def coarse_info(self) -> dict:
+        """Clusters, colours and probe products of the last run's coarse space."""
+        a, b, c = C.c_int(0), C.c_int(0), C.c_int64(0)
+        self._check(self._L.gbba_get_coarse_info(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return {"clusters": a.value, "colours": b.value, "probes": c.value}
+
+    def coarse_space_layout(self, leaf: int, n_instances: int):
+        """The coarse space the current problem would get (no solve): the
+        cluster of every rig instance (insertion order, -1: none) and the
+        colour of every cluster."""
+        cl = np.zeros(n_instances, dtype=np.int32)
+        col = np.zeros(max(1, n_instances), dtype=np.int32)
+        nc, ncol = C.c_int(0), C.c_int(0)
+        self._check(self._L.gbba_coarse_space_layout(
+            self._h, int(leaf), cl.ctypes.data_as(C.POINTER(C.c_int)), int(n_instances),
+            col.ctypes.data_as(C.POINTER(C.c_int)), int(len(col)), C.byref(nc), C.byref(ncol)))
+        return cl, col[:nc.value].copy(), ncol.value
+
     def set_shard(self, rank: int, world_size: int, allreduce=None) -> None:
         """Makes this adjuster rank `rank` of a point-partitioned solve over
         `world_size` GPUs (include/gbba.h, gbba_set_shard).  `allreduce(data,
@@ -789,17 +818,21 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
                         gps: bool = True, constant_cameras: bool = False, max_iterations: int = 100,
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
                         matrix_free: Optional[int] = None, covariances: bool = False, depth=None,
-                        rig_pose=None, bias=None, point_priors=None, pcg_graph: bool = True) -> BundleAdjuster:
+                        rig_pose=None, bias=None, point_priors=None, pcg_graph: bool = True,
+                        coarse_leaf: int = 0) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path).  ``depth``:
     depth priors (observation indices, values, stds, radial flags);
     ``rig_pose``: a fixed rig camera pose (angle-axis, centre) shared by every
     shot (None: the identity); ``bias``: (rotation, translation, scale,
     parameters to optimise) of every camera's bias; ``point_priors``: (point
-    indices, positions, stds) with altitude."""
+    indices, positions, stds) with altitude; ``coarse_leaf``: the two-level
+    preconditioner's cluster size (0: block-Jacobi only)."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
     if not pcg_graph:
         ba.set_pcg_graph(False)
+    if coarse_leaf:
+        ba.set_coarse_preconditioner(coarse_leaf)
     if matrix_free is not None:
         ba.set_matrix_free(matrix_free)
     if covariances:
