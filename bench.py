@@ -223,6 +223,14 @@ def headline(result: dict) -> dict:
             "point_rms_mm": r3(1e3 * c["mixed_vs_fp64_solution"]["point_rms_m"]),
             "centre_rms_mm": r3(1e3 * c["mixed_vs_fp64_solution"]["centre_rms_m"]),
             "rotation_rms_urad": r3(1e6 * c["mixed_vs_fp64_solution"]["rotation_rms_rad"])}
+        tl = c.get("two_level")
+        if tl:
+            h["c3_converge_two_level"] = {
+                "mixed_s": r3(tl["mixed"]["time_to_target_s"]), "fp64_s": r3(tl["fp64"]["time_to_target_s"]),
+                "pcg_iterations_mixed_fp64": [tl["mixed"]["pcg_iterations"], tl["fp64"]["pcg_iterations"]],
+                "final_rel_to_block_jacobi_fp64": [r3(tl["mixed"]["final_rel_to_block_jacobi_fp64"]),
+                                                   r3(tl["fp64"]["final_rel_to_block_jacobi_fp64"])],
+                "clusters": tl["mixed"]["clusters"], "probes": tl["mixed"]["probes"]}
     st = result.get("street")
     if st:
         h["c2_street"] = {
@@ -397,12 +405,14 @@ def cpu_converge_baseline(max_iterations: int = 50) -> dict:
     return out
 
 
-def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_tolerance: float = 1e-3) -> dict:
+def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_tolerance: float = 1e-3,
+                       coarse_leaf: int = 32) -> dict:
     """Time to converge: FP64 and mixed-precision GPU solves of the same
     scene with a fixed objective (robust loss, IRLS off).  The FP64 solve's
     final cost C64 defines the target C64 * (1 + 1e-6); each solve reports
     the wall time (from the start of the solve, setup included) at which its
-    cost first reaches the target."""
+    cost first reaches the target.  With coarse_leaf > 0 both solves run
+    again with the two-level PCG preconditioner, timed to the same target."""
     from opensfm_gb300.pybundle import adjuster_from_scene
     out = {"loss": list(loss), "irls": "none", "max_iterations": max_iterations, "pcg_tolerance": pcg_tolerance}
     runs = {}
@@ -461,6 +471,31 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
         "rotation_rms_rad": float(np.sqrt((dr ** 2).mean())), "rotation_max_rad": float(dr.max())}
     tm, tf = out["mixed"]["time_to_target_s"], out["fp64"]["time_to_target_s"]
     out["speedup_mixed_vs_fp64"] = (tf / tm) if (tm and tf) else None
+    # the same solves with the two-level PCG preconditioner (block-Jacobi plus
+    # similarity modes over clusters of at most coarse_leaf rig instances),
+    # timed to the same target (the block-Jacobi FP64 final cost)
+    if coarse_leaf:
+        two = {"coarse_leaf": coarse_leaf}
+        for precision in ("fp64", "mixed"):
+            ba = adjuster_from_scene(scene, precision=precision, loss=loss, irls="none",
+                                     max_iterations=max_iterations, pcg_tolerance=pcg_tolerance, gps=True,
+                                     coarse_leaf=coarse_leaf)
+            ba.run()
+            s, tr, info = ba.summary(), ba.trace(), ba.coarse_info()
+            del ba
+            hit = np.nonzero(tr[:, 1] <= target)[0]
+            two[precision] = {
+                "time_to_target_s": float(tr[hit[0], 2]) if len(hit) else None,
+                "iterations_to_target": int(tr[hit[0], 0]) if len(hit) else None,
+                "final_cost": s["final_cost"], "final_rel_to_block_jacobi_fp64": (s["final_cost"] - c64) / c64,
+                "iterations": s["iterations"], "solve_s": s["seconds"], "setup_s": s["setup_seconds"],
+                "linear_solver_s": s["linear_solver_seconds"], "pcg_iterations": int(tr[:, 4].sum()),
+                "pcg_per_lm_iteration": tr[1:, 4].astype(int).tolist(), **info}
+        t2m, t2f = two["mixed"]["time_to_target_s"], two["fp64"]["time_to_target_s"]
+        two["speedup_mixed_vs_fp64"] = (t2f / t2m) if (t2m and t2f) else None
+        two["speedup_vs_block_jacobi"] = {
+            "mixed": (tm / t2m) if (tm and t2m) else None, "fp64": (tf / t2f) if (tf and t2f) else None}
+        out["two_level"] = two
     return out
 
 

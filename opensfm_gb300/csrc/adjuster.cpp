@@ -362,7 +362,7 @@ CoarseSpace BundleAdjuster::CoarseLayout(int leaf) {
   std::vector<uint8_t> fm(problem_.instances.size() * 6);
   for (size_t i = 0; i < problem_.instances.size(); ++i)
     for (int k = 0; k < 6; ++k) fm[6 * i + k] = problem_.instances[i].free_mask[k];
-  return build_coarse_space(problem_, fm, leaf);
+  return build_coarse_space(problem_, fm, leaf, point_major_order(problem_));
 }
 
 void BundleAdjuster::Run() {

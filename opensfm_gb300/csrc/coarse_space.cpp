@@ -7,6 +7,7 @@
 #include <array>
 #include <cmath>
 #include <numeric>
+#include <thread>
 
 namespace gbba {
 namespace {
@@ -59,7 +60,7 @@ void split(const std::vector<std::array<double, 3>>& c, std::vector<int>& idx, i
 }  // namespace
 
 CoarseSpace build_coarse_space(const Problem& P, const std::vector<uint8_t>& free_mask, int leaf,
-                               const std::vector<int64_t>* point_major) {
+                               const std::vector<int64_t>& point_major) {
   CoarseSpace cs;
   const int n_inst = int(P.instances.size());
   cs.cluster.assign(n_inst, -1);
@@ -110,46 +111,68 @@ CoarseSpace build_coarse_space(const Problem& P, const std::vector<uint8_t>& fre
     const int inst = (o.shot >= 0 && size_t(o.shot) < P.shots.size()) ? P.shots[o.shot].instance : -1;
     return inst >= 0 ? cs.cluster[inst] : -1;
   };
-  std::vector<int> seen;
-  auto link_point = [&]() {
-    if (seen.size() < 2) return;
-    std::sort(seen.begin(), seen.end());
-    seen.erase(std::unique(seen.begin(), seen.end()), seen.end());
-    for (size_t a = 0; a < seen.size(); ++a)
-      for (size_t b = a + 1; b < seen.size(); ++b) link(seen[a], seen[b]);
-  };
-  const size_t n_pts = P.points.size();
-  if (point_major) {
-    int cur = -1;
-    for (int64_t o : *point_major) {
-      if (o < 0 || size_t(o) >= P.observations.size()) continue;
-      const Observation& ob = P.observations[size_t(o)];
-      if (ob.point != cur) {
-        link_point();
-        seen.clear();
-        cur = ob.point;
+  {
+    // host threads over ranges of whole points, each with its own bitset
+    const std::vector<int64_t>& pm = point_major;
+    const size_t n_pm = pm.size();
+    const int n_thr = int(std::max<size_t>(1, std::min<size_t>(16, std::min<size_t>(
+                                                  std::thread::hardware_concurrency(), n_pm / 65536 + 1))));
+    auto point_of = [&](size_t q) {
+      const int64_t o = pm[q];
+      return (o < 0 || size_t(o) >= P.observations.size()) ? -1 : P.observations[size_t(o)].point;
+    };
+    std::vector<size_t> cut(n_thr + 1, n_pm);
+    cut[0] = 0;
+    for (int k = 1; k < n_thr; ++k) {
+      size_t q = std::max(cut[k - 1], n_pm * size_t(k) / size_t(n_thr));
+      // advance to the first entry of a new point (entries without an
+      // observation may sit inside a point's run)
+      int prev = -2;
+      for (size_t b = q; b > cut[k - 1]; --b)
+        if (point_of(b - 1) >= 0) {
+          prev = point_of(b - 1);
+          break;
+        }
+      while (q < n_pm && (point_of(q) < 0 || point_of(q) == prev)) ++q;
+      cut[k] = q;
+    }
+    const size_t words = (size_t(nc) + 63) / 64;
+    std::vector<std::vector<uint64_t>> part(n_thr, std::vector<uint64_t>(size_t(nc) * words, 0));
+    auto work = [&](int k) {
+      std::vector<uint64_t>& a = part[k];
+      std::vector<int> s;
+      auto flush = [&]() {
+        if (s.size() < 2) return;
+        std::sort(s.begin(), s.end());
+        s.erase(std::unique(s.begin(), s.end()), s.end());
+        for (size_t x = 0; x < s.size(); ++x)
+          for (size_t y = x + 1; y < s.size(); ++y) {
+            a[size_t(s[x]) * words + (s[y] >> 6)] |= uint64_t(1) << (s[y] & 63);
+            a[size_t(s[y]) * words + (s[x] >> 6)] |= uint64_t(1) << (s[x] & 63);
+          }
+      };
+      int cur = -1;
+      for (size_t q = cut[k]; q < cut[k + 1]; ++q) {
+        const int64_t o = pm[q];
+        if (o < 0 || size_t(o) >= P.observations.size()) continue;
+        const Observation& ob = P.observations[size_t(o)];
+        if (ob.point != cur) {
+          flush();
+          s.clear();
+          cur = ob.point;
+        }
+        const int c = cluster_of_obs(ob);
+        if (c >= 0) s.push_back(c);
       }
-      const int c = cluster_of_obs(ob);
-      if (c >= 0) seen.push_back(c);
-    }
-    link_point();
-  } else {
-    std::vector<int64_t> start(n_pts + 1, 0);
-    for (const Observation& o : P.observations)
-      if (o.point >= 0 && size_t(o.point) < n_pts) ++start[o.point + 1];
-    for (size_t p = 0; p < n_pts; ++p) start[p + 1] += start[p];
-    std::vector<int> obs_cluster(static_cast<size_t>(start[n_pts]), -1);
-    {
-      std::vector<int64_t> fill(start.begin(), start.end() - 1);
-      for (const Observation& o : P.observations)
-        if (o.point >= 0 && size_t(o.point) < n_pts) obs_cluster[size_t(fill[o.point]++)] = cluster_of_obs(o);
-    }
-    for (size_t p = 0; p < n_pts; ++p) {
-      seen.clear();
-      for (int64_t q = start[p]; q < start[p + 1]; ++q)
-        if (obs_cluster[size_t(q)] >= 0) seen.push_back(obs_cluster[size_t(q)]);
-      link_point();
-    }
+      flush();
+    };
+    std::vector<std::thread> pool;
+    for (int k = 1; k < n_thr; ++k) pool.emplace_back(work, k);
+    work(0);
+    for (std::thread& th : pool) th.join();
+    for (int k = 0; k < n_thr; ++k)
+      for (int a = 0; a < nc; ++a)
+        for (size_t w = 0; w < words; ++w) adj[a][w] |= part[k][size_t(a) * words + w];
   }
   for (const RelativeTerm& t : P.relative_terms)
     for (int a = 0; a < t.n_shots; ++a)
@@ -216,6 +239,20 @@ CoarseSpace build_coarse_space(const Problem& P, const std::vector<uint8_t>& fre
         for (int j = 0; j < 7; ++j) Z[a * 7 + j] = 0.0;
   }
   return cs;
+}
+
+std::vector<int64_t> point_major_order(const Problem& P) {
+  const size_t n_pts = P.points.size();
+  std::vector<int64_t> start(n_pts + 1, 0);
+  for (const Observation& o : P.observations)
+    if (o.point >= 0 && size_t(o.point) < n_pts) ++start[o.point + 1];
+  for (size_t p = 0; p < n_pts; ++p) start[p + 1] += start[p];
+  std::vector<int64_t> order(static_cast<size_t>(start[n_pts]));
+  for (size_t i = 0; i < P.observations.size(); ++i) {
+    const int p = P.observations[i].point;
+    if (p >= 0 && size_t(p) < n_pts) order[size_t(start[p]++)] = int64_t(i);
+  }
+  return order;
 }
 
 }  // namespace gbba

@@ -56,10 +56,13 @@ constexpr int kMaxCoarseDim = 4096;
 
 // Builds the coarse space of problem P at the instances' current values.
 // free_mask: per instance, six flags of its optimised coordinates (after the
-// solver's own locking).  point_major (optional): the observation indices
-// grouped by point (entries < 0 are skipped), which saves sorting them.
-// Returns n_clusters = 0 when fewer than two clusters would form.
+// solver's own locking).  point_major: the observation indices grouped by
+// point (entries < 0 are skipped), as the solver's point-major slots hold
+// them.  Returns n_clusters = 0 when fewer than two clusters would form.
 CoarseSpace build_coarse_space(const Problem& P, const std::vector<uint8_t>& free_mask, int leaf,
-                               const std::vector<int64_t>* point_major = nullptr);
+                               const std::vector<int64_t>& point_major);
+
+// The observation indices of P grouped by point (a stable counting sort).
+std::vector<int64_t> point_major_order(const Problem& P);
 
 }  // namespace gbba

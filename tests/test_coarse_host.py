@@ -23,9 +23,11 @@ def cluster_graph(scene, cluster):
     return adj
 
 
-@pytest.mark.parametrize("leaf", [4, 8, 16])
-def test_aerial_clusters_and_distance2_colouring(leaf):
-    scene = syn.aerial_scene(seed=3, nx=12, ny=12, n_points=3000)
+@pytest.mark.parametrize("leaf,nx,n_points", [(4, 12, 3000), (8, 12, 3000), (16, 12, 3000), (8, 24, 24000)])
+def test_aerial_clusters_and_distance2_colouring(leaf, nx, n_points):
+    # the larger case (about 200k observations) builds the coupling graph on
+    # several host threads
+    scene = syn.aerial_scene(seed=3, nx=nx, ny=nx, n_points=n_points)
     ba = adjuster_from_scene(scene, precision="fp64")
     n_inst = len(scene.rig_instance_poses)
     cluster, colour, n_col = ba.coarse_space_layout(leaf, n_inst)
@@ -37,7 +39,7 @@ def test_aerial_clusters_and_distance2_colouring(leaf):
     # clusters are compact: the median cluster spans a few camera spacings
     c = scene.rig_instance_poses[:, 3:]
     span = np.median([np.ptp(c[cluster == k, :2], axis=0).max() for k in range(nc)])
-    spacing = np.median(np.linalg.norm(np.diff(c[:12, :2], axis=0), axis=1))
+    spacing = np.median(np.linalg.norm(np.diff(c[:nx, :2], axis=0), axis=1))
     assert span <= 2.0 * np.sqrt(leaf) * spacing
     # distance-2 colouring: within every closed neighbourhood each colour once
     adj = cluster_graph(scene, cluster)
