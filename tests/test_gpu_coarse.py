@@ -55,7 +55,7 @@ def test_two_level_graph_and_host_loop_agree():
         traces.append(ba.trace())
     a, b = traces
     assert a.shape == b.shape
-    np.testing.assert_allclose(a[:, 1], b[:, 1], rtol=1e-10)
+    np.testing.assert_allclose(a[:, 1], b[:, 1], rtol=1e-8)  # FP64 atomics of the passes, as for block-Jacobi
     np.testing.assert_array_equal(a[:, 3], b[:, 3])
     # the iteration counts at the 1e-10 tolerance may differ by a few: the
     # coarse correction goes through the FP32 factor, whose input rounds the

@@ -166,7 +166,9 @@ def test_pcg_graph_and_host_loop_agree(precision):
     # the PCG iterations as one graph launch (device-side stopping test) and
     # kernel by kernel (scalars read on the host): the same kernels in the
     # same order, so the same trajectory (FP64 atomics may sum in another
-    # order, hence the 1e-10).  In mixed precision the FP32 atomics alone
+    # order: over 8 LM steps that has moved the cost by up to 7e-10, hence
+    # the 1e-8; a kernel missing or out of order moves it by far more).  In
+    # mixed precision the FP32 atomics alone
     # move this street problem's trajectory by ~1e-7 per step from run to
     # run (the matrix-free test records the spread), so only FP64 is compared.
     scene = syn.street_scene(n_shots=40, n_points=3000, seed=11, outlier_ratio=0.0)
@@ -179,7 +181,7 @@ def test_pcg_graph_and_host_loop_agree(precision):
         traces.append(ba.trace())
     a, b = traces
     assert a.shape == b.shape
-    np.testing.assert_allclose(a[:, 1], b[:, 1], rtol=1e-10 if precision == "fp64" else 1e-6)
+    np.testing.assert_allclose(a[:, 1], b[:, 1], rtol=1e-8 if precision == "fp64" else 1e-6)
     # the same accepted and rejected steps while the cost still moves; at the
     # optimum the step-quality ratio of a step is rounding noise
     moving = np.abs(np.diff(a[:, 1], prepend=a[0, 1])) > 1e-9 * a[:, 1]
