@@ -214,7 +214,7 @@ def headline(result: dict) -> dict:
          "e2e_mobs": r3(result["e2e"]["value"]), "roofline_frac": r3(result["roofline"]["frac"]),
          "cpu_port_mobs": r3(result.get("cpu_baseline", {}).get("value"))}
     c = result.get("converge")
-    if c:
+    if c and not c.get("two_level_only"):
         h["c3_converge"] = {
             "mixed_s": r3(c["mixed"]["time_to_target_s"]), "fp64_s": r3(c["fp64"]["time_to_target_s"]),
             "speedup": r3(c["speedup_mixed_vs_fp64"]),
@@ -497,6 +497,21 @@ def converge_benchmark(scene, max_iterations: int, loss=("HuberLoss", 2.0), pcg_
             "mixed": (tm / t2m) if (tm and t2m) else None, "fp64": (tf / t2f) if (tf and t2f) else None}
         out["two_level"] = two
     return out
+
+
+def two_level_run(scene, max_iterations: int, coarse_leaf: int, loss=("HuberLoss", 2.0),
+                  pcg_tolerance: float = 1e-3) -> dict:
+    """One mixed-precision solve of the converge configuration with the
+    two-level PCG preconditioner, for launch lists (no target: the
+    block-Jacobi solves that define it are not run)."""
+    from opensfm_gb300.pybundle import adjuster_from_scene
+    ba = adjuster_from_scene(scene, precision="mixed", loss=loss, irls="none", max_iterations=max_iterations,
+                             pcg_tolerance=pcg_tolerance, gps=True, coarse_leaf=max(1, coarse_leaf))
+    ba.run()
+    s, tr = ba.summary(), ba.trace()
+    return {"two_level_only": True, "final_cost": s["final_cost"], "iterations": s["iterations"],
+            "solve_s": s["seconds"], "pcg_iterations": int(tr[:, 4].sum()),
+            "pcg_per_lm_iteration": tr[1:, 4].astype(int).tolist(), **ba.coarse_info()}
 
 
 def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int = 50,
@@ -942,7 +957,10 @@ def run_ours(args) -> None:
             result["cpu_baseline"] = cpu_baseline(scene)
         if not args.no_converge:
             ev.close()
-            result["converge"] = converge_benchmark(scene, args.converge_iterations)
+            if args.two_level_only:
+                result["converge"] = two_level_run(scene, args.converge_iterations, args.coarse_leaf)
+            else:
+                result["converge"] = converge_benchmark(scene, args.converge_iterations, coarse_leaf=args.coarse_leaf)
         if not args.no_autograd:
             ev.close()
             result["autograd"] = autograd_benchmark(n_obs=args.autograd_observations)
@@ -987,6 +1005,10 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-converge", action="store_true")
     ap.add_argument("--converge-iterations", type=int, default=60)
+    ap.add_argument("--coarse-leaf", type=int, default=32,
+                    help="cluster size of the converge leg's two-level runs (0: block-Jacobi only)")
+    ap.add_argument("--two-level-only", action="store_true",
+                    help="converge leg: only the mixed two-level solve (for launch lists)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autograd", action="store_true")
     ap.add_argument("--no-batch", action="store_true")

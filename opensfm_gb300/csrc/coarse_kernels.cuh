@@ -29,27 +29,54 @@ __global__ void coarse_probe_kernel(int n, int n_inst, const double* __restrict_
   v[t] = val;
 }
 
-// E[7 c + i][7 partner(c, k) + j] = sum over the instances s of cluster c of
-// Z_s[:, i] . y_s (y = A v of the probe (k, j)).  One thread per (c, i);
-// each entry of E is written by one probe only, in a fixed order.
+// The seven sums Z_c^T v over the instances of cluster c (one warp: each
+// lane takes every 32nd instance, then a butterfly, so the order is fixed);
+// every lane returns the totals.
+template <typename R>
+__device__ __forceinline__ void cluster_project(int c, const double* __restrict__ basis,
+                                                const int* __restrict__ member_start, const int* __restrict__ members,
+                                                const R* __restrict__ v, double (&out)[7]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int i = 0; i < 7; ++i) out[i] = 0.0;
+  for (int q = member_start[c] + lane; q < member_start[c + 1]; q += 32) {
+    const int s = members[q];
+    const double* Z = basis + int64_t(s) * 42;
+    double x[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) x[a] = double(v[8 * s + a]);
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+      for (int i = 0; i < 7; ++i) out[i] += Z[a * 7 + i] * x[a];
+  }
+#pragma unroll
+  for (int i = 0; i < 7; ++i)
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) out[i] += __shfl_xor_sync(0xffffffffu, out[i], d);
+}
+
+// E[7 c + i][7 partner(c, k) + j] = (Z_c^T y)_i for the probe (k, j) (y = A v):
+// one warp per cluster; each entry of E is written by one probe only.
 template <typename R>
 __global__ void coarse_extract_kernel(int n_clusters, int m, int n_colours, const double* __restrict__ basis,
                                       const int* __restrict__ member_start, const int* __restrict__ members,
                                       const int* __restrict__ partner, int k, int j, const R* __restrict__ y,
                                       double* __restrict__ E) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 7 * n_clusters) return;
-  const int c1 = t / 7, i = t - 7 * c1;
+  const int c1 = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  if (c1 >= n_clusters) return;  // whole warps
   const int c2 = partner[c1 * n_colours + k];
   if (c2 < 0) return;
-  double acc = 0.0;
-  for (int q = member_start[c1]; q < member_start[c1 + 1]; ++q) {
-    const int s = members[q];
-    const double* Z = basis + int64_t(s) * 42;
+  double out[7];
+  cluster_project(c1, basis, member_start, members, y, out);
+  const int lane = threadIdx.x & 31;
+  if (lane < 7) {
+    double val = out[0];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) acc += Z[a * 7 + i] * double(y[8 * s + a]);
+    for (int i = 1; i < 7; ++i)
+      if (lane == i) val = out[i];
+    E[int64_t(7 * c1 + lane) * m + 7 * c2 + j] = val;
   }
-  E[int64_t(7 * c1 + i) * m + 7 * c2 + j] = acc;
 }
 
 // W (lower triangle) = (E + E^T) / 2.
@@ -92,22 +119,23 @@ __global__ void coarse_unit_kernel(int m, double* __restrict__ W) {
   W[int64_t(i) * m + i] = 1.0;
 }
 
-// w = Z^T r, one thread per (c, i) summing over the cluster's instances.
+// w = Z^T r, one warp per cluster.
 template <typename R>
 __global__ void coarse_restrict_kernel(int n_clusters, const double* __restrict__ basis,
                                        const int* __restrict__ member_start, const int* __restrict__ members,
                                        const R* __restrict__ r, double* __restrict__ w) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 7 * n_clusters) return;
-  const int c = t / 7, i = t - 7 * c;
-  double acc = 0.0;
-  for (int q = member_start[c]; q < member_start[c + 1]; ++q) {
-    const int s = members[q];
-    const double* Z = basis + int64_t(s) * 42;
+  const int c = int((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  if (c >= n_clusters) return;  // whole warps
+  double out[7];
+  cluster_project(c, basis, member_start, members, r, out);
+  const int lane = threadIdx.x & 31;
+  if (lane < 7) {
+    double val = out[0];
 #pragma unroll
-    for (int a = 0; a < 6; ++a) acc += Z[a * 7 + i] * double(r[8 * s + a]);
+    for (int i = 1; i < 7; ++i)
+      if (lane == i) val = out[i];
+    w[7 * c + lane] = val;
   }
-  w[t] = acc;
 }
 
 // u = inv w for the m x m FP32 matrix inv (leading dimension ld, a multiple

