@@ -259,6 +259,13 @@ def headline(result: dict) -> dict:
                          "graph_launches": b.get("graph_launches"),
                          "solve_s_device_loop_vs_per_iteration": [r3(b.get("batch_solve_s")),
                                                                   r3(b.get("per_iteration_graph", {}).get("solve_s"))]}
+        ex = b.get("exact_steps")
+        if ex:
+            h["c4_batch"]["exact_steps"] = {"problems": ex["n_problems"], "batch_s": r3(ex["batch_s"]),
+                                            "single_dense_s": r3(ex["single_dense_one_at_a_time_s"]),
+                                            "speedup": r3(ex["speedup"]),
+                                            "converged_both": ex["converged_both"],
+                                            "max_rel_cost_converged": r3(ex["max_rel_cost_batch_vs_single_converged"])}
     d = result.get("dense_rcs")
     if d and d.get("spd"):
         big = d["spd"][-1]
@@ -515,14 +522,16 @@ def two_level_run(scene, max_iterations: int, coarse_leaf: int, loss=("HuberLoss
 
 
 def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int = 50,
-                    loss=("HuberLoss", 2.0), one_at_a_time: bool = True) -> dict:
+                    loss=("HuberLoss", 2.0), one_at_a_time: bool = True, exact_problems: int = 64) -> dict:
     """Batched local bundle adjustment: n_problems uneven problems (5-60
     shots, 500-20k points, 3k-150k observations, log-uniform; Brown, fisheye
     and spherical cameras with fixed intrinsics) solved by one batch
     (per-problem trust regions on the device, one LM iteration replayed as a
     CUDA graph, autotuned slot-kernel grid) against the same problems solved
     one at a time by the single-problem solver.  Mixed precision, PCG
-    tolerance 1e-3, no IRLS."""
+    tolerance 1e-3, no IRLS.  Then exact steps (DENSE_SCHUR) on the first
+    exact_problems problems: one batch against the single-problem dense
+    solver one at a time."""
     from opensfm_gb300 import synthetic as syn
     from opensfm_gb300.pybundle import BundleBatch, adjuster_from_scene
     scenes = syn.local_ba_problems(n_problems, seed=seed)
@@ -594,6 +603,43 @@ def batch_benchmark(n_problems: int = 256, seed: int = 23, max_iterations: int =
         "median_rel_cost_batch_vs_single_unconverged": float(np.median(rel[~both])) if (~both).any() else None,
         "mean_cost_reduction": float(np.mean(1.0 - batch_costs / init_costs)),
     })
+    # exact steps (DENSE_SCHUR, the reference's linear solver for local
+    # bundles): the first exact_problems problems as one batch against the
+    # single-problem dense solver one at a time
+    sub = scenes[:exact_problems]
+
+    def exact_adjusters(single: bool):
+        return [adjuster_from_scene(sc, precision="fp64", loss=loss, irls="none", gps=False, constant_cameras=True,
+                                    max_iterations=max_iterations,
+                                    linear_solver="DENSE_SCHUR" if single else "ITERATIVE_SCHUR") for sc in sub]
+    be = exact_adjusters(False)
+    b2 = BundleBatch()
+    for ba in be:
+        b2.add(ba)
+    b2.set_options(precision="fp64", max_iterations=max_iterations, pcg_iterations=100, pcg_tolerance=1e-3)
+    b2.set_linear_solver_type("DENSE_SCHUR")
+    t0 = time.perf_counter()
+    b2.run()
+    exact_batch_s = time.perf_counter() - t0
+    se = exact_adjusters(True)
+    t0 = time.perf_counter()
+    for ba in se:
+        ba.run()
+    exact_single_s = time.perf_counter() - t0
+    eb = np.array([ba.summary()["final_cost"] for ba in be])
+    es = np.array([ba.summary()["final_cost"] for ba in se])
+    # problems that converge in both: the same exact trajectory; the others
+    # stop at the iteration limit on chaotic non-monotonic paths
+    conv = np.array([x.summary()["iterations"] < max_iterations and y.summary()["iterations"] < max_iterations
+                     for x, y in zip(be, se)])
+    rel = np.abs(eb - es) / es
+    out["exact_steps"] = {
+        "n_problems": len(sub), "n_observations": int(sum(sc.n_observations for sc in sub)),
+        "batch_s": exact_batch_s, "batch_lm_iterations": b2.summary()["lm_iterations"],
+        "single_dense_one_at_a_time_s": exact_single_s, "speedup": exact_single_s / exact_batch_s,
+        "converged_both": int(conv.sum()),
+        "max_rel_cost_batch_vs_single_converged": float(rel[conv].max()) if conv.any() else None,
+        "median_rel_cost_unconverged": float(np.median(rel[~conv])) if (~conv).any() else None}
     return out
 
 

@@ -591,6 +591,16 @@ int gbba_batch_size(const gbba_batch_t* b);
  * kernel by kernel; pick the slot-kernel grid by timing (1). */
 int gbba_batch_set_options(gbba_batch_t* b, int precision, int max_iterations, int pcg_iterations,
                            double pcg_tolerance, int use_graph, int autotune);
+/* The linear solver type of the batch's steps, as
+ * BundleAdjuster::SetLinearSolverType (bundle_adjuster.cc:482) names them
+ * and sfm::BAHelpers picks them for local bundles (DENSE_SCHUR,
+ * ba_helpers.cc:336-337).  An exact type (DENSE_SCHUR, DENSE_QR,
+ * DENSE_NORMAL_CHOLESKY, SPARSE_SCHUR, SPARSE_NORMAL_CHOLESKY) makes every
+ * step exact: FP64 records whatever precision was set, and PCG to a 1e-10
+ * relative residual with at least as many iterations as the largest
+ * problem has camera-side unknowns.  ITERATIVE_SCHUR or CGNR (the default):
+ * the options' precision and PCG.  Unknown names: GBBA_ERR_INVALID_ARGUMENT. */
+int gbba_batch_set_linear_solver(gbba_batch_t* b, const char* type);
 /* A problem has converged when an accepted step changes its cost by at
  * most tolerance * cost (default 1e-7, as gbba_run's convergence test). */
 int gbba_batch_set_function_tolerance(gbba_batch_t* b, double tolerance);

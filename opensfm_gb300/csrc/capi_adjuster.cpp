@@ -763,10 +763,14 @@ int gbba_get_trace(const gbba_adjuster_t* h, int capacity, double* records, int*
 // ---------------------------------------------------------------------------
 // Batched runs: many adjusters solved together on the device.
 
+// relative residual of the batch's exact steps
+constexpr double kBatchExactTolerance = 1e-10;
+
 struct gbba_batch {
   std::vector<gbba_adjuster_t*> items;
   gbba::BatchOptions opts;
   int precision = 1;
+  bool exact = false;  // exact steps (gbba_batch_set_linear_solver)
   gbba::BatchSummary summary;
   bool has_run = false;
 };
@@ -810,6 +814,21 @@ int gbba_batch_set_options(gbba_batch_t* b, int precision, int max_iterations, i
   });
 }
 
+int gbba_batch_set_linear_solver(gbba_batch_t* b, const char* type) {
+  return guarded([&] {
+    if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
+    need(type, "type");
+    const std::string s(type);
+    if (s == "DENSE_SCHUR" || s == "DENSE_QR" || s == "DENSE_NORMAL_CHOLESKY" || s == "SPARSE_SCHUR" ||
+        s == "SPARSE_NORMAL_CHOLESKY")
+      b->exact = true;
+    else if (s == "ITERATIVE_SCHUR" || s == "CGNR")
+      b->exact = false;
+    else
+      throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "Linear solver type " + s + " doesn't exist.");
+  });
+}
+
 int gbba_batch_set_function_tolerance(gbba_batch_t* b, double tolerance) {
   return guarded([&] {
     if (!b) throw ApiError(GBBA_ERR_INVALID_ARGUMENT, "batch handle is NULL");
@@ -841,9 +860,20 @@ int gbba_batch_run(gbba_batch_t* b) {
         }
         problems.push_back(&ba.MutableProblem());
       }
-      auto solver = gbba::make_batch_solver(b->precision);
+      // exact steps: FP64 records and PCG to a 1e-10 relative residual,
+      // with at least as many iterations as the largest problem has
+      // camera-side unknowns (the finite-termination bound of CG)
+      gbba::BatchOptions opts = b->opts;
+      int precision = b->precision;
+      if (b->exact) {
+        precision = GBBA_PRECISION_FP64;
+        opts.pcg_tolerance = std::min(opts.pcg_tolerance, kBatchExactTolerance);
+        for (gbba::Problem* P : problems)
+          opts.pcg_iterations = std::max(opts.pcg_iterations, gbba::camera_side_unknowns(*P));
+      }
+      auto solver = gbba::make_batch_solver(precision);
       try {
-        b->summary = solver->solve_batch(problems, b->opts);
+        b->summary = solver->solve_batch(problems, opts);
       } catch (const std::invalid_argument& e) {
         throw ApiError(GBBA_ERR_INVALID_ARGUMENT, e.what());
       }
@@ -863,7 +893,8 @@ int gbba_batch_run(gbba_batch_t* b) {
       s.termination = p.converged ? "CONVERGENCE" : "NO_CONVERGENCE";
       s.usable = std::isfinite(p.final_cost);
       s.seconds = b->summary.seconds;
-      s.linear_solver = "ITERATIVE_SCHUR (GPU batched implicit Schur, block-Jacobi PCG)";
+      s.linear_solver = b->exact ? "DENSE_SCHUR (GPU batched implicit Schur, FP64 PCG to a 1e-10 relative residual)"
+                                 : "ITERATIVE_SCHUR (GPU batched implicit Schur, block-Jacobi PCG)";
       ba_of(b->items[i]).SetBatchResult(s, std::move(p.errors));
     }
     b->has_run = true;

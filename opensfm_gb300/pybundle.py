@@ -708,6 +708,7 @@ class BundleBatch:
                                                             C.c_int], C.c_int),
                                 ("gbba_batch_run", [_H], C.c_int),
                                 ("gbba_batch_set_function_tolerance", [_H, C.c_double], C.c_int),
+                                ("gbba_batch_set_linear_solver", [_H, C.c_char_p], C.c_int),
                                 ("gbba_batch_get_summary", [_H, C.POINTER(BatchSummary)], C.c_int)):
             f = getattr(L, name)
             f.argtypes = args
@@ -739,6 +740,12 @@ class BundleBatch:
 
     def set_function_tolerance(self, tolerance: float) -> None:
         _lib.check(self._L.gbba_batch_set_function_tolerance(self._h, tolerance))
+
+    def set_linear_solver_type(self, name: str) -> None:
+        """DENSE_SCHUR (or another exact type): every step exact, in FP64
+        (PCG to a 1e-10 relative residual); ITERATIVE_SCHUR (the default):
+        the options' precision and PCG."""
+        _lib.check(self._L.gbba_batch_set_linear_solver(self._h, name.encode()))
 
     def run(self) -> None:
         _lib.check(self._L.gbba_batch_run(self._h))

@@ -98,3 +98,30 @@ def test_batch_rejects_free_intrinsics():
     batch.add(ba)
     with pytest.raises(Exception, match="fixed intrinsics"):
         batch.run()
+
+
+def test_batch_exact_steps_follow_the_dense_single_solver():
+    # DENSE_SCHUR, the reference's choice for local bundles (ba_helpers.cc:
+    # 336-337): every step exact (FP64, PCG to 1e-10, the iteration cap
+    # raised to the camera-side unknowns) although the options ask for mixed
+    # precision, 10 PCG iterations and a 1e-3 tolerance
+    scenes = _problems(n=5, seed=9)
+    bas = _adjusters(scenes, "mixed")
+    batch = BundleBatch()
+    for ba in bas:
+        batch.add(ba)
+    batch.set_options(precision="mixed", max_iterations=100, pcg_iterations=10, pcg_tolerance=1e-3)
+    batch.set_linear_solver_type("DENSE_SCHUR")
+    batch.run()
+    assert batch.summary()["n_converged"] == len(scenes)
+    for scene, ba in zip(scenes, bas):
+        single = adjuster_from_scene(scene, precision="fp64", loss=LOSS, irls="none", gps=False,
+                                     constant_cameras=True, max_iterations=100, linear_solver="DENSE_SCHUR")
+        single.run()
+        ref = single.summary()
+        got = ba.summary()
+        assert "DENSE_SCHUR" in ba.full_report()
+        rel = abs(got["final_cost"] - ref["final_cost"]) / ref["final_cost"]
+        assert rel < 1e-10, (got["final_cost"], ref["final_cost"])
+        assert got["iterations"] == ref["iterations"]
+

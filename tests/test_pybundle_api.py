@@ -215,3 +215,12 @@ def test_heatmap_and_residual_argument_checks(ba):
         pybundle.heatmap_residual(np.zeros(6), 4, 1.0, 0.0, 0.0, 1.0, np.zeros(6))
     r, J = pybundle.heatmap_residual(np.ones(6), 3, 1.0, 0.0, 0.0, 0.5, np.zeros(6))
     assert r == pytest.approx(2.0) and np.all(J == 0.0)  # a constant grid: value / std, no slope
+
+
+def test_batch_linear_solver_names():
+    from opensfm_gb300.pybundle import BundleBatch
+    batch = BundleBatch()
+    for name in ("DENSE_SCHUR", "SPARSE_SCHUR", "ITERATIVE_SCHUR", "CGNR"):
+        batch.set_linear_solver_type(name)
+    with pytest.raises(Exception, match="doesn't exist"):
+        batch.set_linear_solver_type("CHOLMOD")
