@@ -241,6 +241,8 @@ def headline(result: dict) -> dict:
             "pcg_speedup_mixed_vs_fp64": r3(st["pcg_speedup_mixed_vs_fp64"]),
             "pcg_final_rel_mixed_fp64": [r3(st["pcg_mixed"]["final_rel_to_exact"]),
                                          r3(st["pcg_fp64"]["final_rel_to_exact"])],
+            "pcg_mixed_two_level_s": r3(st.get("pcg_mixed_two_level", {}).get("solve_s")),
+            "pcg_mixed_two_level_final_rel": r3(st.get("pcg_mixed_two_level", {}).get("final_rel_to_exact")),
             "inlier_rms_px_exact": r3(st["exact_fp64"]["inlier_rms_px"])}
         if "oracle_rel" in st:
             oc = st["oracle_check"]
@@ -313,8 +315,9 @@ def street_benchmark(n_shots: int = 500, n_points: int = 200_000, seed: int = 7,
         e = e[inliers]
         return float(np.sqrt(np.mean(np.sum(e[:, :2] ** 2, axis=1))) * 1000.0)
 
-    def run(scene, precision, solver, iterations):
-        ba = adjuster_from_scene(scene, precision=precision, max_iterations=iterations, linear_solver=solver, **kw)
+    def run(scene, precision, solver, iterations, coarse_leaf=0):
+        ba = adjuster_from_scene(scene, precision=precision, max_iterations=iterations, linear_solver=solver,
+                                 coarse_leaf=coarse_leaf, **kw)
         t0 = time.perf_counter()
         ba.run()
         wall = time.perf_counter() - t0
@@ -331,7 +334,9 @@ def street_benchmark(n_shots: int = 500, n_points: int = 200_000, seed: int = 7,
     runs = {"exact_fp64": run(scene, "fp64", "SPARSE_SCHUR", max_iterations),
             "exact_fp64_repeat": run(scene, "fp64", "SPARSE_SCHUR", max_iterations),
             "pcg_mixed": run(scene, "mixed", "ITERATIVE_SCHUR", pcg_iterations),
-            "pcg_fp64": run(scene, "fp64", "ITERATIVE_SCHUR", pcg_iterations)}
+            "pcg_fp64": run(scene, "fp64", "ITERATIVE_SCHUR", pcg_iterations),
+            # the two-level PCG preconditioner (clusters of at most 16 shots)
+            "pcg_mixed_two_level": run(scene, "mixed", "ITERATIVE_SCHUR", pcg_iterations, coarse_leaf=16)}
     c64 = runs["exact_fp64"][0]["final_cost"]
     target = c64 * (1.0 + 1e-6)
     for name, (s, tr, errs, wall) in runs.items():
