@@ -420,6 +420,10 @@ DEFAULT_CONFIG = {
     "bundle_irls_gps_density_ratio": 0.00001, "bundle_max_iterations": 100, "local_bundle_radius": 3,
     "local_bundle_min_common_points": 20, "local_bundle_max_shots": 30, "local_bundle_grid": 12,
     "final_bundle_grid": 32,
+    # not a reference key: the two-level PCG preconditioner's cluster size
+    # for bundles solved by PCG (0: block-Jacobi only, as Ceres'
+    # SCHUR_JACOBI); it acts only once a linear solve needs many iterations
+    "bundle_coarse_leaf": 32,
 }
 
 
@@ -629,6 +633,8 @@ def _configure(ba: pybundle.BundleAdjuster, c: dict, n_shots: int) -> None:
     ba.set_group_density_ratio("GCP2D", c["bundle_irls_gcp_density_ratio"])
     ba.set_group_density_ratio("GPS", c["bundle_irls_gps_density_ratio"])
     ba.set_max_num_iterations(int(c["bundle_max_iterations"]))
+    if int(c.get("bundle_coarse_leaf", 0)) > 0:
+        ba.set_coarse_preconditioner(int(c["bundle_coarse_leaf"]))
 
 
 def _up_vector(scene: SceneArrays, gcps, c: dict) -> Optional[np.ndarray]:
