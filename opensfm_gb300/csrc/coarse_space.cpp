@@ -70,8 +70,12 @@ CoarseSpace build_coarse_space(const Problem& P, const std::vector<uint8_t>& fre
   for (int i = 0; i < n_inst; ++i) {
     bool any = false;
     for (int k = 0; k < 6; ++k) any |= free_mask[6 * size_t(i) + k] != 0;
+    bool finite = true;
+    for (int k = 0; k < 6; ++k) finite &= std::isfinite(P.instances[i].value[k]);
     for (int k = 0; k < 3; ++k) centre[i][k] = P.instances[i].value[3 + k];
-    if (any) active.push_back(i);
+    // an instance without a free coordinate (or with a non-finite pose, which
+    // the median splits could not order) joins no cluster
+    if (any && finite) active.push_back(i);
   }
   const int na = int(active.size());
   if (na < 2) return cs;

@@ -826,14 +826,15 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
                         pcg_tolerance: Optional[float] = None, linear_solver: Optional[str] = None,
                         matrix_free: Optional[int] = None, covariances: bool = False, depth=None,
                         rig_pose=None, bias=None, point_priors=None, pcg_graph: bool = True,
-                        coarse_leaf: int = 0) -> BundleAdjuster:
+                        coarse_leaf: int = 0, fixed_instances=None) -> BundleAdjuster:
     """Builds a BundleAdjuster from a SceneArrays (bulk path).  ``depth``:
     depth priors (observation indices, values, stds, radial flags);
     ``rig_pose``: a fixed rig camera pose (angle-axis, centre) shared by every
     shot (None: the identity); ``bias``: (rotation, translation, scale,
     parameters to optimise) of every camera's bias; ``point_priors``: (point
     indices, positions, stds) with altitude; ``coarse_leaf``: the two-level
-    preconditioner's cluster size (0: block-Jacobi only)."""
+    preconditioner's cluster size (0: block-Jacobi only); ``fixed_instances``:
+    rig instance indices added as constant."""
     ba = BundleAdjuster()
     ba.set_precision(precision)
     if not pcg_graph:
@@ -857,12 +858,14 @@ def adjuster_from_scene(scene, precision: str = "mixed", loss: Optional[tuple] =
         from .scene import NUM_PARAMS
         cam = Camera(m, scene.camera_values[c, : NUM_PARAMS[m]])
         ba.add_camera(str(c), cam, cam, constant_cameras)
+    fixed = set() if fixed_instances is None else {int(i) for i in fixed_instances}
     rp = Pose() if rig_pose is None else Pose.from_ba_data(np.asarray(rig_pose, np.float64))
     ba.add_rig_camera("rig", rp, rp, True)
     for s in range(len(scene.shot_camera)):
         inst = int(scene.shot_rig_instance[s])
         pose = Pose.from_ba_data(scene.rig_instance_poses[inst])
-        ba.add_rig_instance(str(inst), pose, {str(s): str(int(scene.shot_camera[s]))}, {str(s): "rig"}, False)
+        ba.add_rig_instance(str(inst), pose, {str(s): str(int(scene.shot_camera[s]))}, {str(s): "rig"},
+                            inst in fixed)
     if gps and "gps" in scene.extras:
         for s in range(len(scene.shot_camera)):
             ba.add_rig_instance_position_prior(str(int(scene.shot_rig_instance[s])), scene.extras["gps"][s],

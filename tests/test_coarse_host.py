@@ -75,3 +75,14 @@ def test_small_problems_get_no_coarse_space_and_bad_sizes_are_refused():
         ba.set_coarse_preconditioner(-1)
     with pytest.raises(Exception):
         ba.coarse_space_layout(4, 35)
+
+
+def test_fixed_instances_join_no_cluster():
+    scene = syn.aerial_scene(seed=3, nx=8, ny=8, n_points=1500)
+    fixed = [0, 9, 27, 63]
+    ba = adjuster_from_scene(scene, precision="fp64", fixed_instances=fixed)
+    cluster, colour, _ = ba.coarse_space_layout(6, 64)
+    assert np.all(cluster[fixed] == -1)
+    free = np.setdiff1d(np.arange(64), fixed)
+    assert np.all(cluster[free] >= 0)
+    assert np.bincount(cluster[free]).max() <= 6
