@@ -816,7 +816,7 @@ class DeviceSolver : public SolverBase {
   bool coarse_built_ = false, coarse_stale_ = true, coarse_active_ = false, coarse_have_e_ = false;
   CoarseSpace cs_;
   int64_t coarse_probes_ = 0;
-  int last_pcg_iterations_ = 0;  // of the previous linear solve
+  int last_pcg_iterations_ = 0, prev_pcg_iterations_ = 0;  // of the last two linear solves
   DeviceArray<double> d_cbasis_, d_cE_, d_cW_, d_cw_, d_cu_, d_cscal_;
   DeviceArray<int> d_ccluster_, d_ccolour_, d_cpartner_, d_cmstart_, d_cmembers_;
   DeviceArray<R> d_czero_, d_cprobe_;
