@@ -12,8 +12,9 @@
 // The medians are exact: a radix selection over the FP64 bit patterns
 // (mapped to order-preserving unsigned keys, 11-bit digits, one histogram
 // pass per digit for both error columns at once, the digit found by a
-// one-block scan on the device) returns the element of the requested rank,
-// so the threshold is the one a sort would give.  The whole selection runs
+// one-block scan on the device; after the third digit only the keys that
+// still match are read) returns the element of the requested rank, so the
+// threshold is the one a sort would give.  The whole selection runs
 // on the stream without a host synchronization.  Products and sums that decide a
 // comparison are rounded without contraction (__dmul_rn / __dadd_rn), as
 // the host computes them.
@@ -66,6 +67,62 @@ __global__ void digit_histogram_kernel(int64_t n, const double* __restrict__ v, 
     if (n_cols > 1) {
       const uint64_t k1 = order_key(v[i * stride + 1]);
       if ((k1 & m1) == p1) atomicAdd(&h[1][uint32_t(k1 >> shift) & digit_mask], 1u);
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < n_cols * kBins; b += blockDim.x)
+    if (h[b / kBins][b % kBins]) atomicAdd(&hist[b], h[b / kBins][b % kBins]);
+}
+
+// The same histogram that also copies the keys it counts (those matching the
+// column's prefix) to the column's candidate list cand[c * cap ..], with a
+// warp-aggregated append; later digits then read only the candidates.
+__global__ void digit_histogram_compact_kernel(int64_t n, const double* __restrict__ v, int stride, int n_cols,
+                                               const SelectState* __restrict__ st, int shift, uint32_t digit_mask,
+                                               unsigned* __restrict__ hist, uint64_t* __restrict__ cand,
+                                               int64_t cap, unsigned long long* __restrict__ count) {
+  __shared__ unsigned h[2][kBins];
+  for (int b = threadIdx.x; b < n_cols * kBins; b += blockDim.x) h[b / kBins][b % kBins] = 0u;
+  __syncthreads();
+  const unsigned lane = threadIdx.x & 31u;
+  const int64_t step = int64_t(gridDim.x) * blockDim.x;
+  // i - lane is the same for the whole warp, so the loop is warp-uniform
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i - lane < n; i += step) {
+    const bool valid = i < n;
+    for (int c = 0; c < n_cols; ++c) {
+      const uint64_t k = valid ? order_key(v[i * stride + c]) : 0ull;
+      const bool match = valid && (k & st[c].mask) == st[c].prefix;
+      if (match) atomicAdd(&h[c][uint32_t(k >> shift) & digit_mask], 1u);
+      const unsigned ballot = __ballot_sync(0xffffffffu, match);
+      if (ballot) {
+        const int leader = __ffs(ballot) - 1;
+        unsigned long long base = 0;
+        if (int(lane) == leader) base = atomicAdd(&count[c], static_cast<unsigned long long>(__popc(ballot)));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        if (match) cand[c * cap + int64_t(base) + __popc(ballot & ((1u << lane) - 1u))] = k;
+      }
+    }
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < n_cols * kBins; b += blockDim.x)
+    if (h[b / kBins][b % kBins]) atomicAdd(&hist[b], h[b / kBins][b % kBins]);
+}
+
+// Histogram of one digit over the candidate keys of each column.
+__global__ void candidate_histogram_kernel(const uint64_t* __restrict__ cand, int64_t cap,
+                                           const unsigned long long* __restrict__ count, int n_cols,
+                                           const SelectState* __restrict__ st, int shift, uint32_t digit_mask,
+                                           unsigned* __restrict__ hist) {
+  __shared__ unsigned h[2][kBins];
+  for (int b = threadIdx.x; b < n_cols * kBins; b += blockDim.x) h[b / kBins][b % kBins] = 0u;
+  __syncthreads();
+  const int64_t step = int64_t(gridDim.x) * blockDim.x;
+  for (int c = 0; c < n_cols; ++c) {
+    const int64_t m = int64_t(count[c]);
+    const uint64_t p = st[c].prefix, mk = st[c].mask;
+    for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < m; i += step) {
+      const uint64_t k = cand[c * cap + i];
+      if ((k & mk) == p) atomicAdd(&h[c][uint32_t(k >> shift) & digit_mask], 1u);
     }
   }
   __syncthreads();
@@ -231,19 +288,34 @@ int grid_for(int64_t n, int block = 256, int cap = 152 * 8) {
 
 // Radix selection of the element of rank st[c].rank (0-based, ascending)
 // of each column c < n_cols of v[i * stride + c], i < n: six passes of an
-// 11-bit digit, each a histogram and a one-block scan on the device, no
-// host synchronization.  The selected keys are left in st[c].prefix.
-void select_ranks(const double* v, int stride, int n_cols, int64_t n, SelectState* st, DeviceArray<unsigned>& hist) {
+// 11-bit digit (the last 9 bits wide), each a histogram and a one-block
+// scan on the device, no host synchronization.  The first two passes read
+// every row; the third also copies the keys that still match (those that
+// share the selected sign, exponent and top mantissa bits: a small set
+// unless many values are nearly equal) to the candidate lists
+// cand[c * n ..], and the last three read only those.  The selected keys
+// are left in st[c].prefix.
+void select_ranks(const double* v, int stride, int n_cols, int64_t n, SelectState* st, DeviceArray<unsigned>& hist,
+                  uint64_t* cand, unsigned long long* count) {
   int top = 64;
+  int pass = 0;
+  GB_CUDA(cudaMemsetAsync(count, 0, 2 * sizeof(unsigned long long)));
   while (top > 0) {
     const int width = top >= kDigitBits ? kDigitBits : top;
     const int shift = top - width;
     const uint32_t dmask = (1u << width) - 1u;
     hist.zero();
-    digit_histogram_kernel<<<grid_for(n), 256>>>(n, v, stride, n_cols, st, shift, dmask, hist.get());
+    if (pass < 2)
+      digit_histogram_kernel<<<grid_for(n), 256>>>(n, v, stride, n_cols, st, shift, dmask, hist.get());
+    else if (pass == 2)
+      digit_histogram_compact_kernel<<<grid_for(n), 256>>>(n, v, stride, n_cols, st, shift, dmask, hist.get(), cand,
+                                                           n, count);
+    else
+      candidate_histogram_kernel<<<grid_for(n), 256>>>(cand, n, count, n_cols, st, shift, dmask, hist.get());
     digit_select_kernel<<<n_cols, kSelectThreads>>>(hist.get(), st, shift, dmask);
     GB_CUDA(cudaGetLastError());
     top = shift;
+    ++pass;
   }
 }
 
@@ -269,6 +341,8 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
   DeviceArray<double> thr(2);
   DeviceArray<unsigned> hist, pobs(n_pts), pout(n_pts);
   DeviceArray<SelectState> st;
+  DeviceArray<uint64_t> cand;                 // AUTO: candidate keys, n per column
+  DeviceArray<unsigned long long> ccount(2);  // AUTO: candidates per column
   DeviceArray<uint8_t> f(static_cast<size_t>(n)), rem(n_pts);
   DeviceArray<unsigned long long> counts(2);
   if (cfg.filter_type == 0) {
@@ -277,6 +351,7 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
   } else {
     hist.resize(2 * kBins);
     dev.resize(size_t(n));
+    cand.resize(2 * size_t(n));
     const long long mid = static_cast<long long>(n / 2);
     const SelectState init[3] = {{0ull, 0ull, mid}, {0ull, 0ull, mid}, {0ull, 0ull, mid}};
     st.upload(init, 3);
@@ -287,10 +362,10 @@ OutlierResult find_outliers(const double* errors, int stride, const double* weig
   if (cfg.filter_type != 0) {
     // medians of the two error columns (one pass per digit for both), then
     // the median deviation, all on the device
-    select_ranks(e.get(), stride, 2, n, st.get(), hist);
+    select_ranks(e.get(), stride, 2, n, st.get(), hist, cand.get(), ccount.get());
     deviation_kernel<<<int((n + 255) / 256), 256>>>(n, e.get(), stride, st.get(), dev.get());
     GB_CUDA(cudaGetLastError());
-    select_ranks(dev.get(), 1, 1, n, st.get() + 2, hist);
+    select_ranks(dev.get(), 1, 1, n, st.get() + 2, hist, cand.get(), ccount.get());
     auto_threshold_kernel<<<1, 1>>>(st.get(), cfg.auto_ratio, thr.get());
     GB_CUDA(cudaGetLastError());
   }
