@@ -86,3 +86,24 @@ def test_fixed_instances_join_no_cluster():
     free = np.setdiff1d(np.arange(64), fixed)
     assert np.all(cluster[free] >= 0)
     assert np.bincount(cluster[free]).max() <= 6
+
+
+def test_host_terms_couple_their_clusters():
+    # a common-position term between shots of two clusters that share a
+    # colour ties those clusters: afterwards their colours differ, and every
+    # closed neighbourhood (observations and host terms) stays distinct
+    scene = syn.aerial_scene(seed=3, nx=12, ny=12, n_points=3000)
+    ba = adjuster_from_scene(scene, precision="fp64")
+    cluster0, colour0, _ = ba.coarse_space_layout(8, 144)
+    a = 0
+    b = int(np.nonzero((colour0 == colour0[a]) & (np.arange(len(colour0)) != a))[0][-1])
+    sa, sb = int(np.nonzero(cluster0 == a)[0][0]), int(np.nonzero(cluster0 == b)[0][0])
+    ba.add_common_position(str(sa), str(sb), 1.0, 0.1)
+    cluster, colour, _ = ba.coarse_space_layout(8, 144)
+    np.testing.assert_array_equal(cluster, cluster0)  # the clusters depend on the centres only
+    assert colour[a] != colour[b]
+    adj = cluster_graph(scene, cluster)
+    adj[a, b] = adj[b, a] = True
+    for k in range(len(colour)):
+        hood = np.concatenate([[k], np.nonzero(adj[k])[0]])
+        assert len(np.unique(colour[hood])) == len(hood)
